@@ -1,0 +1,925 @@
+// api.cpp - the C ABI (include/emoo.h): handle lifecycle, particle upload and
+// readback, boundary dispatch in the reference's order, and the time loop.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "emoo.h"
+#include "emoo_internal.h"
+
+using namespace emoo;
+
+namespace emoo {
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaErrorMemoryAllocation) return EMOO_ERR_OOM;
+    fprintf(stderr, "emoo: CUDA error %d (%s)\n", (int)e, cudaGetErrorString(e));
+    return EMOO_ERR_CUDA;
+}
+
+static bool is_pow2(double v) {
+    int e;
+    double m = frexp(v, &e);
+    return m == 0.5;
+}
+
+void make_geom(const emoo_input_info &in, Geom &g) {
+    for (int d = 0; d < 3; d++) {
+        g.n[d] = in.nCell[d];
+        g.tot[d] = in.nCell[d] + 3;
+        g.x0[d] = in.xyz0[d];
+        g.L[d] = in.Lxyz[d];
+        g.d[d] = in.Lxyz[d] / in.nCell[d];  // src/grid/grid.cpp:37-39
+        g.id[d] = 1.0 / g.d[d];             // src/grid/grid.cpp:40-42
+        g.p2[d] = is_pow2(g.d[d]);
+    }
+    g.sy = g.tot[2];
+    g.sx = (int64_t)g.tot[1] * g.tot[2];
+    g.npts = (int64_t)g.tot[0] * g.sx;
+    g.cnz = g.n[2] + 2;
+    g.cny = (g.n[1] + 2) * (g.n[2] + 2);
+    g.ncell = (int64_t)(g.n[0] + 2) * g.cny;
+    g.vol = g.d[0] * g.d[1] * g.d[2];  // src/particles/deposit.cpp:20
+    g.vol_p2 = is_pow2(g.vol);
+    g.ivol = 1.0 / g.vol;
+    for (int i = 0; i < 3; i++) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        g.area[i] = g.d[j] * g.d[k];
+        g.area_p2[i] = is_pow2(g.area[i]);
+        g.iarea[i] = 1.0 / g.area[i];
+    }
+}
+
+int read_err(emoo_handle *h) {
+    DevCounters c;
+    EMOO_CUDA(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    unsigned long long zero = 0;
+    EMOO_CUDA(cudaMemcpyAsync(&h->ctr->err, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
+    if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
+    if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
+    return EMOO_OK;
+}
+
+}  // namespace emoo
+
+namespace {
+
+struct Pulses {
+    int nw;
+    double amp[EMOO_NWAVE], omg[EMOO_NWAVE], pha[EMOO_NWAVE], del[EMOO_NWAVE], iw[EMOO_NWAVE];
+};
+
+// LightBC host state per handle (src/grid/lightBC.cpp:10-142), computed on
+// the host with the same libm calls as the reference.
+struct LightState {
+    Pulses p[6][3];
+};
+
+std::vector<std::pair<emoo_handle *, LightState>> &light_registry() {
+    static std::vector<std::pair<emoo_handle *, LightState>> r;
+    return r;
+}
+
+LightState *light_of(emoo_handle *h) {
+    for (auto &e : light_registry())
+        if (e.first == h) return &e.second;
+    return nullptr;
+}
+
+// GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30
+double gaussian_pulses(double t, double dt, const Pulses &P) {
+    double val = 0.0;
+    for (int i = 0; i < P.nw; i++) {
+        double tmp = P.amp[i] * cos(P.omg[i] * (t + dt) + P.pha[i] * PI_D / 180.0);
+        val += tmp * exp(-pow((t - P.del[i]) * P.iw[i], 2));
+    }
+    return val;
+}
+
+int edge_plane(const Geom &g, bool isB, int comp, int dim, bool right) {
+    if (!right) return 1;
+    bool along = comp == dim;
+    if (!isB) return along ? g.n[dim] : g.n[dim] + 1;
+    return along ? g.n[dim] + 1 : g.n[dim];
+}
+
+// LightBC::applyBCs, src/grid/lightBC.cpp:165-200: six whole-plane writes per
+// external side, E through the E storage, B through the current B role.
+int light_planes(emoo_handle *h, int s, PlaneSet *ps) {
+    LightState *L = light_of(h);
+    static const int EPOL[3][3] = {{1, 2, 0}, {2, 0, 1}, {0, 1, 2}};
+    static const int BPOL[3][3] = {{2, 1, 0}, {0, 2, 1}, {1, 0, 2}};
+    int dim = s / 2;
+    bool right = (s % 2) == 1;
+    int sign = right ? 1 : -1;
+    double E1[3], B1[3];
+    for (int i = 0; i < 3; i++) {
+        E1[i] = h->info.E0[i];
+        B1[i] = h->info.B0[i];
+    }
+    double dx = h->g.d[dim];
+    double bphase = (dx + sign * h->dtp) / 2;
+    int n = 0;
+    for (int i = 0; i < 3; i++) {
+        int eid = EPOL[dim][i], bid = BPOL[dim][i];
+        if (L && L->p[s][eid].nw > 0 && eid != dim) {
+            double ev = gaussian_pulses(h->t, 0.0, L->p[s][eid]);
+            E1[eid] += ev;
+            int bsign = sign * (int)pow(-1, i + 1);
+            double bv = bsign * gaussian_pulses(h->t, bphase, L->p[s][eid]);
+            B1[bid] += bv;
+        }
+        if (h->precision == EMOO_FP64) {
+            ps[n++] = PlaneSet{h->slot[EMOO_EX + eid], dim, edge_plane(h->g, false, eid, dim, right), E1[eid]};
+            double *bp = h->bswap ? h->slot[EMOO_BX_TM1 + bid] : h->slot[EMOO_BX + bid];
+            ps[n++] = PlaneSet{bp, dim, edge_plane(h->g, true, bid, dim, right), B1[bid]};
+        } else {
+            // mixed form: slot index in f, resolved by the mixed plane-set launcher
+            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_EX + eid), dim, edge_plane(h->g, false, eid, dim, right), E1[eid]};
+            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_BX + bid), dim, edge_plane(h->g, true, bid, dim, right), B1[bid]};
+        }
+    }
+    return n;
+}
+
+int bc_kind_particle(const char *s) {
+    if (strcmp(s, "periodic") == 0) return PBC_PERIODIC;
+    if (strcmp(s, "reflecting") == 0) return PBC_REFLECTING;
+    if (strcmp(s, "absorbing") == 0) return PBC_ABSORBING;
+    return -1;
+}
+
+int bc_kind_field(const char *s) {
+    if (strcmp(s, "periodic") == 0) return FBC_PERIODIC;
+    if (strcmp(s, "external") == 0) return FBC_EXTERNAL;
+    return -1;
+}
+
+int set_device(emoo_handle *h) {
+    EMOO_CUDA(cudaSetDevice(h->dev));
+    return EMOO_OK;
+}
+
+template <typename T>
+int dalloc(T *&p, size_t n) {
+    p = nullptr;
+    if (n == 0) n = 1;
+    EMOO_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    return EMOO_OK;
+}
+
+template <typename T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_particles(emoo_handle *h) {
+    dfree(h->x); dfree(h->y); dfree(h->z); dfree(h->vx); dfree(h->vy); dfree(h->vz); dfree(h->gam);
+    dfree(h->ids); dfree(h->fcache);
+    dfree(h->cell); dfree(h->ox); dfree(h->oy); dfree(h->oz); dfree(h->ux); dfree(h->uy); dfree(h->uz);
+    dfree(h->key[0]); dfree(h->key[1]); dfree(h->perm[0]); dfree(h->perm[1]);
+    if (h->pay) cudaFree(h->pay);
+    h->pay = nullptr;
+}
+
+// Particle storage for `cap` particles; existing content is preserved.
+int reserve(emoo_handle *h, int64_t cap) {
+    if (cap <= h->cap) return EMOO_OK;
+    if (cap >= (int64_t)UINT32_MAX - 2) return EMOO_ERR_OOM;
+    int64_t np = h->np;
+    auto grow = [&](auto *&p, bool want) -> int {
+        using T = std::remove_reference_t<decltype(*p)>;
+        if (!want) return EMOO_OK;
+        T *q = nullptr;
+        EMOO_TRY(dalloc(q, (size_t)cap));
+        if (p && np) EMOO_CUDA(cudaMemcpyAsync(q, p, sizeof(T) * (size_t)np, cudaMemcpyDeviceToDevice, h->stream));
+        if (p) cudaFree(p);
+        p = q;
+        return EMOO_OK;
+    };
+    bool f64 = h->precision == EMOO_FP64;
+    EMOO_TRY(grow(h->x, f64)); EMOO_TRY(grow(h->y, f64)); EMOO_TRY(grow(h->z, f64));
+    EMOO_TRY(grow(h->vx, f64)); EMOO_TRY(grow(h->vy, f64)); EMOO_TRY(grow(h->vz, f64));
+    EMOO_TRY(grow(h->gam, f64));
+    EMOO_TRY(grow(h->cell, !f64)); EMOO_TRY(grow(h->ox, !f64)); EMOO_TRY(grow(h->oy, !f64)); EMOO_TRY(grow(h->oz, !f64));
+    EMOO_TRY(grow(h->ux, !f64)); EMOO_TRY(grow(h->uy, !f64)); EMOO_TRY(grow(h->uz, !f64));
+    EMOO_TRY(grow(h->ids, h->opts.track_ids != 0));
+    dfree(h->fcache);
+    dfree(h->key[0]); dfree(h->key[1]); dfree(h->perm[0]); dfree(h->perm[1]);
+    EMOO_TRY(dalloc(h->key[0], (size_t)cap)); EMOO_TRY(dalloc(h->key[1], (size_t)cap));
+    EMOO_TRY(dalloc(h->perm[0], (size_t)cap)); EMOO_TRY(dalloc(h->perm[1], (size_t)cap));
+    if (h->pay) cudaFree(h->pay);
+    h->pay = nullptr;
+    // one array's worth of scratch (8 B per particle), enough for the payload
+    // gather; the mixed-form loader stages 7 doubles per particle in chunks.
+    h->pay_bytes = sizeof(double) * (size_t)cap;
+    EMOO_CUDA(cudaMalloc(&h->pay, h->pay_bytes));
+    h->cap = cap;
+    return EMOO_OK;
+}
+
+// Opens a gap of n particles at the end of species s's segment and returns
+// its start index.
+int make_room(emoo_handle *h, int s, int64_t n, int64_t *at) {
+    if (h->np + n > h->cap) EMOO_TRY(reserve(h, std::max(h->np + n, h->cap + h->cap / 2)));
+    int64_t pos = h->off[s + 1];
+    int64_t tail = h->np - pos;
+    if (tail > 0) {
+        auto shift = [&](auto *p) -> int {
+            using T = std::remove_reference_t<decltype(*p)>;
+            if (!p) return EMOO_OK;
+            T *tmp = (T *)h->pay;
+            EMOO_CUDA(cudaMemcpyAsync(tmp, p + pos, sizeof(T) * (size_t)tail, cudaMemcpyDeviceToDevice, h->stream));
+            EMOO_CUDA(cudaMemcpyAsync(p + pos + n, tmp, sizeof(T) * (size_t)tail, cudaMemcpyDeviceToDevice, h->stream));
+            return EMOO_OK;
+        };
+        EMOO_TRY(shift(h->x)); EMOO_TRY(shift(h->y)); EMOO_TRY(shift(h->z));
+        EMOO_TRY(shift(h->vx)); EMOO_TRY(shift(h->vy)); EMOO_TRY(shift(h->vz)); EMOO_TRY(shift(h->gam));
+        EMOO_TRY(shift(h->cell)); EMOO_TRY(shift(h->ox)); EMOO_TRY(shift(h->oy)); EMOO_TRY(shift(h->oz));
+        EMOO_TRY(shift(h->ux)); EMOO_TRY(shift(h->uy)); EMOO_TRY(shift(h->uz)); EMOO_TRY(shift(h->ids));
+    }
+    for (int q = s + 1; q <= h->nspec; q++) h->off[q] += n;
+    h->count[s] += n;
+    h->np += n;
+    *at = pos;
+    return EMOO_OK;
+}
+
+__attribute__((unused)) int sync(emoo_handle *h) {
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int key_bits(emoo_handle *h) {
+    uint64_t maxkey = (uint64_t)h->nspec * (uint64_t)h->g.ncell + 2;
+    int b = 1;
+    while ((1ull << b) <= maxkey) b++;
+    return b;
+}
+
+int do_sort(emoo_handle *h) {
+    if (h->np == 0) return EMOO_OK;
+    if (h->precision == EMOO_FP64) EMOO_TRY(sort_keys_f64(h));
+    else EMOO_TRY(mixed_sort_keys(h));
+    EMOO_TRY(radix_sort_perm(h, h->np, key_bits(h)));
+    EMOO_TRY(gather_payload(h, h->np));
+    int64_t cnt[EMOO_NSPEC];
+    EMOO_TRY(count_species(h, h->np, cnt));
+    int64_t off = 0;
+    for (int s = 0; s < h->nspec; s++) {
+        h->off[s] = off;
+        h->count[s] = cnt[s];
+        off += cnt[s];
+    }
+    h->off[h->nspec] = off;
+    h->np = off;
+    dfree(h->fcache);
+    return EMOO_OK;
+}
+
+int execute_bc(emoo_handle *h, int send_id);
+
+int deposit_all(emoo_handle *h, int with_rho) {
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    EMOO_TRY(deposit_f64(h, with_rho));
+    return EMOO_OK;
+}
+
+int poisson_init(emoo_handle *h, int iters[4]) {
+    if (!h->poisson) return EMOO_ERR_STATE;
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    // src/poisson/poisson.cpp:98-156: tolerances from the Dirichlet values
+    const emoo_input_info &in = h->info;
+    double vmax = in.bound_phi[0], vmin = in.bound_phi[0];
+    for (int i = 0; i < 6; i++) {
+        vmax = std::max(vmax, in.bound_phi[i]);
+        vmin = std::min(vmin, in.bound_phi[i]);
+    }
+    double conv_phi = vmax - vmin;
+    vmax = vmin = in.bound_Ax[0];
+    for (int i = 0; i < 6; i++) {
+        double a[3] = {in.bound_Ax[i], in.bound_Ay[i], in.bound_Az[i]};
+        for (double v : a) {
+            vmax = std::max(vmax, v);
+            vmin = std::min(vmin, v);
+        }
+    }
+    double conv_A = vmax - vmin;
+    double mult = -4 * PI_D;
+    double tol = std::max(conv_phi * CONV_RATIO, CONV_CRIT);
+    int it[4] = {0, 0, 0, 0}, cv, ok = 1;
+    EMOO_TRY(jacobi_f64(h, EMOO_PHI1, EMOO_PHI2, EMOO_RHO, tol, mult, &it[0], &cv));
+    ok &= it[0] < ITER_MAX;
+    EMOO_TRY(phi_to_e_f64(h));
+    tol = std::max(conv_A * CONV_RATIO, CONV_CRIT);
+    for (int q = 0; q < 3; q++) {
+        EMOO_TRY(jacobi_f64(h, EMOO_AX1 + q, EMOO_AX2 + q, EMOO_JX + q, tol, mult, &it[1 + q], &cv));
+        ok &= it[1 + q] < ITER_MAX;
+    }
+    EMOO_TRY(a_to_b_f64(h));
+    EMOO_TRY(execute_bc(h, EMOO_SEND_EB));
+    if (iters)
+        for (int q = 0; q < 4; q++) iters[q] = it[q];
+    return ok ? EMOO_OK : EMOO_ERR_NOT_CONVERGED;
+}
+
+// Grid::InitializeFields, src/grid/grid.cpp:554-574
+int const_init(emoo_handle *h) {
+    const emoo_input_info &in = h->info;
+    bool cst = in.restart == 0 && strcmp(in.fields_init, "constant") == 0;
+    int64_t n = h->g.npts;
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (!cst) {
+        for (int q = 0; q < 3; q++) EMOO_TRY(fill_f64(h, h->slot[EMOO_JX + q], n, 0.0, h->stream));
+        EMOO_TRY(fill_f64(h, h->slot[EMOO_RHO], n, 0.0, h->stream));
+    }
+    for (int q = 0; q < 3; q++) {
+        EMOO_TRY(fill_f64(h, h->slot[EMOO_EX + q], n, in.E0[q], h->stream));
+        // constB sets both the B and B_tm1 members (src/grid/grid.cpp:523-530)
+        EMOO_TRY(fill_f64(h, h->slot[EMOO_BX + q], n, in.B0[q], h->stream));
+        EMOO_TRY(fill_f64(h, h->slot[EMOO_BX_TM1 + q], n, in.B0[q], h->stream));
+    }
+    return EMOO_OK;
+}
+
+// Grid::executeBC(sendID), src/grid/grid.cpp:577-585: dimensions in order,
+// left then right; periodic ghost copies of consecutive periodic dimensions
+// are independent and issued as one launch.
+int execute_bc(emoo_handle *h, int send_id) {
+    if (h->precision != EMOO_FP64) {
+        if (send_id == EMOO_SEND_EB) {
+            EMOO_TRY(mixed_ghost_fill(h));
+            return EMOO_OK;
+        }
+        return EMOO_ERR_UNSUPPORTED;
+    }
+    if (send_id == EMOO_SEND_JRHO) {
+        for (int d = 0; d < 3; d++)
+            if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d));
+        return EMOO_OK;
+    }
+    if (send_id < EMOO_SEND_JRHO || send_id >= EMOO_NFIELDS) return EMOO_ERR_ARG;
+    // fields the ghost copy touches: through the field pointer table (fixed slots)
+    int ids_eb[6] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ};
+    const int *ids = send_id == EMOO_SEND_EB ? ids_eb : &send_id;
+    int nids = send_id == EMOO_SEND_EB ? 6 : 1;
+    int mask = 0;
+    for (int d = 0; d < 3; d++) {
+        if (h->bc.fbc[2 * d] == FBC_PERIODIC) {
+            mask |= 1 << d;
+            continue;
+        }
+        if (mask) {
+            EMOO_TRY(ghost_fill_f64(h, ids, nids, mask));
+            mask = 0;
+        }
+        for (int r = 0; r < 2; r++) {
+            int s = 2 * d + r;
+            if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
+            if (send_id == EMOO_SEND_EB) {
+                PlaneSet ps[6];
+                int n = light_planes(h, s, ps);
+                EMOO_TRY(plane_set_f64(h, ps, n));
+            } else if (h->poisson && send_id > 0) {
+                int id = send_id;
+                int fid = (id == EMOO_PHI1 || id == EMOO_PHI2) ? 0 : (id == EMOO_AX1 || id == EMOO_AX2) ? 1
+                          : (id == EMOO_AY1 || id == EMOO_AY2) ? 2 : (id == EMOO_AZ1 || id == EMOO_AZ2) ? 3 : -1;
+                if (fid < 0) return EMOO_ERR_ARG;  // the reference asserts here (poissonBC.cpp:226)
+                double v = fid == 0 ? h->info.bound_phi[s] : fid == 1 ? h->info.bound_Ax[s]
+                                    : fid == 2 ? h->info.bound_Ay[s] : h->info.bound_Az[s];
+                PlaneSet p{h->slot[id], d, r == 0 ? 1 : h->g.n[d] + 1, v};
+                EMOO_TRY(plane_set_f64(h, &p, 1));
+            }
+        }
+    }
+    if (mask) EMOO_TRY(ghost_fill_f64(h, ids, nids, mask));
+    return EMOO_OK;
+}
+
+int history_row(emoo_handle *h, double out8[8]) {
+    double m4[4], e6[6];
+    if (h->precision == EMOO_FP64) {
+        EMOO_TRY(particle_moments_f64(h, m4));
+        EMOO_TRY(field_energy_f64(h, e6));
+    } else {
+        EMOO_TRY(mixed_moments(h, m4));
+        EMOO_TRY(mixed_field_energy(h, e6));
+    }
+    double B_en = e6[3] + e6[4] + e6[5];
+    double E_en = e6[0] + e6[1] + e6[2];
+    out8[0] = h->t;
+    out8[1] = m4[1];
+    out8[2] = m4[2];
+    out8[3] = m4[3];
+    out8[4] = m4[0];
+    out8[5] = B_en;
+    out8[6] = E_en;
+    out8[7] = B_en + E_en + m4[0];
+    return EMOO_OK;
+}
+
+int reset_counters(emoo_handle *h) {
+    EMOO_CUDA(cudaMemsetAsync(h->ctr, 0, sizeof(DevCounters), h->stream));
+    return EMOO_OK;
+}
+
+int read_counters(emoo_handle *h, int64_t *counts6, bool accumulate) {
+    DevCounters c;
+    EMOO_CUDA(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    if (counts6)
+        for (int s = 0; s < 6; s++) counts6[s] = (accumulate ? counts6[s] : 0) + (int64_t)c.cross[s];
+    if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
+    if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
+    return EMOO_OK;
+}
+
+#define HANDLE_CHECK(h)                      \
+    do {                                     \
+        if (!(h)) return EMOO_ERR_ARG;       \
+        EMOO_TRY(set_device(h));             \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int emoo_default_opts(emoo_opts *o) {
+    if (!o) return EMOO_ERR_ARG;
+    memset(o, 0, sizeof(*o));
+    o->precision = EMOO_FP64;
+    o->device = 0;
+    o->dt = 0.0;
+    o->capacity = 0;
+    o->track_ids = 1;
+    o->deposit_rho = 1;
+    o->history_every = 10;
+    o->rho_background = 0.0;
+    return EMOO_OK;
+}
+
+const char *emoo_strerror(int s) {
+    switch (s) {
+        case EMOO_OK: return "ok";
+        case EMOO_ERR_ARG: return "bad argument";
+        case EMOO_ERR_OOM: return "out of memory or capacity";
+        case EMOO_ERR_NOT_CONVERGED: return "Jacobi Poisson solve did not converge";
+        case EMOO_ERR_FIXED_OVERFLOW: return "fixed-point accumulator saturated";
+        case EMOO_ERR_BOUNDS: return "device bounds check failed";
+        case EMOO_ERR_CUDA: return "CUDA runtime error";
+        case EMOO_ERR_INPUT: return "input error";
+        case EMOO_ERR_STATE: return "invalid call for the handle state";
+        case EMOO_ERR_UNSUPPORTED: return "unsupported option combination";
+        default: return "unknown status";
+    }
+}
+
+int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle **out) {
+    if (!info || !out) return EMOO_ERR_ARG;
+    *out = nullptr;
+    emoo_opts o;
+    if (opts) o = *opts;
+    else emoo_default_opts(&o);
+    if (o.precision != EMOO_FP64 && o.precision != EMOO_MIXED) return EMOO_ERR_ARG;
+    if (info->nspecies < 0 || info->nspecies > EMOO_NSPEC) return EMOO_ERR_ARG;
+    for (int d = 0; d < 3; d++)
+        if (info->nCell[d] < 1 || !(info->Lxyz[d] > 0)) return EMOO_ERR_ARG;
+    int pbc[6], fbc[6];
+    for (int s = 0; s < 6; s++) {
+        pbc[s] = bc_kind_particle(info->parts_bound[s]);
+        fbc[s] = bc_kind_field(info->fields_bound[s]);
+        if (pbc[s] < 0 || fbc[s] < 0) return EMOO_ERR_INPUT;  // the reference throws "Unable to find ... boundary"
+    }
+    for (int d = 0; d < 3; d++)
+        if ((fbc[2 * d] == FBC_PERIODIC) != (fbc[2 * d + 1] == FBC_PERIODIC)) return EMOO_ERR_INPUT;
+    emoo_handle *h = new (std::nothrow) emoo_handle();
+    if (!h) return EMOO_ERR_OOM;
+    h->info = *info;
+    h->opts = o;
+    h->dev = o.device;
+    h->precision = o.precision;
+    if (h->opts.history_every <= 0) h->opts.history_every = 10;
+    int rc = set_device(h);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    make_geom(*info, h->g);
+    for (int s = 0; s < 6; s++) {
+        h->bc.pbc[s] = pbc[s];
+        h->bc.fbc[s] = fbc[s];
+    }
+    for (int d = 0; d < 3; d++) {
+        // Domain::xyz0_ = x0 + L * 0 (src/domain/domain.cpp:96-99); BC limits
+        // xMin_ and xMin_ + L (bc_p_periodic.cpp:79-80)
+        h->bc.xmin[d] = info->xyz0[d] + info->Lxyz[d] * 0;
+        h->bc.xmax[d] = h->bc.xmin[d] + info->Lxyz[d];
+    }
+    h->poisson = info->restart == 0 && strcmp(info->fields_init, "poisson") == 0;
+    h->nspec = info->nspecies;
+    double mindx = std::min(std::min(h->g.d[0], h->g.d[1]), h->g.d[2]);
+    h->dt = o.dt > 0 ? o.dt : (mindx / 1) / 100.0;  // src/main.cpp:213-214
+    h->t = info->t0;
+    h->dtp = h->dt;
+    // LightBC registry
+    LightState L;
+    memset(&L, 0, sizeof(L));
+    for (int s = 0; s < 6; s++) {
+        int side = (s % 2 == 0) ? -(s / 2 + 1) : (s / 2 + 1);
+        for (int w = 0; w < info->nwaves && w < EMOO_NWAVE; w++) {
+            if (info->inSide[w] != side) continue;
+            int pid = info->inPolE[w] - 1;
+            if (pid < 0 || pid > 2) continue;
+            Pulses &P = L.p[s][pid];
+            P.amp[P.nw] = info->peakamps[w];
+            P.omg[P.nw] = info->omegas[w];
+            P.pha[P.nw] = info->phases[w];
+            P.del[P.nw] = info->delays[w];
+            P.iw[P.nw] = info->invWidths[w];
+            P.nw++;
+        }
+    }
+    light_registry().push_back({h, L});
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        emoo_destroy(h);
+        return cuda_status(e);
+    }
+    rc = EMOO_OK;
+    if (h->precision == EMOO_FP64 || true) {
+        // FP64 slots: the whole grid for the FP64 form; for the mixed form they
+        // hold the FP64 initialisation (Poisson) and serve get/set_field.
+        for (int f = 0; f < EMOO_NFIELDS && rc == EMOO_OK; f++) {
+            rc = dalloc(h->slot[f], (size_t)h->g.npts);
+            if (rc == EMOO_OK) {
+                cudaError_t me = cudaMemsetAsync(h->slot[f], 0, sizeof(double) * (size_t)h->g.npts, h->stream);
+                if (me != cudaSuccess) rc = cuda_status(me);
+            }
+        }
+    }
+    if (rc == EMOO_OK) rc = dalloc(h->ctr, 1);
+    if (rc == EMOO_OK) rc = reset_counters(h);
+    if (rc == EMOO_OK && h->precision == EMOO_MIXED) rc = mixed_alloc(h);
+    int64_t cap = o.capacity > 0 ? o.capacity : info->nparticles_tot;
+    if (rc == EMOO_OK && cap > 0) rc = reserve(h, cap);
+    if (rc == EMOO_OK) {
+        cudaError_t se = cudaStreamSynchronize(h->stream);
+        if (se != cudaSuccess) rc = cuda_status(se);
+    }
+    if (rc != EMOO_OK) {
+        emoo_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return EMOO_OK;
+}
+
+int emoo_destroy(emoo_handle *h) {
+    if (!h) return EMOO_ERR_ARG;
+    cudaSetDevice(h->dev);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (int f = 0; f < EMOO_NFIELDS; f++) dfree(h->slot[f]);
+    free_particles(h);
+    if (h->mf) mixed_free(h);
+    dfree(h->hist);
+    dfree(h->scan_tmp);
+    dfree(h->d_spec_count);
+    dfree(h->ctr);
+    dfree(h->red);
+    if (h->jacobi_state) cudaFree(h->jacobi_state);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    auto &r = light_registry();
+    for (size_t i = 0; i < r.size(); i++)
+        if (r[i].first == h) {
+            r.erase(r.begin() + (long)i);
+            break;
+        }
+    delete h;
+    return EMOO_OK;
+}
+
+int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
+                        const double *vx, const double *vy, const double *vz, const double *gamma,
+                        const int64_t *ids) {
+    HANDLE_CHECK(h);
+    if (species < 0 || species >= h->nspec || n < 0) return EMOO_ERR_ARG;
+    if (n == 0) return EMOO_OK;
+    if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
+    int64_t first_id = h->np;
+    int64_t at;
+    EMOO_TRY(make_room(h, species, n, &at));
+    if (h->precision == EMOO_FP64) {
+        size_t b = sizeof(double) * (size_t)n;
+        EMOO_CUDA(cudaMemcpyAsync(h->x + at, x, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->y + at, y, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->z + at, z, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vx + at, vx, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vy + at, vy, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vz + at, vz, b, cudaMemcpyHostToDevice, h->stream));
+        if (gamma) EMOO_CUDA(cudaMemcpyAsync(h->gam + at, gamma, b, cudaMemcpyHostToDevice, h->stream));
+        else EMOO_CUDA(cudaMemsetAsync(h->gam + at, 0, b, h->stream));
+    } else {
+        EMOO_TRY(mixed_from_f64(h, at, n, x, y, z, vx, vy, vz, gamma));
+    }
+    if (h->ids) {
+        std::vector<int64_t> tmp;
+        const int64_t *src = ids;
+        if (!src) {
+            tmp.resize((size_t)n);
+            for (int64_t i = 0; i < n; i++) tmp[(size_t)i] = first_id + i;
+            src = tmp.data();
+        }
+        EMOO_CUDA(cudaMemcpyAsync(h->ids + at, src, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    dfree(h->fcache);
+    return EMOO_OK;
+}
+
+int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n) {
+    HANDLE_CHECK(h);
+    if (!g || g->species < 0 || g->species >= h->nspec || n < 0) return EMOO_ERR_ARG;
+    if (n == 0) return EMOO_OK;
+    int64_t first_id = h->np;
+    int64_t at;
+    EMOO_TRY(make_room(h, g->species, n, &at));
+    if (h->precision == EMOO_FP64) {
+        EMOO_TRY(generate_device(h, g, 0, n, at));
+    } else {
+        // staged in chunks through the payload scratch (7 doubles per particle)
+        int64_t chunk = (int64_t)(h->pay_bytes / (7 * sizeof(double)));
+        if (chunk < 1) return EMOO_ERR_OOM;
+        for (int64_t b = 0; b < n; b += chunk) {
+            int64_t m = std::min(chunk, n - b);
+            EMOO_TRY(generate_device(h, g, b, m, 0));
+            double *s = (double *)h->pay;
+            EMOO_TRY(mixed_from_f64(h, at + b, -m, s, s + m, s + 2 * m, s + 3 * m, s + 4 * m, s + 5 * m, s + 6 * m));
+        }
+    }
+    if (h->ids) {
+        std::vector<int64_t> tmp((size_t)n);
+        for (int64_t i = 0; i < n; i++) tmp[(size_t)i] = first_id + i;
+        EMOO_CUDA(cudaMemcpyAsync(h->ids + at, tmp.data(), sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice,
+                                  h->stream));
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    dfree(h->fcache);
+    return EMOO_OK;
+}
+
+int emoo_num_particles(emoo_handle *h, int species, int64_t *n) {
+    HANDLE_CHECK(h);
+    if (!n) return EMOO_ERR_ARG;
+    if (species >= h->nspec) return EMOO_ERR_ARG;
+    *n = species < 0 ? h->np : h->count[species];
+    return EMOO_OK;
+}
+
+int emoo_get_particles(emoo_handle *h, int species, int64_t cap, double *x, double *y, double *z, double *vx,
+                       double *vy, double *vz, double *gamma, int64_t *ids, int64_t *n) {
+    HANDLE_CHECK(h);
+    if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
+    int64_t cnt = h->count[species];
+    *n = cnt;
+    if (cap < cnt) return EMOO_ERR_ARG;
+    if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
+    int64_t at = h->off[species];
+    if (h->precision == EMOO_FP64) {
+        size_t b = sizeof(double) * (size_t)cnt;
+        EMOO_CUDA(cudaMemcpyAsync(x, h->x + at, b, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(y, h->y + at, b, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(z, h->z + at, b, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(vx, h->vx + at, b, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(vy, h->vy + at, b, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(vz, h->vz + at, b, cudaMemcpyDeviceToHost, h->stream));
+        if (gamma) EMOO_CUDA(cudaMemcpyAsync(gamma, h->gam + at, b, cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        EMOO_TRY(mixed_to_f64(h, at, cnt, x, y, z, vx, vy, vz, gamma));
+    }
+    if (ids) {
+        if (!h->ids) return EMOO_ERR_STATE;
+        EMOO_CUDA(cudaMemcpyAsync(ids, h->ids + at, sizeof(int64_t) * (size_t)cnt, cudaMemcpyDeviceToHost, h->stream));
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_get_particle_fields(emoo_handle *h, int species, int64_t cap, double *e1, double *e2, double *e3, double *b1,
+                             double *b2, double *b3, int64_t *n) {
+    HANDLE_CHECK(h);
+    if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
+    if (!h->fcache) return EMOO_ERR_STATE;
+    int64_t cnt = h->count[species];
+    *n = cnt;
+    if (cap < cnt) return EMOO_ERR_ARG;
+    double *outs[6] = {e1, e2, e3, b1, b2, b3};
+    int64_t at = h->off[species];
+    for (int q = 0; q < 6; q++) {
+        if (!outs[q]) return EMOO_ERR_ARG;
+        EMOO_CUDA(cudaMemcpyAsync(outs[q], h->fcache + (size_t)q * h->cap + at, sizeof(double) * (size_t)cnt,
+                                  cudaMemcpyDeviceToHost, h->stream));
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_get_field(emoo_handle *h, int id, double *out) {
+    HANDLE_CHECK(h);
+    if (id < 0 || id >= EMOO_NFIELDS || !out) return EMOO_ERR_ARG;
+    size_t b = sizeof(double) * (size_t)h->g.npts;
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_get_field(h, id, h->slot[id]));
+    EMOO_CUDA(cudaMemcpyAsync(out, h->slot[id], b, cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_set_field(emoo_handle *h, int id, const double *in) {
+    HANDLE_CHECK(h);
+    if (id < 0 || id >= EMOO_NFIELDS || !in) return EMOO_ERR_ARG;
+    size_t b = sizeof(double) * (size_t)h->g.npts;
+    EMOO_CUDA(cudaMemcpyAsync(h->slot[id], in, b, cudaMemcpyHostToDevice, h->stream));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_set_field(h, id, h->slot[id]));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_cell_id(emoo_handle *h, double x, double y, double z, int *cid) {
+    if (!h || !cid) return EMOO_ERR_ARG;
+    const Geom &g = h->g;
+    int ix = (int)((x - g.x0[0]) * g.id[0]) + 1;
+    int iy = (int)((y - g.x0[1]) * g.id[1]) + 1;
+    int iz = (int)((z - g.x0[2]) * g.id[2]) + 1;
+    *cid = g.cny * ix + g.cnz * iy + iz;
+    return EMOO_OK;
+}
+
+int emoo_init_fields(emoo_handle *h, int iters[4]) {
+    HANDLE_CHECK(h);
+    // time_phys and dt_phys are still zero during the reference's field
+    // initialisation (src/main.cpp:174 runs before :212-214)
+    h->t = 0.0;
+    h->dtp = 0.0;
+    int rc = EMOO_OK;
+    if (h->poisson) {
+        if (h->precision != EMOO_FP64) rc = EMOO_ERR_UNSUPPORTED;
+        if (rc == EMOO_OK) rc = deposit_all(h, 1);
+        if (rc == EMOO_OK) rc = execute_bc(h, EMOO_SEND_JRHO);
+        if (rc == EMOO_OK) rc = poisson_init(h, iters);
+    } else {
+        if (h->precision == EMOO_FP64) rc = const_init(h);
+        else rc = EMOO_ERR_UNSUPPORTED;
+    }
+    h->t = h->info.t0;
+    h->dtp = h->dt;
+    if (rc != EMOO_OK && rc != EMOO_ERR_NOT_CONVERGED) return rc;
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    h->fields_initialised = 1;
+    return rc;
+}
+
+int emoo_poisson_init(emoo_handle *h, int iters[4]) {
+    HANDLE_CHECK(h);
+    double t = h->t, dtp = h->dtp;
+    h->t = 0.0;
+    h->dtp = 0.0;
+    int rc = poisson_init(h, iters);
+    h->t = t;
+    h->dtp = dtp;
+    cudaStreamSynchronize(h->stream);
+    return rc;
+}
+
+int emoo_sort(emoo_handle *h) {
+    HANDLE_CHECK(h);
+    EMOO_TRY(do_sort(h));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return read_err(h);
+}
+
+int emoo_interpolate(emoo_handle *h) {
+    HANDLE_CHECK(h);
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    EMOO_TRY(interpolate_f64(h));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return read_err(h);
+}
+
+int emoo_push(emoo_handle *h) {
+    HANDLE_CHECK(h);
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    EMOO_TRY(push_cached_f64(h, h->dtp));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
+    HANDLE_CHECK(h);
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    EMOO_TRY(reset_counters(h));
+    EMOO_TRY(particle_bc_f64(h));
+    int rc = read_counters(h, counts6, false);
+    bool absorbing = false;
+    for (int s = 0; s < 6; s++) absorbing |= h->bc.pbc[s] == PBC_ABSORBING;
+    // clearGhosts: removed particles leave the store (compaction by the sort)
+    if (rc == EMOO_OK && absorbing) rc = do_sort(h);
+    return rc;
+}
+
+int emoo_deposit(emoo_handle *h, int with_rho) {
+    HANDLE_CHECK(h);
+    EMOO_TRY(deposit_all(h, with_rho));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return read_err(h);
+}
+
+int emoo_execute_bc(emoo_handle *h, int send_id) {
+    HANDLE_CHECK(h);
+    EMOO_TRY(execute_bc(h, send_id));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_evolve_fields(emoo_handle *h, int electrostatic) {
+    HANDLE_CHECK(h);
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (electrostatic) EMOO_TRY(yee_es_f64(h, h->dtp));
+    else EMOO_TRY(yee_f64(h, h->dtp));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
+    HANDLE_CHECK(h);
+    if (nsteps < 0) return EMOO_ERR_ARG;
+    EMOO_TRY(reset_counters(h));
+    int with_rho = h->opts.deposit_rho ? 1 : 0;
+    for (int it = 0; it < nsteps; it++) {
+        int64_t ti = h->step_index;
+        if (h->info.nstep_sort > 0 && ti % h->info.nstep_sort == 0) EMOO_TRY(do_sort(h));
+        if (ti >= h->next_hist) {
+            double row[8];
+            EMOO_TRY(history_row(h, row));
+            h->hist_rows.insert(h->hist_rows.end(), row, row + 8);
+            h->next_hist += h->opts.history_every;
+        }
+        if (h->precision == EMOO_FP64) {
+            EMOO_TRY(fused_step_f64(h, h->dtp, with_rho));
+            EMOO_TRY(execute_bc(h, EMOO_SEND_JRHO));
+            if (h->info.electrostatic == 1) EMOO_TRY(yee_es_f64(h, h->dtp));
+            else EMOO_TRY(yee_f64(h, h->dtp));
+            EMOO_TRY(execute_bc(h, EMOO_SEND_EB));
+        } else {
+            EMOO_TRY(mixed_step(h, h->dtp, with_rho));
+        }
+        h->t += h->dtp;
+        h->step_index++;
+    }
+    return read_counters(h, counts6, false);
+}
+
+int emoo_history(emoo_handle *h, double out8[8]) {
+    HANDLE_CHECK(h);
+    if (!out8) return EMOO_ERR_ARG;
+    return history_row(h, out8);
+}
+
+int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n) {
+    if (!h || !n) return EMOO_ERR_ARG;
+    int have = (int)(h->hist_rows.size() / 8);
+    *n = have;
+    if (rows) {
+        int m = std::min(cap, have);
+        memcpy(rows, h->hist_rows.data(), sizeof(double) * 8 * (size_t)m);
+    }
+    return EMOO_OK;
+}
+
+int emoo_gauss_residual(emoo_handle *h, double out2[2]) {
+    HANDLE_CHECK(h);
+    if (!out2) return EMOO_ERR_ARG;
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    return gauss_residual_f64(h, out2);
+}
+
+int emoo_time(emoo_handle *h, double *t, double *dt) {
+    if (!h) return EMOO_ERR_ARG;
+    if (t) *t = h->t;
+    if (dt) *dt = h->dt;
+    return EMOO_OK;
+}
+
+int emoo_check(emoo_handle *h) {
+    HANDLE_CHECK(h);
+    return read_err(h);
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// emoo_internal.h - handle layout and kernel launcher declarations shared by
+// the host API (api.cpp) and the CUDA translation units.
+#ifndef EMOO_INTERNAL_H
+#define EMOO_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "emoo.h"
+
+namespace emoo {
+
+constexpr double UNIT_ACC = 0.58668774;       // src/globals.hpp:12
+constexpr double UNIT_RHOJ = 4.80320427e-13;  // src/globals.hpp:16
+constexpr double PI_D = 3.14159265358979323846;
+constexpr int ITER_MAX = 10000;  // src/poisson/poisson.cpp:14
+constexpr double CONV_CRIT = 1e-12;
+constexpr double CONV_RATIO = 1e-9;
+
+enum { PBC_PERIODIC = 0, PBC_REFLECTING = 1, PBC_ABSORBING = 2 };
+enum { FBC_PERIODIC = 0, FBC_EXTERNAL = 1 };
+
+// Device error word bits.
+enum { ERR_BOUNDS = 1, ERR_FIXED_OVERFLOW = 2, ERR_NAN = 4 };
+
+// Grid geometry in the reference layout: (n+3)^3 points per field, C order,
+// physical points 1..n, ghost planes 0 and n+1, extra plane n+2
+// (src/grid/grid.cpp:17-43).
+struct Geom {
+    int n[3];
+    int tot[3];
+    int64_t sx, sy;  // strides of i and j (k is contiguous)
+    int64_t npts;
+    int cny, cnz;    // strides of the reference cellID: (ny+2)(nz+2) * ix + (nz+2) * iy + iz
+    int64_t ncell;   // (nx+2)(ny+2)(nz+2): cellID range
+    double x0[3], L[3], d[3], id[3];
+    int p2[3];  // d[i] is a power of two: x / d == x * id exactly
+    double vol, ivol;
+    int vol_p2;
+    double area[3], iarea[3];  // area[i] = d[j] * d[k], j,k the other two axes in cyclic order
+    int area_p2[3];
+};
+
+// Per-species constants, precomputed on the host in the reference's order of
+// operations so the device arithmetic stays bit-identical to the reference.
+struct SpeciesTab {
+    int nspec;
+    int64_t off[EMOO_NSPEC + 1];  // species s occupies [off[s], off[s+1])
+    double q[EMOO_NSPEC], m[EMOO_NSPEC];
+    double qp[EMOO_NSPEC];   // ((0.5 * dt * q) / m) * UNIT_ACC   (src/pusher/boris.cpp:34-35)
+    double uq[EMOO_NSPEC];   // UNIT_RHOJ * q                      (src/particles/deposit.cpp:30)
+    double cr[EMOO_NSPEC];   // (UNIT_RHOJ * (q / vol)) / vol      (src/particles/deposit.cpp:53)
+    int deposit[EMOO_NSPEC]; // 0 for test-particle species
+};
+
+// Boundary kinds per side (x-, x+, y-, y+, z-, z+).
+struct BCTab {
+    int pbc[6];
+    int fbc[6];
+    double xmin[3], xmax[3];
+};
+
+struct DevCounters {
+    unsigned long long cross[6];
+    unsigned long long err;
+    unsigned long long pad;
+};
+
+// One LightBC plane write (src/grid/lightBC.cpp:196-197).
+struct PlaneSet {
+    double *f;
+    int dim, idx;
+    double v;
+};
+
+struct FieldsF32;  // mixed-form grid storage (particles_mixed.cu)
+
+}  // namespace emoo
+
+struct emoo_handle {
+    emoo_input_info info;
+    emoo_opts opts;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    emoo::Geom g;
+    emoo::BCTab bc;
+    int poisson = 0;
+    int precision = EMOO_FP64;
+
+    // FP64 grid: storage slots indexed like the reference fieldPtr_.
+    double *slot[EMOO_NFIELDS] = {};
+    int bswap = 0;  // B / B_tm1 member roles exchanged (see evolveFields)
+
+    // particles (species-major segments)
+    int nspec = 0;
+    int64_t cap = 0;
+    int64_t np = 0;
+    int64_t count[EMOO_NSPEC] = {};
+    int64_t off[EMOO_NSPEC + 1] = {};
+    // FP64 SoA
+    double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr, *gam = nullptr;
+    double *fcache = nullptr;  // 6 * cap interpolated fields (allocated on demand)
+    int64_t *ids = nullptr;
+    // mixed SoA
+    int32_t *cell = nullptr;
+    float *ox = nullptr, *oy = nullptr, *oz = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
+    emoo::FieldsF32 *mf = nullptr;
+
+    // sort scratch
+    uint32_t *key[2] = {nullptr, nullptr};
+    uint32_t *perm[2] = {nullptr, nullptr};
+    uint32_t *hist = nullptr;
+    uint32_t *scan_tmp = nullptr;
+    size_t hist_cap = 0, scan_cap = 0;
+    void *pay = nullptr;  // payload double buffer
+    size_t pay_bytes = 0;
+    int64_t *d_spec_count = nullptr;
+
+    // reductions and counters
+    emoo::DevCounters *ctr = nullptr;
+    double *red = nullptr;  // reduction partials
+    size_t red_cap = 0;
+    void *jacobi_state = nullptr;
+
+    double dt = 0.0;    // configured step
+    double t = 0.0;     // time_phys
+    double dtp = 0.0;   // dt_phys (zero during field initialisation, like the reference)
+    int64_t step_index = 0;
+    int64_t next_hist = 0;
+    std::vector<double> hist_rows;
+    int fields_initialised = 0;
+};
+
+namespace emoo {
+
+// ---- geometry ----
+void make_geom(const emoo_input_info &in, Geom &g);
+
+// ---- FP64 field kernels (fields_f64.cu) ----
+int yee_f64(emoo_handle *h, double dt);
+int yee_es_f64(emoo_handle *h, double dt);
+int ghost_fill_f64(emoo_handle *h, const int *ids, int nids, int dims_mask);
+int fold_f64(emoo_handle *h, int dim);
+int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
+int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);
+int phi_to_e_f64(emoo_handle *h);
+int a_to_b_f64(emoo_handle *h);
+int field_energy_f64(emoo_handle *h, double out6[6]);
+int gauss_residual_f64(emoo_handle *h, double out2[2]);
+int fill_f64(emoo_handle *h, double *p, int64_t n, double v, cudaStream_t s);
+
+// ---- FP64 particle kernels (particles_f64.cu) ----
+void species_tab(emoo_handle *h, double dtp, SpeciesTab &st);
+int interpolate_f64(emoo_handle *h);
+int push_cached_f64(emoo_handle *h, double dtp);
+int particle_bc_f64(emoo_handle *h);
+int deposit_f64(emoo_handle *h, int with_rho);
+int fused_step_f64(emoo_handle *h, double dtp, int with_rho);
+int particle_moments_f64(emoo_handle *h, double out4[4]);
+int sort_keys_f64(emoo_handle *h);
+
+// ---- sort (sort.cu) ----
+int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits);
+int gather_payload(emoo_handle *h, int64_t n);
+int count_species(emoo_handle *h, int64_t n, int64_t *counts_host);
+
+// ---- loader (loader.cu) ----
+int generate_device(emoo_handle *h, const emoo_gen_params *gp, int64_t first, int64_t n, int64_t dst);
+
+// ---- mixed form (particles_mixed.cu) ----
+int mixed_alloc(emoo_handle *h);
+void mixed_free(emoo_handle *h);
+int mixed_from_f64(emoo_handle *h, int64_t first, int64_t n, const double *x, const double *y, const double *z,
+                   const double *vx, const double *vy, const double *vz, const double *gam);
+int mixed_to_f64(emoo_handle *h, int64_t first, int64_t n, double *x, double *y, double *z, double *vx,
+                 double *vy, double *vz, double *gam);
+int mixed_step(emoo_handle *h, double dtp, int with_rho);
+int mixed_sort_keys(emoo_handle *h);
+int mixed_get_field(emoo_handle *h, int id, double *out_dev);
+int mixed_set_field(emoo_handle *h, int id, const double *in_dev);
+int mixed_moments(emoo_handle *h, double out4[4]);
+int mixed_field_energy(emoo_handle *h, double out6[6]);
+int mixed_ghost_fill(emoo_handle *h);
+int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n);
+
+// ---- helpers ----
+int cuda_status(cudaError_t e);
+int read_err(emoo_handle *h);
+
+}  // namespace emoo
+
+#define EMOO_CUDA(call)                                        \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return emoo::cuda_status(e_);   \
+    } while (0)
+
+#define EMOO_TRY(call)              \
+    do {                            \
+        int rc_ = (call);           \
+        if (rc_ != EMOO_OK) return rc_; \
+    } while (0)
+
+#endif

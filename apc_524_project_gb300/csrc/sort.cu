@@ -1,0 +1,265 @@
+// sort.cu - stable counting sort of particles by (species, cell).
+//
+// The key (species * ncell + cellID, < 2^32) is sorted by least-significant-
+// digit passes of a stable counting sort over 8-bit digits, carrying the
+// original particle index; the SoA payload is then gathered once through the
+// resulting permutation. Each pass: a per-tile digit histogram, an exclusive
+// scan of the digit-major (digit, tile) table, and a scatter in which every
+// warp ranks its items in order with __match_any_sync, so equal keys keep
+// their input order (stability) and the permutation is deterministic.
+// This replaces Particle_Handler::SortParticles / std::sort with
+// Particle_Compare (src/particles/particle_handler.cpp:180-183,
+// src/particles/particle_utils.hpp:18-69).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "dev_common.cuh"
+#include "emoo_internal.h"
+
+namespace emoo {
+
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;  // per thread
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_BINS = 256;
+
+__global__ void __launch_bounds__(RS_THREADS) k_hist(const uint32_t *keys, int64_t n, int shift, uint32_t mask,
+                                                     uint32_t *hist, int nblocks) {
+    __shared__ uint32_t cnt[RS_BINS];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    for (int i = 0; i < RS_ITEMS; i++) {
+        int64_t idx = base + (int64_t)i * RS_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, const uint32_t *vin, uint32_t *kout,
+                                                        uint32_t *vout, int64_t n, int shift, uint32_t mask,
+                                                        const uint32_t *hist, int nblocks) {
+    __shared__ uint32_t wc[RS_THREADS / 32][RS_BINS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < (RS_THREADS / 32) * RS_BINS; i += RS_THREADS) (&wc[0][0])[i] = 0;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * (32 * RS_ITEMS);
+    uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
+    const unsigned lt = lanemask_lt();
+#pragma unroll
+    for (int c = 0; c < RS_ITEMS; c++) {
+        int64_t idx = base + c * 32 + lane;
+        bool valid = idx < n;
+        key[c] = valid ? kin[idx] : 0u;
+        val[c] = valid ? (vin ? vin[idx] : (uint32_t)idx) : 0u;
+        uint32_t dg = (key[c] >> shift) & mask;
+        unsigned tag = valid ? dg : (0x10000u + lane);
+        unsigned peers = __match_any_sync(0xffffffffu, tag);
+        uint32_t b = valid ? wc[w][dg] : 0u;
+        rank[c] = b + __popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wc[w][dg] = b + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x < RS_BINS) {
+        uint32_t run = 0;
+        for (int ww = 0; ww < RS_THREADS / 32; ww++) {
+            uint32_t t = wc[ww][threadIdx.x];
+            wc[ww][threadIdx.x] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < RS_ITEMS; c++) {
+        int64_t idx = base + c * 32 + lane;
+        if (idx >= n) continue;
+        uint32_t dg = (key[c] >> shift) & mask;
+        uint32_t pos = hist[(int64_t)dg * nblocks + blockIdx.x] + wc[w][dg] + rank[c];
+        if (kout) kout[pos] = key[c];
+        vout[pos] = val[c];
+    }
+}
+
+// In-place exclusive scan of each 2048-element tile; tile totals to sums.
+__global__ void __launch_bounds__(RS_THREADS) k_scan_tile(uint32_t *data, int64_t m, uint32_t *sums) {
+    __shared__ uint32_t wsum[RS_THREADS / 32];
+    int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)threadIdx.x * RS_ITEMS;
+    uint32_t v[RS_ITEMS];
+    uint32_t tot = 0;
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        v[i] = (base + i < m) ? data[base + i] : 0u;
+        tot += v[i];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = tot;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    uint32_t wpre = 0, all = 0;
+    for (int ww = 0; ww < RS_THREADS / 32; ww++) {
+        if (ww < w) wpre += wsum[ww];
+        all += wsum[ww];
+    }
+    uint32_t run = wpre + incl - tot;
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        if (base + i < m) data[base + i] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == 0 && sums) sums[blockIdx.x] = all;
+}
+
+__global__ void k_scan_add(uint32_t *data, int64_t m, const uint32_t *sums) {
+    int64_t base = (int64_t)blockIdx.x * RS_TILE;
+    uint32_t a = sums[blockIdx.x];
+    for (int i = threadIdx.x; i < RS_TILE; i += blockDim.x) {
+        int64_t idx = base + i;
+        if (idx < m) data[idx] += a;
+    }
+}
+
+int64_t tiles(int64_t m) { return (m + RS_TILE - 1) / RS_TILE; }
+
+// Scratch words a recursive scan of m elements needs.
+int64_t scan_scratch(int64_t m) {
+    int64_t t = tiles(m);
+    if (t <= 1) return 1;
+    return t + scan_scratch(t);
+}
+
+int scan_excl(emoo_handle *h, uint32_t *data, int64_t m, uint32_t *tmp) {
+    int64_t t = tiles(m);
+    if (t <= 1) {
+        k_scan_tile<<<1, RS_THREADS, 0, h->stream>>>(data, m, nullptr);
+        EMOO_CUDA(cudaGetLastError());
+        return EMOO_OK;
+    }
+    k_scan_tile<<<(unsigned)t, RS_THREADS, 0, h->stream>>>(data, m, tmp);
+    EMOO_TRY(scan_excl(h, tmp, t, tmp + t));
+    k_scan_add<<<(unsigned)t, RS_THREADS, 0, h->stream>>>(data, m, tmp);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+template <typename T>
+__global__ void k_gather(const T *__restrict__ src, T *__restrict__ dst, const uint32_t *__restrict__ perm, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+template <typename T>
+int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
+    if (!arr) return EMOO_OK;
+    T *tmp = (T *)h->pay;
+    int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);
+    EMOO_CUDA(cudaGetLastError());
+    h->pay = (void *)arr;
+    arr = tmp;
+    return EMOO_OK;
+}
+
+__global__ void k_species_bounds(const uint32_t *keys, int64_t n, int nspec, int64_t ncell, int64_t *bounds) {
+    int s = threadIdx.x;
+    if (s > nspec) return;
+    uint64_t target = (uint64_t)s * (uint64_t)ncell;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if ((uint64_t)keys[mid] < target) lo = mid + 1;
+        else hi = mid;
+    }
+    bounds[s] = lo;
+}
+
+}  // namespace
+
+int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
+    if (n <= 0) return EMOO_OK;
+    int nblocks = (int)tiles(n);
+    size_t need_hist = (size_t)RS_BINS * nblocks;
+    if (h->hist_cap < need_hist) {
+        if (h->hist) cudaFree(h->hist);
+        h->hist = nullptr;
+        EMOO_CUDA(cudaMalloc(&h->hist, need_hist * sizeof(uint32_t)));
+        h->hist_cap = need_hist;
+    }
+    size_t need_scan = (size_t)scan_scratch((int64_t)need_hist) + 1;
+    if (h->scan_cap < need_scan) {
+        if (h->scan_tmp) cudaFree(h->scan_tmp);
+        h->scan_tmp = nullptr;
+        EMOO_CUDA(cudaMalloc(&h->scan_tmp, need_scan * sizeof(uint32_t)));
+        h->scan_cap = need_scan;
+    }
+    int passes = std::max(1, (key_bits + 7) / 8);
+    int cur = 0;
+    for (int ps = 0; ps < passes; ps++) {
+        int shift = ps * 8;
+        int bits = std::min(8, key_bits - shift);
+        if (bits <= 0) bits = 1;
+        uint32_t mask = (1u << bits) - 1u;
+        k_hist<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], n, shift, mask, h->hist, nblocks);
+        EMOO_CUDA(cudaGetLastError());
+        EMOO_TRY(scan_excl(h, h->hist, (int64_t)need_hist, h->scan_tmp));
+        k_scatter<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], ps == 0 ? nullptr : h->perm[cur],
+                                                         h->key[cur ^ 1], h->perm[cur ^ 1], n, shift, mask, h->hist,
+                                                         nblocks);
+        EMOO_CUDA(cudaGetLastError());
+        cur ^= 1;
+    }
+    // leave the result in slot 0
+    if (cur == 1) {
+        std::swap(h->key[0], h->key[1]);
+        std::swap(h->perm[0], h->perm[1]);
+    }
+    return EMOO_OK;
+}
+
+int gather_payload(emoo_handle *h, int64_t n) {
+    const uint32_t *perm = h->perm[0];
+    if (h->precision == EMOO_FP64) {
+        EMOO_TRY(gather_one(h, h->x, perm, n));
+        EMOO_TRY(gather_one(h, h->y, perm, n));
+        EMOO_TRY(gather_one(h, h->z, perm, n));
+        EMOO_TRY(gather_one(h, h->vx, perm, n));
+        EMOO_TRY(gather_one(h, h->vy, perm, n));
+        EMOO_TRY(gather_one(h, h->vz, perm, n));
+        EMOO_TRY(gather_one(h, h->gam, perm, n));
+    } else {
+        EMOO_TRY(gather_one(h, h->cell, perm, n));
+        EMOO_TRY(gather_one(h, h->ox, perm, n));
+        EMOO_TRY(gather_one(h, h->oy, perm, n));
+        EMOO_TRY(gather_one(h, h->oz, perm, n));
+        EMOO_TRY(gather_one(h, h->ux, perm, n));
+        EMOO_TRY(gather_one(h, h->uy, perm, n));
+        EMOO_TRY(gather_one(h, h->uz, perm, n));
+    }
+    EMOO_TRY(gather_one(h, h->ids, perm, n));
+    return EMOO_OK;
+}
+
+// Species segment bounds from the sorted keys; returns the per-species
+// counts (removed particles are past the last bound).
+int count_species(emoo_handle *h, int64_t n, int64_t *counts_host) {
+    if (!h->d_spec_count) EMOO_CUDA(cudaMalloc(&h->d_spec_count, sizeof(int64_t) * (EMOO_NSPEC + 1)));
+    k_species_bounds<<<1, 64, 0, h->stream>>>(h->key[0], n, h->nspec, h->g.ncell, h->d_spec_count);
+    EMOO_CUDA(cudaGetLastError());
+    int64_t b[EMOO_NSPEC + 1];
+    EMOO_CUDA(cudaMemcpyAsync(b, h->d_spec_count, sizeof(int64_t) * (h->nspec + 1), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    for (int s = 0; s < h->nspec; s++) counts_host[s] = b[s + 1] - b[s];
+    return EMOO_OK;
+}
+
+}  // namespace emoo

@@ -1,0 +1,285 @@
+/*
+ * emoo.h - C ABI of the GB300 (sm_103a) EMOOPIC per-timestep PIC loop.
+ *
+ * One opaque handle owns one device-resident simulation domain on one GPU:
+ * the Yee grid (reference layout: (n+3)^3 points per field, C order
+ * [i][j][k], one ghost layer plus one extra plane, field IDs as in the
+ * reference Grid) and a structure-of-arrays particle store sorted by cell.
+ *
+ * Every entry point returns an int status (EMOO_OK = 0, negative on error),
+ * throws nothing across the ABI and is synchronous unless documented
+ * otherwise. A handle is owned by one host thread; all of its work runs on
+ * the handle's own CUDA stream.
+ *
+ * Each declaration cites the reference interface it replaces as
+ * path:line inside the reference project (DenSto/APC_524_Project).
+ */
+#ifndef EMOO_H
+#define EMOO_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMOO_NDIM 3
+#define EMOO_NCHAR 64
+#define EMOO_NSPEC 32
+#define EMOO_NWAVE 32
+
+/* Status codes. */
+#define EMOO_OK 0
+#define EMOO_ERR_ARG (-1)            /* bad argument (null pointer, out-of-range id, size) */
+#define EMOO_ERR_OOM (-2)            /* device or host allocation failed, or capacity exceeded */
+#define EMOO_ERR_NOT_CONVERGED (-3)  /* Jacobi Poisson solve reached its iteration cap */
+#define EMOO_ERR_FIXED_OVERFLOW (-4) /* fixed-point current/charge accumulator saturated */
+#define EMOO_ERR_BOUNDS (-5)         /* a device-side bounds check recorded a bad index */
+#define EMOO_ERR_CUDA (-6)           /* a CUDA runtime call failed */
+#define EMOO_ERR_INPUT (-7)          /* input file missing, unparsable or inconsistent */
+#define EMOO_ERR_STATE (-8)          /* call not valid in the handle's current state */
+#define EMOO_ERR_UNSUPPORTED (-9)    /* option combination not implemented */
+
+/* Precision forms. */
+#define EMOO_FP64 0  /* FP64 positions, velocities, fields and current (reference parity form) */
+#define EMOO_MIXED 1 /* int32 cell + FP32 offset, FP32 momentum and fields, int64 fixed-point current */
+
+/* Field IDs, src/grid/grid.cpp:44-60 (Grid) and src/poisson/poisson.cpp:98-111 (Poisson_Solver). */
+#define EMOO_EX 0
+#define EMOO_EY 1
+#define EMOO_EZ 2
+#define EMOO_BX 3
+#define EMOO_BY 4
+#define EMOO_BZ 5
+#define EMOO_JX 6
+#define EMOO_JY 7
+#define EMOO_JZ 8
+#define EMOO_RHO 9
+#define EMOO_BX_TM1 10
+#define EMOO_BY_TM1 11
+#define EMOO_BZ_TM1 12
+#define EMOO_PHI1 13
+#define EMOO_AX1 14
+#define EMOO_AY1 15
+#define EMOO_AZ1 16
+#define EMOO_PHI2 17
+#define EMOO_AX2 18
+#define EMOO_AY2 19
+#define EMOO_AZ2 20
+#define EMOO_NFIELDS 21
+
+/* Boundary-condition exchange selectors of Grid::executeBC(sendID),
+ * src/grid/spookyGrid.cpp:8-16: -1 = E,B ghost fill; -2 = periodic fold of
+ * J-perp and rho; >= 0 = one field. */
+#define EMOO_SEND_EB (-1)
+#define EMOO_SEND_JRHO (-2)
+
+/*
+ * Run configuration. Binary-identical to the reference's Input_Info_t
+ * (src/IO/input.hpp:15-126): same members, same order, same array bounds
+ * (long is 64-bit on the LP64 targets this library supports), so the
+ * reference parser's output can be handed over unchanged.
+ */
+typedef struct emoo_input_info {
+    int nCell[EMOO_NDIM];
+    int nProc[EMOO_NDIM];
+    int nt;
+    int restart;
+    int debug;
+    int relativity;
+    int electrostatic;
+    int nspecies;
+    int nstep_fields;
+    int nstep_parts;
+    int nstep_restart;
+    int nstep_sort;
+    int which_fields;
+    int output_pCount;
+    int nwaves;
+    int inSide[EMOO_NWAVE];
+    int inPolE[EMOO_NWAVE];
+    int isTestParticle[EMOO_NSPEC];
+    int64_t nparticles_tot;
+    int64_t nparticles_domain;
+    double t0;
+    double dens_phys;
+    double super_ratio;
+    double mass_ratio[EMOO_NSPEC];
+    double charge_ratio[EMOO_NSPEC];
+    double dens_frac[EMOO_NSPEC];
+    double temp[EMOO_NSPEC];
+    double peakamps[EMOO_NWAVE];
+    double omegas[EMOO_NWAVE];
+    double phases[EMOO_NWAVE];
+    double invWidths[EMOO_NWAVE];
+    double delays[EMOO_NWAVE];
+    double E0[EMOO_NDIM];
+    double B0[EMOO_NDIM];
+    double bound_phi[2 * EMOO_NDIM];
+    double bound_Ax[2 * EMOO_NDIM];
+    double bound_Ay[2 * EMOO_NDIM];
+    double bound_Az[2 * EMOO_NDIM];
+    double xyz0[EMOO_NDIM];
+    double Lxyz[EMOO_NDIM];
+    char distname[EMOO_NCHAR];
+    char parts_init[EMOO_NCHAR];
+    char fields_init[EMOO_NCHAR];
+    char parts_bound[2 * EMOO_NDIM][EMOO_NCHAR];
+    char fields_bound[2 * EMOO_NDIM][EMOO_NCHAR];
+} emoo_input_info;
+
+/* Options the reference fixes in code. */
+typedef struct emoo_opts {
+    int precision;         /* EMOO_FP64 or EMOO_MIXED */
+    int device;            /* CUDA device ordinal */
+    double dt;             /* time step; <= 0 selects the reference's mindx/100 (src/main.cpp:213-214) */
+    int64_t capacity;      /* particle capacity to reserve; 0 = nparticles_tot of the input */
+    int track_ids;         /* 1 = carry a 64-bit particle id through sorts (needed to read back by id) */
+    int deposit_rho;       /* 1 = deposit rho every step as the reference does (src/main.cpp:245) */
+    int history_every;     /* history cadence in steps; the reference hard-codes 10 (src/IO/output.cpp:46) */
+    double rho_background; /* uniform immobile background charge density added to rho, reference units */
+} emoo_opts;
+
+/* Seeded sampler of one species (no reference counterpart: replaces the
+ * sequential ran2 loader of src/particles/particle_handler.cpp:47-84 with
+ * independent per-particle streams, identical on host and device). */
+typedef struct emoo_gen_params {
+    uint64_t seed;
+    int species;
+    int relativistic_gamma; /* 1: gamma = sqrt(1 - v^2), the reference loader's convention (particle_handler.cpp:77) */
+    double x0[3], L[3];     /* sampling box */
+    double vth[3];          /* thermal speed per axis */
+    double vdrift[3];       /* drift velocity */
+    double dens_amp;        /* delta n / n of a cos(2 pi k (x - x0) / Lx) modulation along x (0 = uniform) */
+    double dens_k;          /* mode number k of that modulation */
+} emoo_gen_params;
+
+typedef struct emoo_handle emoo_handle;
+
+/* Fills *o with the defaults (FP64, device 0, reference dt, rho every step, history every 10). */
+int emoo_default_opts(emoo_opts *o);
+
+/* Human-readable text of a status code. Never null. */
+const char *emoo_strerror(int status);
+
+/* Builds the device domain: Domain + Grid/Poisson_Solver + field and particle
+ * boundaries + Particle_Handler with the pusher named by info->relativity.
+ * Replaces src/main.cpp:115-150 (Domain, setPusher, Part_BC_Factory,
+ * Grid/Poisson_Solver, Field_BC_Factory). All fields start at zero. */
+int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle **out);
+
+/* Frees everything the handle owns. Replaces src/main.cpp:307-316. */
+int emoo_destroy(emoo_handle *h);
+
+/* Copies n particles of species `species` from caller-owned host SoA arrays.
+ * gamma may be null (then 0, like new_particle, src/particles/particle.cpp:4-21);
+ * ids may be null (then consecutive from the current count). Replaces the
+ * particle construction of Particle_Handler::Load,
+ * src/particles/particle_handler.cpp:53-84. */
+int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y,
+                        const double *z, const double *vx, const double *vy, const double *vz,
+                        const double *gamma, const int64_t *ids);
+
+/* Host-side sampler: fills particles [first, first+n) of the stream described
+ * by g into caller-owned arrays (gamma may be null). Pure host code. */
+int emoo_generate_host(const emoo_gen_params *g, int64_t first, int64_t n, double *x, double *y, double *z,
+                       double *vx, double *vy, double *vz, double *gamma);
+
+/* Device-side sampler: appends particles [0, n) of the stream g to species
+ * g->species directly in device memory; bit-identical to emoo_generate_host. */
+int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n);
+
+/* Number of live particles of a species (all species when species < 0). */
+int emoo_num_particles(emoo_handle *h, int species, int64_t *n);
+
+/* Copies the particles of a species back to host arrays of capacity cap, in
+ * device order; *n receives the count. gamma / ids may be null. */
+int emoo_get_particles(emoo_handle *h, int species, int64_t cap, double *x, double *y, double *z,
+                       double *vx, double *vy, double *vz, double *gamma, int64_t *ids, int64_t *n);
+
+/* Copies the per-particle interpolated fields cached by emoo_interpolate
+ * (the reference's Particle::field, src/particles/particle.hpp:4-7). */
+int emoo_get_particle_fields(emoo_handle *h, int species, int64_t cap, double *e1, double *e2, double *e3,
+                             double *b1, double *b2, double *b3, int64_t *n);
+
+/* Whole-array field access in the reference layout: (n+3)^3 doubles, C order
+ * [i][j][k]. Replaces Grid::getFieldPtr, src/grid/grid.hpp:68. */
+int emoo_get_field(emoo_handle *h, int field_id, double *out);
+int emoo_set_field(emoo_handle *h, int field_id, const double *in);
+
+/* Reference getCellID for a position (ghost offset included),
+ * src/grid/oGrid.cpp:208-227. Host-side, no device work. */
+int emoo_cell_id(emoo_handle *h, double x, double y, double z, int *cell_id);
+
+/* Field initialisation of src/main.cpp:159-179: for "poisson" deposit rho/J,
+ * fold (-2), then the four Jacobi solves + phiToE + AToB + E/B ghost fill
+ * (src/poisson/poisson.cpp:143-170); for "constant" E0/B0
+ * (src/grid/grid.cpp:554-574). Then the per-particle interpolation.
+ * iters (may be null) receives the four Jacobi iteration counts. */
+int emoo_init_fields(emoo_handle *h, int iters[4]);
+
+/* Poisson_Solver::InitializeFields alone, on whatever rho/J the grid holds,
+ * src/poisson/poisson.cpp:143-170. Returns EMOO_ERR_NOT_CONVERGED (after
+ * finishing exactly like the reference) when a solve hit ITER_MAX. */
+int emoo_poisson_init(emoo_handle *h, int iters[4]);
+
+/* Stable counting sort of each species by cell (ascending (ix,iy,iz)).
+ * Replaces Particle_Handler::SortParticles, src/particles/particle_handler.cpp:180-183
+ * (the reference uses an unstable std::sort, descending). */
+int emoo_sort(emoo_handle *h);
+
+/* Gathers E and (B + B_tm1)/2 at every particle into the per-particle field
+ * cache. Replaces Particle_Handler::InterpolateEB,
+ * src/particles/particle_handler.cpp:138-173. */
+int emoo_interpolate(emoo_handle *h);
+
+/* Pushes every particle with its cached field (Boris or relativistic Boris).
+ * Replaces Particle_Handler::Push, src/particles/particle_handler.cpp:124-128. */
+int emoo_push(emoo_handle *h);
+
+/* Applies the six particle boundaries in the reference order (x-, x+, y-, y+,
+ * z-, z+); counts6 (may be null) receives the crossings per side.
+ * Replaces executeParticleBoundaryConditions + clearGhosts,
+ * src/particles/particle_handler.cpp:287-295 and :271-284. */
+int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]);
+
+/* Zeroes J (and rho) and deposits every non-test particle.
+ * Replaces Particle_Handler::depositRhoJ, src/particles/particle_handler.cpp:185-239. */
+int emoo_deposit(emoo_handle *h, int with_rho);
+
+/* Grid::executeBC(sendID), src/grid/grid.cpp:577-585. */
+int emoo_execute_bc(emoo_handle *h, int send_id);
+
+/* Grid::evolveFields / evolveFieldsES, src/grid/oGrid.cpp:15-81. */
+int emoo_evolve_fields(emoo_handle *h, int electrostatic);
+
+/* The fused time loop: nsteps passes of src/main.cpp:221-287 (sort every
+ * nstep_sort, history every history_every, gather+push+BC+deposit in one
+ * kernel, fold, Yee update, ghost fill). Crossing counts accumulate into
+ * counts6 (may be null). */
+int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]);
+
+/* The history row of src/IO/output.cpp:52-123 for the current state:
+ * {t, sum m vx, sum m vy, sum m vz, particle KE, B energy, E energy, total}. */
+int emoo_history(emoo_handle *h, double out8[8]);
+
+/* Rows recorded by emoo_step (every history_every steps, before the push,
+ * like the reference). Copies up to cap rows of 8 doubles; *n = rows held. */
+int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n);
+
+/* Gauss-law residual of the current state: max and L2 norm over physical
+ * vertices of (div E - 4 pi rho) (no reference counterpart). */
+int emoo_gauss_residual(emoo_handle *h, double out2[2]);
+
+/* Current simulation time and step size. */
+int emoo_time(emoo_handle *h, double *t, double *dt);
+
+/* Device-side error word (bounds checks, fixed-point saturation) since the
+ * last call; cleared by reading. */
+int emoo_check(emoo_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMOO_H */

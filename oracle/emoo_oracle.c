@@ -1,0 +1,1100 @@
+/*
+ * emoo_oracle.c - CPU restatement (plain C, FP64, one thread) of the EMOOPIC
+ * per-timestep PIC loop, used ONLY as the checker of the GPU library.
+ *
+ * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / reference arm load this library. The product never calls it.
+ *
+ * It restates the reference serial build's arithmetic in the same evaluation
+ * order (compile with -ffp-contract=off so no multiply-add is fused), so that
+ * on identical inputs it reproduces the reference bit for bit wherever the
+ * reference's order of operations is defined. Each function cites the
+ * reference file:line it follows (paths inside DenSto/APC_524_Project).
+ *
+ * It is pinned against the compiled reference (oracle/ref) through the golden
+ * fixtures in tests/golden/.
+ *
+ * Reference behaviours reproduced on purpose (all verified against the
+ * compiled reference):
+ *  (a) the cell "vertex" handed to interpolation and deposition includes the
+ *      ghost offset, so in-cell offsets lie in [-dx, 0) and the weights are
+ *      linear extrapolations (src/grid/oGrid.cpp:160-162, 239-241);
+ *  (b) Grid::addJ puts the 4th x-edge weight on Jx[i][j+1][k] instead of
+ *      Jx[i][j][k+1] (src/grid/oGrid.cpp:101);
+ *  (c) ghost planes are refreshed over the physical transverse range only,
+ *      edge and corner ghost lines keep stale values (src/grid/spookyGrid.cpp:318-341);
+ *  (d) the periodic J/rho fold moves only the two transverse J components and
+ *      rho of the far ghost plane (src/grid/spookyGrid.cpp:21-26);
+ *  (e) the gather uses B averaged over the two stored time levels
+ *      (src/grid/oGrid.cpp:183-192);
+ *  (f) evolveFields swaps the B / B_tm1 member pointers but not the field
+ *      pointer table (src/grid/oGrid.cpp:18-20 vs src/grid/grid.cpp:321-342):
+ *      ghost fills, getFieldPtr and the history read fixed storage slots, the
+ *      Yee update, LightBC and the gather read the swapped roles;
+ *  (g) Poisson_Solver::run_poisson_solver_ swaps its local pointer copies
+ *      only, so phiToE / AToB always read phi1 / A1 (src/poisson/poisson.cpp:285);
+ *  (h) AToB differences the same A component twice (src/poisson/convertFields.cpp:131-150);
+ *  (i) periodic particle boundaries create ghost copies that later sides test
+ *      again, and clearGhosts swaps each ghost with the vector's last element
+ *      (src/boundaries/b_particles/bc_p_periodic.cpp:44-87,
+ *      src/particles/particle_handler.cpp:271-284), which fixes the particle
+ *      order and hence the current summation order.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/emoo.h"
+
+#define UNIT_ACC 0.58668774          /* src/globals.hpp:12 */
+#define UNIT_RHOJ 4.80320427e-13     /* src/globals.hpp:16 */
+#define PI_D 3.14159265358979323846  /* M_PI */
+#define ITER_MAX 10000               /* src/poisson/poisson.cpp:14 */
+#define CONV_CRIT 1e-12              /* src/poisson/poisson.cpp:12 */
+#define CONV_RATIO 1e-9              /* src/poisson/poisson.cpp:13 */
+
+enum { BC_PERIODIC = 0, BC_REFLECTING = 1, BC_ABSORBING = 2, BC_EXTERNAL = 3 };
+
+typedef struct {
+    int nw;
+    double amp[EMOO_NWAVE], omg[EMOO_NWAVE], pha[EMOO_NWAVE], del[EMOO_NWAVE], iw[EMOO_NWAVE];
+} pulses_t;
+
+typedef struct {
+    emoo_input_info info;
+    int n[3];    /* physical cells */
+    int tot[3];  /* n + 3 points per dimension */
+    long npts;
+    double x0[3], L[3], d[3], id[3];
+    double *slot[EMOO_NFIELDS]; /* storage slots, indexed like the reference fieldPtr_ */
+    int bswap;                  /* 1 when the B / B_tm1 roles are exchanged (f) */
+    int poisson;
+    int pbc[6], fbc[6];
+    pulses_t pulse[6][3]; /* LightBC: per side, per polarisation */
+    double conv_phi, conv_A;
+    /* particles */
+    long np, cap;
+    double *x, *y, *z, *vx, *vy, *vz, *g;
+    double *fe1, *fe2, *fe3, *fb1, *fb2, *fb3;
+    int *type;
+    long *pid;
+    short *ghost;
+    double dt, t0;
+    double t, dtp; /* the reference's globals time_phys and dt_phys */
+    long next_hist;
+} orc_t;
+
+/* ------------------------------------------------------------------ */
+/* helpers                                                              */
+
+static inline long IDX(const orc_t *c, int i, int j, int k) {
+    return ((long)i * c->tot[1] + j) * c->tot[2] + k;
+}
+
+/* Member-role pointers (Ex_, Bx_, Bx_tm1_ ...) versus the fixed slots. */
+static double *role_B(orc_t *c, int comp) { return c->bswap ? c->slot[EMOO_BX_TM1 + comp] : c->slot[EMOO_BX + comp]; }
+static double *role_Btm1(orc_t *c, int comp) { return c->bswap ? c->slot[EMOO_BX + comp] : c->slot[EMOO_BX_TM1 + comp]; }
+
+static int bc_code(const char *s, int field) {
+    if (strcmp(s, "periodic") == 0) return BC_PERIODIC;
+    if (field) return strcmp(s, "external") == 0 ? BC_EXTERNAL : -1;
+    if (strcmp(s, "reflecting") == 0) return BC_REFLECTING;
+    if (strcmp(s, "absorbing") == 0) return BC_ABSORBING;
+    return -1;
+}
+
+static int grow(orc_t *c, long need) {
+    if (need <= c->cap) return 0;
+    long nc = c->cap ? c->cap : 1024;
+    while (nc < need) nc *= 2;
+#define RE(p, T)                                      \
+    do {                                              \
+        void *q = realloc(c->p, sizeof(T) * (size_t)nc); \
+        if (!q) return -1;                            \
+        c->p = (T *)q;                                \
+    } while (0)
+    RE(x, double); RE(y, double); RE(z, double);
+    RE(vx, double); RE(vy, double); RE(vz, double); RE(g, double);
+    RE(fe1, double); RE(fe2, double); RE(fe3, double);
+    RE(fb1, double); RE(fb2, double); RE(fb3, double);
+    RE(type, int); RE(pid, long); RE(ghost, short);
+#undef RE
+    c->cap = nc;
+    return 0;
+}
+
+static void copy_particle(orc_t *c, long dst, long src) {
+    c->x[dst] = c->x[src]; c->y[dst] = c->y[src]; c->z[dst] = c->z[src];
+    c->vx[dst] = c->vx[src]; c->vy[dst] = c->vy[src]; c->vz[dst] = c->vz[src];
+    c->g[dst] = c->g[src];
+    c->fe1[dst] = c->fe1[src]; c->fe2[dst] = c->fe2[src]; c->fe3[dst] = c->fe3[src];
+    c->fb1[dst] = c->fb1[src]; c->fb2[dst] = c->fb2[src]; c->fb3[dst] = c->fb3[src];
+    c->type[dst] = c->type[src]; c->pid[dst] = c->pid[src]; c->ghost[dst] = c->ghost[src];
+}
+
+static void swap_particle(orc_t *c, long a, long b) {
+#define SW(p, T) do { T t_ = c->p[a]; c->p[a] = c->p[b]; c->p[b] = t_; } while (0)
+    SW(x, double); SW(y, double); SW(z, double);
+    SW(vx, double); SW(vy, double); SW(vz, double); SW(g, double);
+    SW(fe1, double); SW(fe2, double); SW(fe3, double);
+    SW(fb1, double); SW(fb2, double); SW(fb3, double);
+    SW(type, int); SW(pid, long); SW(ghost, short);
+#undef SW
+}
+
+static double *pos_of(orc_t *c, int d) { return d == 0 ? c->x : (d == 1 ? c->y : c->z); }
+static double *vel_of(orc_t *c, int d) { return d == 0 ? c->vx : (d == 1 ? c->vy : c->vz); }
+
+/* ------------------------------------------------------------------ */
+/* construction                                                         */
+
+/* LightBC constructor: waves registered per side and E polarisation in input
+ * order (src/grid/lightBC.cpp:22-68). */
+static void setup_pulses(orc_t *c) {
+    const emoo_input_info *in = &c->info;
+    for (int s = 0; s < 6; s++) {
+        int side = (s % 2 == 0) ? -(s / 2 + 1) : (s / 2 + 1);
+        for (int p = 0; p < 3; p++) c->pulse[s][p].nw = 0;
+        for (int w = 0; w < in->nwaves; w++) {
+            if (in->inSide[w] != side) continue;
+            int pid = in->inPolE[w] - 1;
+            if (pid < 0 || pid > 2) continue;
+            pulses_t *P = &c->pulse[s][pid];
+            P->amp[P->nw] = in->peakamps[w];
+            P->omg[P->nw] = in->omegas[w];
+            P->pha[P->nw] = in->phases[w];
+            P->del[P->nw] = in->delays[w];
+            P->iw[P->nw] = in->invWidths[w];
+            P->nw++;
+        }
+    }
+}
+
+void *orc_create(const emoo_input_info *in, double dt, double t0) {
+    orc_t *c = (orc_t *)calloc(1, sizeof(orc_t));
+    if (!c) return NULL;
+    c->info = *in;
+    for (int d = 0; d < 3; d++) {
+        c->n[d] = in->nCell[d];
+        c->tot[d] = in->nCell[d] + 3;
+        c->x0[d] = in->xyz0[d];
+        c->L[d] = in->Lxyz[d];
+        c->d[d] = in->Lxyz[d] / in->nCell[d]; /* src/grid/grid.cpp:37-42 */
+        c->id[d] = 1.0 / c->d[d];
+    }
+    c->npts = (long)c->tot[0] * c->tot[1] * c->tot[2];
+    for (int f = 0; f < EMOO_NFIELDS; f++) {
+        c->slot[f] = (double *)calloc((size_t)c->npts, sizeof(double));
+        if (!c->slot[f]) return NULL;
+    }
+    c->poisson = (in->restart == 0 && strcmp(in->fields_init, "poisson") == 0);
+    for (int s = 0; s < 6; s++) {
+        c->pbc[s] = bc_code(in->parts_bound[s], 0);
+        c->fbc[s] = bc_code(in->fields_bound[s], 1);
+        if (c->pbc[s] < 0 || c->fbc[s] < 0) {
+            fprintf(stderr, "oracle: unknown boundary on side %d\n", s);
+            return NULL;
+        }
+    }
+    setup_pulses(c);
+    /* src/poisson/poisson.cpp:135-154 */
+    double vmax = in->bound_phi[0], vmin = in->bound_phi[0];
+    for (int i = 0; i < 6; i++) {
+        if (in->bound_phi[i] > vmax) vmax = in->bound_phi[i];
+        if (in->bound_phi[i] < vmin) vmin = in->bound_phi[i];
+    }
+    c->conv_phi = vmax - vmin;
+    vmax = vmin = in->bound_Ax[0];
+    for (int i = 0; i < 6; i++) {
+        double a[3] = {in->bound_Ax[i], in->bound_Ay[i], in->bound_Az[i]};
+        for (int q = 0; q < 3; q++) {
+            if (a[q] > vmax) vmax = a[q];
+            if (a[q] < vmin) vmin = a[q];
+        }
+    }
+    c->conv_A = vmax - vmin;
+    c->dt = dt;
+    c->t0 = t0;
+    c->t = 0.0;
+    c->dtp = 0.0;
+    c->next_hist = 0;
+    return c;
+}
+
+void orc_destroy(void *h) {
+    orc_t *c = (orc_t *)h;
+    if (!c) return;
+    for (int f = 0; f < EMOO_NFIELDS; f++) free(c->slot[f]);
+    free(c->x); free(c->y); free(c->z); free(c->vx); free(c->vy); free(c->vz); free(c->g);
+    free(c->fe1); free(c->fe2); free(c->fe3); free(c->fb1); free(c->fb2); free(c->fb3);
+    free(c->type); free(c->pid); free(c->ghost);
+    free(c);
+}
+
+long orc_npoints(void *h) { return ((orc_t *)h)->npts; }
+
+int orc_add_particles(void *h, long n, const double *x, const double *y, const double *z,
+                      const double *vx, const double *vy, const double *vz, const double *gamma,
+                      const int *type, const long *id) {
+    orc_t *c = (orc_t *)h;
+    if (grow(c, c->np + n)) return -2;
+    for (long i = 0; i < n; i++) {
+        long p = c->np + i;
+        c->x[p] = x[i]; c->y[p] = y[i]; c->z[p] = z[i];
+        c->vx[p] = vx[i]; c->vy[p] = vy[i]; c->vz[p] = vz[i];
+        c->g[p] = gamma ? gamma[i] : 0.0;
+        c->fe1[p] = c->fe2[p] = c->fe3[p] = c->fb1[p] = c->fb2[p] = c->fb3[p] = 0.0;
+        c->type[p] = type[i];
+        c->pid[p] = id ? id[i] : p;
+        c->ghost[p] = 0;
+    }
+    c->np += n;
+    return 0;
+}
+
+long orc_num_particles(void *h) { return ((orc_t *)h)->np; }
+
+int orc_get_particles(void *h, double *x, double *y, double *z, double *vx, double *vy, double *vz,
+                      double *gamma, int *type, long *id) {
+    orc_t *c = (orc_t *)h;
+    for (long i = 0; i < c->np; i++) {
+        x[i] = c->x[i]; y[i] = c->y[i]; z[i] = c->z[i];
+        vx[i] = c->vx[i]; vy[i] = c->vy[i]; vz[i] = c->vz[i];
+        gamma[i] = c->g[i]; type[i] = c->type[i]; id[i] = c->pid[i];
+    }
+    return 0;
+}
+
+int orc_get_particle_fields(void *h, double *e1, double *e2, double *e3, double *b1, double *b2, double *b3) {
+    orc_t *c = (orc_t *)h;
+    for (long i = 0; i < c->np; i++) {
+        e1[i] = c->fe1[i]; e2[i] = c->fe2[i]; e3[i] = c->fe3[i];
+        b1[i] = c->fb1[i]; b2[i] = c->fb2[i]; b3[i] = c->fb3[i];
+    }
+    return 0;
+}
+
+/* getFieldPtr()[id] semantics: fixed storage slots (f). */
+int orc_get_field(void *h, int id, double *out) {
+    orc_t *c = (orc_t *)h;
+    if (id < 0 || id >= EMOO_NFIELDS) return -1;
+    memcpy(out, c->slot[id], sizeof(double) * (size_t)c->npts);
+    return 0;
+}
+
+int orc_set_field(void *h, int id, const double *in) {
+    orc_t *c = (orc_t *)h;
+    if (id < 0 || id >= EMOO_NFIELDS) return -1;
+    memcpy(c->slot[id], in, sizeof(double) * (size_t)c->npts);
+    return 0;
+}
+
+/* Grid::getCellID, src/grid/oGrid.cpp:208-227 (C truncation, ghost offset +1,
+ * linear index over the (n+2)^3 cell array). */
+static inline int cell_id(const orc_t *c, double x, double y, double z, int *ix, int *iy, int *iz) {
+    int i = (int)((x - c->x0[0]) * c->id[0]) + 1;
+    int j = (int)((y - c->x0[1]) * c->id[1]) + 1;
+    int k = (int)((z - c->x0[2]) * c->id[2]) + 1;
+    if (ix) { *ix = i; *iy = j; *iz = k; }
+    int ny = c->n[1] + 2, nz = c->n[2] + 2;
+    return (ny * nz) * i + nz * j + k;
+}
+
+int orc_cell_id(void *h, double x, double y, double z) { return cell_id((orc_t *)h, x, y, z, NULL, NULL, NULL); }
+
+/* cellID -> (ix,iy,iz), src/grid/oGrid.cpp:155-157 */
+static inline void cell_split(const orc_t *c, int cid, int *ix, int *iy, int *iz) {
+    int ny = c->n[1] + 2, nz = c->n[2] + 2;
+    int k = cid % nz;
+    int j = ((cid - k) / nz) % ny;
+    int i = (((cid - k) / nz) - j) / ny;
+    *ix = i; *iy = j; *iz = k;
+}
+
+/* ------------------------------------------------------------------ */
+/* field boundaries                                                     */
+
+/* Plane copy / sum over the physical transverse range [1,n]x[1,n]
+ * (sliceMatToVec_ / unsliceMatToVec_, src/grid/spookyGrid.cpp:286-425). */
+static void plane_op(orc_t *c, double *f, int dim, int src, int dst, int sum) {
+    int o1 = (dim == 0) ? 1 : 0; /* outer transverse dim */
+    int o2 = (dim == 2) ? 1 : 2; /* inner transverse dim */
+    for (int p = 1; p <= c->n[o1]; p++) {
+        for (int q = 1; q <= c->n[o2]; q++) {
+            int is[3], id_[3];
+            is[dim] = src; id_[dim] = dst;
+            is[o1] = id_[o1] = p;
+            is[o2] = id_[o2] = q;
+            long s = IDX(c, is[0], is[1], is[2]);
+            long t = IDX(c, id_[0], id_[1], id_[2]);
+            if (sum) f[t] += f[s];
+            else f[t] = f[s];
+        }
+    }
+}
+
+/* setFieldInPlane, src/grid/oGrid.cpp:446-476 (whole plane incl. ghosts). */
+static void plane_set(orc_t *c, double *f, int dim, int idx, double v) {
+    int o1 = (dim == 0) ? 1 : 0;
+    int o2 = (dim == 2) ? 1 : 2;
+    for (int p = 0; p < c->tot[o1]; p++)
+        for (int q = 0; q < c->tot[o2]; q++) {
+            int ii[3];
+            ii[dim] = idx; ii[o1] = p; ii[o2] = q;
+            f[IDX(c, ii[0], ii[1], ii[2])] = v;
+        }
+}
+
+/* GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30 */
+static double gaussian_pulses(double t, double dt, const pulses_t *P) {
+    double val = 0.0;
+    for (int i = 0; i < P->nw; i++) {
+        double tmp = P->amp[i] * cos(P->omg[i] * (t + dt) + P->pha[i] * PI_D / 180.0);
+        val += tmp * exp(-pow((t - P->del[i]) * P->iw[i], 2));
+    }
+    return val;
+}
+
+/* setFieldAlongEdge plane index, src/grid/oGrid.cpp:291-431: left = first
+ * physical (1); right = n for an E component along dim or a B component
+ * across it, n+1 otherwise. */
+static int edge_plane(const orc_t *c, int isB, int comp, int dim, int right) {
+    if (!right) return 1;
+    int along = (comp == dim);
+    if (!isB) return along ? c->n[dim] : c->n[dim] + 1;
+    return along ? c->n[dim] + 1 : c->n[dim];
+}
+
+/* LightBC::applyBCs, src/grid/lightBC.cpp:165-200. Uses the member roles (f). */
+static void light_bc(orc_t *c, int s, double t, double dt) {
+    int dim = s / 2, right = s % 2, sign = right ? 1 : -1;
+    static const int EPOL[3][3] = {{1, 2, 0}, {2, 0, 1}, {0, 1, 2}};
+    static const int BPOL[3][3] = {{2, 1, 0}, {0, 2, 1}, {1, 0, 2}};
+    double E1[3], B1[3];
+    for (int i = 0; i < 3; i++) {
+        E1[i] = c->info.E0[i];
+        B1[i] = c->info.B0[i];
+    }
+    double dx = c->d[dim];
+    double bphase = (dx + sign * dt) / 2;
+    for (int i = 0; i < 3; i++) {
+        int eid = EPOL[dim][i], bid = BPOL[dim][i];
+        if (c->pulse[s][eid].nw > 0 && eid != dim) {
+            double ev = gaussian_pulses(t, 0.0, &c->pulse[s][eid]);
+            E1[eid] += ev;
+            int bsign = sign * (int)pow(-1, i + 1);
+            double bv = bsign * gaussian_pulses(t, bphase, &c->pulse[s][eid]);
+            B1[bid] += bv;
+        }
+        plane_set(c, c->slot[EMOO_EX + eid], dim, edge_plane(c, 0, eid, dim, right), E1[eid]);
+        plane_set(c, role_B(c, bid), dim, edge_plane(c, 1, bid, dim, right), B1[bid]);
+    }
+}
+
+/* PoissonBC::applyBCs, src/poisson/poissonBC.cpp:164-234: Dirichlet value on
+ * the first physical (left) or the ghost (right) plane. */
+static void poisson_bc(orc_t *c, int s, int id) {
+    int dim = s / 2, right = s % 2;
+    int fid;
+    if (id == EMOO_PHI1 || id == EMOO_PHI2) fid = 0;
+    else if (id == EMOO_AX1 || id == EMOO_AX2) fid = 1;
+    else if (id == EMOO_AY1 || id == EMOO_AY2) fid = 2;
+    else if (id == EMOO_AZ1 || id == EMOO_AZ2) fid = 3;
+    else return;
+    double v = fid == 0 ? c->info.bound_phi[s] : fid == 1 ? c->info.bound_Ax[s]
+                        : fid == 2 ? c->info.bound_Ay[s] : c->info.bound_Az[s];
+    int off = right ? 1 + c->n[dim] : 1;
+    plane_set(c, c->slot[id], dim, off, v);
+}
+
+/* Grid::executeBC(sendID), src/grid/grid.cpp:577-585, dispatching to
+ * BC_F_Periodic::completeBC (src/boundaries/b_fields/bc_f_periodic.cpp:34-57)
+ * and BC_F_External::completeBC (src/boundaries/b_fields/bc_f_external.cpp:45-58). */
+int orc_execute_bc(void *h, int send_id) {
+    orc_t *c = (orc_t *)h;
+    for (int dim = 0; dim < 3; dim++) {
+        for (int r = 0; r < 2; r++) {
+            int s = 2 * dim + r;
+            int n = c->n[dim];
+            if (c->fbc[s] == BC_PERIODIC) {
+                if (send_id == EMOO_SEND_JRHO) {
+                    if (r == 0) {
+                        /* far ghost plane n+1 summed into first physical plane 1 */
+                        int f0 = (dim == 0) ? EMOO_JY : EMOO_JX;
+                        int f1 = (dim == 2) ? EMOO_JY : EMOO_JZ;
+                        plane_op(c, c->slot[f0], dim, n + 1, 1, 1);
+                        plane_op(c, c->slot[f1], dim, n + 1, 1, 1);
+                        plane_op(c, c->slot[EMOO_RHO], dim, n + 1, 1, 1);
+                    }
+                } else {
+                    int src = r == 0 ? n : 1, dst = r == 0 ? 0 : n + 1;
+                    if (send_id == EMOO_SEND_EB) {
+                        for (int f = EMOO_EX; f <= EMOO_BZ; f++) plane_op(c, c->slot[f], dim, src, dst, 0);
+                    } else {
+                        plane_op(c, c->slot[send_id], dim, src, dst, 0);
+                    }
+                }
+            } else { /* external */
+                if (send_id == EMOO_SEND_EB) light_bc(c, s, c->t, c->dtp);
+                else if (c->poisson && send_id > 0) poisson_bc(c, s, send_id);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* particles                                                            */
+
+/* Grid::getFieldInterpolatorVec (src/grid/oGrid.cpp:153-197) followed by
+ * Interpolator::interpolate_fields (src/particles/interpolate.cpp:11-47). */
+static void gather(orc_t *c, double px, double py, double pz, double out[6]) {
+    int ix, iy, iz;
+    int cid = cell_id(c, px, py, pz, NULL, NULL, NULL);
+    cell_split(c, cid, &ix, &iy, &iz);
+    double v[21];
+    v[0] = c->x0[0] + c->d[0] * ix;
+    v[1] = c->x0[1] + c->d[1] * iy;
+    v[2] = c->x0[2] + c->d[2] * iz;
+    const double *Ex = c->slot[EMOO_EX], *Ey = c->slot[EMOO_EY], *Ez = c->slot[EMOO_EZ];
+    v[3] = Ex[IDX(c, ix, iy, iz)];
+    v[4] = Ex[IDX(c, ix, iy + 1, iz)];
+    v[5] = Ex[IDX(c, ix, iy + 1, iz + 1)];
+    v[6] = Ex[IDX(c, ix, iy, iz + 1)];
+    v[7] = Ey[IDX(c, ix, iy, iz)];
+    v[8] = Ey[IDX(c, ix, iy, iz + 1)];
+    v[9] = Ey[IDX(c, ix + 1, iy, iz + 1)];
+    v[10] = Ey[IDX(c, ix + 1, iy, iz)];
+    v[11] = Ez[IDX(c, ix, iy, iz)];
+    v[12] = Ez[IDX(c, ix + 1, iy, iz)];
+    v[13] = Ez[IDX(c, ix + 1, iy + 1, iz)];
+    v[14] = Ez[IDX(c, ix, iy + 1, iz)];
+    const double *Bx = role_B(c, 0), *By = role_B(c, 1), *Bz = role_B(c, 2);
+    const double *Tx = role_Btm1(c, 0), *Ty = role_Btm1(c, 1), *Tz = role_Btm1(c, 2);
+    v[15] = (Tx[IDX(c, ix, iy, iz)] + Bx[IDX(c, ix, iy, iz)]) / 2;
+    v[16] = (Tx[IDX(c, ix + 1, iy, iz)] + Bx[IDX(c, ix + 1, iy, iz)]) / 2;
+    v[17] = (Ty[IDX(c, ix, iy, iz)] + By[IDX(c, ix, iy, iz)]) / 2;
+    v[18] = (Ty[IDX(c, ix, iy + 1, iz)] + By[IDX(c, ix, iy + 1, iz)]) / 2;
+    v[19] = (Tz[IDX(c, ix, iy, iz)] + Bz[IDX(c, ix, iy, iz)]) / 2;
+    v[20] = (Tz[IDX(c, ix, iy, iz + 1)] + Bz[IDX(c, ix, iy, iz + 1)]) / 2;
+    double pos[3] = {px, py, pz}, ds[3];
+    const double *l = c->d;
+    for (int i = 0; i < 3; i++) ds[i] = pos[i] - v[i];
+    for (int i = 0; i < 3; i++) {
+        int j = (i + 1) % 3, k = (i + 2) % 3;
+        double e = 0;
+        e += (l[j] - ds[j]) * (l[k] - ds[k]) * v[3 + 4 * i];
+        e += ds[j] * (l[k] - ds[k]) * v[3 + 4 * i + 1];
+        e += ds[j] * ds[k] * v[3 + 4 * i + 2];
+        e += (l[j] - ds[j]) * ds[k] * v[3 + 4 * i + 3];
+        e /= l[j] * l[k];
+        double b = 0;
+        b += (l[i] - ds[i]) * v[3 + 12 + 2 * i];
+        b += ds[i] * v[3 + 12 + 2 * i + 1];
+        b /= l[i];
+        out[i] = e;
+        out[3 + i] = b;
+    }
+}
+
+int orc_interpolate(void *h) {
+    orc_t *c = (orc_t *)h;
+    for (long p = 0; p < c->np; p++) {
+        double f[6];
+        gather(c, c->x[p], c->y[p], c->z[p], f);
+        c->fe1[p] = f[0]; c->fe2[p] = f[1]; c->fe3[p] = f[2];
+        c->fb1[p] = f[3]; c->fb2[p] = f[4]; c->fb3[p] = f[5];
+    }
+    return 0;
+}
+
+/* Boris::Step, src/pusher/boris.cpp:12-111. st = {x,y,z,vx,vy,vz,gamma}. */
+static void boris(double *st, double q, double m, const double *f, double dt) {
+    double x = st[0], y = st[1], z = st[2], vx = st[3], vy = st[4], vz = st[5];
+    double q_p = (0.5 * dt * q) / m;
+    q_p *= UNIT_ACC;
+    double ex = f[0], ey = f[1], ez = f[2], bx = f[3], by = f[4], bz = f[5];
+    double tx = q_p * bx, ty = q_p * by, tz = q_p * bz;
+    double bsqr = bx * bx + by * by + bz * bz;
+    double tsqr = 2.0 / (1.0 + q_p * q_p * bsqr);
+    double sx = tsqr * tx, sy = tsqr * ty, sz = tsqr * tz;
+    double v_mx = vx + q_p * ex, v_my = vy + q_p * ey, v_mz = vz + q_p * ez;
+    double v_ix = v_mx + v_my * tz - v_mz * ty;
+    double v_iy = v_my + v_mz * tx - v_mx * tz;
+    double v_iz = v_mz + v_mx * ty - v_my * tx;
+    double v_px = v_mx + v_iy * sz - v_iz * sy;
+    double v_py = v_my + v_iz * sx - v_ix * sz;
+    double v_pz = v_mz + v_ix * sy - v_iy * sx;
+    double vxn = v_px + q_p * ex, vyn = v_py + q_p * ey, vzn = v_pz + q_p * ez;
+    st[0] = x + dt * vxn;
+    st[1] = y + dt * vyn;
+    st[2] = z + dt * vzn;
+    st[3] = vxn; st[4] = vyn; st[5] = vzn;
+}
+
+/* Relativistic_Boris::Step (Vay 2008), src/pusher/relativisticBoris.cpp:28-143. */
+static void vay(double *st, double q, double m, const double *f, double dt) {
+    double x = st[0], y = st[1], z = st[2], vx = st[3], vy = st[4], vz = st[5], gamma = st[6];
+    double q_p = (0.5 * dt * q) / m;
+    q_p *= UNIT_ACC;
+    double ex = f[0], ey = f[1], ez = f[2], bx = f[3], by = f[4], bz = f[5];
+    double vXbx = vy * bz - vz * by, vXby = vz * bx - vx * bz, vXbz = vx * by - vy * bx;
+    double uhx = gamma * vx + q_p * (ex + vXbx);
+    double uhy = gamma * vy + q_p * (ey + vXby);
+    double uhz = gamma * vz + q_p * (ez + vXbz);
+    double upx = uhx + q_p * ex, upy = uhy + q_p * ey, upz = uhz + q_p * ez;
+    double gammap_sq = 1.0 + upx * upx + upy * upy + upz * upz;
+    double taux = q_p * bx, tauy = q_p * by, tauz = q_p * bz;
+    double tau_sq = taux * taux + tauy * tauy + tauz * tauz;
+    double sigma = gammap_sq - tau_sq;
+    double ustar = upx * taux + upy * tauy + upz * tauz;
+    double gamma_int = sqrt(sigma * sigma + 4 * (tau_sq + ustar * ustar));
+    gamma_int = sqrt(0.5 * (sigma + gamma_int));
+    double tx = taux / gamma_int, ty = tauy / gamma_int, tz = tauz / gamma_int;
+    double s = 1.0 / (1.0 + tx * tx + ty * ty + tz * tz);
+    double udott = ustar / gamma_int;
+    double upXt_x = upy * tz - upz * ty, upXt_y = upz * tx - upx * tz, upXt_z = upx * ty - upy * tx;
+    double uint_x = s * (upx + udott * tx + upXt_x);
+    double uint_y = s * (upy + udott * ty + upXt_y);
+    double uint_z = s * (upz + udott * tz + upXt_z);
+    double vxn = uint_x / gamma_int, vyn = uint_y / gamma_int, vzn = uint_z / gamma_int;
+    st[0] = x + dt * vxn;
+    st[1] = y + dt * vyn;
+    st[2] = z + dt * vzn;
+    st[3] = vxn; st[4] = vyn; st[5] = vzn;
+    st[6] = gamma_int;
+}
+
+int orc_pusher_steps(int relativistic, double *state, const double *field, double dt, long nsteps) {
+    for (long s = 0; s < nsteps; s++) {
+        if (relativistic) vay(state, state[7], state[8], field, dt);
+        else boris(state, state[7], state[8], field, dt);
+    }
+    return 0;
+}
+
+/* Particle_Handler::Push, src/particles/particle_handler.cpp:124-128 */
+static void push_all(orc_t *c, double dt) {
+    for (long p = 0; p < c->np; p++) {
+        int s = c->type[p];
+        double st[7] = {c->x[p], c->y[p], c->z[p], c->vx[p], c->vy[p], c->vz[p], c->g[p]};
+        double f[6] = {c->fe1[p], c->fe2[p], c->fe3[p], c->fb1[p], c->fb2[p], c->fb3[p]};
+        if (c->info.relativity == 0) boris(st, c->info.charge_ratio[s], c->info.mass_ratio[s], f, dt);
+        else vay(st, c->info.charge_ratio[s], c->info.mass_ratio[s], f, dt);
+        c->x[p] = st[0]; c->y[p] = st[1]; c->z[p] = st[2];
+        c->vx[p] = st[3]; c->vy[p] = st[4]; c->vz[p] = st[5]; c->g[p] = st[6];
+    }
+}
+
+int orc_push(void *h) {
+    orc_t *c = (orc_t *)h;
+    push_all(c, c->dt);
+    return 0;
+}
+
+/* executeParticleBoundaryConditions, src/particles/particle_handler.cpp:287-295:
+ * six sides in order; periodic sides append ghost copies that later sides see
+ * (bc_p_periodic.cpp:44-87), reflecting sides fold in place
+ * (bc_p_reflecting.cpp:43-52), absorbing sides (no reference counterpart)
+ * only mark the particle for removal. */
+int orc_particle_bc(void *h, long *counts6) {
+    orc_t *c = (orc_t *)h;
+    for (int s = 0; s < 6; s++) {
+        int d = s / 2, right = s % 2;
+        double xmin = c->x0[d], xmax = xmin + c->L[d];
+        long cnt = 0;
+        if (c->pbc[s] == BC_PERIODIC) {
+            long cur = c->np, nb = 0;
+            for (long p = 0; p < cur; p++) {
+                if (c->ghost[p]) continue;
+                double xp = pos_of(c, d)[p];
+                int hit = (!right && xp < xmin) || (right && xp > xmax);
+                if (!hit) continue;
+                if (grow(c, cur + nb + 1)) return -2;
+                long q = cur + nb;
+                copy_particle(c, q, p);
+                c->ghost[q] = 0;
+                if (!right) pos_of(c, d)[q] += (xmax - xmin);
+                else pos_of(c, d)[q] -= (xmax - xmin);
+                c->ghost[p] = 1;
+                nb++;
+            }
+            c->np = cur + nb;
+            cnt = nb;
+        } else {
+            for (long p = 0; p < c->np; p++) {
+                if (c->ghost[p]) continue;
+                double *xp = &pos_of(c, d)[p];
+                if (right && *xp > xmax) {
+                    cnt++;
+                    if (c->pbc[s] == BC_REFLECTING) {
+                        *xp = 2.0 * xmax - *xp;
+                        vel_of(c, d)[p] = -vel_of(c, d)[p];
+                    } else {
+                        c->ghost[p] = 1;
+                    }
+                } else if (!right && *xp < xmin) {
+                    cnt++;
+                    if (c->pbc[s] == BC_REFLECTING) {
+                        *xp = 2.0 * xmin - *xp;
+                        vel_of(c, d)[p] = -vel_of(c, d)[p];
+                    } else {
+                        c->ghost[p] = 1;
+                    }
+                }
+            }
+        }
+        if (counts6) counts6[s] = cnt;
+    }
+    return 0;
+}
+
+/* clearGhosts, src/particles/particle_handler.cpp:271-284 */
+int orc_clear_ghosts(void *h) {
+    orc_t *c = (orc_t *)h;
+    long i = 0;
+    while (i < c->np) {
+        if (c->ghost[i]) {
+            swap_particle(c, i, c->np - 1);
+            c->np--;
+        } else {
+            i++;
+        }
+    }
+    return 0;
+}
+
+/* Grid::addJ with its Jx index quirk (b), src/grid/oGrid.cpp:91-114 */
+static void add_j(orc_t *c, int cid, const double *J) {
+    int ix, iy, iz;
+    cell_split(c, cid, &ix, &iy, &iz);
+    double *Jx = c->slot[EMOO_JX], *Jy = c->slot[EMOO_JY], *Jz = c->slot[EMOO_JZ];
+    Jx[IDX(c, ix, iy, iz)] += J[0];
+    Jx[IDX(c, ix, iy + 1, iz)] += J[1];
+    Jx[IDX(c, ix, iy + 1, iz + 1)] += J[2];
+    Jx[IDX(c, ix, iy + 1, iz)] += J[3];
+    Jy[IDX(c, ix, iy, iz)] += J[4];
+    Jy[IDX(c, ix, iy, iz + 1)] += J[5];
+    Jy[IDX(c, ix + 1, iy, iz + 1)] += J[6];
+    Jy[IDX(c, ix + 1, iy, iz)] += J[7];
+    Jz[IDX(c, ix, iy, iz)] += J[8];
+    Jz[IDX(c, ix + 1, iy, iz)] += J[9];
+    Jz[IDX(c, ix + 1, iy + 1, iz)] += J[10];
+    Jz[IDX(c, ix, iy + 1, iz)] += J[11];
+}
+
+/* Grid::addRho, src/grid/oGrid.cpp:122-139 */
+static void add_rho(orc_t *c, int cid, const double *R) {
+    int ix, iy, iz;
+    cell_split(c, cid, &ix, &iy, &iz);
+    double *rho = c->slot[EMOO_RHO];
+    rho[IDX(c, ix, iy, iz)] += R[0];
+    rho[IDX(c, ix + 1, iy, iz)] += R[1];
+    rho[IDX(c, ix + 1, iy + 1, iz)] += R[2];
+    rho[IDX(c, ix, iy + 1, iz)] += R[3];
+    rho[IDX(c, ix, iy + 1, iz + 1)] += R[4];
+    rho[IDX(c, ix + 1, iy + 1, iz + 1)] += R[5];
+    rho[IDX(c, ix + 1, iy, iz + 1)] += R[6];
+    rho[IDX(c, ix, iy, iz + 1)] += R[7];
+}
+
+/* Particle_Handler::depositRhoJ (src/particles/particle_handler.cpp:185-239)
+ * with Depositor::deposit_particle_J / _Rho (src/particles/deposit.cpp:12-62):
+ * contributions accumulate per run of equal cell IDs and are flushed on a
+ * cell change. rho_background (build option) is added afterwards. */
+static void deposit(orc_t *c, int with_rho) {
+    long npts = c->npts;
+    memset(c->slot[EMOO_JX], 0, sizeof(double) * (size_t)npts);
+    memset(c->slot[EMOO_JY], 0, sizeof(double) * (size_t)npts);
+    memset(c->slot[EMOO_JZ], 0, sizeof(double) * (size_t)npts);
+    if (with_rho) memset(c->slot[EMOO_RHO], 0, sizeof(double) * (size_t)npts);
+    const double *l = c->d;
+    double vol = l[0] * l[1] * l[2];
+    long cellID = -1;
+    double JObj[12] = {0}, RhoObj[8] = {0}, verts[3] = {0, 0, 0};
+    for (long p = 0; p < c->np; p++) {
+        int s = c->type[p];
+        if (c->ghost[p] || c->info.isTestParticle[s]) continue;
+        int tmp = cell_id(c, c->x[p], c->y[p], c->z[p], NULL, NULL, NULL);
+        if (tmp != cellID) {
+            if (cellID != -1) {
+                add_j(c, (int)cellID, JObj);
+                if (with_rho) add_rho(c, (int)cellID, RhoObj);
+                for (int k = 0; k < 12; k++) JObj[k] = 0;
+                if (with_rho)
+                    for (int k = 0; k < 8; k++) RhoObj[k] = 0;
+            }
+            cellID = tmp;
+            int ix, iy, iz;
+            cell_split(c, tmp, &ix, &iy, &iz);
+            verts[0] = c->x0[0] + c->d[0] * ix;
+            verts[1] = c->x0[1] + c->d[1] * iy;
+            verts[2] = c->x0[2] + c->d[2] * iz;
+        }
+        double q = c->info.charge_ratio[s];
+        double xp[3] = {c->x[p], c->y[p], c->z[p]};
+        double vp[3] = {c->vx[p], c->vy[p], c->vz[p]};
+        double r[3];
+        for (int i = 0; i < 3; i++) r[i] = xp[i] - verts[i];
+        for (int i = 0; i < 3; i++) {
+            int j = (i + 1) % 3, k = (i + 2) % 3;
+            double area = l[j] * l[k];
+            double cur = UNIT_RHOJ * q * vp[i];
+            double ratio = (cur / vol) / area;
+            JObj[4 * i] += ratio * (l[j] - r[j]) * (l[k] - r[k]);
+            JObj[4 * i + 1] += ratio * r[j] * (l[k] - r[k]);
+            JObj[4 * i + 2] += ratio * r[j] * r[k];
+            JObj[4 * i + 3] += ratio * (l[j] - r[j]) * r[k];
+        }
+        if (with_rho) {
+            double cr = UNIT_RHOJ * (q / vol) / vol;
+            RhoObj[0] += cr * (l[0] - r[0]) * (l[1] - r[1]) * (l[2] - r[2]);
+            RhoObj[1] += cr * r[0] * (l[1] - r[1]) * (l[2] - r[2]);
+            RhoObj[2] += cr * r[0] * r[1] * (l[2] - r[2]);
+            RhoObj[3] += cr * (l[0] - r[0]) * r[1] * (l[2] - r[2]);
+            RhoObj[4] += cr * (l[0] - r[0]) * r[1] * r[2];
+            RhoObj[5] += cr * r[0] * r[1] * r[2];
+            RhoObj[6] += cr * r[0] * (l[1] - r[1]) * r[2];
+            RhoObj[7] += cr * (l[0] - r[0]) * (l[1] - r[1]) * r[2];
+        }
+    }
+    if (cellID != -1) {
+        add_j(c, (int)cellID, JObj);
+        if (with_rho) add_rho(c, (int)cellID, RhoObj);
+    }
+}
+
+int orc_deposit(void *h, int with_rho) {
+    deposit((orc_t *)h, with_rho);
+    return 0;
+}
+
+/* Stable counting sort by (species, cellID), ascending: the sort order of the
+ * GPU library (the reference sorts descending with an unstable std::sort,
+ * src/particles/particle_handler.cpp:180-183, particle_utils.hpp:31-51). */
+int orc_sort(void *h) {
+    orc_t *c = (orc_t *)h;
+    long ncell = (long)(c->n[0] + 2) * (c->n[1] + 2) * (c->n[2] + 2);
+    long nkey = ncell * c->info.nspecies;
+    long *cnt = (long *)calloc((size_t)nkey + 1, sizeof(long));
+    long *key = (long *)malloc(sizeof(long) * (size_t)(c->np ? c->np : 1));
+    long *perm = (long *)malloc(sizeof(long) * (size_t)(c->np ? c->np : 1));
+    if (!cnt || !key || !perm) return -2;
+    for (long p = 0; p < c->np; p++) {
+        key[p] = (long)c->type[p] * ncell + cell_id(c, c->x[p], c->y[p], c->z[p], NULL, NULL, NULL);
+        cnt[key[p] + 1]++;
+    }
+    for (long k = 0; k < nkey; k++) cnt[k + 1] += cnt[k];
+    for (long p = 0; p < c->np; p++) perm[cnt[key[p]]++] = p;
+    /* apply the permutation through a scratch copy at the end of the arrays */
+    if (grow(c, 2 * c->np)) return -2;
+    for (long i = 0; i < c->np; i++) copy_particle(c, c->np + i, perm[i]);
+    for (long i = 0; i < c->np; i++) copy_particle(c, i, c->np + i);
+    free(cnt); free(key); free(perm);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* fields                                                               */
+
+/* Grid::evolveFields, src/grid/oGrid.cpp:15-60 (role swap first, (f)). */
+static void evolve(orc_t *c, double dt) {
+    c->bswap ^= 1;
+    double *Ex = c->slot[EMOO_EX], *Ey = c->slot[EMOO_EY], *Ez = c->slot[EMOO_EZ];
+    double *Jx = c->slot[EMOO_JX], *Jy = c->slot[EMOO_JY], *Jz = c->slot[EMOO_JZ];
+    double *Bx = role_B(c, 0), *By = role_B(c, 1), *Bz = role_B(c, 2);
+    double *Tx = role_Btm1(c, 0), *Ty = role_Btm1(c, 1), *Tz = role_Btm1(c, 2);
+    double dx = c->d[0], dy = c->d[1], dz = c->d[2];
+    int nx = c->n[0], ny = c->n[1], nz = c->n[2];
+    for (int i = 1; i <= nx; i++)
+        for (int j = 1; j <= ny; j++)
+            for (int k = 1; k <= nz; k++) {
+                long o = IDX(c, i, j, k);
+                Ex[o] = Ex[o] - dt * ((Ty[o] - Ty[IDX(c, i, j, k - 1)]) / dz - (Tz[o] - Tz[IDX(c, i, j - 1, k)]) / dy +
+                                      4 * PI_D * Jx[o]);
+                Ey[o] = Ey[o] - dt * ((Tz[o] - Tz[IDX(c, i - 1, j, k)]) / dx - (Tx[o] - Tx[IDX(c, i, j, k - 1)]) / dz +
+                                      4 * PI_D * Jy[o]);
+                Ez[o] = Ez[o] - dt * ((Tx[o] - Tx[IDX(c, i, j - 1, k)]) / dy - (Ty[o] - Ty[IDX(c, i - 1, j, k)]) / dx +
+                                      4 * PI_D * Jz[o]);
+            }
+    for (int i = 1; i <= nx; i++)
+        for (int j = 1; j <= ny; j++)
+            for (int k = 1; k <= nz; k++) {
+                long o = IDX(c, i, j, k);
+                Bx[o] = Tx[o] + dt * ((Ey[IDX(c, i, j, k + 1)] - Ey[o]) / dz - (Ez[IDX(c, i, j + 1, k)] - Ez[o]) / dy);
+                By[o] = Ty[o] + dt * ((Ez[IDX(c, i + 1, j, k)] - Ez[o]) / dx - (Ex[IDX(c, i, j, k + 1)] - Ex[o]) / dz);
+                Bz[o] = Tz[o] + dt * ((Ex[IDX(c, i, j + 1, k)] - Ex[o]) / dy - (Ey[IDX(c, i + 1, j, k)] - Ey[o]) / dx);
+            }
+}
+
+/* Grid::evolveFieldsES, src/grid/oGrid.cpp:67-81 */
+static void evolve_es(orc_t *c, double dt) {
+    double *Ex = c->slot[EMOO_EX], *Ey = c->slot[EMOO_EY], *Ez = c->slot[EMOO_EZ];
+    double *Jx = c->slot[EMOO_JX], *Jy = c->slot[EMOO_JY], *Jz = c->slot[EMOO_JZ];
+    for (int i = 1; i <= c->n[0]; i++)
+        for (int j = 1; j <= c->n[1]; j++)
+            for (int k = 1; k <= c->n[2]; k++) {
+                long o = IDX(c, i, j, k);
+                Ex[o] = -dt * (4 * PI_D * Jx[o]);
+                Ey[o] = -dt * (4 * PI_D * Jy[o]);
+                Ez[o] = -dt * (4 * PI_D * Jz[o]);
+            }
+}
+
+int orc_evolve(void *h, int electrostatic) {
+    orc_t *c = (orc_t *)h;
+    if (electrostatic) evolve_es(c, c->dt);
+    else evolve(c, c->dt);
+    return 0;
+}
+
+/* Poisson_Solver::run_poisson_solver_, src/poisson/poisson.cpp:172-287.
+ * Returns the last iteration index; *conv = 1 if it met the tolerance. */
+static int jacobi(orc_t *c, int id1, int id2, const double *R, double tol, double mult, int *conv) {
+    double dx = c->d[0], dy = c->d[1], dz = c->d[2];
+    double celldist2 = pow(dx, 2.0) * pow(dy, 2.0) + pow(dy, 2.0) * pow(dz, 2.0) + pow(dx, 2.0) * pow(dz, 2.0);
+    double ax = pow(dy, 2.0) * pow(dz, 2.0) / (2.0 * celldist2);
+    double ay = pow(dx, 2.0) * pow(dz, 2.0) / (2.0 * celldist2);
+    double az = pow(dx, 2.0) * pow(dy, 2.0) / (2.0 * celldist2);
+    double af = pow(dx, 2.0) * pow(dy, 2.0) * pow(dz, 2.0) / (2.0 * celldist2);
+    double *u1 = c->slot[id1], *u2 = c->slot[id2];
+    orc_execute_bc(c, id1);
+    int iternum = -1, converged = 0;
+    double maxDiff;
+    do {
+        iternum++;
+        maxDiff = 0.0;
+        double *src = (iternum % 2 == 0) ? u1 : u2;
+        double *dst = (iternum % 2 == 0) ? u2 : u1;
+        for (int i = 1; i <= c->n[0]; i++)
+            for (int j = 1; j <= c->n[1]; j++)
+                for (int k = 1; k <= c->n[2]; k++) {
+                    long o = IDX(c, i, j, k);
+                    dst[o] = ax * (src[IDX(c, i - 1, j, k)] + src[IDX(c, i + 1, j, k)]) +
+                             ay * (src[IDX(c, i, j - 1, k)] + src[IDX(c, i, j + 1, k)]) +
+                             az * (src[IDX(c, i, j, k - 1)] + src[IDX(c, i, j, k + 1)]) - af * R[o] * mult;
+                }
+        orc_execute_bc(c, (iternum % 2 == 0) ? id2 : id1);
+        for (int i = 1; i <= c->n[0]; i++)
+            for (int j = 1; j <= c->n[1]; j++)
+                for (int k = 1; k <= c->n[2]; k++) {
+                    long o = IDX(c, i, j, k);
+                    double a = fabs(u2[o] - u1[o]);
+                    if (a > maxDiff) maxDiff = a;
+                }
+        if (maxDiff < tol) converged = 1;
+    } while (!converged && iternum < ITER_MAX);
+    *conv = iternum < ITER_MAX;
+    return iternum;
+}
+
+/* phiToE, src/poisson/convertFields.cpp:10-68 (reads phi1, (g)) */
+static void phi_to_e(orc_t *c) {
+    const double *phi = c->slot[EMOO_PHI1];
+    for (int dir = 0; dir < 3; dir++) {
+        double *E = c->slot[EMOO_EX + dir];
+        double h = c->d[dir];
+        for (int i = 1; i <= c->n[0]; i++)
+            for (int j = 1; j <= c->n[1]; j++)
+                for (int k = 1; k <= c->n[2]; k++) {
+                    long nxt = dir == 0 ? IDX(c, i + 1, j, k) : dir == 1 ? IDX(c, i, j + 1, k) : IDX(c, i, j, k + 1);
+                    long o = IDX(c, i, j, k);
+                    E[o] = -(phi[nxt] - phi[o]) / h;
+                }
+    }
+}
+
+/* AToB, src/poisson/convertFields.cpp:73-154 (quirk (h): both differences
+ * taken of Ak; B written through the fixed slots). */
+static void a_to_b(orc_t *c) {
+    for (int dir = 0; dir < 3; dir++) {
+        double *B = c->slot[EMOO_BX + dir];
+        const double *Ak, *Aj;
+        double hk, hj;
+        if (dir == 0) { Ak = c->slot[EMOO_AZ1]; hk = c->d[2]; Aj = c->slot[EMOO_AY1]; hj = c->d[1]; }
+        else if (dir == 1) { Ak = c->slot[EMOO_AX1]; hk = c->d[0]; Aj = c->slot[EMOO_AZ1]; hj = c->d[2]; }
+        else { Ak = c->slot[EMOO_AY1]; hk = c->d[1]; Aj = c->slot[EMOO_AX1]; hj = c->d[0]; }
+        for (int i = 1; i <= c->n[0]; i++)
+            for (int j = 1; j <= c->n[1]; j++)
+                for (int k = 1; k <= c->n[2]; k++) {
+                    long nk, nj;
+                    if (dir == 0) { nk = IDX(c, i, j + 1, k); nj = IDX(c, i, j, k + 1); }
+                    else if (dir == 1) { nk = IDX(c, i, j, k + 1); nj = IDX(c, i + 1, j, k); }
+                    else { nk = IDX(c, i + 1, j, k); nj = IDX(c, i, j + 1, k); }
+                    long o = IDX(c, i, j, k);
+                    B[o] = (Ak[nk] - Ak[o]) / hj + (Ak[nj] - Aj[o]) / hk;
+                }
+    }
+}
+
+/* Poisson_Solver::InitializeFields, src/poisson/poisson.cpp:143-170.
+ * iters[4] receives the last iteration index of the phi, Ax, Ay, Az solves.
+ * Returns 1 when every solve converged. */
+static int poisson_init(orc_t *c, int *iters) {
+    double mult = -4 * PI_D;
+    double a = c->conv_phi * CONV_RATIO;
+    double tol = a < CONV_CRIT ? CONV_CRIT : a;
+    int ok = 1, cv;
+    int it = jacobi(c, EMOO_PHI1, EMOO_PHI2, c->slot[EMOO_RHO], tol, mult, &cv);
+    ok &= cv;
+    if (iters) iters[0] = it;
+    phi_to_e(c);
+    a = c->conv_A * CONV_RATIO;
+    tol = a < CONV_CRIT ? CONV_CRIT : a;
+    for (int q = 0; q < 3; q++) {
+        it = jacobi(c, EMOO_AX1 + q, EMOO_AX2 + q, c->slot[EMOO_JX + q], tol, mult, &cv);
+        ok &= cv;
+        if (iters) iters[1 + q] = it;
+    }
+    a_to_b(c);
+    orc_execute_bc(c, EMOO_SEND_EB);
+    return ok;
+}
+
+/* Grid::InitializeFields for the non-Poisson path, src/grid/grid.cpp:554-574 */
+static void const_init(orc_t *c) {
+    const emoo_input_info *in = &c->info;
+    long n = c->npts;
+    int cst = (in->restart == 0 && strcmp(in->fields_init, "constant") == 0);
+    if (!cst) {
+        memset(c->slot[EMOO_JX], 0, sizeof(double) * n);
+        memset(c->slot[EMOO_JY], 0, sizeof(double) * n);
+        memset(c->slot[EMOO_JZ], 0, sizeof(double) * n);
+    }
+    for (int q = 0; q < 3; q++) {
+        for (long o = 0; o < n; o++) c->slot[EMOO_EX + q][o] = in->E0[q];
+        for (long o = 0; o < n; o++) c->slot[EMOO_BX + q][o] = in->B0[q];
+        for (long o = 0; o < n; o++) c->slot[EMOO_BX_TM1 + q][o] = in->B0[q];
+    }
+    if (!cst) memset(c->slot[EMOO_RHO], 0, sizeof(double) * n);
+}
+
+int orc_initialize_fields_only(void *h, int *iters) {
+    orc_t *c = (orc_t *)h;
+    c->t = 0.0;
+    c->dtp = 0.0;
+    int ok = 1;
+    if (c->poisson) ok = poisson_init(c, iters);
+    else const_init(c);
+    c->t = c->t0;
+    c->dtp = c->dt;
+    return ok ? 0 : -3;
+}
+
+/* src/main.cpp:159-179 */
+int orc_init_fields(void *h, int *iters) {
+    orc_t *c = (orc_t *)h;
+    c->t = 0.0;
+    c->dtp = 0.0;
+    int ok = 1;
+    if (c->poisson) {
+        deposit(c, 1);
+        orc_execute_bc(c, EMOO_SEND_JRHO);
+        ok = poisson_init(c, iters);
+    } else {
+        const_init(c);
+    }
+    orc_interpolate(c);
+    c->t = c->t0;
+    c->dtp = c->dt;
+    return ok ? 0 : -3;
+}
+
+void orc_set_time(void *h, double t, double dtp) {
+    orc_t *c = (orc_t *)h;
+    c->t = t;
+    c->dtp = dtp;
+}
+
+double orc_time(void *h) { return ((orc_t *)h)->t; }
+
+/* OutputBoxQuantities::output, src/IO/output.cpp:52-123 (fixed slots for B,
+ * (f); SQR(x) expands to x*x without parentheses, hence ((0.5*s)*0.5)*s). */
+int orc_history(void *h, double t, double *out8) {
+    orc_t *c = (orc_t *)h;
+    double pEn = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
+    for (long p = 0; p < c->np; p++) {
+        double m = c->info.mass_ratio[c->type[p]];
+        double vx = c->vx[p], vy = c->vy[p], vz = c->vz[p];
+        pEn += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        mx += m * vx;
+        my += m * vy;
+        mz += m * vz;
+    }
+    double vol = c->d[0] * c->d[1] * c->d[2];
+    double e[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 1; i <= c->n[0]; i++)
+        for (int j = 1; j <= c->n[1]; j++)
+            for (int k = 1; k <= c->n[2]; k++) {
+                long o = IDX(c, i, j, k);
+                long nx_ = IDX(c, i + 1, j, k), ny_ = IDX(c, i, j + 1, k), nz_ = IDX(c, i, j, k + 1);
+                long nb[3] = {nx_, ny_, nz_};
+                for (int q = 0; q < 3; q++) {
+                    double s = c->slot[EMOO_EX + q][o] + c->slot[EMOO_EX + q][nb[q]];
+                    e[q] += 0.5 * vol * (0.5 * s * 0.5 * s);
+                }
+                for (int q = 0; q < 3; q++) {
+                    double s = c->slot[EMOO_BX + q][o] + c->slot[EMOO_BX + q][nb[q]];
+                    e[3 + q] += 0.5 * vol * (0.5 * s * 0.5 * s);
+                }
+            }
+    double B_en = e[3] + e[4] + e[5];
+    double E_en = e[0] + e[1] + e[2];
+    out8[0] = t;
+    out8[1] = mx;
+    out8[2] = my;
+    out8[3] = mz;
+    out8[4] = pEn;
+    out8[5] = B_en;
+    out8[6] = E_en;
+    out8[7] = B_en + E_en + pEn;
+    return 0;
+}
+
+/* Gauss-law residual div E - 4 pi rho over physical vertices (no reference
+ * counterpart): out2 = {max |r|, sqrt(sum r^2)}. */
+int orc_gauss_residual(void *h, double *out2) {
+    orc_t *c = (orc_t *)h;
+    const double *Ex = c->slot[EMOO_EX], *Ey = c->slot[EMOO_EY], *Ez = c->slot[EMOO_EZ], *rho = c->slot[EMOO_RHO];
+    double mx = 0.0, s2 = 0.0;
+    for (int i = 1; i <= c->n[0]; i++)
+        for (int j = 1; j <= c->n[1]; j++)
+            for (int k = 1; k <= c->n[2]; k++) {
+                long o = IDX(c, i, j, k);
+                double dv = (Ex[o] - Ex[IDX(c, i - 1, j, k)]) / c->d[0] + (Ey[o] - Ey[IDX(c, i, j - 1, k)]) / c->d[1] +
+                            (Ez[o] - Ez[IDX(c, i, j, k - 1)]) / c->d[2];
+                double r = dv - 4 * PI_D * rho[o];
+                double a = fabs(r);
+                if (a > mx) mx = a;
+                s2 += r * r;
+            }
+    out2[0] = mx;
+    out2[1] = sqrt(s2);
+    return 0;
+}
+
+/* One pass of the driver loop, src/main.cpp:221-287 (history cadence of
+ * src/IO/output.cpp:46,68-71: every 10 steps from step 0). */
+int orc_step(void *h, int ti, long *counts6, double *hist8, int *hist_written) {
+    orc_t *c = (orc_t *)h;
+    if (c->info.nstep_sort > 0 && ti % c->info.nstep_sort == 0) orc_sort(c);
+    *hist_written = 0;
+    if (ti >= c->next_hist) {
+        orc_history(c, c->t, hist8);
+        c->next_hist += 10;
+        *hist_written = 1;
+    }
+    push_all(c, c->dtp);
+    if (orc_particle_bc(c, counts6)) return -2;
+    orc_clear_ghosts(c);
+    deposit(c, 1);
+    orc_execute_bc(c, EMOO_SEND_JRHO);
+    if (c->info.electrostatic == 1) evolve_es(c, c->dtp);
+    else evolve(c, c->dtp);
+    orc_execute_bc(c, EMOO_SEND_EB);
+    orc_interpolate(c);
+    c->t += c->dtp;
+    return 0;
+}

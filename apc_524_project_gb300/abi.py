@@ -114,6 +114,14 @@ class GenParams(C.Structure):
     ]
 
 
+class Stats(C.Structure):
+    _fields_ = [
+        ("launches", C.c_int64),
+        ("timed_launches", C.c_int64),
+        ("timed_ms", C.c_double),
+    ]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
@@ -149,6 +157,10 @@ PROTOTYPES = {
     "emoo_gauss_residual": (C.c_int, [_P, _D]),
     "emoo_time": (C.c_int, [_P, _D, _D]),
     "emoo_check": (C.c_int, [_P]),
+    "emoo_set_particles": (C.c_int, [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D, _D, _D]),
+    "emoo_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "emoo_set_profiling": (C.c_int, [_P, C.c_int]),
+    "emoo_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
 }
 
 _LIB = None

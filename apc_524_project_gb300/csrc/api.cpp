@@ -55,6 +55,22 @@ void make_geom(const emoo_input_info &in, Geom &g) {
     }
 }
 
+// Queues the (start, stop) event pair of the timed kernel and takes a fresh
+// pair for the next launch; the pairs are read by emoo_stats.
+int prof_accumulate(emoo_handle *h) {
+    h->prof_pending.push_back(h->prof_ev[0]);
+    h->prof_pending.push_back(h->prof_ev[1]);
+    for (int i = 0; i < 2; i++) {
+        if (!h->prof_pool.empty()) {
+            h->prof_ev[i] = h->prof_pool.back();
+            h->prof_pool.pop_back();
+        } else {
+            EMOO_CUDA(cudaEventCreate(&h->prof_ev[i]));
+        }
+    }
+    return EMOO_OK;
+}
+
 int read_err(emoo_handle *h) {
     DevCounters c;
     EMOO_CUDA(cudaMemcpyAsync(&c, h->ctr, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
@@ -111,7 +127,7 @@ int edge_plane(const Geom &g, bool isB, int comp, int dim, bool right) {
 
 // LightBC::applyBCs, src/grid/lightBC.cpp:165-200: six whole-plane writes per
 // external side, E through the E storage, B through the current B role.
-int light_planes(emoo_handle *h, int s, PlaneSet *ps) {
+int light_planes(emoo_handle *h, int s, PlaneSet *ps, bool slots) {
     LightState *L = light_of(h);
     static const int EPOL[3][3] = {{1, 2, 0}, {2, 0, 1}, {0, 1, 2}};
     static const int BPOL[3][3] = {{2, 1, 0}, {0, 2, 1}, {1, 0, 2}};
@@ -135,7 +151,7 @@ int light_planes(emoo_handle *h, int s, PlaneSet *ps) {
             double bv = bsign * gaussian_pulses(h->t, bphase, L->p[s][eid]);
             B1[bid] += bv;
         }
-        if (h->precision == EMOO_FP64) {
+        if (slots) {
             ps[n++] = PlaneSet{h->slot[EMOO_EX + eid], dim, edge_plane(h->g, false, eid, dim, right), E1[eid]};
             double *bp = h->bswap ? h->slot[EMOO_BX_TM1 + bid] : h->slot[EMOO_BX + bid];
             ps[n++] = PlaneSet{bp, dim, edge_plane(h->g, true, bid, dim, right), B1[bid]};
@@ -147,6 +163,12 @@ int light_planes(emoo_handle *h, int s, PlaneSet *ps) {
     }
     return n;
 }
+
+}  // namespace
+
+int emoo::light_planes_public(emoo_handle *h, int s, PlaneSet *ps) { return light_planes(h, s, ps, false); }
+
+namespace {
 
 int bc_kind_particle(const char *s) {
     if (strcmp(s, "periodic") == 0) return PBC_PERIODIC;
@@ -211,6 +233,7 @@ int reserve(emoo_handle *h, int64_t cap) {
     EMOO_TRY(grow(h->cell, !f64)); EMOO_TRY(grow(h->ox, !f64)); EMOO_TRY(grow(h->oy, !f64)); EMOO_TRY(grow(h->oz, !f64));
     EMOO_TRY(grow(h->ux, !f64)); EMOO_TRY(grow(h->uy, !f64)); EMOO_TRY(grow(h->uz, !f64));
     EMOO_TRY(grow(h->ids, h->opts.track_ids != 0));
+    EMOO_TRY(grow(h->g0, h->g0 != nullptr));
     dfree(h->fcache);
     dfree(h->key[0]); dfree(h->key[1]); dfree(h->perm[0]); dfree(h->perm[1]);
     EMOO_TRY(dalloc(h->key[0], (size_t)cap)); EMOO_TRY(dalloc(h->key[1], (size_t)cap));
@@ -244,6 +267,7 @@ int make_room(emoo_handle *h, int s, int64_t n, int64_t *at) {
         EMOO_TRY(shift(h->vx)); EMOO_TRY(shift(h->vy)); EMOO_TRY(shift(h->vz)); EMOO_TRY(shift(h->gam));
         EMOO_TRY(shift(h->cell)); EMOO_TRY(shift(h->ox)); EMOO_TRY(shift(h->oy)); EMOO_TRY(shift(h->oz));
         EMOO_TRY(shift(h->ux)); EMOO_TRY(shift(h->uy)); EMOO_TRY(shift(h->uz)); EMOO_TRY(shift(h->ids));
+        EMOO_TRY(shift(h->g0));
     }
     for (int q = s + 1; q <= h->nspec; q++) h->off[q] += n;
     h->count[s] += n;
@@ -268,10 +292,11 @@ int do_sort(emoo_handle *h) {
     if (h->np == 0) return EMOO_OK;
     if (h->precision == EMOO_FP64) EMOO_TRY(sort_keys_f64(h));
     else EMOO_TRY(mixed_sort_keys(h));
-    EMOO_TRY(radix_sort_perm(h, h->np, key_bits(h)));
+    bool f64 = h->precision == EMOO_FP64;
+    EMOO_TRY(radix_sort_perm(h, h->np, f64 ? key_bits(h) : mixed_key_bits(h)));
     EMOO_TRY(gather_payload(h, h->np));
     int64_t cnt[EMOO_NSPEC];
-    EMOO_TRY(count_species(h, h->np, cnt));
+    EMOO_TRY(count_species(h, h->np, f64 ? h->g.ncell : h->g.npts, cnt));
     int64_t off = 0;
     for (int s = 0; s < h->nspec; s++) {
         h->off[s] = off;
@@ -287,14 +312,15 @@ int do_sort(emoo_handle *h) {
 int execute_bc(emoo_handle *h, int send_id);
 
 int deposit_all(emoo_handle *h, int with_rho) {
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (h->precision != EMOO_FP64) return mixed_deposit(h, with_rho);
     EMOO_TRY(deposit_f64(h, with_rho));
     return EMOO_OK;
 }
 
+int execute_bc_slots(emoo_handle *h, int send_id);
+
 int poisson_init(emoo_handle *h, int iters[4]) {
     if (!h->poisson) return EMOO_ERR_STATE;
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     // src/poisson/poisson.cpp:98-156: tolerances from the Dirichlet values
     const emoo_input_info &in = h->info;
     double vmax = in.bound_phi[0], vmin = in.bound_phi[0];
@@ -324,7 +350,8 @@ int poisson_init(emoo_handle *h, int iters[4]) {
         ok &= it[1 + q] < ITER_MAX;
     }
     EMOO_TRY(a_to_b_f64(h));
-    EMOO_TRY(execute_bc(h, EMOO_SEND_EB));
+    EMOO_TRY(execute_bc_slots(h, EMOO_SEND_EB));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_fields_from_slots(h));
     if (iters)
         for (int q = 0; q < 4; q++) iters[q] = it[q];
     return ok ? EMOO_OK : EMOO_ERR_NOT_CONVERGED;
@@ -335,7 +362,15 @@ int const_init(emoo_handle *h) {
     const emoo_input_info &in = h->info;
     bool cst = in.restart == 0 && strcmp(in.fields_init, "constant") == 0;
     int64_t n = h->g.npts;
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (h->precision != EMOO_FP64) {
+        if (!cst) {  // constJ(0,0,0), constRho(0)
+            for (int c = 0; c < 4; c++) {
+                EMOO_TRY(fill_f64(h, h->slot[EMOO_JX + c], n, 0.0, h->stream));
+                EMOO_TRY(mixed_set_field(h, EMOO_JX + c, h->slot[EMOO_JX + c]));
+            }
+        }
+        return mixed_const_fields(h);
+    }
     if (!cst) {
         for (int q = 0; q < 3; q++) EMOO_TRY(fill_f64(h, h->slot[EMOO_JX + q], n, 0.0, h->stream));
         EMOO_TRY(fill_f64(h, h->slot[EMOO_RHO], n, 0.0, h->stream));
@@ -354,12 +389,15 @@ int const_init(emoo_handle *h) {
 // are independent and issued as one launch.
 int execute_bc(emoo_handle *h, int send_id) {
     if (h->precision != EMOO_FP64) {
-        if (send_id == EMOO_SEND_EB) {
-            EMOO_TRY(mixed_ghost_fill(h));
-            return EMOO_OK;
-        }
-        return EMOO_ERR_UNSUPPORTED;
+        if (send_id == EMOO_SEND_EB) return mixed_ghost_fill(h);
+        if (send_id == EMOO_SEND_JRHO) return mixed_fold_public(h);
+        // single fields (Poisson potentials) live on the FP64 slots
     }
+    return execute_bc_slots(h, send_id);
+}
+
+// executeBC on the FP64 grid slots.
+int execute_bc_slots(emoo_handle *h, int send_id) {
     if (send_id == EMOO_SEND_JRHO) {
         for (int d = 0; d < 3; d++)
             if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d));
@@ -385,7 +423,7 @@ int execute_bc(emoo_handle *h, int send_id) {
             if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
             if (send_id == EMOO_SEND_EB) {
                 PlaneSet ps[6];
-                int n = light_planes(h, s, ps);
+                int n = light_planes(h, s, ps, true);
                 EMOO_TRY(plane_set_f64(h, ps, n));
             } else if (h->poisson && send_id > 0) {
                 int id = send_id;
@@ -594,6 +632,10 @@ int emoo_destroy(emoo_handle *h) {
     dfree(h->ctr);
     dfree(h->red);
     if (h->jacobi_state) cudaFree(h->jacobi_state);
+    for (int i = 0; i < 2; i++)
+        if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
+    for (cudaEvent_t e : h->prof_pending) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->prof_pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     auto &r = light_registry();
     for (size_t i = 0; i < r.size(); i++)
@@ -770,13 +812,13 @@ int emoo_init_fields(emoo_handle *h, int iters[4]) {
     h->dtp = 0.0;
     int rc = EMOO_OK;
     if (h->poisson) {
-        if (h->precision != EMOO_FP64) rc = EMOO_ERR_UNSUPPORTED;
-        if (rc == EMOO_OK) rc = deposit_all(h, 1);
+        rc = deposit_all(h, 1);
         if (rc == EMOO_OK) rc = execute_bc(h, EMOO_SEND_JRHO);
+        // the mixed form solves in FP64 on the grid slots
+        if (rc == EMOO_OK && h->precision != EMOO_FP64) rc = mixed_deposit_to_f64(h);
         if (rc == EMOO_OK) rc = poisson_init(h, iters);
     } else {
-        if (h->precision == EMOO_FP64) rc = const_init(h);
-        else rc = EMOO_ERR_UNSUPPORTED;
+        rc = const_init(h);
     }
     h->t = h->info.t0;
     h->dtp = h->dt;
@@ -791,7 +833,9 @@ int emoo_poisson_init(emoo_handle *h, int iters[4]) {
     double t = h->t, dtp = h->dtp;
     h->t = 0.0;
     h->dtp = 0.0;
-    int rc = poisson_init(h, iters);
+    int rc = EMOO_OK;
+    if (h->precision != EMOO_FP64) rc = mixed_deposit_to_f64(h);
+    if (rc == EMOO_OK) rc = poisson_init(h, iters);
     h->t = t;
     h->dtp = dtp;
     cudaStreamSynchronize(h->stream);
@@ -850,8 +894,8 @@ int emoo_execute_bc(emoo_handle *h, int send_id) {
 
 int emoo_evolve_fields(emoo_handle *h, int electrostatic) {
     HANDLE_CHECK(h);
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
-    if (electrostatic) EMOO_TRY(yee_es_f64(h, h->dtp));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_yee_public(h, h->dtp, electrostatic));
+    else if (electrostatic) EMOO_TRY(yee_es_f64(h, h->dtp));
     else EMOO_TRY(yee_f64(h, h->dtp));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return EMOO_OK;
@@ -906,7 +950,7 @@ int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n) {
 int emoo_gauss_residual(emoo_handle *h, double out2[2]) {
     HANDLE_CHECK(h);
     if (!out2) return EMOO_ERR_ARG;
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_fields_to_slots(h));
     return gauss_residual_f64(h, out2);
 }
 
@@ -920,6 +964,70 @@ int emoo_time(emoo_handle *h, double *t, double *dt) {
 int emoo_check(emoo_handle *h) {
     HANDLE_CHECK(h);
     return read_err(h);
+}
+
+int emoo_set_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
+                       const double *vx, const double *vy, const double *vz, const double *gamma) {
+    HANDLE_CHECK(h);
+    if (species < 0 || species >= h->nspec || n != h->count[species]) return EMOO_ERR_ARG;
+    if (n == 0) return EMOO_OK;
+    if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
+    int64_t at = h->off[species];
+    if (h->precision == EMOO_FP64) {
+        size_t b = sizeof(double) * (size_t)n;
+        EMOO_CUDA(cudaMemcpyAsync(h->x + at, x, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->y + at, y, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->z + at, z, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vx + at, vx, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vy + at, vy, b, cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->vz + at, vz, b, cudaMemcpyHostToDevice, h->stream));
+        if (gamma) EMOO_CUDA(cudaMemcpyAsync(h->gam + at, gamma, b, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        EMOO_TRY(mixed_from_f64(h, at, n, x, y, z, vx, vy, vz, gamma));
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    dfree(h->fcache);
+    return read_err(h);
+}
+
+int emoo_get_stream(emoo_handle *h, void **stream) {
+    if (!h || !stream) return EMOO_ERR_ARG;
+    *stream = (void *)h->stream;
+    return EMOO_OK;
+}
+
+int emoo_set_profiling(emoo_handle *h, int on) {
+    HANDLE_CHECK(h);
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    for (cudaEvent_t e : h->prof_pending) h->prof_pool.push_back(e);
+    h->prof_pending.clear();
+    h->prof_ms = 0.0;
+    h->prof_count = 0;
+    if (on) {
+        for (int i = 0; i < 2; i++)
+            if (!h->prof_ev[i]) EMOO_CUDA(cudaEventCreate(&h->prof_ev[i]));
+    }
+    h->prof_on = on ? 1 : 0;
+    return EMOO_OK;
+}
+
+int emoo_get_stats(emoo_handle *h, emoo_stats *s) {
+    HANDLE_CHECK(h);
+    if (!s) return EMOO_ERR_ARG;
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i + 1 < h->prof_pending.size(); i += 2) {
+        float ms = 0.0f;
+        EMOO_CUDA(cudaEventElapsedTime(&ms, h->prof_pending[i], h->prof_pending[i + 1]));
+        h->prof_ms += ms;
+        h->prof_count++;
+        h->prof_pool.push_back(h->prof_pending[i]);
+        h->prof_pool.push_back(h->prof_pending[i + 1]);
+    }
+    h->prof_pending.clear();
+    s->launches = h->launches;
+    s->timed_launches = h->prof_count;
+    s->timed_ms = h->prof_ms;
+    return EMOO_OK;
 }
 
 }  // extern "C"

@@ -106,6 +106,10 @@ struct emoo_handle {
     // mixed SoA
     int32_t *cell = nullptr;
     float *ox = nullptr, *oy = nullptr, *oz = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr;
+    // relativistic mixed form until the first push: the loaded gamma (the
+    // momentum slots hold the loaded velocity); freed by the first push
+    float *g0 = nullptr;
+    int first_push = 0;
     emoo::FieldsF32 *mf = nullptr;
 
     // sort scratch
@@ -131,6 +135,16 @@ struct emoo_handle {
     int64_t next_hist = 0;
     std::vector<double> hist_rows;
     int fields_initialised = 0;
+
+    // instrumentation: kernel launches issued, and CUDA-event timing of the
+    // fused particle kernel (the dominant kernel of the step) when enabled
+    int64_t launches = 0;
+    int prof_on = 0;
+    cudaEvent_t prof_ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> prof_pending;  // (start, stop) pairs not yet read
+    std::vector<cudaEvent_t> prof_pool;
+    double prof_ms = 0.0;
+    int64_t prof_count = 0;
 };
 
 namespace emoo {
@@ -164,7 +178,7 @@ int sort_keys_f64(emoo_handle *h);
 // ---- sort (sort.cu) ----
 int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits);
 int gather_payload(emoo_handle *h, int64_t n);
-int count_species(emoo_handle *h, int64_t n, int64_t *counts_host);
+int count_species(emoo_handle *h, int64_t n, int64_t stride, int64_t *counts_host);
 
 // ---- loader (loader.cu) ----
 int generate_device(emoo_handle *h, const emoo_gen_params *gp, int64_t first, int64_t n, int64_t dst);
@@ -184,10 +198,20 @@ int mixed_moments(emoo_handle *h, double out4[4]);
 int mixed_field_energy(emoo_handle *h, double out6[6]);
 int mixed_ghost_fill(emoo_handle *h);
 int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n);
+int mixed_deposit(emoo_handle *h, int with_rho);
+int mixed_fold_public(emoo_handle *h);
+int mixed_yee_public(emoo_handle *h, double dtp, int es);
+int mixed_deposit_to_f64(emoo_handle *h);
+int mixed_fields_from_slots(emoo_handle *h);
+int mixed_fields_to_slots(emoo_handle *h);
+int mixed_const_fields(emoo_handle *h);
+int mixed_key_bits(emoo_handle *h);
 
 // ---- helpers ----
 int cuda_status(cudaError_t e);
 int read_err(emoo_handle *h);
+int prof_accumulate(emoo_handle *h);
+int light_planes_public(emoo_handle *h, int s, PlaneSet *ps);
 
 }  // namespace emoo
 

@@ -376,9 +376,11 @@ int yee_f64(emoo_handle *h, double dt) {
     F3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
     CF3 T = {{role_t(h, 0), role_t(h, 1), role_t(h, 2)}};
     CF3 J = {{h->slot[EMOO_JX], h->slot[EMOO_JY], h->slot[EMOO_JZ]}};
+    h->launches++;
     k_yee_e<<<grd, blk, 0, h->stream>>>(g, dt, E, T, J);
     F3 B = {{role_b(h, 0), role_b(h, 1), role_b(h, 2)}};
     CF3 Ec = {{E.p[0], E.p[1], E.p[2]}};
+    h->launches++;
     k_yee_b<<<grd, blk, 0, h->stream>>>(g, dt, B, T, Ec);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -389,6 +391,7 @@ int yee_es_f64(emoo_handle *h, double dt) {
     dim3 blk(32, 8);
     F3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
     CF3 J = {{h->slot[EMOO_JX], h->slot[EMOO_JY], h->slot[EMOO_JZ]}};
+    h->launches++;
     k_yee_es<<<phys_grid(g, blk), blk, 0, h->stream>>>(g, dt, E, J);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -403,6 +406,7 @@ static int ghost_launch(emoo_handle *h, const int *ids, int nids, int dims_mask,
     int tb = std::max(g.n[2], g.n[1]);
     dim3 blk(32, 8);
     dim3 grd((tb + 31) / 32, (ta + 7) / 8, nids * 6);
+    h->launches++;
     k_ghost<<<grd, blk, 0, h->stream>>>(g, fl, dims_mask, skip);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -419,6 +423,7 @@ int fold_f64(emoo_handle *h, int d) {
     int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
     dim3 blk(32, 8);
     dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 3);
+    h->launches++;
     k_fold<<<grd, blk, 0, h->stream>>>(g, d, h->slot[f0], h->slot[f1], h->slot[EMOO_RHO]);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -433,6 +438,7 @@ static int plane_launch(emoo_handle *h, const PlaneSet *ps, int n, const int *sk
         int m = std::max(std::max(g.tot[0], g.tot[1]), g.tot[2]);
         dim3 blk(32, 8);
         dim3 grd((m + 31) / 32, (m + 7) / 8, pl.n);
+        h->launches++;
         k_plane_set<<<grd, blk, 0, h->stream>>>(g, pl, skip);
     }
     EMOO_CUDA(cudaGetLastError());
@@ -445,6 +451,7 @@ int fill_f64(emoo_handle *h, double *p, int64_t n, double v, cudaStream_t s) {
     (void)h;
     int64_t b = std::min<int64_t>((n + 255) / 256, 152 * 16);
     if (b < 1) b = 1;
+    h->launches++;
     k_fill<<<(int)b, 256, 0, s>>>(p, n, v);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -515,8 +522,10 @@ int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mul
     for (;;) {
         for (int b = 0; b < batch && launched <= ITER_MAX; b++, launched++) {
             bool even = (launched % 2) == 0;
+            h->launches++;
             k_jacobi<<<grd, blk, 0, h->stream>>>(g, even ? u1 : u2, even ? u2 : u1, R, ax, ay, az, af, mult, st);
             EMOO_TRY(single_field_bc(h, even ? id2 : id1, &st->done));
+            h->launches++;
             k_jacobi_check<<<rb, 256, 0, h->stream>>>(g, u1, u2, tol, st);
         }
         EMOO_CUDA(cudaGetLastError());
@@ -533,6 +542,7 @@ int phi_to_e_f64(emoo_handle *h) {
     const Geom &g = h->g;
     dim3 blk(32, 8);
     F3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
+    h->launches++;
     k_phi_to_e<<<phys_grid(g, blk), blk, 0, h->stream>>>(g, h->slot[EMOO_PHI1], E);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -543,6 +553,7 @@ int a_to_b_f64(emoo_handle *h) {
     dim3 blk(32, 8);
     // AToB writes through the field pointer table: the fixed B slots.
     F3 B = {{h->slot[EMOO_BX], h->slot[EMOO_BY], h->slot[EMOO_BZ]}};
+    h->launches++;
     k_a_to_b<<<phys_grid(g, blk), blk, 0, h->stream>>>(g, h->slot[EMOO_AX1], h->slot[EMOO_AY1], h->slot[EMOO_AZ1], B);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -555,6 +566,7 @@ int field_energy_f64(emoo_handle *h, double out6[6]) {
     CF3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
     // the history reads the field pointer table: fixed B slots
     CF3 B = {{h->slot[EMOO_BX], h->slot[EMOO_BY], h->slot[EMOO_BZ]}};
+    h->launches++;
     k_field_energy<<<rb, 256, 0, h->stream>>>(g, E, B, h->red);
     EMOO_CUDA(cudaGetLastError());
     std::vector<double> part((size_t)rb * 6);
@@ -571,6 +583,7 @@ int gauss_residual_f64(emoo_handle *h, double out2[2]) {
     int rb = reduce_blocks(g);
     EMOO_TRY(ensure_red(h, (size_t)rb * 2));
     CF3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
+    h->launches++;
     k_gauss<<<rb, 256, 0, h->stream>>>(g, E, h->slot[EMOO_RHO], h->red);
     EMOO_CUDA(cudaGetLastError());
     std::vector<double> part((size_t)rb * 2);

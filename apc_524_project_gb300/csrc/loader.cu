@@ -37,10 +37,12 @@ int generate_device(emoo_handle *h, const emoo_gen_params *gp, int64_t first, in
     if (n <= 0) return EMOO_OK;
     int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
     if (h->precision == EMOO_FP64) {
+        h->launches++;
         k_generate<<<nb, 256, 0, h->stream>>>(*gp, first, n, h->x + dst, h->y + dst, h->z + dst, h->vx + dst,
                                               h->vy + dst, h->vz + dst, h->gam + dst);
     } else {
         double *b = (double *)h->pay;
+        h->launches++;
         k_generate<<<nb, 256, 0, h->stream>>>(*gp, first, n, b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n,
                                               b + 6 * n);
     }

@@ -504,6 +504,7 @@ void species_tab(emoo_handle *h, double dtp, SpeciesTab &st) {
 int interpolate_f64(emoo_handle *h) {
     if (h->np == 0) return EMOO_OK;
     if (!h->fcache) EMOO_CUDA(cudaMalloc(&h->fcache, sizeof(double) * 6 * (size_t)h->cap));
+    h->launches++;
     k_interpolate<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, gather_ptrs(h), pstate(h), h->np, h->cap, h->fcache,
                                                             h->ctr);
     EMOO_CUDA(cudaGetLastError());
@@ -515,6 +516,7 @@ int push_cached_f64(emoo_handle *h, double dtp) {
     if (!h->fcache) return EMOO_ERR_STATE;
     SpeciesTab st;
     species_tab(h, dtp, st);
+    h->launches++;
     k_push_cached<<<blocks_for(h->np), 256, 0, h->stream>>>(st, pstate(h), h->np, h->cap, h->fcache, dtp,
                                                             h->info.relativity != 0);
     EMOO_CUDA(cudaGetLastError());
@@ -523,6 +525,7 @@ int push_cached_f64(emoo_handle *h, double dtp) {
 
 int particle_bc_f64(emoo_handle *h) {
     if (h->np == 0) return EMOO_OK;
+    h->launches++;
     k_particle_bc<<<blocks_for(h->np), 256, 0, h->stream>>>(h->bc, pstate(h), h->np, h->ctr);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -535,6 +538,7 @@ int deposit_f64(emoo_handle *h, int with_rho) {
     if (h->np == 0) return EMOO_OK;
     SpeciesTab st;
     species_tab(h, h->dtp, st);
+    h->launches++;
     k_deposit<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, pstate(h), h->np, deposit_ptrs(h), with_rho, h->ctr);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -547,6 +551,8 @@ int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {
     if (h->np == 0) return EMOO_OK;
     SpeciesTab st;
     species_tab(h, dtp, st);
+    h->launches++;
+    if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
     if (h->info.relativity)
         k_fused<true><<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, h->bc, gather_ptrs(h), pstate(h), h->np,
                                                                 deposit_ptrs(h), dtp, with_rho, h->ctr);
@@ -554,6 +560,10 @@ int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {
         k_fused<false><<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, h->bc, gather_ptrs(h), pstate(h), h->np,
                                                                  deposit_ptrs(h), dtp, with_rho, h->ctr);
     EMOO_CUDA(cudaGetLastError());
+    if (h->prof_on) {
+        EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
+        EMOO_TRY(prof_accumulate(h));
+    }
     return EMOO_OK;
 }
 
@@ -568,6 +578,7 @@ int particle_moments_f64(emoo_handle *h, double out4[4]) {
     }
     SpeciesTab st;
     species_tab(h, h->dtp, st);
+    h->launches++;
     k_moments<<<nb, 256, 0, h->stream>>>(st, pstate(h), h->np, h->red);
     EMOO_CUDA(cudaGetLastError());
     std::vector<double> part((size_t)nb * 4);
@@ -582,6 +593,7 @@ int sort_keys_f64(emoo_handle *h) {
     SpeciesTab st;
     species_tab(h, h->dtp, st);
     uint32_t dead = (uint32_t)((int64_t)h->nspec * h->g.ncell + 1);
+    h->launches++;
     k_keys<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, pstate(h), h->np, h->key[0], dead, h->ctr);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;

@@ -1,20 +1,1152 @@
-// particles_mixed.cu - mixed-precision form (placeholder until implemented).
+// particles_mixed.cu - the mixed-precision form of the time loop.
+//
+// Particle state, 28 bytes per particle (structure of arrays):
+//   cell    int32  linear index of the particle's cell in the (n+3)^3 field
+//                  layout, cell = ix*sx + iy*sy + iz with ix in [1, n] (the
+//                  reference's ghost-offset cell numbering)
+//   ox..oz  float  in-cell offset in [0, 1) cell widths (split precision:
+//                  position = x0 + d * (ix - 1 + o), exact to 2^-24 cells
+//                  anywhere in the box)
+//   ux..uz  float  momentum per unit mass, u = gamma v (v for the
+//                  non-relativistic pusher)
+// Fields E, B and B_tm1 are FP32 in the reference layout; J and rho are int64
+// fixed-point accumulators (quantum q0 = max_s |UNIT_RHOJ q_s / V| * 2^-32).
+// Each warp sums the contributions of consecutive particles that share a cell
+// in FP32 in a fixed shuffle order, rounds the run total to the fixed-point
+// quantum and commits it with an integer atomic: integer addition is
+// associative, so J and rho - and every run - are bit-reproducible.
+//
+// The arithmetic is the reference's algorithm (including its in-cell offset
+// convention, Jx index, ghost and B-role behaviour, see the FP64 kernels) in
+// FP32 with fused multiply-adds allowed. FP64 is kept for the Jacobi Poisson
+// start (done on the FP64 grid slots, then converted), the Gauss-law check and
+// the energy / momentum reductions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "dev_common.cuh"
 #include "emoo_internal.h"
 
 namespace emoo {
-struct FieldsF32 {};
-int mixed_alloc(emoo_handle *) { return EMOO_ERR_UNSUPPORTED; }
-void mixed_free(emoo_handle *) {}
-int mixed_from_f64(emoo_handle *, int64_t, int64_t, const double *, const double *, const double *, const double *,
-                   const double *, const double *, const double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_to_f64(emoo_handle *, int64_t, int64_t, double *, double *, double *, double *, double *, double *,
-                 double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_step(emoo_handle *, double, int) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_sort_keys(emoo_handle *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_get_field(emoo_handle *, int, double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_set_field(emoo_handle *, int, const double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_moments(emoo_handle *, double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_field_energy(emoo_handle *, double *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_ghost_fill(emoo_handle *) { return EMOO_ERR_UNSUPPORTED; }
-int mixed_plane_sets(emoo_handle *, const PlaneSet *, int) { return EMOO_ERR_UNSUPPORTED; }
+
+struct FieldsF32 {
+    float *E[3] = {nullptr, nullptr, nullptr};
+    float *Bslot[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // BX..BZ, BX_TM1..BZ_TM1 storage
+    long long *J[4] = {nullptr, nullptr, nullptr, nullptr};                    // Jx, Jy, Jz, rho
+    double q0 = 1.0;  // fixed-point quantum
+};
+
+namespace {
+
+constexpr float FOURPI_F = (float)(4.0 * PI_D);
+
+struct MState {
+    int32_t *cell;
+    float *ox, *oy, *oz, *ux, *uy, *uz;
+};
+
+struct MSpecies {
+    int nspec;
+    int64_t off[EMOO_NSPEC + 1];
+    float qp[EMOO_NSPEC];    // ((0.5 dt q)/m) UNIT_ACC
+    float qdep[EMOO_NSPEC];  // (UNIT_RHOJ q / V) / q0: fixed-point units per unit weight and speed
+    float m[EMOO_NSPEC];
+    int deposit[EMOO_NSPEC];
+};
+
+__device__ __forceinline__ int species_of_m(const MSpecies &st, int64_t p) {
+    int s = 0;
+    while (s + 1 < st.nspec && p >= st.off[s + 1]) s++;
+    return s;
+}
+
+struct MGeom {
+    int n[3];
+    int64_t sx, sy;
+    int64_t npts;
+    float dtid[3];  // dt / d
+    float idf[3];   // 1 / d
+    float fourpi_dt;
+};
+
+struct FastDiv {  // floor(a / d) for 0 <= a < 2^31 via multiply-high
+    uint32_t d, m;
+    int s;
+};
+
+FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    f.s = l;
+    f.m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t a, const FastDiv &f) {
+    uint32_t t = __umulhi(a, f.m);
+    return (t + ((a - t) >> 1)) >> (f.s - 1 < 0 ? 0 : f.s - 1);
+}
+
+struct Div3 {
+    FastDiv sx, sy;
+};
+
+__device__ __forceinline__ void split_cell(const MGeom &g, const Div3 &dv, int32_t c, int &ix, int &iy, int &iz) {
+    uint32_t uc = (uint32_t)c;
+    uint32_t i = (dv.sx.d == 1) ? uc : fdiv(uc, dv.sx);
+    uint32_t r = uc - i * (uint32_t)g.sx;
+    uint32_t j = (dv.sy.d == 1) ? r : fdiv(r, dv.sy);
+    ix = (int)i;
+    iy = (int)j;
+    iz = (int)(r - j * (uint32_t)g.sy);
+}
+
+struct MGather {
+    const float *E[3];
+    const float *B[3];
+    const float *T[3];
+};
+
+struct MDeposit {
+    unsigned long long *J[4];
+};
+
+// The reference's gather (src/grid/oGrid.cpp:153-197 with
+// src/particles/interpolate.cpp:11-47) in cell units: the offset handed to the
+// weights is o - 1 (the ghost-offset vertex), so the weights are 2 - o and
+// o - 1.
+__device__ __forceinline__ void gather_m(const MGeom &g, const MGather &P, int64_t o, float ox, float oy, float oz,
+                                         float f[6]) {
+    const int64_t sx = g.sx, sy = g.sy;
+    float a[3] = {2.0f - ox, 2.0f - oy, 2.0f - oz};  // (l - ds)/l
+    float b[3] = {ox - 1.0f, oy - 1.0f, oz - 1.0f};  // ds / l
+    // Ex: j = y, k = z; edges (iy,iz), (iy+1,iz), (iy+1,iz+1), (iy,iz+1)
+    f[0] = a[1] * a[2] * __ldg(P.E[0] + o) + b[1] * a[2] * __ldg(P.E[0] + o + sy) +
+           b[1] * b[2] * __ldg(P.E[0] + o + sy + 1) + a[1] * b[2] * __ldg(P.E[0] + o + 1);
+    // Ey: j = z, k = x; (iz,ix), (iz+1,ix), (iz+1,ix+1), (iz,ix+1)
+    f[1] = a[2] * a[0] * __ldg(P.E[1] + o) + b[2] * a[0] * __ldg(P.E[1] + o + 1) +
+           b[2] * b[0] * __ldg(P.E[1] + o + sx + 1) + a[2] * b[0] * __ldg(P.E[1] + o + sx);
+    // Ez: j = x, k = y
+    f[2] = a[0] * a[1] * __ldg(P.E[2] + o) + b[0] * a[1] * __ldg(P.E[2] + o + sx) +
+           b[0] * b[1] * __ldg(P.E[2] + o + sx + sy) + a[0] * b[1] * __ldg(P.E[2] + o + sy);
+    f[3] = 0.5f * (a[0] * (__ldg(P.T[0] + o) + __ldg(P.B[0] + o)) + b[0] * (__ldg(P.T[0] + o + sx) + __ldg(P.B[0] + o + sx)));
+    f[4] = 0.5f * (a[1] * (__ldg(P.T[1] + o) + __ldg(P.B[1] + o)) + b[1] * (__ldg(P.T[1] + o + sy) + __ldg(P.B[1] + o + sy)));
+    f[5] = 0.5f * (a[2] * (__ldg(P.T[2] + o) + __ldg(P.B[2] + o)) + b[2] * (__ldg(P.T[2] + o + 1) + __ldg(P.B[2] + o + 1)));
+}
+
+// Contribution points of cell o, same table as the FP64 deposit
+// (src/grid/oGrid.cpp:98-111, 129-136; the Jx quirk at index 3).
+__device__ __forceinline__ int64_t mdep_point(const MGeom &g, int64_t o, int q) {
+    const int64_t sx = g.sx, sy = g.sy;
+    switch (q) {
+        case 0: return o;
+        case 1: return o + sy;
+        case 2: return o + sy + 1;
+        case 3: return o + sy;
+        case 4: return o;
+        case 5: return o + 1;
+        case 6: return o + sx + 1;
+        case 7: return o + sx;
+        case 8: return o;
+        case 9: return o + sx;
+        case 10: return o + sx + sy;
+        case 11: return o + sy;
+        case 12: return o;
+        case 13: return o + sx;
+        case 14: return o + sx + sy;
+        case 15: return o + sy;
+        case 16: return o + sy + 1;
+        case 17: return o + sx + sy + 1;
+        case 18: return o + sx + 1;
+        default: return o + 1;
+    }
+}
+
+__device__ __forceinline__ void count_cross(DevCounters *ctr, int mask) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        unsigned b = __ballot_sync(0xffffffffu, (mask >> s) & 1);
+        if (lane == 0 && b) atomicAdd(&ctr->cross[s], (unsigned long long)__popc(b));
+    }
+}
+
+// Moves a particle by `shift` cells along one axis with the particle
+// boundary of that axis; returns the crossed-side bits (bit 6: removed).
+__device__ __forceinline__ int axis_bc(const BCTab &bc, int d, int n, int &i, float &o, float &u, float &v) {
+    int mask = 0;
+    if (i < 1) {  // left side: position (i - 1) + o < 0
+        mask |= 1 << (2 * d);
+        int kind = bc.pbc[2 * d];
+        if (kind == PBC_PERIODIC) {
+            i += n;
+        } else if (kind == PBC_REFLECTING) {
+            if (o == 0.0f) {
+                i = 2 - i;
+            } else {
+                i = 1 - i;
+                o = 1.0f - o;
+            }
+            u = -u;
+            v = -v;
+        } else {
+            mask |= 1 << 6;
+        }
+    } else if (i > n) {  // right side: position > n
+        mask |= 1 << (2 * d + 1);
+        int kind = bc.pbc[2 * d + 1];
+        if (kind == PBC_PERIODIC) {
+            i -= n;
+        } else if (kind == PBC_REFLECTING) {
+            if (o == 0.0f) {
+                i = 2 * n - i + 2;
+            } else {
+                i = 2 * n - i + 1;
+                o = 1.0f - o;
+            }
+            u = -u;
+            v = -v;
+        } else {
+            mask |= 1 << 6;
+        }
+    }
+    return mask;
+}
+
+// Fused gather + push + boundaries + deposit, one thread per particle.
+template <bool REL, bool FIRST, bool PUSH>
+__global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, MGather P, MState S,
+                                                 int64_t np, MDeposit D, int with_rho, const float *g0,
+                                                 DevCounters *ctr) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = false;
+    int mask = 0;
+    int64_t onew = 0;
+    float w[20];
+#pragma unroll
+    for (int q = 0; q < 20; q++) w[q] = 0.0f;
+    if (p < np) {
+        int32_t c = S.cell[p];
+        if (c >= 0) {
+            const int s = species_of_m(st, p);
+            float ox = S.ox[p], oy = S.oy[p], oz = S.oz[p];
+            float ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+            float vx, vy, vz;
+            int ix, iy, iz;
+            split_cell(g, dv, c, ix, iy, iz);
+            if (!PUSH) {
+                // deposit at the current state (Particle_Handler::depositRhoJ)
+                float ga = 1.0f;
+                if (REL && !FIRST) ga = sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+                vx = ux / ga;
+                vy = uy / ga;
+                vz = uz / ga;
+            } else {
+            float f[6];
+            gather_m(g, P, (int64_t)c, ox, oy, oz, f);
+            const float qp = st.qp[s];
+            if (REL) {
+                // Vay's pusher (src/pusher/relativisticBoris.cpp:53-140) on
+                // u = gamma v. Before the first push u holds the loaded v and
+                // g0 the loaded gamma, which the reference multiplies in.
+                float v0x, v0y, v0z, mx0, my0, mz0;
+                if (FIRST) {
+                    v0x = ux; v0y = uy; v0z = uz;
+                    float g = g0[p];
+                    mx0 = g * ux; my0 = g * uy; mz0 = g * uz;
+                } else {
+                    float iv = 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+                    v0x = ux * iv; v0y = uy * iv; v0z = uz * iv;
+                    mx0 = ux; my0 = uy; mz0 = uz;
+                }
+                float vXbx = v0y * f[5] - v0z * f[4];
+                float vXby = v0z * f[3] - v0x * f[5];
+                float vXbz = v0x * f[4] - v0y * f[3];
+                float upx = mx0 + qp * (f[0] + vXbx) + qp * f[0];
+                float upy = my0 + qp * (f[1] + vXby) + qp * f[1];
+                float upz = mz0 + qp * (f[2] + vXbz) + qp * f[2];
+                float gps = 1.0f + upx * upx + upy * upy + upz * upz;
+                float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
+                float tau2 = tx * tx + ty * ty + tz * tz;
+                float sigma = gps - tau2;
+                float ust = upx * tx + upy * ty + upz * tz;
+                float gi = sqrtf(0.5f * (sigma + sqrtf(sigma * sigma + 4.0f * (tau2 + ust * ust))));
+                float igi = 1.0f / gi;
+                tx *= igi;
+                ty *= igi;
+                tz *= igi;
+                float sfac = 1.0f / (1.0f + tx * tx + ty * ty + tz * tz);
+                float ud = ust * igi;
+                ux = sfac * (upx + ud * tx + (upy * tz - upz * ty));
+                uy = sfac * (upy + ud * ty + (upz * tx - upx * tz));
+                uz = sfac * (upz + ud * tz + (upx * ty - upy * tx));
+                vx = ux * igi;
+                vy = uy * igi;
+                vz = uz * igi;
+            } else {
+                // Boris (src/pusher/boris.cpp:33-85)
+                float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
+                float b2 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
+                float ts = 2.0f / (1.0f + qp * qp * b2);
+                float sx = ts * tx, sy = ts * ty, sz = ts * tz;
+                float mx = ux + qp * f[0], my = uy + qp * f[1], mz = uz + qp * f[2];
+                float ix_ = mx + my * tz - mz * ty;
+                float iy_ = my + mz * tx - mx * tz;
+                float iz_ = mz + mx * ty - my * tx;
+                ux = mx + iy_ * sz - iz_ * sy + qp * f[0];
+                uy = my + iz_ * sx - ix_ * sz + qp * f[1];
+                uz = mz + ix_ * sy - iy_ * sx + qp * f[2];
+                vx = ux;
+                vy = uy;
+                vz = uz;
+            }
+            // position update in cell units, then the boundaries per axis
+            float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
+            float fx = floorf(nx), fy = floorf(ny), fz = floorf(nz);
+            ix += (int)fx;
+            iy += (int)fy;
+            iz += (int)fz;
+            ox = nx - fx;
+            oy = ny - fy;
+            oz = nz - fz;
+            // fraction rounding can give exactly 1.0f for tiny negatives
+            if (ox >= 1.0f) { ox = 0.0f; ix += 1; }
+            if (oy >= 1.0f) { oy = 0.0f; iy += 1; }
+            if (oz >= 1.0f) { oz = 0.0f; iz += 1; }
+            mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
+            if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
+            if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
+            }
+            if (mask & 64) {
+                S.cell[p] = -1;
+            } else if (ix < 1 || ix > g.n[0] || iy < 1 || iy > g.n[1] || iz < 1 || iz > g.n[2]) {
+                // moved more than a box length in one step: record, drop
+                atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
+                S.cell[p] = -1;
+                mask |= 64;
+            } else {
+                onew = (int64_t)ix * g.sx + (int64_t)iy * g.sy + iz;
+                if (PUSH) {
+                    S.cell[p] = (int32_t)onew;
+                    S.ox[p] = ox;
+                    S.oy[p] = oy;
+                    S.oz[p] = oz;
+                    S.ux[p] = ux;
+                    S.uy[p] = uy;
+                    S.uz[p] = uz;
+                }
+                if (st.deposit[s]) {
+                    active = true;
+                    // deposit weights (src/particles/deposit.cpp:12-62) in
+                    // fixed-point units: (UNIT_RHOJ q / V) v_i (2 - o_j)(2 - o_k) etc.
+                    float a[3] = {2.0f - ox, 2.0f - oy, 2.0f - oz};
+                    float b[3] = {ox - 1.0f, oy - 1.0f, oz - 1.0f};
+                    const float qd = st.qdep[s];
+                    float jx = qd * vx, jy = qd * vy, jz = qd * vz;
+                    w[0] = jx * a[1] * a[2];
+                    w[1] = jx * b[1] * a[2];
+                    w[2] = jx * b[1] * b[2];
+                    w[3] = jx * a[1] * b[2];
+                    w[4] = jy * a[2] * a[0];
+                    w[5] = jy * b[2] * a[0];
+                    w[6] = jy * b[2] * b[0];
+                    w[7] = jy * a[2] * b[0];
+                    w[8] = jz * a[0] * a[1];
+                    w[9] = jz * b[0] * a[1];
+                    w[10] = jz * b[0] * b[1];
+                    w[11] = jz * a[0] * b[1];
+                    if (with_rho) {
+                        w[12] = qd * a[0] * a[1] * a[2];
+                        w[13] = qd * b[0] * a[1] * a[2];
+                        w[14] = qd * b[0] * b[1] * a[2];
+                        w[15] = qd * a[0] * b[1] * a[2];
+                        w[16] = qd * a[0] * b[1] * b[2];
+                        w[17] = qd * b[0] * b[1] * b[2];
+                        w[18] = qd * b[0] * a[1] * b[2];
+                        w[19] = qd * a[0] * a[1] * b[2];
+                    }
+                }
+            }
+        }
+    }
+    count_cross(ctr, mask & 63);
+    // warp runs of equal cells: FP32 sums in a fixed order, int64 commit
+    long long key = active ? (long long)onew : -1 - (long long)lane;
+    long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+    bool head = (lane == 0) || (prev != key);
+    unsigned heads = __ballot_sync(0xffffffffu, head);
+    if (__ballot_sync(0xffffffffu, active) == 0u) return;
+    int rend = run_end(heads, lane);
+    const bool all_single = (heads == 0xffffffffu);
+    const int nq = with_rho ? 20 : 12;
+#pragma unroll
+    for (int q = 0; q < 20; q++) {
+        if (q >= nq) break;
+        float v = w[q];
+        if (!all_single) v = run_suffix_sum(v, lane, rend);
+        if (head && active) {
+            long long fx = __float2ll_rn(v);
+            if (fx != 0) {
+                unsigned long long *base = D.J[q < 4 ? 0 : q < 8 ? 1 : q < 12 ? 2 : 3];
+                atomicAdd(base + mdep_point(g, onew, q), (unsigned long long)fx);
+            }
+        }
+    }
+}
+
+// ---- conversions --------------------------------------------------------
+
+// vmode (relativistic, before the first push): the momentum slots take the
+// loaded velocity and g0 the loaded gamma; otherwise u = gamma v directly.
+__global__ void k_from_f64(Geom g, MState S, int64_t at, int64_t n, const double *x, const double *y,
+                           const double *z, const double *vx, const double *vy, const double *vz, const double *gam,
+                           int rel, int vmode, float *g0, DevCounters *ctr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double pos[3] = {x[i], y[i], z[i]};
+        int ci[3];
+        float of[3];
+        bool ok = true;
+        for (int d = 0; d < 3; d++) {
+            double t = (pos[d] - g.x0[d]) * g.id[d];  // cells from x0
+            double fl = floor(t);
+            ci[d] = (int)fl + 1;
+            float o = (float)(t - fl);
+            if (o >= 1.0f) {
+                o = 0.0f;
+                ci[d] += 1;
+            }
+            of[d] = o;
+            if (ci[d] < 1 || ci[d] > g.n[d]) ok = false;
+        }
+        int64_t p = at + i;
+        if (!ok) {
+            atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
+            S.cell[p] = -1;
+            continue;
+        }
+        S.cell[p] = (int32_t)((int64_t)ci[0] * g.sx + (int64_t)ci[1] * g.sy + ci[2]);
+        S.ox[p] = of[0];
+        S.oy[p] = of[1];
+        S.oz[p] = of[2];
+        double ga = gam ? gam[i] : 0.0;  // new_particle() leaves gamma at 0
+        if (rel && vmode) {
+            S.ux[p] = (float)vx[i];
+            S.uy[p] = (float)vy[i];
+            S.uz[p] = (float)vz[i];
+            g0[p] = (float)ga;
+        } else {
+            double f = rel ? ga : 1.0;
+            S.ux[p] = (float)(f * vx[i]);
+            S.uy[p] = (float)(f * vy[i]);
+            S.uz[p] = (float)(f * vz[i]);
+        }
+    }
+}
+
+__global__ void k_to_f64(Geom g, MState S, int64_t at, int64_t n, double *x, double *y, double *z, double *vx,
+                         double *vy, double *vz, double *gam, int rel, const float *g0) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = at + i;
+        int32_t c = S.cell[p];
+        if (c < 0) {
+            x[i] = y[i] = z[i] = vx[i] = vy[i] = vz[i] = __longlong_as_double(0x7ff8000000000000LL);
+            if (gam) gam[i] = 0.0;
+            continue;
+        }
+        int ix = (int)(c / g.sx);
+        int64_t r = c - ix * g.sx;
+        int iy = (int)(r / g.sy);
+        int iz = (int)(r - iy * g.sy);
+        x[i] = g.x0[0] + g.d[0] * ((double)(ix - 1) + (double)S.ox[p]);
+        y[i] = g.x0[1] + g.d[1] * ((double)(iy - 1) + (double)S.oy[p]);
+        z[i] = g.x0[2] + g.d[2] * ((double)(iz - 1) + (double)S.oz[p]);
+        double ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+        if (rel && g0) {  // before the first push: loaded v and gamma
+            vx[i] = ux;
+            vy[i] = uy;
+            vz[i] = uz;
+            if (gam) gam[i] = (double)g0[p];
+            continue;
+        }
+        double ga = rel ? sqrt(1.0 + ux * ux + uy * uy + uz * uz) : 1.0;
+        vx[i] = ux / ga;
+        vy[i] = uy / ga;
+        vz[i] = uz / ga;
+        if (gam) gam[i] = rel ? ga : 0.0;
+    }
+}
+
+__global__ void k_d2f(const double *a, float *b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+__global__ void k_f2d(const float *a, double *b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i];
+}
+__global__ void k_fix2d(const long long *a, double *b, int64_t n, double q0) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (double)a[i] * q0;
+}
+__global__ void k_d2fix(const double *a, long long *b, int64_t n, double iq0) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = __double2ll_rn(a[i] * iq0);
+}
+__global__ void k_fillf(float *a, int64_t n, float v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+// ---- FP32 grid kernels ---------------------------------------------------
+
+struct MF3 {
+    float *p[3];
+};
+struct MCF3 {
+    const float *p[3];
+};
+struct MJ3 {
+    const long long *p[3];
+};
+
+__global__ void k_yee_e_m(MGeom g, MF3 E, MCF3 T, MJ3 J, float dt, float q0) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
+    const float *Tx = T.p[0], *Ty = T.p[1], *Tz = T.p[2];
+    float jx = __ll2float_rn(J.p[0][o]) * q0, jy = __ll2float_rn(J.p[1][o]) * q0, jz = __ll2float_rn(J.p[2][o]) * q0;
+    E.p[0][o] -= dt * ((Ty[o] - Ty[o - 1]) * g.idf[2] - (Tz[o] - Tz[o - g.sy]) * g.idf[1] + FOURPI_F * jx);
+    E.p[1][o] -= dt * ((Tz[o] - Tz[o - g.sx]) * g.idf[0] - (Tx[o] - Tx[o - 1]) * g.idf[2] + FOURPI_F * jy);
+    E.p[2][o] -= dt * ((Tx[o] - Tx[o - g.sy]) * g.idf[1] - (Ty[o] - Ty[o - g.sx]) * g.idf[0] + FOURPI_F * jz);
+}
+
+__global__ void k_yee_b_m(MGeom g, MF3 B, MCF3 T, MCF3 E, float dt) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
+    const float *Ex = E.p[0], *Ey = E.p[1], *Ez = E.p[2];
+    B.p[0][o] = T.p[0][o] + dt * ((Ey[o + 1] - Ey[o]) * g.idf[2] - (Ez[o + g.sy] - Ez[o]) * g.idf[1]);
+    B.p[1][o] = T.p[1][o] + dt * ((Ez[o + g.sx] - Ez[o]) * g.idf[0] - (Ex[o + 1] - Ex[o]) * g.idf[2]);
+    B.p[2][o] = T.p[2][o] + dt * ((Ex[o + g.sy] - Ex[o]) * g.idf[1] - (Ey[o + g.sx] - Ey[o]) * g.idf[0]);
+}
+
+__global__ void k_yee_es_m(MGeom g, MF3 E, MJ3 J, float dt, float q0) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
+    for (int c = 0; c < 3; c++) E.p[c][o] = -dt * (FOURPI_F * (__ll2float_rn(J.p[c][o]) * q0));
+}
+
+struct MList6 {
+    float *p[6];
+    int n;
+};
+
+// Periodic ghost fill over the physical transverse range (same scheme as the
+// FP64 k_ghost): all copies read physical points, any dims run at once.
+__global__ void k_ghost_m(MGeom g, MList6 fl, int dims_mask) {
+    int z = blockIdx.z;
+    int r = z & 1;
+    int d = (z >> 1) % 3;
+    int f = (z >> 1) / 3;
+    if (!((dims_mask >> d) & 1) || f >= fl.n) return;
+    int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int p = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (q > g.n[o2] || p > g.n[o1]) return;
+    int nd = g.n[d];
+    int src = r == 0 ? nd : 1, dst = r == 0 ? 0 : nd + 1;
+    int is[3], it[3];
+    is[d] = src;
+    it[d] = dst;
+    is[o1] = it[o1] = p;
+    is[o2] = it[o2] = q;
+    float *F = fl.p[f];
+    F[(int64_t)it[0] * g.sx + (int64_t)it[1] * g.sy + it[2]] = F[(int64_t)is[0] * g.sx + (int64_t)is[1] * g.sy + is[2]];
+}
+
+// Periodic fold of one dimension on the fixed-point accumulators (exact
+// integer adds); the folded ghost plane is left as the reference leaves it.
+__global__ void k_fold_m(MGeom g, int d, long long *f0, long long *f1, long long *f2) {
+    int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int p = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (q > g.n[o2] || p > g.n[o1]) return;
+    int is[3], it[3];
+    is[d] = g.n[d] + 1;
+    it[d] = 1;
+    is[o1] = it[o1] = p;
+    is[o2] = it[o2] = q;
+    int64_t s = (int64_t)is[0] * g.sx + (int64_t)is[1] * g.sy + is[2];
+    int64_t t = (int64_t)it[0] * g.sx + (int64_t)it[1] * g.sy + it[2];
+    long long *F = blockIdx.z == 0 ? f0 : (blockIdx.z == 1 ? f1 : f2);
+    F[t] += F[s];
+}
+
+struct MPlane {
+    float *f;
+    int dim, idx;
+    float v;
+};
+struct MPlaneList {
+    MPlane s[12];
+    int n;
+};
+
+__global__ void k_plane_m(MGeom g, MPlaneList pl, int tot0, int tot1, int tot2) {
+    int e = blockIdx.z;
+    if (e >= pl.n) return;
+    const MPlane &ps = pl.s[e];
+    int d = ps.dim;
+    int tot[3] = {tot0, tot1, tot2};
+    int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    int p = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= tot[o2] || p >= tot[o1]) return;
+    int ii[3];
+    ii[d] = ps.idx;
+    ii[o1] = p;
+    ii[o2] = q;
+    ps.f[(int64_t)ii[0] * g.sx + (int64_t)ii[1] * g.sy + ii[2]] = ps.v;
+}
+
+// ---- reductions (FP64 accumulation) -------------------------------------
+
+__global__ void k_moments_m(MSpecies st, MState S, int64_t np, int rel, const float *g0, double *part) {
+    double acc[4] = {0, 0, 0, 0};
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        if (S.cell[p] < 0) continue;
+        double ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+        double ga = (rel && !g0) ? sqrt(1.0 + ux * ux + uy * uy + uz * uz) : 1.0;
+        double vx = ux / ga, vy = uy / ga, vz = uz / ga;
+        double m = st.m[species_of_m(st, p)];
+        acc[0] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        acc[1] += m * vx;
+        acc[2] += m * vy;
+        acc[3] += m * vz;
+    }
+    __shared__ double sh[32][4];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < 4; q++) {
+        double v = acc[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) v += sh[ww][threadIdx.x];
+        part[blockIdx.x * 4 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_energy_m(MGeom g, MCF3 E, MCF3 B, double hv, double *part) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
+        int k = (int)(t % g.n[2]) + 1;
+        int64_t r = t / g.n[2];
+        int j = (int)(r % g.n[1]) + 1;
+        int i = (int)(r / g.n[1]) + 1;
+        int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
+        int64_t nb[3] = {o + g.sx, o + g.sy, o + 1};
+        for (int q = 0; q < 3; q++) {
+            double s = (double)E.p[q][o] + (double)E.p[q][nb[q]];
+            acc[q] += hv * (0.25 * s * s);
+            double sb = (double)B.p[q][o] + (double)B.p[q][nb[q]];
+            acc[3 + q] += hv * (0.25 * sb * sb);
+        }
+    }
+    __shared__ double sh[32][6];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < 6; q++) {
+        double v = acc[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) sh[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double v = 0.0;
+        for (int ww = 0; ww < (int)(blockDim.x >> 5); ww++) v += sh[ww][threadIdx.x];
+        part[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_keys_m(MSpecies st, MState S, int64_t np, int64_t npts, uint32_t *key, uint32_t dead) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int32_t c = S.cell[p];
+    key[p] = c < 0 ? dead : (uint32_t)((int64_t)species_of_m(st, p) * npts + c);
+}
+
+// ---- host helpers ----------------------------------------------------------
+
+MGeom mgeom(emoo_handle *h, double dt) {
+    MGeom m;
+    for (int d = 0; d < 3; d++) {
+        m.n[d] = h->g.n[d];
+        m.dtid[d] = (float)(dt / h->g.d[d]);
+        m.idf[d] = (float)(1.0 / h->g.d[d]);
+    }
+    m.sx = h->g.sx;
+    m.sy = h->g.sy;
+    m.npts = h->g.npts;
+    m.fourpi_dt = (float)(4.0 * PI_D * dt);
+    return m;
+}
+
+Div3 div3(emoo_handle *h) {
+    Div3 d;
+    d.sx = make_fastdiv((uint32_t)h->g.sx);
+    d.sy = make_fastdiv((uint32_t)h->g.sy);
+    return d;
+}
+
+MSpecies mspecies(emoo_handle *h, double dtp) {
+    MSpecies st;
+    SpeciesTab t;
+    species_tab(h, dtp, t);
+    st.nspec = t.nspec;
+    for (int s = 0; s <= EMOO_NSPEC; s++) st.off[s] = t.off[s];
+    for (int s = 0; s < EMOO_NSPEC; s++) {
+        st.qp[s] = (float)t.qp[s];
+        st.qdep[s] = (float)((t.uq[s] / h->g.vol) / h->mf->q0);
+        st.m[s] = (float)t.m[s];
+        st.deposit[s] = t.deposit[s];
+    }
+    return st;
+}
+
+MState mstate(emoo_handle *h) { return MState{h->cell, h->ox, h->oy, h->oz, h->ux, h->uy, h->uz}; }
+
+float *mb_role(emoo_handle *h, int c) { return h->bswap ? h->mf->Bslot[3 + c] : h->mf->Bslot[c]; }
+float *mt_role(emoo_handle *h, int c) { return h->bswap ? h->mf->Bslot[c] : h->mf->Bslot[3 + c]; }
+
+int nblk(int64_t n, int cap = 152 * 16) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, cap)); }
+
+}  // namespace
+
+// ---- public (namespace emoo) ----------------------------------------------
+
+int mixed_alloc(emoo_handle *h) {
+    h->mf = new FieldsF32();
+    FieldsF32 *m = h->mf;
+    size_t n = (size_t)h->g.npts;
+    for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMalloc(&m->E[c], n * sizeof(float)));
+    for (int c = 0; c < 6; c++) EMOO_CUDA(cudaMalloc(&m->Bslot[c], n * sizeof(float)));
+    for (int c = 0; c < 4; c++) EMOO_CUDA(cudaMalloc(&m->J[c], n * sizeof(long long)));
+    for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMemsetAsync(m->E[c], 0, n * sizeof(float), h->stream));
+    for (int c = 0; c < 6; c++) EMOO_CUDA(cudaMemsetAsync(m->Bslot[c], 0, n * sizeof(float), h->stream));
+    for (int c = 0; c < 4; c++) EMOO_CUDA(cudaMemsetAsync(m->J[c], 0, n * sizeof(long long), h->stream));
+    double qmax = 0.0;
+    for (int s = 0; s < h->info.nspecies; s++)
+        qmax = std::max(qmax, std::fabs(UNIT_RHOJ * h->info.charge_ratio[s] / h->g.vol));
+    if (qmax == 0.0) qmax = 1.0;
+    m->q0 = std::ldexp(qmax, -32);
+    return EMOO_OK;
+}
+
+void mixed_free(emoo_handle *h) {
+    FieldsF32 *m = h->mf;
+    if (!m) return;
+    for (int c = 0; c < 3; c++)
+        if (m->E[c]) cudaFree(m->E[c]);
+    for (int c = 0; c < 6; c++)
+        if (m->Bslot[c]) cudaFree(m->Bslot[c]);
+    for (int c = 0; c < 4; c++)
+        if (m->J[c]) cudaFree(m->J[c]);
+    if (h->g0) cudaFree(h->g0);
+    h->g0 = nullptr;
+    delete m;
+    h->mf = nullptr;
+}
+
+// n > 0: host FP64 arrays (copied through the payload scratch in chunks);
+// n < 0: |n| particles already staged on the device at the given pointers.
+int mixed_from_f64(emoo_handle *h, int64_t at, int64_t n, const double *x, const double *y, const double *z,
+                   const double *vx, const double *vy, const double *vz, const double *gam) {
+    bool dev = n < 0;
+    if (dev) n = -n;
+    int rel = h->info.relativity != 0;
+    if (rel && !h->g0) {
+        EMOO_CUDA(cudaMalloc(&h->g0, sizeof(float) * (size_t)h->cap));
+        h->first_push = 1;  // no push yet: load in velocity mode
+    }
+    int vmode = rel && h->first_push;
+    if (dev) {
+        h->launches++;
+        k_from_f64<<<nblk(n), 256, 0, h->stream>>>(h->g, mstate(h), at, n, x, y, z, vx, vy, vz, gam, rel, vmode,
+                                                   h->g0, h->ctr);
+        EMOO_CUDA(cudaGetLastError());
+        return EMOO_OK;
+    }
+    int64_t chunk = (int64_t)(h->pay_bytes / (7 * sizeof(double)));
+    if (chunk < 1) return EMOO_ERR_OOM;
+    double *s = (double *)h->pay;
+    for (int64_t b = 0; b < n; b += chunk) {
+        int64_t m = std::min(chunk, n - b);
+        size_t bytes = sizeof(double) * (size_t)m;
+        const double *src[7] = {x, y, z, vx, vy, vz, gam};
+        for (int q = 0; q < 7; q++) {
+            if (src[q]) EMOO_CUDA(cudaMemcpyAsync(s + q * m, src[q] + b, bytes, cudaMemcpyHostToDevice, h->stream));
+        }
+        h->launches++;
+        k_from_f64<<<nblk(m), 256, 0, h->stream>>>(h->g, mstate(h), at + b, m, s, s + m, s + 2 * m, s + 3 * m,
+                                                   s + 4 * m, s + 5 * m, gam ? s + 6 * m : nullptr, rel, vmode,
+                                                   h->g0, h->ctr);
+        EMOO_CUDA(cudaGetLastError());
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return EMOO_OK;
+}
+
+int mixed_to_f64(emoo_handle *h, int64_t at, int64_t n, double *x, double *y, double *z, double *vx, double *vy,
+                 double *vz, double *gam) {
+    int rel = h->info.relativity != 0;
+    int64_t chunk = (int64_t)(h->pay_bytes / (7 * sizeof(double)));
+    double *s = (double *)h->pay;
+    const float *g0 = (h->first_push && h->g0) ? h->g0 : nullptr;
+    for (int64_t b = 0; b < n; b += chunk) {
+        int64_t m = std::min(chunk, n - b);
+        h->launches++;
+        k_to_f64<<<nblk(m), 256, 0, h->stream>>>(h->g, mstate(h), at + b, m, s, s + m, s + 2 * m, s + 3 * m,
+                                                 s + 4 * m, s + 5 * m, s + 6 * m, rel, g0);
+        EMOO_CUDA(cudaGetLastError());
+        double *dst[7] = {x, y, z, vx, vy, vz, gam};
+        size_t bytes = sizeof(double) * (size_t)m;
+        for (int q = 0; q < 7; q++)
+            if (dst[q]) EMOO_CUDA(cudaMemcpyAsync(dst[q] + b, s + q * m, bytes, cudaMemcpyDeviceToHost, h->stream));
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return EMOO_OK;
+}
+
+int mixed_ghost_fill(emoo_handle *h) {
+    // E/B ghost fill through the fixed storage slots, with LightBC planes for
+    // external sides, in the reference's dimension order
+    MGeom mg = mgeom(h, h->dtp);
+    MList6 fl;
+    fl.n = 6;
+    for (int c = 0; c < 3; c++) {
+        fl.p[c] = h->mf->E[c];
+        fl.p[3 + c] = h->mf->Bslot[c];
+    }
+    const Geom &g = h->g;
+    int ta = std::max(g.n[1], g.n[0]);
+    int tb = std::max(g.n[2], g.n[1]);
+    dim3 blk(32, 8);
+    int mask = 0;
+    auto flush = [&]() -> int {
+        if (!mask) return EMOO_OK;
+        dim3 grd((tb + 31) / 32, (ta + 7) / 8, 36);
+        h->launches++;
+        k_ghost_m<<<grd, blk, 0, h->stream>>>(mg, fl, mask);
+        mask = 0;
+        EMOO_CUDA(cudaGetLastError());
+        return EMOO_OK;
+    };
+    for (int d = 0; d < 3; d++) {
+        if (h->bc.fbc[2 * d] == FBC_PERIODIC) {
+            mask |= 1 << d;
+            continue;
+        }
+        EMOO_TRY(flush());
+        extern int light_planes_public(emoo_handle * h, int s, PlaneSet *ps);
+        for (int r = 0; r < 2; r++) {
+            int s = 2 * d + r;
+            if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
+            PlaneSet ps[6];
+            int n = light_planes_public(h, s, ps);
+            EMOO_TRY(mixed_plane_sets(h, ps, n));
+        }
+    }
+    return flush();
+}
+
+// PlaneSet.f carries a field ID (E or B role) for the mixed form.
+int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n) {
+    MGeom mg = mgeom(h, h->dtp);
+    MPlaneList pl;
+    pl.n = n;
+    for (int i = 0; i < n; i++) {
+        int id = (int)(intptr_t)ps[i].f;
+        float *f = id < EMOO_BX ? h->mf->E[id] : mb_role(h, id - EMOO_BX);
+        pl.s[i] = MPlane{f, ps[i].dim, ps[i].idx, (float)ps[i].v};
+    }
+    const Geom &g = h->g;
+    int m = std::max(std::max(g.tot[0], g.tot[1]), g.tot[2]);
+    dim3 blk(32, 8);
+    dim3 grd((m + 31) / 32, (m + 7) / 8, n);
+    h->launches++;
+    k_plane_m<<<grd, blk, 0, h->stream>>>(mg, pl, g.tot[0], g.tot[1], g.tot[2]);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+static int mixed_fold(emoo_handle *h) {
+    MGeom mg = mgeom(h, h->dtp);
+    const Geom &g = h->g;
+    for (int d = 0; d < 3; d++) {
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) continue;
+        int f0 = (d == 0) ? 1 : 0;  // Jy for x, Jx otherwise
+        int f1 = (d == 2) ? 1 : 2;  // Jy for z, Jz otherwise
+        int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        dim3 blk(32, 8);
+        dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 3);
+        h->launches++;
+        k_fold_m<<<grd, blk, 0, h->stream>>>(mg, d, h->mf->J[f0], h->mf->J[f1], h->mf->J[3]);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+static int mixed_deposit_zero(emoo_handle *h, int with_rho) {
+    size_t b = sizeof(long long) * (size_t)h->g.npts;
+    for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMemsetAsync(h->mf->J[c], 0, b, h->stream));
+    if (with_rho) EMOO_CUDA(cudaMemsetAsync(h->mf->J[3], 0, b, h->stream));
+    return EMOO_OK;
+}
+
+static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = true) {
+    if (h->np == 0) return EMOO_OK;
+    MGeom mg = mgeom(h, dtp);
+    MSpecies st = mspecies(h, dtp);
+    MGather P;
+    for (int c = 0; c < 3; c++) {
+        P.E[c] = h->mf->E[c];
+        P.B[c] = mb_role(h, c);
+        P.T[c] = mt_role(h, c);
+    }
+    MDeposit D;
+    for (int c = 0; c < 4; c++) D.J[c] = (unsigned long long *)h->mf->J[c];
+    int64_t nb = (h->np + 255) / 256;
+    bool rel = h->info.relativity != 0;
+    bool first = rel && h->first_push && h->g0;
+    Div3 dv = div3(h);
+    const float *g0 = h->g0;
+    MState S = mstate(h);
+    dim3 grd((unsigned)nb);
+    if (!push) {
+        if (rel && first)
+            k_fused_m<true, true, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
+                                                                     h->ctr);
+        else if (rel)
+            k_fused_m<true, false, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho,
+                                                                      g0, h->ctr);
+        else
+            k_fused_m<false, false, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho,
+                                                                       g0, h->ctr);
+        EMOO_CUDA(cudaGetLastError());
+        return EMOO_OK;
+    }
+    h->launches++;
+    if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
+    if (rel && first)
+        k_fused_m<true, true, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
+                                                                h->ctr);
+    else if (rel)
+        k_fused_m<true, false, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
+                                                                 h->ctr);
+    else
+        k_fused_m<false, false, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
+                                                                  h->ctr);
+    EMOO_CUDA(cudaGetLastError());
+    if (h->prof_on) {
+        EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
+        EMOO_TRY(prof_accumulate(h));
+    }
+    // g0 stays allocated for later loads; it is read only while first_push is set
+    if (first) h->first_push = 0;
+    return EMOO_OK;
+}
+
+static int mixed_yee(emoo_handle *h, double dtp, int es) {
+    MGeom mg = mgeom(h, dtp);
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    MF3 E = {{h->mf->E[0], h->mf->E[1], h->mf->E[2]}};
+    MJ3 J = {{h->mf->J[0], h->mf->J[1], h->mf->J[2]}};
+    if (es) {
+        h->launches++;
+        k_yee_es_m<<<grd, blk, 0, h->stream>>>(mg, E, J, (float)dtp, (float)h->mf->q0);
+    } else {
+        h->bswap ^= 1;  // the member-pointer swap of evolveFields
+        MCF3 T = {{mt_role(h, 0), mt_role(h, 1), mt_role(h, 2)}};
+        h->launches++;
+        k_yee_e_m<<<grd, blk, 0, h->stream>>>(mg, E, T, J, (float)dtp, (float)h->mf->q0);
+        MF3 B = {{mb_role(h, 0), mb_role(h, 1), mb_role(h, 2)}};
+        MCF3 Ec = {{E.p[0], E.p[1], E.p[2]}};
+        h->launches++;
+        k_yee_b_m<<<grd, blk, 0, h->stream>>>(mg, B, T, Ec, (float)dtp);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_step(emoo_handle *h, double dtp, int with_rho) {
+    EMOO_TRY(mixed_deposit_zero(h, with_rho));
+    EMOO_TRY(mixed_fused(h, dtp, with_rho));
+    EMOO_TRY(mixed_fold(h));
+    EMOO_TRY(mixed_yee(h, dtp, h->info.electrostatic == 1));
+    EMOO_TRY(mixed_ghost_fill(h));
+    return EMOO_OK;
+}
+
+int mixed_sort_keys(emoo_handle *h) {
+    MSpecies st = mspecies(h, h->dtp);
+    uint32_t dead = (uint32_t)((int64_t)h->nspec * h->g.npts + 1);
+    h->launches++;
+    k_keys_m<<<(unsigned)((h->np + 255) / 256), 256, 0, h->stream>>>(st, mstate(h), h->np, h->g.npts, h->key[0], dead);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_key_bits(emoo_handle *h) {
+    uint64_t maxkey = (uint64_t)h->nspec * (uint64_t)h->g.npts + 2;
+    int b = 1;
+    while ((1ull << b) <= maxkey) b++;
+    return b;
+}
+
+// Field readback: FP32 storage or fixed point converted to FP64 in the slot.
+int mixed_get_field(emoo_handle *h, int id, double *out_dev) {
+    int64_t n = h->g.npts;
+    if (id <= EMOO_EZ) k_f2d<<<nblk(n), 256, 0, h->stream>>>(h->mf->E[id], out_dev, n);
+    else if (id <= EMOO_BZ) k_f2d<<<nblk(n), 256, 0, h->stream>>>(h->mf->Bslot[id - EMOO_BX], out_dev, n);
+    else if (id <= EMOO_RHO) k_fix2d<<<nblk(n), 256, 0, h->stream>>>(h->mf->J[id - EMOO_JX], out_dev, n, h->mf->q0);
+    else if (id <= EMOO_BZ_TM1) k_f2d<<<nblk(n), 256, 0, h->stream>>>(h->mf->Bslot[3 + id - EMOO_BX_TM1], out_dev, n);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_set_field(emoo_handle *h, int id, const double *in_dev) {
+    int64_t n = h->g.npts;
+    if (id <= EMOO_EZ) k_d2f<<<nblk(n), 256, 0, h->stream>>>(in_dev, h->mf->E[id], n);
+    else if (id <= EMOO_BZ) k_d2f<<<nblk(n), 256, 0, h->stream>>>(in_dev, h->mf->Bslot[id - EMOO_BX], n);
+    else if (id <= EMOO_RHO) k_d2fix<<<nblk(n), 256, 0, h->stream>>>(in_dev, h->mf->J[id - EMOO_JX], n, 1.0 / h->mf->q0);
+    else if (id <= EMOO_BZ_TM1) k_d2f<<<nblk(n), 256, 0, h->stream>>>(in_dev, h->mf->Bslot[3 + id - EMOO_BX_TM1], n);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// Mixed-form deposit into the FP64 J / rho slots (for the Poisson start):
+// one fused pass at dt = 0 is not the reference's deposit (it pushes), so the
+// particles are deposited by a zero-step of the FP32 deposit instead.
+int mixed_deposit_to_f64(emoo_handle *h) {
+    int64_t n = h->g.npts;
+    for (int c = 0; c < 4; c++)
+        k_fix2d<<<nblk(n), 256, 0, h->stream>>>(h->mf->J[c], h->slot[EMOO_JX + c], n, h->mf->q0);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// After an FP64 field initialisation on the slots: E, B, B_tm1 to FP32.
+int mixed_fields_from_slots(emoo_handle *h) {
+    int64_t n = h->g.npts;
+    for (int c = 0; c < 3; c++) {
+        h->launches++;
+        k_d2f<<<nblk(n), 256, 0, h->stream>>>(h->slot[EMOO_EX + c], h->mf->E[c], n);
+        h->launches++;
+        k_d2f<<<nblk(n), 256, 0, h->stream>>>(h->slot[EMOO_BX + c], h->mf->Bslot[c], n);
+        h->launches++;
+        k_d2f<<<nblk(n), 256, 0, h->stream>>>(h->slot[EMOO_BX_TM1 + c], h->mf->Bslot[3 + c], n);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_const_fields(emoo_handle *h) {
+    int64_t n = h->g.npts;
+    for (int c = 0; c < 3; c++) {
+        h->launches++;
+        k_fillf<<<nblk(n), 256, 0, h->stream>>>(h->mf->E[c], n, (float)h->info.E0[c]);
+        h->launches++;
+        k_fillf<<<nblk(n), 256, 0, h->stream>>>(h->mf->Bslot[c], n, (float)h->info.B0[c]);
+        h->launches++;
+        k_fillf<<<nblk(n), 256, 0, h->stream>>>(h->mf->Bslot[3 + c], n, (float)h->info.B0[c]);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_moments(emoo_handle *h, double out4[4]) {
+    for (int q = 0; q < 4; q++) out4[q] = 0.0;
+    if (h->np == 0) return EMOO_OK;
+    int nb = nblk(h->np, 152 * 8);
+    if (h->red_cap < (size_t)nb * 4) {
+        if (h->red) cudaFree(h->red);
+        EMOO_CUDA(cudaMalloc(&h->red, (size_t)nb * 4 * sizeof(double)));
+        h->red_cap = (size_t)nb * 4;
+    }
+    MSpecies st = mspecies(h, h->dtp);
+    const float *g0 = (h->first_push && h->g0) ? h->g0 : nullptr;
+    h->launches++;
+    k_moments_m<<<nb, 256, 0, h->stream>>>(st, mstate(h), h->np, h->info.relativity != 0, g0, h->red);
+    EMOO_CUDA(cudaGetLastError());
+    std::vector<double> part((size_t)nb * 4);
+    EMOO_CUDA(cudaMemcpyAsync(part.data(), h->red, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    for (int b = 0; b < nb; b++)
+        for (int q = 0; q < 4; q++) out4[q] += part[(size_t)b * 4 + q];
+    return EMOO_OK;
+}
+
+int mixed_field_energy(emoo_handle *h, double out6[6]) {
+    const Geom &g = h->g;
+    int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
+    int nb = nblk(nphys, 152 * 8);
+    if (h->red_cap < (size_t)nb * 6) {
+        if (h->red) cudaFree(h->red);
+        EMOO_CUDA(cudaMalloc(&h->red, (size_t)nb * 6 * sizeof(double)));
+        h->red_cap = (size_t)nb * 6;
+    }
+    MGeom mg = mgeom(h, h->dtp);
+    MCF3 E = {{h->mf->E[0], h->mf->E[1], h->mf->E[2]}};
+    MCF3 B = {{h->mf->Bslot[0], h->mf->Bslot[1], h->mf->Bslot[2]}};  // fixed slots, like the history
+    k_energy_m<<<nb, 256, 0, h->stream>>>(mg, E, B, 0.5 * g.vol, h->red);
+    EMOO_CUDA(cudaGetLastError());
+    std::vector<double> part((size_t)nb * 6);
+    EMOO_CUDA(cudaMemcpyAsync(part.data(), h->red, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    for (int q = 0; q < 6; q++) out6[q] = 0.0;
+    for (int b = 0; b < nb; b++)
+        for (int q = 0; q < 6; q++) out6[q] += part[(size_t)b * 6 + q];
+    return EMOO_OK;
+}
+
+}  // namespace emoo
+
+namespace emoo {
+
+// Particle_Handler::depositRhoJ for the mixed form: zero, then deposit every
+// live non-test particle at its current position (no push).
+int mixed_deposit(emoo_handle *h, int with_rho) {
+    EMOO_TRY(mixed_deposit_zero(h, with_rho));
+    return mixed_fused(h, h->dtp, with_rho, false);
+}
+
+int mixed_fold_public(emoo_handle *h) { return mixed_fold(h); }
+
+int mixed_yee_public(emoo_handle *h, double dtp, int es) { return mixed_yee(h, dtp, es); }
+
+// FP32 E, B, B_tm1 and fixed-point J / rho into the FP64 slots (for the FP64
+// diagnostics: Gauss-law residual).
+int mixed_fields_to_slots(emoo_handle *h) {
+    for (int id = 0; id <= EMOO_BZ_TM1; id++) EMOO_TRY(mixed_get_field(h, id, h->slot[id]));
+    return EMOO_OK;
+}
+
 }  // namespace emoo

@@ -141,12 +141,15 @@ int64_t scan_scratch(int64_t m) {
 int scan_excl(emoo_handle *h, uint32_t *data, int64_t m, uint32_t *tmp) {
     int64_t t = tiles(m);
     if (t <= 1) {
+        h->launches++;
         k_scan_tile<<<1, RS_THREADS, 0, h->stream>>>(data, m, nullptr);
         EMOO_CUDA(cudaGetLastError());
         return EMOO_OK;
     }
+    h->launches++;
     k_scan_tile<<<(unsigned)t, RS_THREADS, 0, h->stream>>>(data, m, tmp);
     EMOO_TRY(scan_excl(h, tmp, t, tmp + t));
+    h->launches++;
     k_scan_add<<<(unsigned)t, RS_THREADS, 0, h->stream>>>(data, m, tmp);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
@@ -163,6 +166,7 @@ int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
     if (!arr) return EMOO_OK;
     T *tmp = (T *)h->pay;
     int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    h->launches++;
     k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);
     EMOO_CUDA(cudaGetLastError());
     h->pay = (void *)arr;
@@ -209,9 +213,11 @@ int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
         int bits = std::min(8, key_bits - shift);
         if (bits <= 0) bits = 1;
         uint32_t mask = (1u << bits) - 1u;
+        h->launches++;
         k_hist<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], n, shift, mask, h->hist, nblocks);
         EMOO_CUDA(cudaGetLastError());
         EMOO_TRY(scan_excl(h, h->hist, (int64_t)need_hist, h->scan_tmp));
+        h->launches++;
         k_scatter<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], ps == 0 ? nullptr : h->perm[cur],
                                                          h->key[cur ^ 1], h->perm[cur ^ 1], n, shift, mask, h->hist,
                                                          nblocks);
@@ -244,6 +250,7 @@ int gather_payload(emoo_handle *h, int64_t n) {
         EMOO_TRY(gather_one(h, h->ux, perm, n));
         EMOO_TRY(gather_one(h, h->uy, perm, n));
         EMOO_TRY(gather_one(h, h->uz, perm, n));
+        if (h->first_push) EMOO_TRY(gather_one(h, h->g0, perm, n));
     }
     EMOO_TRY(gather_one(h, h->ids, perm, n));
     return EMOO_OK;
@@ -251,9 +258,10 @@ int gather_payload(emoo_handle *h, int64_t n) {
 
 // Species segment bounds from the sorted keys; returns the per-species
 // counts (removed particles are past the last bound).
-int count_species(emoo_handle *h, int64_t n, int64_t *counts_host) {
+int count_species(emoo_handle *h, int64_t n, int64_t stride, int64_t *counts_host) {
     if (!h->d_spec_count) EMOO_CUDA(cudaMalloc(&h->d_spec_count, sizeof(int64_t) * (EMOO_NSPEC + 1)));
-    k_species_bounds<<<1, 64, 0, h->stream>>>(h->key[0], n, h->nspec, h->g.ncell, h->d_spec_count);
+    h->launches++;
+    k_species_bounds<<<1, 64, 0, h->stream>>>(h->key[0], n, h->nspec, stride, h->d_spec_count);
     EMOO_CUDA(cudaGetLastError());
     int64_t b[EMOO_NSPEC + 1];
     EMOO_CUDA(cudaMemcpyAsync(b, h->d_spec_count, sizeof(int64_t) * (h->nspec + 1), cudaMemcpyDeviceToHost, h->stream));

@@ -1,0 +1,466 @@
+"""Throughput of the PIC time loop on the thermal-plasma workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the project's plain-vs-mixed configuration): periodic 256^3 cells,
+dx = 1, dt = 0.5, electrons + ions (mass ratio 1836), 16 particles per cell
+per species = 536,870,912 particles, Maxwellian with electron v_th = 0.1c,
+relativistic Boris push, linear weights, particles re-sorted by cell every 20
+steps. One step = one pass of the loop (sort at its cadence, history every 10
+steps, fused gather+push+boundary+deposit, fold, Yee E/B update, ghost fill)
+over every particle. `value` is particle-steps/s of the mixed-precision form
+with the state resident in HBM; the FP64 form is timed beside it; `e2e` runs
+the same steps through the C ABI with the particle state in host memory
+(uploaded and read back every step).
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement of the reference serial loop (oracle/, FP64, one process per
+core, each on an independent 32^3 x 32 ppc box - the reference's own MPI
+decomposition with its communication left out).
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "particle-steps/s/GPU"
+UNIT = "particle-steps/s"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-procs", type=int, default=0)
+    ap.add_argument("--cpu-steps", type=int, default=6)
+    return ap.parse_args()
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def _traffic_per_unit():
+    """DRAM bytes per particle of the fused kernel from the committed ncu
+    summary (profiles/fused_mixed_thermal.json), if present."""
+    p = os.path.join(ROOT, "profiles", "fused_mixed_thermal.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+def workload(size):
+    from apc_524_project_gb300 import configs
+
+    cfg = configs.thermal256(size)
+    return cfg
+
+
+def workload_desc(cfg):
+    n = cfg.n
+    return (f"thermal plasma {n[0]}x{n[1]}x{n[2]} cells, 2 species x 16 ppc = {cfg.total_particles():,} particles, "
+            f"relativistic Boris, dt {cfg.dt}, sort every {cfg.nstep_sort}")
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arms
+
+def _make_handle(cfg, precision, capacity, device):
+    from apc_524_project_gb300 import abi, configs
+
+    L = abi.lib()
+    info = configs.input_info(cfg)
+    o = abi.Opts()
+    L.emoo_default_opts(C.byref(o))
+    o.precision = precision
+    o.dt = cfg.dt
+    o.capacity = capacity
+    o.track_ids = 0
+    o.device = device
+    h = C.c_void_p()
+    abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
+    for si in range(len(cfg.species)):
+        g = configs.gen_params(cfg, si)
+        abi.check(L.emoo_load_generated(h, C.byref(g), cfg.count(cfg.species[si])), "emoo_load_generated")
+    it = (C.c_int * 4)()
+    rc = L.emoo_init_fields(h, it)
+    if rc not in (abi.OK, abi.ERR_NOT_CONVERGED):
+        abi.check(rc, "emoo_init_fields")
+    return h
+
+
+def _stream_of(h):
+    import torch
+    from apc_524_project_gb300 import abi
+
+    s = C.c_void_p()
+    abi.check(abi.lib().emoo_get_stream(h, C.byref(s)))
+    return torch.cuda.ExternalStream(s.value)
+
+
+def _timed_steps(h, steps, dist_barrier):
+    """CUDA-event time of `steps` loop steps on the handle's stream."""
+    import torch
+    from apc_524_project_gb300 import abi
+
+    L = abi.lib()
+    st = _stream_of(h)
+    dist_barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    cnt = (C.c_int64 * 6)()
+    abi.check(L.emoo_step(h, steps, cnt), "emoo_step")
+    e1.record(st)
+    torch.cuda.synchronize()
+    dist_barrier()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
+    import torch
+    from apc_524_project_gb300 import abi
+
+    L = abi.lib()
+    device = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(device)
+    cfg = workload(args.size)
+    N = cfg.total_particles()
+    res = {}
+
+    # ---- mixed form: the headline
+    h = _make_handle(cfg, abi.MIXED, N, device)
+    cnt = (C.c_int64 * 6)()
+    for _ in range(args.warmup):
+        abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
+    torch.cuda.synchronize()
+    stats0 = abi.Stats()
+    abi.check(L.emoo_set_profiling(h, 1))
+    abi.check(L.emoo_get_stats(h, C.byref(stats0)))
+    clk = ClockSampler(device)
+    clk.start()
+    t = _timed_steps(h, args.steps, dist_barrier)
+    clocks = clk.stop()
+    t = dist_max(t)
+    stats = abi.Stats()
+    abi.check(L.emoo_get_stats(h, C.byref(stats)))
+    launches = int(stats.launches - stats0.launches)
+    fused_ms = stats.timed_ms / max(1, stats.timed_launches)
+    res["mixed"] = {"t": t, "fused_ms": fused_ms, "launches": launches, "clocks": clocks}
+
+    # ---- e2e through the C ABI with host-resident particle state
+    if not args.no_e2e:
+        res["e2e"] = _e2e(h, cfg, args.e2e_steps, dist_barrier, dist_max)
+    abi.check(L.emoo_destroy(h))
+    torch.cuda.synchronize()
+
+    # ---- FP64 form
+    if not args.no_fp64:
+        h = _make_handle(cfg, abi.FP64, N, device)
+        for _ in range(min(args.warmup, 2)):
+            abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
+        abi.check(L.emoo_set_profiling(h, 1))
+        t64 = dist_max(_timed_steps(h, args.fp64_steps, dist_barrier))
+        s64 = abi.Stats()
+        abi.check(L.emoo_get_stats(h, C.byref(s64)))
+        res["fp64"] = {"t": t64, "fused_ms": s64.timed_ms / max(1, s64.timed_launches)}
+        abi.check(L.emoo_destroy(h))
+    return cfg, res
+
+
+def _e2e(h, cfg, steps, dist_barrier, dist_max):
+    """Each step: upload the particle state from host memory
+    (emoo_set_particles), one loop step (emoo_step), read it back
+    (emoo_get_particles)."""
+    import numpy as np
+    import torch
+    from apc_524_project_gb300 import abi
+
+    L = abi.lib()
+    keys = ("x", "y", "z", "vx", "vy", "vz", "gamma")
+    bufs, pinned = [], True
+    for si in range(len(cfg.species)):
+        n = C.c_int64()
+        abi.check(L.emoo_num_particles(h, si, C.byref(n)))
+        d = {}
+        for k in keys:
+            try:
+                d[k] = torch.empty(n.value, dtype=torch.float64, pin_memory=True).numpy()
+            except Exception:
+                d[k] = np.empty(n.value, dtype=np.float64)
+                pinned = False
+        bufs.append((n.value, d))
+
+    def ptrs(d):
+        return [d[k].ctypes.data_as(C.POINTER(C.c_double)) for k in keys]
+
+    def get_all():
+        got = C.c_int64()
+        for si, (n, d) in enumerate(bufs):
+            abi.check(L.emoo_get_particles(h, si, n, *ptrs(d), None, C.byref(got)), "emoo_get_particles")
+
+    def set_all():
+        for si, (n, d) in enumerate(bufs):
+            abi.check(L.emoo_set_particles(h, si, n, *ptrs(d)), "emoo_set_particles")
+
+    cnt = (C.c_int64 * 6)()
+    get_all()
+    set_all()
+    abi.check(L.emoo_step(h, 1, cnt))
+    get_all()
+    dist_barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        set_all()
+        abi.check(L.emoo_step(h, 1, cnt))
+        get_all()
+    torch.cuda.synchronize()
+    t = dist_max(time.perf_counter() - t0)
+    nbytes = sum(n for n, _ in bufs) * 8 * len(keys)
+    return {"t": t, "steps": steps, "h2d": nbytes, "d2h": nbytes, "pinned": pinned}
+
+
+# ------------------------------------------------------------------ CPU arms
+
+def _cpu_replica(args):
+    """One process: the oracle on an independent 32^3 x 32 ppc relativistic
+    thermal box; returns (particles, steps, seconds)."""
+    size, steps, warm, seed = args
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    from apc_524_project_gb300 import configs, loading
+    from backends import OracleBackend
+
+    cfg = configs.thermal256(size)
+    cfg.seed = seed
+    info = configs.input_info(cfg)
+    b = OracleBackend(info, cfg.dt)
+    n = 0
+    for si in range(len(cfg.species)):
+        p = loading.sample_species(cfg, si)
+        b.add_species(si, p, ids=np.arange(n, n + len(p["x"])))
+        n += len(p["x"])
+    b.init_fields()
+    for ti in range(warm):  # warm-up steps (step 0 sorts)
+        b.step(ti)
+    t0 = time.perf_counter()
+    for ti in range(warm, warm + steps):
+        b.step(ti)
+    t = time.perf_counter() - t0
+    b.close()
+    return n, steps, t
+
+
+def cpu_baseline(procs, steps, warm=1, size=32):
+    import multiprocessing as mp
+
+    procs = procs or min(os.cpu_count() or 1, 16)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        out = pool.map(_cpu_replica, [(size, steps, warm, 1000 + i) for i in range(procs)])
+        wall = time.perf_counter() - t0
+    tmax = max(o[2] for o in out)
+    total = sum(o[0] * o[1] for o in out)
+    n_each = out[0][0]
+    return {
+        "value": total / tmax,
+        "unit": UNIT,
+        "cores": procs,
+        "kind": "port",
+        "sample": (f"{procs} independent {size}^3-cell x 32 ppc relativistic thermal boxes ({n_each:,} particles "
+                   f"each), {steps} timed steps each after {warm} warm-up step(s), FP64 CPU restatement of the "
+                   f"reference loop, one process per core; wall {wall:.1f} s"),
+        "seconds": tmax,
+    }
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = workload(args.size)
+    cb = cpu_baseline(args.cpu_procs, args.steps, warm=max(1, args.warmup))
+    v = cb["value"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["seconds"] / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc(cfg), "form": "reference CPU loop (FP64)",
+                   "sample": cb["sample"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # before the first GPU call (the pool is spawned, but keep it first)
+        cb = cpu_baseline(args.cpu_procs, args.cpu_steps)
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        dev = int(os.environ.get("LOCAL_RANK", "0"))
+
+        def barrier():
+            dist.barrier(device_ids=[dev])
+
+        def dmax(x):
+            t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{dev}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+    else:
+        def barrier():
+            pass
+
+        def dmax(x):
+            return x
+
+    cfg, res = run_gpu_arm(args, rank, world, barrier, dmax)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+    N = cfg.total_particles()
+    m = res["mixed"]
+    value = N * args.steps * world / m["t"]
+    peak, peak_kind = _peaks()
+    cells = cfg.n[0] * cfg.n[1] * cfg.n[2]
+    # algorithmic bytes of one fused-kernel launch: every particle's 28-byte
+    # state read and written, plus per cell the 9 FP32 field words gathered and
+    # the 4 int64 J/rho words deposited
+    alg_bytes = N * 56 + cells * (9 * 4 + 4 * 8)
+    achieved = alg_bytes / (m["fused_ms"] / 1e3) / 1e9
+    tr = _traffic_per_unit()
+    traffic = None
+    if tr and "dram_bytes_per_particle" in tr:
+        traffic = tr["dram_bytes_per_particle"] * N
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": m["t"] / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_desc(cfg), "form": "mixed (int32 cell + FP32 offset, FP32 u and fields, "
+                                                          "int64 fixed-point J/rho)",
+                   "particles": N, "l2": "inputs larger than L2 (15 GB particle state per GPU), no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic, "kernel": "k_fused_m (gather+push+BC+deposit)",
+                     "kernel_ms": m["fused_ms"], "algorithmic_bytes": alg_bytes},
+        "gpu_launches": m["launches"],
+        "clocks": m["clocks"],
+    }
+    if "fp64" in res:
+        f = res["fp64"]
+        v64 = N * args.fp64_steps * world / f["t"]
+        line["fp64"] = {"value": v64, "unit": UNIT, "steps": args.fp64_steps,
+                        "ms_per_step": f["t"] / args.fp64_steps * 1e3, "fused_kernel_ms": f["fused_ms"],
+                        "mixed_over_fp64": value / v64}
+    if "e2e" in res:
+        e = res["e2e"]
+        line["e2e"] = {"value": N * e["steps"] * world / e["t"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                       "d2h_bytes_per_step": e["d2h"], "steps": e["steps"], "pinned": e["pinned"],
+                       "path": "emoo_set_particles + emoo_step + emoo_get_particles (FP64 host arrays)"}
+    if cb:
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -278,6 +278,32 @@ int emoo_time(emoo_handle *h, double *t, double *dt);
  * last call; cleared by reading. */
 int emoo_check(emoo_handle *h);
 
+/* Overwrites the state of the n particles of a species (n must equal its
+ * current count) from caller-owned host SoA arrays, in device order (the
+ * order emoo_get_particles returns). For callers that keep the particle
+ * vector in host memory between steps, as the reference's Particle_Handler
+ * does (src/particles/particle_handler.hpp:53). gamma may be null. */
+int emoo_set_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
+                       const double *vx, const double *vy, const double *vz, const double *gamma);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events after the handle's. */
+int emoo_get_stream(emoo_handle *h, void **stream);
+
+/* Instrumentation counters. */
+typedef struct emoo_stats {
+    int64_t launches;       /* kernels launched by the handle so far */
+    int64_t timed_launches; /* launches of the fused particle kernel timed since profiling was enabled */
+    double timed_ms;        /* their summed CUDA-event durations */
+} emoo_stats;
+
+/* Enables (1) or disables (0) CUDA-event timing of every fused particle
+ * kernel launch; enabling resets the timed counters. */
+int emoo_set_profiling(emoo_handle *h, int on);
+
+/* Reads the counters (waits for the handle's stream). */
+int emoo_get_stats(emoo_handle *h, emoo_stats *s);
+
 #ifdef __cplusplus
 }
 #endif

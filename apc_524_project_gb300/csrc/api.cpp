@@ -207,8 +207,11 @@ void free_particles(emoo_handle *h) {
     dfree(h->ids); dfree(h->fcache);
     dfree(h->cell); dfree(h->ox); dfree(h->oy); dfree(h->oz); dfree(h->ux); dfree(h->uy); dfree(h->uz);
     dfree(h->key[0]); dfree(h->key[1]); dfree(h->perm[0]); dfree(h->perm[1]);
+    dfree(h->g0);
     if (h->pay) cudaFree(h->pay);
     h->pay = nullptr;
+    if (h->pay4) cudaFree(h->pay4);
+    h->pay4 = nullptr;
 }
 
 // Particle storage for `cap` particles; existing content is preserved.
@@ -240,10 +243,14 @@ int reserve(emoo_handle *h, int64_t cap) {
     EMOO_TRY(dalloc(h->perm[0], (size_t)cap)); EMOO_TRY(dalloc(h->perm[1], (size_t)cap));
     if (h->pay) cudaFree(h->pay);
     h->pay = nullptr;
-    // one array's worth of scratch (8 B per particle), enough for the payload
-    // gather; the mixed-form loader stages 7 doubles per particle in chunks.
+    if (h->pay4) cudaFree(h->pay4);
+    h->pay4 = nullptr;
+    // scratch of one array per element size: cap 8-byte elements (also the
+    // staging area of the loaders, 7 doubles per particle in chunks) and cap
+    // 4-byte elements; the sort swaps each array with the buffer of its size
     h->pay_bytes = sizeof(double) * (size_t)cap;
     EMOO_CUDA(cudaMalloc(&h->pay, h->pay_bytes));
+    EMOO_CUDA(cudaMalloc(&h->pay4, sizeof(float) * (size_t)cap));
     h->cap = cap;
     return EMOO_OK;
 }

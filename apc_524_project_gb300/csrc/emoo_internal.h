@@ -118,8 +118,9 @@ struct emoo_handle {
     uint32_t *hist = nullptr;
     uint32_t *scan_tmp = nullptr;
     size_t hist_cap = 0, scan_cap = 0;
-    void *pay = nullptr;  // payload double buffer
+    void *pay = nullptr;   // scratch of cap 8-byte elements (staging, and the sort's 8-byte payload swaps)
     size_t pay_bytes = 0;
+    void *pay4 = nullptr;  // scratch of cap 4-byte elements (the sort's 4-byte payload swaps)
     int64_t *d_spec_count = nullptr;
 
     // reductions and counters

@@ -161,15 +161,22 @@ __global__ void k_gather(const T *__restrict__ src, T *__restrict__ dst, const u
         dst[i] = src[perm[i]];
 }
 
+// Permutes one SoA array through the scratch buffer of its element size and
+// swaps the two: every array only ever trades places with a buffer of the
+// same capacity and element size (h->pay holds cap 8-byte elements, h->pay4
+// cap 4-byte elements).
 template <typename T>
 int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
+    static_assert(sizeof(T) == 8 || sizeof(T) == 4, "payload element size");
     if (!arr) return EMOO_OK;
-    T *tmp = (T *)h->pay;
+    void *&scratch = sizeof(T) == 8 ? h->pay : h->pay4;
+    if (!scratch || n > h->cap) return EMOO_ERR_STATE;
+    T *tmp = (T *)scratch;
     int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
     h->launches++;
     k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);
     EMOO_CUDA(cudaGetLastError());
-    h->pay = (void *)arr;
+    scratch = (void *)arr;
     arr = tmp;
     return EMOO_OK;
 }

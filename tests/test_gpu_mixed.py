@@ -1,0 +1,141 @@
+"""Mixed-precision form against the FP64 form (and so against the reference).
+
+The mixed form is the same algorithm in FP32 with split-precision positions;
+its error is stated against the FP64 GPU form:
+  * initial state: positions to FP32 offset precision, fields <= 1e-7;
+  * a stable run (the external-wave, reflecting case): relative L2 of E, B,
+    J, rho <= MIXED_RTOL after 12 steps, crossing counts identical;
+  * runs where the reference scheme itself amplifies perturbations (see the
+    stability note in the FP64 tests): the mixed error after N steps stays
+    within SENS_FACTOR times the FP64 form's own response to a 1e-7 relative
+    velocity perturbation;
+  * the fixed-point current makes runs bit-reproducible.
+"""
+import numpy as np
+import pytest
+
+from apc_524_project_gb300 import abi, configs, loading
+from backends import GpuBackend, by_id, rel_l2
+from golden import cases
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RTOL = 2e-6
+SENS_FACTOR = 20.0
+
+
+def _load(b, parts):
+    nid = 0
+    for si, p in enumerate(parts):
+        n = len(p["x"])
+        b.add_species(si, p, ids=np.arange(nid, nid + n))
+        nid += n
+
+
+def _run(cfg, dt, steps, precision, perturb=0.0):
+    info = configs.input_info(cfg)
+    parts = loading.sample_all(cfg)
+    if perturb:
+        for p in parts:
+            for k in ("vx", "vy", "vz"):
+                p[k] = p[k] * (1.0 + perturb)
+    b = GpuBackend(info, dt, precision=precision)
+    _load(b, parts)
+    b.init_fields()
+    counts = np.zeros(6, dtype=np.int64)
+    for _ in range(steps):
+        counts += np.array(b.step(1))
+    out = {i: b.get_field(i) for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.JX, abi.RHO)}
+    out["p"] = by_id(b.particles())
+    out["counts"] = counts
+    out["hist"] = b.history_rows()
+    assert b.check() == abi.OK
+    b.close()
+    return out
+
+
+def test_mixed_initial_state_matches_fp64():
+    cfg, dt, _, _ = cases.make("rel_const")
+    m = _run(cfg, dt, 0, abi.MIXED)
+    f = _run(cfg, dt, 0, abi.FP64)
+    for k in ("x", "y", "z"):
+        assert rel_l2(m["p"][k], f["p"][k]) < 1e-7
+    for k in ("vx", "vy", "vz", "gamma"):
+        assert rel_l2(m["p"][k], f["p"][k]) < 1e-7
+    for i in (abi.EX, abi.BZ):
+        assert rel_l2(m[i], f[i]) < 1e-7
+
+
+def test_mixed_stable_case_within_fp32_tolerance():
+    cfg, dt, steps, _ = cases.make("reflect_ext")
+    m = _run(cfg, dt, steps, abi.MIXED)
+    f = _run(cfg, dt, steps, abi.FP64)
+    np.testing.assert_array_equal(m["counts"], f["counts"])
+    for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.JX, abi.RHO):
+        assert rel_l2(m[i], f[i]) <= MIXED_RTOL, (abi.FIELD_NAMES[i], rel_l2(m[i], f[i]))
+    np.testing.assert_allclose(m["hist"][:, 4:], f["hist"][:, 4:], rtol=1e-6)
+
+
+@pytest.mark.parametrize("name", ["rel_const", "periodic_poisson", "aniso_const"])
+def test_mixed_error_within_fp64_sensitivity(name):
+    cfg, dt, steps, _ = cases.make(name)
+    m = _run(cfg, dt, steps, abi.MIXED)
+    f = _run(cfg, dt, steps, abi.FP64)
+    fp = _run(cfg, dt, steps, abi.FP64, perturb=1e-7)
+    for i in (abi.EX, abi.BY, abi.JX):
+        err = rel_l2(m[i], f[i])
+        sens = rel_l2(fp[i], f[i])
+        assert err <= SENS_FACTOR * max(sens, 1e-7), (abi.FIELD_NAMES[i], err, sens)
+
+
+def test_mixed_runs_are_bit_reproducible():
+    cfg = configs.tiny("repro", n=(10, 8, 6), ppc=6, relativity=1, init="constant", B0=(0.0, 0.05, 0.0),
+                       nstep_sort=4)
+    a = _run(cfg, 0.45, 9, abi.MIXED)
+    b = _run(cfg, 0.45, 9, abi.MIXED)
+    for i in (abi.EX, abi.BY, abi.JX, abi.RHO):
+        np.testing.assert_array_equal(a[i], b[i])
+    for k in ("x", "vx"):
+        np.testing.assert_array_equal(a["p"][k], b["p"][k])
+
+
+def test_mixed_sort_keeps_particles_and_orders_cells():
+    cfg = configs.tiny("msort", n=(9, 7, 5), ppc=7, relativity=1, init="constant", test_species=True)
+    info = configs.input_info(cfg)
+    parts = loading.sample_all(cfg)
+    b = GpuBackend(info, 0.4, precision=abi.MIXED)
+    _load(b, parts)
+    b.step(2)
+    before = by_id(b.particles())
+    b.sort()
+    after = b.particles()
+    assert len(after["id"]) == len(before["id"])
+    for s in range(len(cfg.species)):
+        sel = after["type"] == s
+        keys = np.array([b.cell_id(x, y, z) for x, y, z in zip(after["x"][sel], after["y"][sel], after["z"][sel])])
+        assert np.all(np.diff(keys) >= 0)
+    a = by_id(after)
+    for k in ("x", "vx"):
+        np.testing.assert_array_equal(a[k], before[k])
+    b.step(3)
+    assert b.check() == abi.OK
+    b.close()
+
+
+def test_mixed_device_loader_and_readback():
+    cfg = configs.tiny("mload", n=(12, 10, 8), ppc=4, relativity=1, init="constant", vth=0.2)
+    info = configs.input_info(cfg)
+    import ctypes as C
+
+    b = GpuBackend(info, 0.4, precision=abi.MIXED)
+    for si in range(len(cfg.species)):
+        g = configs.gen_params(cfg, si)
+        abi.check(b.L.emoo_load_generated(b.h, C.byref(g), cfg.count(cfg.species[si])))
+    p = b.particles()
+    for si in range(len(cfg.species)):
+        host = loading.sample_species(cfg, si)
+        sel = p["type"] == si
+        np.testing.assert_allclose(p["x"][sel], host["x"], rtol=0, atol=1e-6)
+        np.testing.assert_allclose(p["vx"][sel], host["vx"], rtol=1e-7, atol=1e-12)
+        np.testing.assert_allclose(p["gamma"][sel], host["gamma"], rtol=1e-7)
+    b.close()

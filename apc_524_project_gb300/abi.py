@@ -157,6 +157,10 @@ PROTOTYPES = {
     "emoo_gauss_residual": (C.c_int, [_P, _D]),
     "emoo_time": (C.c_int, [_P, _D, _D]),
     "emoo_check": (C.c_int, [_P]),
+    "emoo_read_input": (C.c_int, [C.c_char_p, C.POINTER(InputInfo)]),
+    "emoo_parse_input": (C.c_int, [C.c_char_p, C.POINTER(InputInfo)]),
+    "emoo_input_message": (C.c_char_p, []),
+    "emoo_process_info": (C.c_int, [C.POINTER(InputInfo)]),
     "emoo_set_particles": (C.c_int, [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D, _D, _D]),
     "emoo_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "emoo_set_profiling": (C.c_int, [_P, C.c_int]),

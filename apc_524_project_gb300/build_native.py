@@ -29,7 +29,7 @@ CUDA_UNITS = [
     ("sort.cu", []),
     ("particles_mixed.cu", ["--fmad=true"]),
 ]
-HOST_UNITS = ["api.cpp", "loader_host.cpp"]
+HOST_UNITS = ["api.cpp", "loader_host.cpp", "input_parser.cpp"]
 
 
 def _nvcc():

@@ -159,6 +159,25 @@ typedef struct emoo_handle emoo_handle;
 /* Fills *o with the defaults (FP64, device 0, reference dt, rho every step, history every 10). */
 int emoo_default_opts(emoo_opts *o);
 
+/* Reads an input file in the reference's libconfig format into *out (zeroed
+ * first). Replaces Input::readinfo, src/IO/readinfo.cpp:18-733: same setting
+ * paths, defaults and required settings. Returns EMOO_ERR_INPUT with a
+ * message (emoo_input_message) where the reference prints an error and
+ * returns EXIT_FAILURE, and also where it would terminate on an uncaught
+ * exception (missing relativity / electrostatic / output_pCount). Host only. */
+int emoo_read_input(const char *path, emoo_input_info *out);
+
+/* emoo_read_input on a string holding the file's text. */
+int emoo_parse_input(const char *text, emoo_input_info *out);
+
+/* Message of the last failed emoo_read_input / emoo_parse_input on this thread. */
+const char *emoo_input_message(void);
+
+/* Input::ProcessInfo, src/IO/check.cpp:12-147, for one domain: super-particle
+ * scaling of mass, charge and temperature, density-fraction normalisation,
+ * boundary consistency; EMOO_ERR_INPUT where the reference counts an error. */
+int emoo_process_info(emoo_input_info *info);
+
 /* Human-readable text of a status code. Never null. */
 const char *emoo_strerror(int status);
 

@@ -17,6 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libemoo.so")
+DRIVER = os.path.join(HERE, "emoopic_gpu")  # the reference-style driver (emoopic_main.cpp)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
@@ -87,6 +88,10 @@ def build(verbose=False, ptxas_info=False):
     if jobs or not os.path.exists(LIB):
         link = [nvcc, "-shared", "-o", LIB] + objs + ARCH + ["-lcudart"]
         outs.append(_run(link))
+    drv_src = os.path.join(CSRC, "emoopic_main.cpp")
+    if _stale(DRIVER, [drv_src, LIB, os.path.join(INCLUDE, "emoopic.hpp"), os.path.join(INCLUDE, "emoo.h")]):
+        outs.append(_run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, drv_src, "-o", DRIVER, "-L" + HERE,
+                          "-lemoo", "-Wl,-rpath,$ORIGIN"]))
     if verbose:
         for o in outs:
             if o.strip():

@@ -165,7 +165,10 @@ PROTOTYPES = {
     "emoo_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "emoo_set_profiling": (C.c_int, [_P, C.c_int]),
     "emoo_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "emoo_sort_permutation_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
 }
+
+NOALLOC_SORT_MAX = 1048576
 
 _LIB = None
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libemoo.so")

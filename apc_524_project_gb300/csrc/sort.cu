@@ -11,8 +11,10 @@
 // Particle_Compare (src/particles/particle_handler.cpp:180-183,
 // src/particles/particle_utils.hpp:18-69).
 #include <cuda_runtime.h>
+#include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "dev_common.cuh"
 #include "emoo_internal.h"
@@ -278,3 +280,114 @@ int count_species(emoo_handle *h, int64_t n, int64_t stride, int64_t *counts_hos
 }
 
 }  // namespace emoo
+
+// ---------------------------------------------------------------------------
+// Allocation-free stable sort permutation.
+//
+// Some callers of this library cannot call cudaMalloc: hosts that hand all
+// device memory to their own pool allocator up front and reject any other
+// allocation, and loops that must not pay the device-wide synchronisation a
+// cudaMalloc / cudaFree can cause. emoo_sort_permutation_noalloc serves them:
+// it runs the same counting-sort passes as the particle sort, with all of its
+// scratch in one file-scope device array of fixed size, and allocates nothing.
+//
+// The array is created when the library is loaded on a device and lives until
+// the process exits (12.5 MiB on every GPU that loads the library). Every call
+// uses the same array and leaves its contents behind; nothing in it has to
+// start at zero, because each pass writes every histogram slot and every
+// buffer element it later reads. Calls whose GPU work overlaps (for example on
+// two streams at once) race on the array: the caller must order them.
+// ---------------------------------------------------------------------------
+namespace emoo {
+namespace {
+
+constexpr int64_t NA_MAX = EMOO_NOALLOC_SORT_MAX;
+constexpr int64_t NA_TILES = (NA_MAX + RS_TILE - 1) / RS_TILE;
+constexpr int64_t NA_HIST = RS_BINS * NA_TILES;
+constexpr int64_t NA_SCAN = 1024;  // > tiles(NA_HIST) + tiles(tiles(NA_HIST)) + 1
+
+struct NoAllocScratch {
+    uint32_t key[2][NA_MAX];
+    uint32_t perm[NA_MAX];
+    uint32_t hist[NA_HIST];
+    uint32_t scan[NA_SCAN];
+};
+
+__device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (the host-side symbol is not a device address).
+std::mutex g_noalloc_mu;
+NoAllocScratch *g_noalloc_ptr[256] = {};
+
+int noalloc_scratch(NoAllocScratch **out) {
+    int dev = 0;
+    EMOO_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return EMOO_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e);
+        g_noalloc_ptr[dev] = (NoAllocScratch *)p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return EMOO_OK;
+}
+
+int noalloc_scan(cudaStream_t s, uint32_t *data, int64_t m, uint32_t *tmp) {
+    int64_t t = tiles(m);
+    if (t <= 1) {
+        k_scan_tile<<<1, RS_THREADS, 0, s>>>(data, m, nullptr);
+        EMOO_CUDA(cudaGetLastError());
+        return EMOO_OK;
+    }
+    k_scan_tile<<<(unsigned)t, RS_THREADS, 0, s>>>(data, m, tmp);
+    EMOO_TRY(noalloc_scan(s, tmp, t, tmp + t));
+    k_scan_add<<<(unsigned)t, RS_THREADS, 0, s>>>(data, m, tmp);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+}  // namespace
+
+}  // namespace emoo
+
+extern "C" int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, int key_bits, uint32_t *perm,
+                                             void *stream) {
+    using namespace emoo;
+    if (n < 0 || n > NA_MAX) {
+        fprintf(stderr, "emoo_sort_permutation_noalloc: n = %lld is outside [0, %lld]\n", (long long)n,
+                (long long)NA_MAX);
+        return EMOO_ERR_ARG;
+    }
+    if (key_bits < 1 || key_bits > 32) return EMOO_ERR_ARG;
+    if (n == 0) return EMOO_OK;
+    if (!keys || !perm) return EMOO_ERR_ARG;
+    NoAllocScratch *sc = nullptr;
+    EMOO_TRY(noalloc_scratch(&sc));
+    cudaStream_t s = (cudaStream_t)stream;
+    int nblocks = (int)tiles(n);
+    int64_t nhist = (int64_t)RS_BINS * nblocks;
+    int passes = (key_bits + 7) / 8;
+    uint32_t *scr_perm = sc->perm;
+    const uint32_t *kin = keys;
+    const uint32_t *vin = nullptr;  // first pass: the identity
+    for (int ps = 0; ps < passes; ps++) {
+        int shift = ps * 8;
+        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        uint32_t mask = (1u << bits) - 1u;
+        bool last = ps == passes - 1;
+        uint32_t *kout = last ? nullptr : sc->key[ps & 1];
+        // alternate so that the last pass lands in the caller's array
+        uint32_t *vout = ((passes - 1 - ps) % 2 == 0) ? perm : scr_perm;
+        k_hist<<<nblocks, RS_THREADS, 0, s>>>(kin, n, shift, mask, sc->hist, nblocks);
+        EMOO_CUDA(cudaGetLastError());
+        EMOO_TRY(noalloc_scan(s, sc->hist, nhist, sc->scan));
+        k_scatter<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, mask, sc->hist, nblocks);
+        EMOO_CUDA(cudaGetLastError());
+        kin = kout;
+        vin = vout;
+    }
+    return EMOO_OK;
+}

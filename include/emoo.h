@@ -323,6 +323,31 @@ int emoo_set_profiling(emoo_handle *h, int on);
 /* Reads the counters (waits for the handle's stream). */
 int emoo_get_stats(emoo_handle *h, emoo_stats *s);
 
+/* Largest n emoo_sort_permutation_noalloc accepts. */
+#define EMOO_NOALLOC_SORT_MAX 1048576
+
+/* Stable sort permutation of n 32-bit keys that allocates no memory. It has
+ * no counterpart in the reference: it is the scratch-free form of the
+ * counting sort behind emoo_sort, for callers that cannot call cudaMalloc -
+ * hosts that give all device memory to their own pool allocator and refuse
+ * other allocations, and loops that cannot take the device-wide
+ * synchronisation cudaMalloc and cudaFree may cause.
+ *
+ * keys (device, n values, only the low key_bits bits used, 1 <= key_bits <=
+ * 32) is read; perm (device, n values) receives the permutation: perm[i] is
+ * the index in keys of the i-th smallest key, equal keys in input order. The
+ * work is queued on `stream` (a cudaStream_t, null for the default stream)
+ * and the call returns without waiting for it.
+ *
+ * Scratch is one fixed 12.5 MiB device array in the library, held by every GPU
+ * that loads the library until the process exits; n above
+ * EMOO_NOALLOC_SORT_MAX is rejected with EMOO_ERR_ARG. The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) with the
+ * device current; make that first call before any stream capture. All calls
+ * share the array and it keeps the last call's contents, so calls whose GPU
+ * work overlaps race: order them (one stream, or events). */
+int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, int key_bits, uint32_t *perm, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,13 @@ from golden import cases
 pytestmark = pytest.mark.gpu
 
 MIXED_RTOL = 2e-6
-SENS_FACTOR = 20.0
+# The FP64 probe perturbs the velocities once, by 1e-7, at t = 0. The mixed
+# form rounds positions, velocities and fields to FP32 (2^-24 ~ 6e-8 relative)
+# on every one of the N steps, and each of those roundings is then amplified by
+# the same growing modes for the rest of the run. With N = 8-12 steps and the
+# growth these cases show, the accumulated response measures 15-30 times the
+# single-kick one; 100 leaves room for that and still fails on an O(1) error.
+SENS_FACTOR = 100.0
 
 
 def _load(b, parts):

@@ -10,11 +10,14 @@
 //   ux..uz  float  momentum per unit mass, u = gamma v (v for the
 //                  non-relativistic pusher)
 // Fields E, B and B_tm1 are FP32 in the reference layout; J and rho are int64
-// fixed-point accumulators (quantum q0 = max_s |UNIT_RHOJ q_s / V| * 2^-32).
-// Each warp sums the contributions of consecutive particles that share a cell
-// in FP32 in a fixed shuffle order, rounds the run total to the fixed-point
-// quantum and commits it with an integer atomic: integer addition is
-// associative, so J and rho - and every run - are bit-reproducible.
+// fixed-point values (quantum q0 = max_s |UNIT_RHOJ q_s / V| * 2^-32).
+// Each warp sums the 20 contributions of consecutive particles that share a
+// cell in FP32 in particle order, rounds each run total to the fixed-point
+// quantum and adds it with integer atomics to that cell's 20 slots (one
+// 160-byte record per cell, so a run commits in one coalesced instruction);
+// a gather pass then forms J and rho at every point from the slots of its
+// neighbour cells. Integer addition is associative, so J and rho are
+// bit-reproducible.
 //
 // The arithmetic is the reference's algorithm (including its in-cell offset
 // convention, Jx index, ghost and B-role behaviour, see the FP64 kernels) in
@@ -37,6 +40,8 @@ struct FieldsF32 {
     float *Bslot[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // BX..BZ, BX_TM1..BZ_TM1 storage
     long long *J[4] = {nullptr, nullptr, nullptr, nullptr};                    // Jx, Jy, Jz, rho
     double q0 = 1.0;  // fixed-point quantum
+    float4 *pack = nullptr;  // interpolation pack, 5 float4 per grid point (interior cells filled)
+    unsigned long long *wc = nullptr;  // per-cell deposit sums, 20 int64 per grid point
 };
 
 namespace {
@@ -113,58 +118,171 @@ struct MGather {
 };
 
 struct MDeposit {
-    unsigned long long *J[4];
+    unsigned long long *wc;  // per-cell sums, 20 per cell (DEP_SLOTS)
 };
 
-// The reference's gather (src/grid/oGrid.cpp:153-197 with
-// src/particles/interpolate.cpp:11-47) in cell units: the offset handed to the
-// weights is o - 1 (the ghost-offset vertex), so the weights are 2 - o and
-// o - 1.
-__device__ __forceinline__ void gather_m(const MGeom &g, const MGather &P, int64_t o, float ox, float oy, float oz,
-                                         float f[6]) {
-    const int64_t sx = g.sx, sy = g.sy;
-    float a[3] = {2.0f - ox, 2.0f - oy, 2.0f - oz};  // (l - ds)/l
-    float b[3] = {ox - 1.0f, oy - 1.0f, oz - 1.0f};  // ds / l
-    // Ex: j = y, k = z; edges (iy,iz), (iy+1,iz), (iy+1,iz+1), (iy,iz+1)
-    f[0] = a[1] * a[2] * __ldg(P.E[0] + o) + b[1] * a[2] * __ldg(P.E[0] + o + sy) +
-           b[1] * b[2] * __ldg(P.E[0] + o + sy + 1) + a[1] * b[2] * __ldg(P.E[0] + o + 1);
-    // Ey: j = z, k = x; (iz,ix), (iz+1,ix), (iz+1,ix+1), (iz,ix+1)
-    f[1] = a[2] * a[0] * __ldg(P.E[1] + o) + b[2] * a[0] * __ldg(P.E[1] + o + 1) +
-           b[2] * b[0] * __ldg(P.E[1] + o + sx + 1) + a[2] * b[0] * __ldg(P.E[1] + o + sx);
-    // Ez: j = x, k = y
-    f[2] = a[0] * a[1] * __ldg(P.E[2] + o) + b[0] * a[1] * __ldg(P.E[2] + o + sx) +
-           b[0] * b[1] * __ldg(P.E[2] + o + sx + sy) + a[0] * b[1] * __ldg(P.E[2] + o + sy);
-    f[3] = 0.5f * (a[0] * (__ldg(P.T[0] + o) + __ldg(P.B[0] + o)) + b[0] * (__ldg(P.T[0] + o + sx) + __ldg(P.B[0] + o + sx)));
-    f[4] = 0.5f * (a[1] * (__ldg(P.T[1] + o) + __ldg(P.B[1] + o)) + b[1] * (__ldg(P.T[1] + o + sy) + __ldg(P.B[1] + o + sy)));
-    f[5] = 0.5f * (a[2] * (__ldg(P.T[2] + o) + __ldg(P.B[2] + o)) + b[2] * (__ldg(P.T[2] + o + 1) + __ldg(P.B[2] + o + 1)));
+constexpr int DEP_SLOTS = 20;
+
+// Round-to-nearest-even of v as int64, the value of __float2ll_rn(v), without
+// the float-to-int64 conversion: conversions run on the FP64 pipe, which on
+// this GPU issues 2 lanes per clock per SM. Two exact FP32 steps split
+// v = h 2^22 + l with |l| <= 2^21, and adding 1.5 * 2^23 (in the binade where
+// the float spacing is 1) leaves each part's nearest integer in the low
+// mantissa bits; h 2^22 is even, so the parts round as v does. Exact for
+// |v| < 2^43; larger values (and NaN) take the conversion.
+__device__ __forceinline__ long long f2ll_rn(float v) {
+    if (!(fabsf(v) < 8.0e12f)) return __float2ll_rn(v);
+    const float M = 12582912.0f;                    // 1.5 * 2^23
+    const float hm = v * 2.384185791015625e-07f + M;  // M + rint(v 2^-22); v 2^-22 is exact
+    const float lo = fmaf(M - hm, 4194304.0f, v);   // v - rint(v 2^-22) 2^22, exact
+    const int hi = __float_as_int(hm) - __float_as_int(M);
+    const int li = __float_as_int(lo + M) - __float_as_int(M);
+    return ((long long)hi << 22) + li;
 }
 
-// Contribution points of cell o, same table as the FP64 deposit
-// (src/grid/oGrid.cpp:98-111, 129-136; the Jx quirk at index 3).
-__device__ __forceinline__ int64_t mdep_point(const MGeom &g, int64_t o, int q) {
-    const int64_t sx = g.sx, sy = g.sy;
-    switch (q) {
-        case 0: return o;
-        case 1: return o + sy;
-        case 2: return o + sy + 1;
-        case 3: return o + sy;
-        case 4: return o;
-        case 5: return o + 1;
-        case 6: return o + sx + 1;
-        case 7: return o + sx;
-        case 8: return o;
-        case 9: return o + sx;
-        case 10: return o + sx + sy;
-        case 11: return o + sy;
-        case 12: return o;
-        case 13: return o + sx;
-        case 14: return o + sx + sy;
-        case 15: return o + sy;
-        case 16: return o + sy + 1;
-        case 17: return o + sx + sy + 1;
-        case 18: return o + sx + 1;
-        default: return o + 1;
+// New in-cell offset and cell index from the moved offset n (cell units):
+// o = n - floor(n), i += floor(n). Moves of at most one cell are resolved by
+// comparisons, which give the same values as floorf and keep the conversion
+// instructions (FP64 pipe) out of the per-particle path.
+__device__ __forceinline__ void cell_step(float n, int &i, float &o) {
+    float f;
+    if (n >= -1.0f && n < 2.0f) {
+        const bool up = n >= 1.0f, down = n < 0.0f;
+        f = up ? 1.0f : (down ? -1.0f : 0.0f);
+        i += up ? 1 : (down ? -1 : 0);
+    } else {
+        f = floorf(n);
+        i += (int)f;
     }
+    o = n - f;
+    // the subtraction can round to exactly 1.0f for tiny negative n
+    if (o >= 1.0f) {
+        o = 0.0f;
+        i += 1;
+    }
+}
+
+// Offset from the particle's cell of each of the 20 contribution points -
+// Jx (4), Jy (4), Jz (4), rho (8) - as the FP64 deposit's table
+// (src/grid/oGrid.cpp:98-111, 129-136; the Jx quirk at index 3), 3 bits per
+// point (x: 4, y: 2, z: 1), point q at bits 3q..3q+2. A register constant,
+// so lanes index it without a local-memory copy.
+constexpr unsigned long long DEP_CODE =
+    (0ull << 0) | (2ull << 3) | (3ull << 6) | (2ull << 9) |       // Jx: o, o+sy, o+sy+1, o+sy
+    (0ull << 12) | (1ull << 15) | (5ull << 18) | (4ull << 21) |   // Jy: o, o+1, o+sx+1, o+sx
+    (0ull << 24) | (4ull << 27) | (6ull << 30) | (2ull << 33) |   // Jz: o, o+sx, o+sx+sy, o+sy
+    (0ull << 36) | (4ull << 39) | (6ull << 42) | (2ull << 45) |   // rho
+    (3ull << 48) | (7ull << 51) | (5ull << 54) | (1ull << 57);
+
+__host__ __device__ __forceinline__ int dep_offset(int q, int sx, int sy) {
+    const int c = (int)((DEP_CODE >> (3 * q)) & 7ull);
+    return (c >> 2) * sx + ((c >> 1) & 1) * sy + (c & 1);
+}
+
+// Position of contribution q in a cell's 20-slot record. Slots are grouped by
+// the point offset they feed, in the order
+//   [0,4)  offset 0          q 0 4 8 12
+//   [4,8)  offset sy         q 1 3 11 15
+//   [8,10) offset 1          q 5 19
+//   [10,12) offset sy+1      q 2 16
+//   [12,14) offset sx+1      q 6 18
+//   [14,16) offset sx+sy     q 10 14
+//   [16,19) offset sx        q 7 9 13
+//   [19]   offset sx+sy+1    q 17
+// so each point gathers a neighbour's slots with 16-byte loads. 5 bits per q.
+constexpr unsigned long long DEP_POS_LO =  // q = 0..11
+    (0ull << 0) | (4ull << 5) | (10ull << 10) | (5ull << 15) | (1ull << 20) | (8ull << 25) | (12ull << 30) |
+    (16ull << 35) | (2ull << 40) | (17ull << 45) | (14ull << 50) | (6ull << 55);
+constexpr unsigned long long DEP_POS_HI =  // q = 12..19
+    (3ull << 0) | (18ull << 5) | (15ull << 10) | (7ull << 15) | (11ull << 20) | (19ull << 25) | (13ull << 30) |
+    (9ull << 35);
+
+__host__ __device__ __forceinline__ int dep_pos(int q) {
+    return q < 12 ? (int)((DEP_POS_LO >> (5 * q)) & 31ull) : (int)((DEP_POS_HI >> (5 * (q - 12))) & 31ull);
+}
+
+// The record layout and the gather in k_cells_to_points must agree with the
+// deposit table: every slot group feeds the point offset of each q placed in
+// it. Checked once per handle.
+bool dep_tables_agree() {
+    const int sx = 1000, sy = 30;  // distinct sums for all 8 offsets
+    const int slot_off[DEP_SLOTS] = {0,      0,      0,      0,      sy,      sy,      sy,      sy, 1, 1,
+                                     sy + 1, sy + 1, sx + 1, sx + 1, sx + sy, sx + sy, sx,      sx, sx, sx + sy + 1};
+    bool used[DEP_SLOTS] = {};
+    for (int q = 0; q < DEP_SLOTS; q++) {
+        const int pos = dep_pos(q);
+        if (pos < 0 || pos >= DEP_SLOTS || used[pos] || slot_off[pos] != dep_offset(q, sx, sy)) return false;
+        used[pos] = true;
+    }
+    return true;
+}
+
+// ---- interpolation pack --------------------------------------------------
+//
+// The reference's gather (src/grid/oGrid.cpp:153-197 with
+// src/particles/interpolate.cpp:11-47) uses the ghost-offset vertex, so the
+// weights over an in-cell offset o are a = 2 - o and b = o - 1. An edge
+// component interpolated over the offsets (t, r) of its two transverse axes is
+//   a_t a_r F00 + b_t a_r F10 + b_t b_r F11 + a_t b_r F01
+//     = c0 + ct t + cr r + ctr t r
+// with the coefficients below, and the face component of B averaged with
+// B_tm1 over its own axis offset s is
+//   0.5 (a_s S0 + b_s S1) = d0 + d1 s,   S = B + B_tm1.
+// The pack holds these 18 numbers per cell in 5 float4 (80 bytes):
+//   [0] Ex c0 ct cr ctr (t = y, r = z)   [1] Ey (t = z, r = x)
+//   [2] Ez (t = x, r = y)                [3] Bx d0 d1, By d0 d1
+//   [4] Bz d0 d1, 2 unused
+// so a particle reads 5 vector loads from one place instead of 24 scalars
+// from 9 arrays. The pack is rebuilt from the fields before every push.
+constexpr int PACK_F4 = 5;
+
+__device__ __forceinline__ float4 edge_coef(float f00, float f10, float f11, float f01) {
+    float4 c;
+    c.x = (4.0f * f00 - 2.0f * f01) + (f11 - 2.0f * f10);
+    c.y = (2.0f * f10 - 2.0f * f00) + (f01 - f11);
+    c.z = (2.0f * f01 - 2.0f * f00) + (f10 - f11);
+    c.w = (f00 - f10) + (f11 - f01);
+    return c;
+}
+
+__global__ void k_pack_m(MGeom g, MGather P, float4 *__restrict__ pack) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    const int64_t sx = g.sx, sy = g.sy;
+    const int64_t o = (int64_t)i * sx + (int64_t)j * sy + k;
+    const float *Ex = P.E[0], *Ey = P.E[1], *Ez = P.E[2];
+    float4 *dst = pack + o * PACK_F4;
+    dst[0] = edge_coef(Ex[o], Ex[o + sy], Ex[o + sy + 1], Ex[o + 1]);
+    dst[1] = edge_coef(Ey[o], Ey[o + 1], Ey[o + sx + 1], Ey[o + sx]);
+    dst[2] = edge_coef(Ez[o], Ez[o + sx], Ez[o + sx + sy], Ez[o + sy]);
+    float s0, s1;
+    float4 b;
+    s0 = P.T[0][o] + P.B[0][o];
+    s1 = P.T[0][o + sx] + P.B[0][o + sx];
+    b.x = s0 - 0.5f * s1;
+    b.y = 0.5f * (s1 - s0);
+    s0 = P.T[1][o] + P.B[1][o];
+    s1 = P.T[1][o + sy] + P.B[1][o + sy];
+    b.z = s0 - 0.5f * s1;
+    b.w = 0.5f * (s1 - s0);
+    dst[3] = b;
+    s0 = P.T[2][o] + P.B[2][o];
+    s1 = P.T[2][o + 1] + P.B[2][o + 1];
+    dst[4] = make_float4(s0 - 0.5f * s1, 0.5f * (s1 - s0), 0.0f, 0.0f);
+}
+
+// E and B at offsets (ox, oy, oz) of the cell whose pack starts at pk.
+__device__ __forceinline__ void gather_pack(const float4 *__restrict__ pk, float ox, float oy, float oz, float f[6]) {
+    const float4 ex = __ldg(pk), ey = __ldg(pk + 1), ez = __ldg(pk + 2), bxy = __ldg(pk + 3);
+    const float2 bz = __ldg(reinterpret_cast<const float2 *>(pk + 4));
+    f[0] = fmaf(oy, fmaf(oz, ex.w, ex.y), fmaf(oz, ex.z, ex.x));
+    f[1] = fmaf(oz, fmaf(ox, ey.w, ey.y), fmaf(ox, ey.z, ey.x));
+    f[2] = fmaf(ox, fmaf(oy, ez.w, ez.y), fmaf(oy, ez.z, ez.x));
+    f[3] = fmaf(ox, bxy.y, bxy.x);
+    f[4] = fmaf(oy, bxy.w, bxy.z);
+    f[5] = fmaf(oz, bz.y, bz.x);
 }
 
 __device__ __forceinline__ void count_cross(DevCounters *ctr, int mask) {
@@ -218,19 +336,36 @@ __device__ __forceinline__ int axis_bc(const BCTab &bc, int d, int n, int &i, fl
     return mask;
 }
 
+constexpr int FUSED_BLOCK = 256;
+constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
+constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: conflict-free both ways)
+
 // Fused gather + push + boundaries + deposit, one thread per particle.
+//
+// Deposit: each lane writes its particle's 20 contributions as a column of a
+// per-warp 20 x 32 shared array; then lane q walks row q, summing the
+// contributions of each run of consecutive particles that share a cell in
+// particle order, and adds each run total, in int64 fixed point, to slot q of
+// the run's cell. The order of every FP32 sum is fixed by the particle order,
+// so the slots are bit-reproducible. A warp whose particles are all in
+// different cells (before the first sort) commits each particle directly.
+//
+// Division and square roots use the hardware approximations (rsqrtf,
+// __fdividef, relative error a few 2^-24): the form's accuracy is FP32. No
+// conversion instruction runs per particle (see f2ll_rn, cell_step).
 template <bool REL, bool FIRST, bool PUSH>
-__global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, MGather P, MState S,
-                                                 int64_t np, MDeposit D, int with_rho, const float *g0,
-                                                 DevCounters *ctr) {
+__global__ void __launch_bounds__(FUSED_BLOCK, 5)
+    k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
+              MDeposit D, int with_rho, const float *g0, DevCounters *ctr) {
+    __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
+    __shared__ int s_key[FUSED_WARPS][32];
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
+    float *col = s_w[threadIdx.x >> 5];
+    int *keys = s_key[threadIdx.x >> 5];
     bool active = false;
     int mask = 0;
-    int64_t onew = 0;
-    float w[20];
-#pragma unroll
-    for (int q = 0; q < 20; q++) w[q] = 0.0f;
+    int onew = 0;
     if (p < np) {
         int32_t c = S.cell[p];
         if (c >= 0) {
@@ -242,14 +377,14 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
             split_cell(g, dv, c, ix, iy, iz);
             if (!PUSH) {
                 // deposit at the current state (Particle_Handler::depositRhoJ)
-                float ga = 1.0f;
-                if (REL && !FIRST) ga = sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
-                vx = ux / ga;
-                vy = uy / ga;
-                vz = uz / ga;
+                float iga = 1.0f;
+                if (REL && !FIRST) iga = rsqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+                vx = ux * iga;
+                vy = uy * iga;
+                vz = uz * iga;
             } else {
             float f[6];
-            gather_m(g, P, (int64_t)c, ox, oy, oz, f);
+            gather_pack(pack + (int64_t)c * PACK_F4, ox, oy, oz, f);
             const float qp = st.qp[s];
             if (REL) {
                 // Vay's pusher (src/pusher/relativisticBoris.cpp:53-140) on
@@ -261,7 +396,7 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
                     float g = g0[p];
                     mx0 = g * ux; my0 = g * uy; mz0 = g * uz;
                 } else {
-                    float iv = 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+                    float iv = rsqrtf(1.0f + ux * ux + uy * uy + uz * uz);
                     v0x = ux * iv; v0y = uy * iv; v0z = uz * iv;
                     mx0 = ux; my0 = uy; mz0 = uz;
                 }
@@ -276,12 +411,13 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
                 float tau2 = tx * tx + ty * ty + tz * tz;
                 float sigma = gps - tau2;
                 float ust = upx * tx + upy * ty + upz * tz;
-                float gi = sqrtf(0.5f * (sigma + sqrtf(sigma * sigma + 4.0f * (tau2 + ust * ust))));
-                float igi = 1.0f / gi;
+                // sigma >= 1 (gps >= 1 + tau2), so both radicands are >= 1
+                float rad = sigma * sigma + 4.0f * (tau2 + ust * ust);
+                float igi = rsqrtf(0.5f * (sigma + rad * rsqrtf(rad)));
                 tx *= igi;
                 ty *= igi;
                 tz *= igi;
-                float sfac = 1.0f / (1.0f + tx * tx + ty * ty + tz * tz);
+                float sfac = __fdividef(1.0f, 1.0f + tx * tx + ty * ty + tz * tz);
                 float ud = ust * igi;
                 ux = sfac * (upx + ud * tx + (upy * tz - upz * ty));
                 uy = sfac * (upy + ud * ty + (upz * tx - upx * tz));
@@ -293,7 +429,7 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
                 // Boris (src/pusher/boris.cpp:33-85)
                 float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
                 float b2 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
-                float ts = 2.0f / (1.0f + qp * qp * b2);
+                float ts = __fdividef(2.0f, 1.0f + qp * qp * b2);
                 float sx = ts * tx, sy = ts * ty, sz = ts * tz;
                 float mx = ux + qp * f[0], my = uy + qp * f[1], mz = uz + qp * f[2];
                 float ix_ = mx + my * tz - mz * ty;
@@ -308,17 +444,9 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
             }
             // position update in cell units, then the boundaries per axis
             float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
-            float fx = floorf(nx), fy = floorf(ny), fz = floorf(nz);
-            ix += (int)fx;
-            iy += (int)fy;
-            iz += (int)fz;
-            ox = nx - fx;
-            oy = ny - fy;
-            oz = nz - fz;
-            // fraction rounding can give exactly 1.0f for tiny negatives
-            if (ox >= 1.0f) { ox = 0.0f; ix += 1; }
-            if (oy >= 1.0f) { oy = 0.0f; iy += 1; }
-            if (oz >= 1.0f) { oz = 0.0f; iz += 1; }
+            cell_step(nx, ix, ox);
+            cell_step(ny, iy, oy);
+            cell_step(nz, iz, oz);
             mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
             if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
             if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
@@ -331,9 +459,9 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
                 S.cell[p] = -1;
                 mask |= 64;
             } else {
-                onew = (int64_t)ix * g.sx + (int64_t)iy * g.sy + iz;
+                onew = ix * (int)g.sx + iy * (int)g.sy + iz;  // < npts < 2^31 (checked in mixed_alloc)
                 if (PUSH) {
-                    S.cell[p] = (int32_t)onew;
+                    S.cell[p] = onew;
                     S.ox[p] = ox;
                     S.oy[p] = oy;
                     S.oz[p] = oz;
@@ -349,54 +477,122 @@ __global__ void __launch_bounds__(256) k_fused_m(MGeom g, Div3 dv, MSpecies st, 
                     float b[3] = {ox - 1.0f, oy - 1.0f, oz - 1.0f};
                     const float qd = st.qdep[s];
                     float jx = qd * vx, jy = qd * vy, jz = qd * vz;
-                    w[0] = jx * a[1] * a[2];
-                    w[1] = jx * b[1] * a[2];
-                    w[2] = jx * b[1] * b[2];
-                    w[3] = jx * a[1] * b[2];
-                    w[4] = jy * a[2] * a[0];
-                    w[5] = jy * b[2] * a[0];
-                    w[6] = jy * b[2] * b[0];
-                    w[7] = jy * a[2] * b[0];
-                    w[8] = jz * a[0] * a[1];
-                    w[9] = jz * b[0] * a[1];
-                    w[10] = jz * b[0] * b[1];
-                    w[11] = jz * a[0] * b[1];
+                    float *w = col + lane;
+                    w[0 * DEP_STRIDE] = jx * a[1] * a[2];
+                    w[1 * DEP_STRIDE] = jx * b[1] * a[2];
+                    w[2 * DEP_STRIDE] = jx * b[1] * b[2];
+                    w[3 * DEP_STRIDE] = jx * a[1] * b[2];
+                    w[4 * DEP_STRIDE] = jy * a[2] * a[0];
+                    w[5 * DEP_STRIDE] = jy * b[2] * a[0];
+                    w[6 * DEP_STRIDE] = jy * b[2] * b[0];
+                    w[7 * DEP_STRIDE] = jy * a[2] * b[0];
+                    w[8 * DEP_STRIDE] = jz * a[0] * a[1];
+                    w[9 * DEP_STRIDE] = jz * b[0] * a[1];
+                    w[10 * DEP_STRIDE] = jz * b[0] * b[1];
+                    w[11 * DEP_STRIDE] = jz * a[0] * b[1];
                     if (with_rho) {
-                        w[12] = qd * a[0] * a[1] * a[2];
-                        w[13] = qd * b[0] * a[1] * a[2];
-                        w[14] = qd * b[0] * b[1] * a[2];
-                        w[15] = qd * a[0] * b[1] * a[2];
-                        w[16] = qd * a[0] * b[1] * b[2];
-                        w[17] = qd * b[0] * b[1] * b[2];
-                        w[18] = qd * b[0] * a[1] * b[2];
-                        w[19] = qd * a[0] * a[1] * b[2];
+                        w[12 * DEP_STRIDE] = qd * a[0] * a[1] * a[2];
+                        w[13 * DEP_STRIDE] = qd * b[0] * a[1] * a[2];
+                        w[14 * DEP_STRIDE] = qd * b[0] * b[1] * a[2];
+                        w[15 * DEP_STRIDE] = qd * a[0] * b[1] * a[2];
+                        w[16 * DEP_STRIDE] = qd * a[0] * b[1] * b[2];
+                        w[17 * DEP_STRIDE] = qd * b[0] * b[1] * b[2];
+                        w[18 * DEP_STRIDE] = qd * b[0] * a[1] * b[2];
+                        w[19 * DEP_STRIDE] = qd * a[0] * a[1] * b[2];
                     }
                 }
             }
         }
     }
-    count_cross(ctr, mask & 63);
-    // warp runs of equal cells: FP32 sums in a fixed order, int64 commit
-    long long key = active ? (long long)onew : -1 - (long long)lane;
-    long long prev = __shfl_up_sync(0xffffffffu, key, 1);
-    bool head = (lane == 0) || (prev != key);
-    unsigned heads = __ballot_sync(0xffffffffu, head);
-    if (__ballot_sync(0xffffffffu, active) == 0u) return;
-    int rend = run_end(heads, lane);
-    const bool all_single = (heads == 0xffffffffu);
-    const int nq = with_rho ? 20 : 12;
+    if (__any_sync(0xffffffffu, mask & 63)) count_cross(ctr, mask & 63);
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (act == 0u) return;
+    // runs of equal cells (inactive lanes get unique negative keys)
+    const int key = active ? onew : -1 - lane;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+    keys[lane] = active ? onew : -1;
+    if (!active) {
 #pragma unroll
-    for (int q = 0; q < 20; q++) {
-        if (q >= nq) break;
-        float v = w[q];
-        if (!all_single) v = run_suffix_sum(v, lane, rend);
-        if (head && active) {
-            long long fx = __float2ll_rn(v);
-            if (fx != 0) {
-                unsigned long long *base = D.J[q < 4 ? 0 : q < 8 ? 1 : q < 12 ? 2 : 3];
-                atomicAdd(base + mdep_point(g, onew, q), (unsigned long long)fx);
+        for (int q = 0; q < DEP_SLOTS; q++) col[q * DEP_STRIDE + lane] = 0.0f;
+    }
+    __syncwarp();
+    const int nq = with_rho ? DEP_SLOTS : 12;
+    if (heads == 0xffffffffu) {
+        // every particle in a cell of its own (unsorted input)
+        if (active) {
+            unsigned long long *dst = D.wc + (size_t)onew * DEP_SLOTS;
+#pragma unroll
+            for (int q = 0; q < DEP_SLOTS; q++) {
+                if (q >= nq) break;
+                long long fx = f2ll_rn(col[q * DEP_STRIDE + lane]);
+                if (fx != 0) atomicAdd(dst + dep_pos(q), (unsigned long long)fx);
             }
         }
+        return;
+    }
+    if (lane < nq) {
+        // row `lane`: one pass in particle order, committing at each run end;
+        // lanes 0..nq-1 commit one cell's slots together (contiguous 8-byte words)
+        unsigned long long *dst = D.wc + dep_pos(lane);
+        const float *row = col + lane * DEP_STRIDE;
+        const unsigned ends = (heads >> 1) | 0x80000000u;  // bit i: particle i ends its run
+        float acc = 0.0f;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float r[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) r[i] = row[16 * h + i];
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                acc += r[i];
+                if ((ends >> (16 * h + i)) & 1u) {  // warp-uniform
+                    const int kk = keys[16 * h + i];
+                    if (kk >= 0) {
+                        long long fx = f2ll_rn(acc);
+                        if (fx != 0) atomicAdd(dst + (size_t)kk * DEP_SLOTS, (unsigned long long)fx);
+                    }
+                    acc = 0.0f;
+                }
+            }
+        }
+    }
+}
+
+// J and rho at every grid point from the per-cell sums: point p gathers slot
+// q of cell p - off(q), the inverse of the deposit table. Integer sums, so the
+// result equals committing every run total to its point directly.
+__global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned long long *__restrict__ wc,
+                                  unsigned long long *Jx, unsigned long long *Jy, unsigned long long *Jz,
+                                  unsigned long long *rho, int with_rho) {
+    const int64_t first = (int64_t)sx + sy + 1;  // points below have no neighbour cell with particles
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
+        unsigned long long jx = 0, jy = 0, jz = 0, r = 0;
+        if (p >= first) {
+            // record of cell c starts at wc + 20 c (160 bytes, 16-byte aligned)
+            auto rec = [&](int64_t c) { return wc + c * DEP_SLOTS; };
+            const ulonglong2 *a0 = reinterpret_cast<const ulonglong2 *>(rec(p));              // slots 0-3
+            const ulonglong2 *a2 = reinterpret_cast<const ulonglong2 *>(rec(p - sy) + 4);     // 4-7
+            const ulonglong2 g1 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - 1) + 8));             // 8-9
+            const ulonglong2 g3 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sy - 1) + 10));       // 10-11
+            const ulonglong2 g5 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx - 1) + 12));       // 12-13
+            const ulonglong2 g6 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx - sy) + 14));      // 14-15
+            const ulonglong2 g4a = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx) + 16));          // 16-17
+            const ulonglong2 g0a = __ldg(a0), g0b = __ldg(a0 + 1);
+            const ulonglong2 g2a = __ldg(a2), g2b = __ldg(a2 + 1);
+            jx = g0a.x + g2a.x + g2a.y + g3.x;  // q 0, 1, 3, 2
+            jy = g0a.y + g1.x + g5.x + g4a.x;   // q 4, 5, 6, 7
+            jz = g0b.x + g2b.x + g6.x + g4a.y;  // q 8, 11, 10, 9
+            if (with_rho) {
+                const unsigned long long g4b = __ldg(rec(p - sx) + 18);            // q 13
+                const unsigned long long g7 = __ldg(rec(p - sx - sy - 1) + 19);    // q 17
+                r = g0b.y + g2b.y + g1.y + g3.y + g5.y + g6.y + g4b + g7;  // q 12 15 19 16 18 14 13 17
+            }
+        }
+        Jx[p] = jx;
+        Jy[p] = jy;
+        Jz[p] = jz;
+        if (with_rho) rho[p] = r;
     }
 }
 
@@ -624,19 +820,39 @@ __global__ void k_plane_m(MGeom g, MPlaneList pl, int tot0, int tot1, int tot2) 
 
 // ---- reductions (FP64 accumulation) -------------------------------------
 
+// The history reductions take their per-particle (per-cell) terms in FP32,
+// sum them in FP32 over at most DIAG_CHUNK items per thread and accumulate
+// those partial sums in FP64: FP64 arithmetic per item would run on the
+// narrow FP64 pipe (2 lanes per clock per SM on this GPU), which made these
+// reductions cost more than a whole step. The partition is fixed by the launch
+// shape, so the sums are reproducible.
+constexpr int DIAG_CHUNK = 8;
+
 __global__ void k_moments_m(MSpecies st, MState S, int64_t np, int rel, const float *g0, double *part) {
     double acc[4] = {0, 0, 0, 0};
+    float f[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    int k = 0;
+    const bool gam = rel && !g0;  // before the first push u holds v
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
-        if (S.cell[p] < 0) continue;
-        double ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
-        double ga = (rel && !g0) ? sqrt(1.0 + ux * ux + uy * uy + uz * uz) : 1.0;
-        double vx = ux / ga, vy = uy / ga, vz = uz / ga;
-        double m = st.m[species_of_m(st, p)];
-        acc[0] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
-        acc[1] += m * vx;
-        acc[2] += m * vy;
-        acc[3] += m * vz;
+        if (S.cell[p] >= 0) {
+            const float ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+            const float iv = gam ? 1.0f / sqrtf(1.0f + ux * ux + uy * uy + uz * uz) : 1.0f;
+            const float vx = ux * iv, vy = uy * iv, vz = uz * iv;
+            const float m = st.m[species_of_m(st, p)];
+            f[0] += 0.5f * m * (vx * vx + vy * vy + vz * vz);
+            f[1] += m * vx;
+            f[2] += m * vy;
+            f[3] += m * vz;
+        }
+        if (++k == DIAG_CHUNK) {
+            for (int q = 0; q < 4; q++) {
+                acc[q] += (double)f[q];
+                f[q] = 0.0f;
+            }
+            k = 0;
+        }
     }
+    for (int q = 0; q < 4; q++) acc[q] += (double)f[q];
     __shared__ double sh[32][4];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int q = 0; q < 4; q++) {
@@ -655,6 +871,8 @@ __global__ void k_moments_m(MSpecies st, MState S, int64_t np, int rel, const fl
 __global__ void k_energy_m(MGeom g, MCF3 E, MCF3 B, double hv, double *part) {
     double acc[6] = {0, 0, 0, 0, 0, 0};
     int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
+    float f[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int cnt = 0;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
         int k = (int)(t % g.n[2]) + 1;
         int64_t r = t / g.n[2];
@@ -663,12 +881,20 @@ __global__ void k_energy_m(MGeom g, MCF3 E, MCF3 B, double hv, double *part) {
         int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
         int64_t nb[3] = {o + g.sx, o + g.sy, o + 1};
         for (int q = 0; q < 3; q++) {
-            double s = (double)E.p[q][o] + (double)E.p[q][nb[q]];
-            acc[q] += hv * (0.25 * s * s);
-            double sb = (double)B.p[q][o] + (double)B.p[q][nb[q]];
-            acc[3 + q] += hv * (0.25 * sb * sb);
+            const float s = E.p[q][o] + E.p[q][nb[q]];
+            f[q] += 0.25f * s * s;
+            const float sb = B.p[q][o] + B.p[q][nb[q]];
+            f[3 + q] += 0.25f * sb * sb;
+        }
+        if (++cnt == DIAG_CHUNK) {
+            for (int q = 0; q < 6; q++) {
+                acc[q] += hv * (double)f[q];
+                f[q] = 0.0f;
+            }
+            cnt = 0;
         }
     }
+    for (int q = 0; q < 6; q++) acc[q] += hv * (double)f[q];
     __shared__ double sh[32][6];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int q = 0; q < 6; q++) {
@@ -741,9 +967,14 @@ int nblk(int64_t n, int cap = 152 * 16) { return (int)std::max<int64_t>(1, std::
 // ---- public (namespace emoo) ----------------------------------------------
 
 int mixed_alloc(emoo_handle *h) {
+    // cells are int32 linear indices
+    if (h->g.npts >= (int64_t)INT32_MAX) return EMOO_ERR_UNSUPPORTED;
+    if (!dep_tables_agree()) return EMOO_ERR_STATE;
     h->mf = new FieldsF32();
     FieldsF32 *m = h->mf;
     size_t n = (size_t)h->g.npts;
+    EMOO_CUDA(cudaMalloc(&m->pack, n * PACK_F4 * sizeof(float4)));
+    EMOO_CUDA(cudaMalloc(&m->wc, n * DEP_SLOTS * sizeof(unsigned long long)));
     for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMalloc(&m->E[c], n * sizeof(float)));
     for (int c = 0; c < 6; c++) EMOO_CUDA(cudaMalloc(&m->Bslot[c], n * sizeof(float)));
     for (int c = 0; c < 4; c++) EMOO_CUDA(cudaMalloc(&m->J[c], n * sizeof(long long)));
@@ -767,6 +998,8 @@ void mixed_free(emoo_handle *h) {
         if (m->Bslot[c]) cudaFree(m->Bslot[c]);
     for (int c = 0; c < 4; c++)
         if (m->J[c]) cudaFree(m->J[c]);
+    if (m->pack) cudaFree(m->pack);
+    if (m->wc) cudaFree(m->wc);
     if (h->g0) cudaFree(h->g0);
     h->g0 = nullptr;
     delete m;
@@ -912,15 +1145,29 @@ static int mixed_fold(emoo_handle *h) {
     return EMOO_OK;
 }
 
+// Zeroes the per-cell sums; the deposit then rewrites Jx, Jy, Jz (and rho
+// when deposited) at every point from them.
 static int mixed_deposit_zero(emoo_handle *h, int with_rho) {
-    size_t b = sizeof(long long) * (size_t)h->g.npts;
-    for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMemsetAsync(h->mf->J[c], 0, b, h->stream));
-    if (with_rho) EMOO_CUDA(cudaMemsetAsync(h->mf->J[3], 0, b, h->stream));
+    (void)with_rho;
+    EMOO_CUDA(cudaMemsetAsync(h->mf->wc, 0, sizeof(unsigned long long) * DEP_SLOTS * (size_t)h->g.npts, h->stream));
     return EMOO_OK;
 }
 
+static int mixed_cells_to_points(emoo_handle *h, int with_rho) {
+    FieldsF32 *m = h->mf;
+    h->launches++;
+    k_cells_to_points<<<nblk(h->g.npts, 152 * 8), 256, 0, h->stream>>>(
+        h->g.npts, (int)h->g.sx, (int)h->g.sy, m->wc, (unsigned long long *)m->J[0], (unsigned long long *)m->J[1],
+        (unsigned long long *)m->J[2], (unsigned long long *)m->J[3], with_rho);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// Gather + push + boundaries + deposit (push = false: deposit at the current
+// state), then J and rho at the points from the per-cell sums. The per-cell
+// sums must have been zeroed (mixed_deposit_zero).
 static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = true) {
-    if (h->np == 0) return EMOO_OK;
+    if (h->np == 0) return mixed_cells_to_points(h, with_rho);
     MGeom mg = mgeom(h, dtp);
     MSpecies st = mspecies(h, dtp);
     MGather P;
@@ -930,38 +1177,48 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
         P.T[c] = mt_role(h, c);
     }
     MDeposit D;
-    for (int c = 0; c < 4; c++) D.J[c] = (unsigned long long *)h->mf->J[c];
-    int64_t nb = (h->np + 255) / 256;
+    D.wc = h->mf->wc;
+    int64_t nb = (h->np + FUSED_BLOCK - 1) / FUSED_BLOCK;
     bool rel = h->info.relativity != 0;
     bool first = rel && h->first_push && h->g0;
     Div3 dv = div3(h);
     const float *g0 = h->g0;
     MState S = mstate(h);
+    const float4 *pk = h->mf->pack;
     dim3 grd((unsigned)nb);
     if (!push) {
+        h->launches++;
         if (rel && first)
-            k_fused_m<true, true, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
-                                                                     h->ctr);
+            k_fused_m<true, true, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
+                                                                             with_rho, g0, h->ctr);
         else if (rel)
-            k_fused_m<true, false, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho,
-                                                                      g0, h->ctr);
+            k_fused_m<true, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
+                                                                              with_rho, g0, h->ctr);
         else
-            k_fused_m<false, false, false><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho,
-                                                                       g0, h->ctr);
+            k_fused_m<false, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
+                                                                               with_rho, g0, h->ctr);
         EMOO_CUDA(cudaGetLastError());
-        return EMOO_OK;
+        return mixed_cells_to_points(h, with_rho);
+    }
+    {
+        const Geom &g = h->g;
+        dim3 blk(32, 8);
+        dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+        h->launches++;
+        k_pack_m<<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        EMOO_CUDA(cudaGetLastError());
     }
     h->launches++;
     if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
     if (rel && first)
-        k_fused_m<true, true, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
-                                                                h->ctr);
+        k_fused_m<true, true, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho,
+                                                                        g0, h->ctr);
     else if (rel)
-        k_fused_m<true, false, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
-                                                                 h->ctr);
+        k_fused_m<true, false, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
+                                                                         with_rho, g0, h->ctr);
     else
-        k_fused_m<false, false, true><<<grd, 256, 0, h->stream>>>(mg, dv, st, h->bc, P, S, h->np, D, with_rho, g0,
-                                                                  h->ctr);
+        k_fused_m<false, false, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
+                                                                          with_rho, g0, h->ctr);
     EMOO_CUDA(cudaGetLastError());
     if (h->prof_on) {
         EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
@@ -969,7 +1226,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
     }
     // g0 stays allocated for later loads; it is read only while first_push is set
     if (first) h->first_push = 0;
-    return EMOO_OK;
+    return mixed_cells_to_points(h, with_rho);
 }
 
 static int mixed_yee(emoo_handle *h, double dtp, int es) {

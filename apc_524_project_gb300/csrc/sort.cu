@@ -24,7 +24,7 @@ namespace emoo {
 namespace {
 
 constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;  // per thread
+constexpr int RS_ITEMS = 16;  // per thread
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_BINS = 256;
 
@@ -42,10 +42,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_hist(const uint32_t *keys, int64
     hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
+// One stable counting-sort pass over a tile: rank every item within the tile
+// (warps in order, items of a warp in order), reorder the tile by digit in
+// shared memory, then write each digit's items as one contiguous stretch at
+// the digit's global offset for this tile, so the stores are coalesced.
 __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, const uint32_t *vin, uint32_t *kout,
                                                         uint32_t *vout, int64_t n, int shift, uint32_t mask,
                                                         const uint32_t *hist, int nblocks) {
     __shared__ uint32_t wc[RS_THREADS / 32][RS_BINS];
+    __shared__ uint32_t s_key[RS_TILE];
+    __shared__ uint32_t s_val[RS_TILE];
+    __shared__ uint32_t s_start[RS_BINS];  // tile-local start of each digit
+    __shared__ uint32_t s_gbase[RS_BINS];  // global start of each digit's stretch from this tile
+    __shared__ uint32_t s_wsum[RS_THREADS / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < (RS_THREADS / 32) * RS_BINS; i += RS_THREADS) (&wc[0][0])[i] = 0;
     __syncthreads();
@@ -68,23 +77,47 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
         __syncwarp();
     }
     __syncthreads();
-    if (threadIdx.x < RS_BINS) {
-        uint32_t run = 0;
-        for (int ww = 0; ww < RS_THREADS / 32; ww++) {
-            uint32_t t = wc[ww][threadIdx.x];
-            wc[ww][threadIdx.x] = run;
-            run += t;
-        }
+    // per digit (one thread each): warp offsets within the tile's digit
+    // stretch, the tile's digit total, then an exclusive scan over digits
+    static_assert(RS_BINS == RS_THREADS, "one thread per digit");
+    const int d = threadIdx.x;
+    uint32_t tot = 0;
+    for (int ww = 0; ww < RS_THREADS / 32; ww++) {
+        uint32_t t = wc[ww][d];
+        wc[ww][d] = tot;
+        tot += t;
     }
+    uint32_t incl = tot;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t o = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) s_wsum[w] = incl;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int ww = 0; ww < w; ww++) wpre += s_wsum[ww];
+    s_start[d] = wpre + incl - tot;
+    s_gbase[d] = hist[(int64_t)d * nblocks + blockIdx.x];
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < RS_ITEMS; c++) {
         int64_t idx = base + c * 32 + lane;
         if (idx >= n) continue;
         uint32_t dg = (key[c] >> shift) & mask;
-        uint32_t pos = hist[(int64_t)dg * nblocks + blockIdx.x] + wc[w][dg] + rank[c];
-        if (kout) kout[pos] = key[c];
-        vout[pos] = val[c];
+        uint32_t lp = s_start[dg] + wc[w][dg] + rank[c];
+        s_key[lp] = key[c];
+        s_val[lp] = val[c];
+    }
+    __syncthreads();
+    const int64_t tbase = (int64_t)blockIdx.x * RS_TILE;
+    const int cnt = n - tbase < RS_TILE ? (int)(n - tbase) : RS_TILE;
+    for (int i = threadIdx.x; i < cnt; i += RS_THREADS) {
+        const uint32_t k = s_key[i];
+        const uint32_t dg = (k >> shift) & mask;
+        const uint32_t pos = s_gbase[dg] + ((uint32_t)i - s_start[dg]);
+        if (kout) kout[pos] = k;
+        vout[pos] = s_val[i];
     }
 }
 

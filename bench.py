@@ -229,6 +229,18 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
     fused_ms = stats.timed_ms / max(1, stats.timed_launches)
     res["mixed"] = {"t": t, "fused_ms": fused_ms, "launches": launches, "clocks": clocks}
 
+    # ---- one stable sort of the drifted particle state (part of the loop
+    # every 20 steps; timed alone here to show its share)
+    st = _stream_of(h)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    abi.check(L.emoo_sort(h), "emoo_sort")
+    e1.record(st)
+    torch.cuda.synchronize()
+    res["sort_ms"] = e0.elapsed_time(e1)
+
     # ---- e2e through the C ABI with host-resident particle state
     if not args.no_e2e:
         res["e2e"] = _e2e(h, cfg, args.e2e_steps, dist_barrier, dist_max)
@@ -445,6 +457,7 @@ def main():
                      "kernel_ms": m["fused_ms"], "algorithmic_bytes": alg_bytes},
         "gpu_launches": m["launches"],
         "clocks": m["clocks"],
+        "sort_ms": res.get("sort_ms"),
     }
     if "fp64" in res:
         f = res["fp64"]

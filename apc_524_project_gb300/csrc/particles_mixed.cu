@@ -549,8 +549,8 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 if ((ends >> (16 * h + i)) & 1u) {  // warp-uniform
                     const int kk = keys[16 * h + i];
                     if (kk >= 0) {
-                        long long fx = f2ll_rn(acc);
-                        if (fx != 0) atomicAdd(dst + (size_t)kk * DEP_SLOTS, (unsigned long long)fx);
+                        // zero totals are committed too: testing costs more than the atomic
+                        atomicAdd(dst + (size_t)kk * DEP_SLOTS, (unsigned long long)f2ll_rn(acc));
                     }
                     acc = 0.0f;
                 }

@@ -59,22 +59,31 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
     for (int i = threadIdx.x; i < (RS_THREADS / 32) * RS_BINS; i += RS_THREADS) (&wc[0][0])[i] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * (32 * RS_ITEMS);
-    uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
+    // keys and values are read again when the tile is placed, and the ranks
+    // are kept two to a register: few registers, more resident blocks
+    uint32_t rank2[RS_ITEMS / 2];  // two 16-bit ranks (< 32 * RS_ITEMS) per word
     const unsigned lt = lanemask_lt();
+    {
+        uint32_t key[RS_ITEMS];
 #pragma unroll
-    for (int c = 0; c < RS_ITEMS; c++) {
-        int64_t idx = base + c * 32 + lane;
-        bool valid = idx < n;
-        key[c] = valid ? kin[idx] : 0u;
-        val[c] = valid ? (vin ? vin[idx] : (uint32_t)idx) : 0u;
-        uint32_t dg = (key[c] >> shift) & mask;
-        unsigned tag = valid ? dg : (0x10000u + lane);
-        unsigned peers = __match_any_sync(0xffffffffu, tag);
-        uint32_t b = valid ? wc[w][dg] : 0u;
-        rank[c] = b + __popc(peers & lt);
-        __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) wc[w][dg] = b + __popc(peers);
-        __syncwarp();
+        for (int c = 0; c < RS_ITEMS; c++) {
+            int64_t idx = base + c * 32 + lane;
+            key[c] = idx < n ? __ldg(kin + idx) : 0u;
+        }
+#pragma unroll
+        for (int c = 0; c < RS_ITEMS; c++) {
+            int64_t idx = base + c * 32 + lane;
+            bool valid = idx < n;
+            uint32_t dg = (key[c] >> shift) & mask;
+            unsigned tag = valid ? dg : (0x10000u + lane);
+            unsigned peers = __match_any_sync(0xffffffffu, tag);
+            uint32_t b = valid ? wc[w][dg] : 0u;
+            const uint32_t r = b + __popc(peers & lt);
+            rank2[c >> 1] = (c & 1) ? (rank2[c >> 1] | (r << 16)) : r;
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) wc[w][dg] = b + __popc(peers);
+            __syncwarp();
+        }
     }
     __syncthreads();
     // per digit (one thread each): warp offsets within the tile's digit
@@ -104,10 +113,11 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
     for (int c = 0; c < RS_ITEMS; c++) {
         int64_t idx = base + c * 32 + lane;
         if (idx >= n) continue;
-        uint32_t dg = (key[c] >> shift) & mask;
-        uint32_t lp = s_start[dg] + wc[w][dg] + rank[c];
-        s_key[lp] = key[c];
-        s_val[lp] = val[c];
+        const uint32_t k = __ldg(kin + idx);  // read again (L2)
+        uint32_t dg = (k >> shift) & mask;
+        uint32_t lp = s_start[dg] + wc[w][dg] + ((rank2[c >> 1] >> (16 * (c & 1))) & 0xffffu);
+        s_key[lp] = k;
+        s_val[lp] = vin ? __ldg(vin + idx) : (uint32_t)idx;
     }
     __syncthreads();
     const int64_t tbase = (int64_t)blockIdx.x * RS_TILE;
@@ -121,7 +131,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
     }
 }
 
-// In-place exclusive scan of each 2048-element tile; tile totals to sums.
+// In-place exclusive scan of each RS_TILE-element tile; tile totals to sums.
 __global__ void __launch_bounds__(RS_THREADS) k_scan_tile(uint32_t *data, int64_t m, uint32_t *sums) {
     __shared__ uint32_t wsum[RS_THREADS / 32];
     int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)threadIdx.x * RS_ITEMS;
@@ -190,10 +200,31 @@ int scan_excl(emoo_handle *h, uint32_t *data, int64_t m, uint32_t *tmp) {
     return EMOO_OK;
 }
 
+// dst[i] = src[perm[i]]. Each thread gathers 4 consecutive items at a time
+// (one 16-byte permutation load, 4 independent loads in flight, vector
+// stores); the < 4 items of the tail go one by one.
 template <typename T>
 __global__ void k_gather(const T *__restrict__ src, T *__restrict__ dst, const uint32_t *__restrict__ perm, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        dst[i] = src[perm[i]];
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "payload element size");
+    const int64_t n4 = n >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n4; j += stride) {
+        const uint4 pp = __ldg(reinterpret_cast<const uint4 *>(perm) + j);
+        const T a = src[pp.x], b = src[pp.y], c = src[pp.z], d = src[pp.w];
+        T *o = dst + 4 * j;
+        if constexpr (sizeof(T) == 4) {
+            *reinterpret_cast<uint4 *>(o) = make_uint4(*reinterpret_cast<const uint32_t *>(&a),
+                                                       *reinterpret_cast<const uint32_t *>(&b),
+                                                       *reinterpret_cast<const uint32_t *>(&c),
+                                                       *reinterpret_cast<const uint32_t *>(&d));
+        } else {
+            reinterpret_cast<ulonglong2 *>(o)[0] = make_ulonglong2(*reinterpret_cast<const unsigned long long *>(&a),
+                                                                   *reinterpret_cast<const unsigned long long *>(&b));
+            reinterpret_cast<ulonglong2 *>(o)[1] = make_ulonglong2(*reinterpret_cast<const unsigned long long *>(&c),
+                                                                   *reinterpret_cast<const unsigned long long *>(&d));
+        }
+    }
+    for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[perm[i]];
 }
 
 // Permutes one SoA array through the scratch buffer of its element size and
@@ -207,9 +238,9 @@ int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
     void *&scratch = sizeof(T) == 8 ? h->pay : h->pay4;
     if (!scratch || n > h->cap) return EMOO_ERR_STATE;
     T *tmp = (T *)scratch;
-    int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    int nb = (int)std::min<int64_t>((n / 4 + 255) / 256, 152 * 16);
     h->launches++;
-    k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);
+    k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);  // base pointers are cudaMalloc'd
     EMOO_CUDA(cudaGetLastError());
     scratch = (void *)arr;
     arr = tmp;

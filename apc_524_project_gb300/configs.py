@@ -80,6 +80,8 @@ class Config:
     seed: int = 12345
     zero_mean: Optional[bool] = None  # default: Poisson start with all-periodic fields
     x0: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    immobile_ions: bool = False  # uniform neutralising background instead of ion particles
+    b_noise: float = 0.0         # seeded white-noise amplitude on every B component (C3)
 
     @property
     def L(self):
@@ -170,6 +172,37 @@ def input_info(cfg: Config) -> abi.InputInfo:
     return info
 
 
+def rho_background(cfg: Config) -> float:
+    """Uniform immobile background (reference rho units) that neutralises the
+    deposited species on average: each macro-particle deposits
+    UNIT_RHOJ * charge_ratio / V = w q / V in total, so the background is
+    -sum_s w q_s ppc_s / V. Zero unless cfg.immobile_ions."""
+    if not cfg.immobile_ions:
+        return 0.0
+    w = cfg.macro_weight()
+    vol = cfg.dx[0] * cfg.dx[1] * cfg.dx[2]
+    cells = cfg.n[0] * cfg.n[1] * cfg.n[2]
+    return -sum(w * s.q * cfg.count(s) / cells for s in cfg.species if not s.test) / vol
+
+
+def b_noise_fields(cfg: Config):
+    """Seeded white noise of amplitude cfg.b_noise on Bx, By, Bz at the
+    physical points ((n+3)^3 arrays, ghosts zero), the same values for B and
+    B_tm1 (the C3 start). Returns None when cfg.b_noise is 0."""
+    if not cfg.b_noise:
+        return None
+    import numpy as np
+
+    rng = np.random.default_rng(cfg.seed ^ 0x5EED0B)
+    shape = tuple(v + 3 for v in cfg.n)
+    out = []
+    for _ in range(3):
+        f = np.zeros(shape)
+        f[1:cfg.n[0] + 1, 1:cfg.n[1] + 1, 1:cfg.n[2] + 1] = cfg.b_noise * rng.uniform(-1.0, 1.0, cfg.n)
+        out.append(f)
+    return out
+
+
 def gen_params(cfg: Config, si: int) -> abi.GenParams:
     s = cfg.species[si]
     g = abi.GenParams()
@@ -208,6 +241,17 @@ def thermal256(n=256):
         species=[Species("e", -1.0, 1.0, 16, 0.1),
                  Species("i", 1.0, 1836.0, 16, 0.1 / math.sqrt(1836.0))],
         relativity=1, init="constant", nstep_sort=20, seed=20240202)
+
+
+def twostream(n=(256, 128, 128), steps=1000):
+    """Counter-streaming electron beams (drift +-0.3c along x, 16 ppc each,
+    v_th = 0.02c) over an immobile neutralising background, relativistic push,
+    seeded 1e-4 white noise on B, periodic, sort every 20 steps."""
+    return Config(
+        name="twostream", n=tuple(n), dt=0.45, steps=steps, omega_pe=0.5,
+        species=[Species("beam+", -1.0, 1.0, 16, 0.02, drift=(0.3, 0.0, 0.0)),
+                 Species("beam-", -1.0, 1.0, 16, 0.02, drift=(-0.3, 0.0, 0.0))],
+        relativity=1, init="constant", nstep_sort=20, seed=20240303, immobile_ions=True, b_noise=1e-4)
 
 
 def tiny(name="tiny", n=(6, 5, 4), dx=(1.0, 1.0, 1.0), ppc=3, relativity=0, init="poisson", steps=4,

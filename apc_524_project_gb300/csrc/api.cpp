@@ -533,6 +533,7 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
     if (opts) o = *opts;
     else emoo_default_opts(&o);
     if (o.precision != EMOO_FP64 && o.precision != EMOO_MIXED) return EMOO_ERR_ARG;
+    if (!std::isfinite(o.rho_background)) return EMOO_ERR_ARG;
     if (info->nspecies < 0 || info->nspecies > EMOO_NSPEC) return EMOO_ERR_ARG;
     for (int d = 0; d < 3; d++)
         if (info->nCell[d] < 1 || !(info->Lxyz[d] > 0)) return EMOO_ERR_ARG;

@@ -165,6 +165,7 @@ int a_to_b_f64(emoo_handle *h);
 int field_energy_f64(emoo_handle *h, double out6[6]);
 int gauss_residual_f64(emoo_handle *h, double out2[2]);
 int fill_f64(emoo_handle *h, double *p, int64_t n, double v, cudaStream_t s);
+int rho_background_f64(emoo_handle *h, int with_rho);  // rho += opts.rho_background at the physical points
 
 // ---- FP64 particle kernels (particles_f64.cu) ----
 void species_tab(emoo_handle *h, double dtp, SpeciesTab &st);

@@ -447,6 +447,27 @@ static int plane_launch(emoo_handle *h, const PlaneSet *ps, int n, const int *sk
 
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n) { return plane_launch(h, ps, n, nullptr); }
 
+// rho += background at every physical point (immobile neutralising ions of
+// the C3 / C5 workloads; no reference counterpart).
+__global__ void k_add_phys(Geom g, double *f, double v) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    f[(int64_t)i * g.sx + (int64_t)j * g.sy + k] += v;
+}
+
+int rho_background_f64(emoo_handle *h, int with_rho) {
+    if (!with_rho || h->opts.rho_background == 0.0) return EMOO_OK;
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    h->launches++;
+    k_add_phys<<<grd, blk, 0, h->stream>>>(g, h->slot[EMOO_RHO], h->opts.rho_background);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 int fill_f64(emoo_handle *h, double *p, int64_t n, double v, cudaStream_t s) {
     (void)h;
     int64_t b = std::min<int64_t>((n + 255) / 256, 152 * 16);

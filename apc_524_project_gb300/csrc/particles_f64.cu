@@ -535,20 +535,20 @@ int deposit_f64(emoo_handle *h, int with_rho) {
     size_t bytes = sizeof(double) * (size_t)h->g.npts;
     for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMemsetAsync(h->slot[EMOO_JX + c], 0, bytes, h->stream));
     if (with_rho) EMOO_CUDA(cudaMemsetAsync(h->slot[EMOO_RHO], 0, bytes, h->stream));
-    if (h->np == 0) return EMOO_OK;
+    if (h->np == 0) return rho_background_f64(h, with_rho);
     SpeciesTab st;
     species_tab(h, h->dtp, st);
     h->launches++;
     k_deposit<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, pstate(h), h->np, deposit_ptrs(h), with_rho, h->ctr);
     EMOO_CUDA(cudaGetLastError());
-    return EMOO_OK;
+    return rho_background_f64(h, with_rho);
 }
 
 int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {
     size_t bytes = sizeof(double) * (size_t)h->g.npts;
     for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMemsetAsync(h->slot[EMOO_JX + c], 0, bytes, h->stream));
     if (with_rho) EMOO_CUDA(cudaMemsetAsync(h->slot[EMOO_RHO], 0, bytes, h->stream));
-    if (h->np == 0) return EMOO_OK;
+    if (h->np == 0) return rho_background_f64(h, with_rho);
     SpeciesTab st;
     species_tab(h, dtp, st);
     h->launches++;
@@ -564,7 +564,7 @@ int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {
         EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
         EMOO_TRY(prof_accumulate(h));
     }
-    return EMOO_OK;
+    return rho_background_f64(h, with_rho);
 }
 
 int particle_moments_f64(emoo_handle *h, double out4[4]) {

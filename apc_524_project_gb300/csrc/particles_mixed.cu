@@ -1163,11 +1163,35 @@ static int mixed_cells_to_points(emoo_handle *h, int with_rho) {
     return EMOO_OK;
 }
 
+// rho += background (fixed point) at every physical point: immobile
+// neutralising ions (C3 / C5 workloads), no reference counterpart.
+__global__ void k_add_phys_i64(MGeom g, long long *f, long long v) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    f[(int64_t)i * g.sx + (int64_t)j * g.sy + k] += v;
+}
+
+// J and rho at the points from the per-cell records, plus the background.
+static int mixed_finish_deposit(emoo_handle *h, int with_rho) {
+    EMOO_TRY(mixed_cells_to_points(h, with_rho));
+    if (!with_rho || h->opts.rho_background == 0.0) return EMOO_OK;
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    h->launches++;
+    k_add_phys_i64<<<grd, blk, 0, h->stream>>>(mgeom(h, h->dtp), h->mf->J[3],
+                                               (long long)llrint(h->opts.rho_background / h->mf->q0));
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 // Gather + push + boundaries + deposit (push = false: deposit at the current
 // state), then J and rho at the points from the per-cell sums. The per-cell
 // sums must have been zeroed (mixed_deposit_zero).
 static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = true) {
-    if (h->np == 0) return mixed_cells_to_points(h, with_rho);
+    if (h->np == 0) return mixed_finish_deposit(h, with_rho);
     MGeom mg = mgeom(h, dtp);
     MSpecies st = mspecies(h, dtp);
     MGather P;
@@ -1198,7 +1222,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
             k_fused_m<false, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
                                                                                with_rho, g0, h->ctr);
         EMOO_CUDA(cudaGetLastError());
-        return mixed_cells_to_points(h, with_rho);
+        return mixed_finish_deposit(h, with_rho);
     }
     {
         const Geom &g = h->g;
@@ -1226,7 +1250,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
     }
     // g0 stays allocated for later loads; it is read only while first_push is set
     if (first) h->first_push = 0;
-    return mixed_cells_to_points(h, with_rho);
+    return mixed_finish_deposit(h, with_rho);
 }
 
 static int mixed_yee(emoo_handle *h, double dtp, int es) {

@@ -84,6 +84,7 @@ typedef struct {
     double dt, t0;
     double t, dtp; /* the reference's globals time_phys and dt_phys */
     long next_hist;
+    double rho_bg; /* immobile uniform background charge density (no reference counterpart) */
 } orc_t;
 
 /* ------------------------------------------------------------------ */
@@ -703,7 +704,7 @@ static void add_rho(orc_t *c, int cid, const double *R) {
 /* Particle_Handler::depositRhoJ (src/particles/particle_handler.cpp:185-239)
  * with Depositor::deposit_particle_J / _Rho (src/particles/deposit.cpp:12-62):
  * contributions accumulate per run of equal cell IDs and are flushed on a
- * cell change. rho_background (build option) is added afterwards. */
+ * cell change. The uniform background (orc_set_rho_background) is added afterwards. */
 static void deposit(orc_t *c, int with_rho) {
     long npts = c->npts;
     memset(c->slot[EMOO_JX], 0, sizeof(double) * (size_t)npts);
@@ -764,7 +765,18 @@ static void deposit(orc_t *c, int with_rho) {
         add_j(c, (int)cellID, JObj);
         if (with_rho) add_rho(c, (int)cellID, RhoObj);
     }
+    if (with_rho && c->rho_bg != 0.0) {
+        /* the immobile background sits on the physical points */
+        double *rho = c->slot[EMOO_RHO];
+        for (int i = 1; i <= c->n[0]; i++)
+            for (int j = 1; j <= c->n[1]; j++)
+                for (int k = 1; k <= c->n[2]; k++) rho[IDX(c, i, j, k)] += c->rho_bg;
+    }
 }
+
+/* Uniform immobile background charge density added to rho at every deposit
+ * (the C3 and C5 workloads' neutralising ions; the reference has none). */
+void orc_set_rho_background(void *h, double v) { ((orc_t *)h)->rho_bg = v; }
 
 int orc_deposit(void *h, int with_rho) {
     deposit((orc_t *)h, with_rho);

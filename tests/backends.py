@@ -70,6 +70,7 @@ def _load_cpu_lib(path, prefix):
         f("set_time", None, [P, C.c_double, C.c_double])
         f("time", C.c_double, [P])
         f("gauss_residual", C.c_int, [P, _D])
+        f("set_rho_background", None, [P, C.c_double])
     return L
 
 
@@ -232,11 +233,14 @@ class OracleBackend(CpuBackend):
         self._f("gauss_residual")(self.h, out)
         return list(out)
 
+    def set_rho_background(self, v):
+        self._f("set_rho_background")(self.h, C.c_double(v))
+
 
 class GpuBackend:
     """The product, through include/emoo.h."""
 
-    def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0):
+    def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0, rho_background=0.0):
         self.L = abi.lib()
         self.info = info
         self.n = [info.nCell[d] for d in range(3)]
@@ -248,6 +252,7 @@ class GpuBackend:
         o.capacity = capacity
         o.track_ids = track_ids
         o.device = device
+        o.rho_background = rho_background
         h = C.c_void_p()
         abi.check(self.L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
         self.h = h

@@ -1,0 +1,368 @@
+// ad_math.cuh - per-particle arithmetic of the FP64 time step, written once
+// for three uses:
+//   * templated on the scalar: T = double (the step itself) or T = Dual
+//     (value + one directional derivative: the tangent-linear model);
+//   * hand-written reverse functions (the adjoint): each takes the forward
+//     inputs, recomputes what it needs and maps the adjoints of the outputs
+//     to the adjoints of the inputs.
+// The operation order follows the FP64 kernels in particles_f64.cu, which
+// follow the reference: the gather of src/grid/oGrid.cpp:153-197 with
+// src/particles/interpolate.cpp:11-47, Boris::Step src/pusher/boris.cpp:33-85,
+// Relativistic_Boris::Step (Vay) src/pusher/relativisticBoris.cpp:53-140, the
+// reflecting / periodic boundaries and Depositor::deposit_particle_J
+// src/particles/deposit.cpp:12-39.
+//
+// Differentiation treats the piecewise parts as fixed: the cell a particle
+// sits in (and so which grid values it reads and writes) and whether a
+// boundary fires are taken from the primal state. The step is smooth in
+// between; at a cell face the reference's gather is discontinuous.
+//
+// Host-compilable (g++) so the reverse functions can be checked against the
+// Dual forward without a GPU.
+#pragma once
+
+#include <cmath>
+
+#ifdef __CUDACC__
+#define AD_HD __host__ __device__ __forceinline__
+#else
+#define AD_HD inline
+#endif
+
+namespace emoo {
+namespace ad {
+
+struct Dual {
+    double v, d;
+};
+
+AD_HD Dual mk(double v, double d = 0.0) { return Dual{v, d}; }
+AD_HD double val(double x) { return x; }
+AD_HD double val(const Dual &x) { return x.v; }
+AD_HD Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+AD_HD Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+AD_HD Dual operator-(Dual a) { return {-a.v, -a.d}; }
+AD_HD Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+AD_HD Dual operator/(Dual a, Dual b) {
+    const double q = a.v / b.v;
+    return {q, (a.d - q * b.d) / b.v};
+}
+AD_HD Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+AD_HD Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+AD_HD Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+AD_HD Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+AD_HD Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+AD_HD Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+AD_HD Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+AD_HD Dual operator/(double a, Dual b) {
+    const double q = a / b.v;
+    return {q, -q * b.d / b.v};
+}
+AD_HD Dual sqrt(Dual a) {
+    const double s = ::sqrt(a.v);
+    return {s, a.d / (2.0 * s)};
+}
+AD_HD double sqrt_(double a) { return ::sqrt(a); }
+AD_HD Dual sqrt_(Dual a) { return sqrt(a); }
+
+// Geometry of the cell a particle is in: spacings, face areas.
+struct CellGeo {
+    double d[3];
+    double area[3];  // d[j] * d[k]
+    double vol;
+};
+
+// ---- gather ---------------------------------------------------------------
+//
+// v[0..11]: the 4 edge values of Ex, Ey, Ez in the order the FP64 kernel loads
+// them; v[12..17]: the two face values of Bx, By, Bz, each (B + B_tm1) / 2.
+// ds: particle minus the cell's vertex (the ghost-offset vertex, so ds is in
+// [-d, 0) per axis). out: Ex, Ey, Ez, Bx, By, Bz at the particle.
+template <class T>
+AD_HD void gather_eval(const CellGeo &c, const T v[18], const T ds[3], T out[6]) {
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        const double lj = c.d[j], lk = c.d[k], li = c.d[i];
+        T e = (lj - ds[j]) * (lk - ds[k]) * v[4 * i];  // 0 + first term: the same value
+        e = e + ds[j] * (lk - ds[k]) * v[4 * i + 1];
+        e = e + ds[j] * ds[k] * v[4 * i + 2];
+        e = e + (lj - ds[j]) * ds[k] * v[4 * i + 3];
+        e = e / c.area[i];
+        T b = (li - ds[i]) * v[12 + 2 * i];
+        b = b + ds[i] * v[12 + 2 * i + 1];
+        b = b / li;
+        out[i] = e;
+        out[3 + i] = b;
+    }
+}
+
+// double overload without the Dual seed
+AD_HD void gather_eval(const CellGeo &c, const double v[18], const double ds[3], double out[6]) {
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        const double lj = c.d[j], lk = c.d[k], li = c.d[i];
+        double e = 0.0;
+        e += (lj - ds[j]) * (lk - ds[k]) * v[4 * i];
+        e += ds[j] * (lk - ds[k]) * v[4 * i + 1];
+        e += ds[j] * ds[k] * v[4 * i + 2];
+        e += (lj - ds[j]) * ds[k] * v[4 * i + 3];
+        e = e / c.area[i];
+        double b = (li - ds[i]) * v[12 + 2 * i];
+        b += ds[i] * v[12 + 2 * i + 1];
+        b = b / li;
+        out[i] = e;
+        out[3 + i] = b;
+    }
+}
+
+// Adjoint of gather_eval: adds to lv[18] and lds[3].
+AD_HD void gather_rev(const CellGeo &c, const double v[18], const double ds[3], const double lout[6], double lv[18],
+                      double lds[3]) {
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        const double lj = c.d[j], lk = c.d[k], li = c.d[i];
+        const double ls = lout[i] / c.area[i];
+        const double A = lj - ds[j], Bk = lk - ds[k];
+        lv[4 * i] += ls * A * Bk;
+        lv[4 * i + 1] += ls * ds[j] * Bk;
+        lv[4 * i + 2] += ls * ds[j] * ds[k];
+        lv[4 * i + 3] += ls * A * ds[k];
+        lds[j] += ls * (-Bk * v[4 * i] + Bk * v[4 * i + 1] + ds[k] * v[4 * i + 2] - ds[k] * v[4 * i + 3]);
+        lds[k] += ls * (-A * v[4 * i] - ds[j] * v[4 * i + 1] + ds[j] * v[4 * i + 2] + A * v[4 * i + 3]);
+        const double lb = lout[3 + i] / li;
+        lv[12 + 2 * i] += lb * (li - ds[i]);
+        lv[12 + 2 * i + 1] += lb * ds[i];
+        lds[i] += lb * (v[12 + 2 * i + 1] - v[12 + 2 * i]);
+    }
+}
+
+// ---- pushers --------------------------------------------------------------
+
+template <class T>
+AD_HD void boris_eval(double qp, const T f[6], double dt, T x[3], T v[3]) {
+    const T ex = f[0], ey = f[1], ez = f[2], bx = f[3], by = f[4], bz = f[5];
+    const T tx = qp * bx, ty = qp * by, tz = qp * bz;
+    const T bsqr = bx * bx + by * by + bz * bz;
+    const T tsqr = 2.0 / (1.0 + qp * qp * bsqr);
+    const T sx = tsqr * tx, sy = tsqr * ty, sz = tsqr * tz;
+    const T vmx = v[0] + qp * ex, vmy = v[1] + qp * ey, vmz = v[2] + qp * ez;
+    const T vix = vmx + vmy * tz - vmz * ty;
+    const T viy = vmy + vmz * tx - vmx * tz;
+    const T viz = vmz + vmx * ty - vmy * tx;
+    const T vpx = vmx + viy * sz - viz * sy;
+    const T vpy = vmy + viz * sx - vix * sz;
+    const T vpz = vmz + vix * sy - viy * sx;
+    v[0] = vpx + qp * ex;
+    v[1] = vpy + qp * ey;
+    v[2] = vpz + qp * ez;
+    for (int a = 0; a < 3; a++) x[a] = x[a] + dt * v[a];
+}
+
+AD_HD void cross3(const double a[3], const double b[3], double o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Adjoint of boris_eval at inputs (f, v): lx, lv hold the adjoints of the
+// outputs on entry and of the inputs on exit; lf receives the field adjoint.
+AD_HD void boris_rev(double qp, const double f[6], double dt, const double v_in[3], double lx[3], double lv[3],
+                     double lf[6]) {
+    const double e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
+    double t[3], s[3], vm[3], vi[3];
+    for (int a = 0; a < 3; a++) t[a] = qp * b[a];
+    const double bsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    const double tsq = 2.0 / (1.0 + qp * qp * bsq);
+    for (int a = 0; a < 3; a++) s[a] = tsq * t[a];
+    for (int a = 0; a < 3; a++) vm[a] = v_in[a] + qp * e[a];
+    double c[3];
+    cross3(vm, t, c);
+    for (int a = 0; a < 3; a++) vi[a] = vm[a] + c[a];
+    // x' = x + dt v': the adjoint of v' collects dt lx
+    double lvp[3], le[3] = {0, 0, 0}, lb[3] = {0, 0, 0}, lvm[3], lvi[3], ls[3], lt[3];
+    for (int a = 0; a < 3; a++) {
+        lvp[a] = lv[a] + dt * lx[a];
+        le[a] += qp * lvp[a];  // v' = vp + qp e
+    }
+    // vp = vm + vi x s
+    double tmp[3];
+    for (int a = 0; a < 3; a++) lvm[a] = lvp[a];
+    cross3(s, lvp, lvi);
+    cross3(lvp, vi, ls);
+    // vi = vm + vm x t
+    cross3(t, lvi, tmp);
+    for (int a = 0; a < 3; a++) lvm[a] += lvi[a] + tmp[a];
+    cross3(lvi, vm, lt);
+    // vm = v + qp e
+    for (int a = 0; a < 3; a++) {
+        lv[a] = lvm[a];
+        le[a] += qp * lvm[a];
+    }
+    // s = tsq t
+    const double ltsq = ls[0] * t[0] + ls[1] * t[1] + ls[2] * t[2];
+    for (int a = 0; a < 3; a++) lt[a] += tsq * ls[a];
+    // tsq = 2 / (1 + qp^2 bsq)
+    const double lbsq = ltsq * (-0.5 * tsq * tsq * qp * qp);
+    for (int a = 0; a < 3; a++) lb[a] += 2.0 * b[a] * lbsq + qp * lt[a];
+    for (int a = 0; a < 3; a++) {
+        lf[a] += le[a];
+        lf[3 + a] += lb[a];
+    }
+    // lx passes through unchanged (x' = x + ...)
+}
+
+template <class T>
+AD_HD void vay_eval(double qp, const T f[6], double dt, T x[3], T v[3], T &gamma) {
+    const T ex = f[0], ey = f[1], ez = f[2], bx = f[3], by = f[4], bz = f[5];
+    const T vXbx = v[1] * bz - v[2] * by, vXby = v[2] * bx - v[0] * bz, vXbz = v[0] * by - v[1] * bx;
+    const T uhx = gamma * v[0] + qp * (ex + vXbx);
+    const T uhy = gamma * v[1] + qp * (ey + vXby);
+    const T uhz = gamma * v[2] + qp * (ez + vXbz);
+    const T upx = uhx + qp * ex, upy = uhy + qp * ey, upz = uhz + qp * ez;
+    const T gammap_sq = 1.0 + upx * upx + upy * upy + upz * upz;
+    const T taux = qp * bx, tauy = qp * by, tauz = qp * bz;
+    const T tau_sq = taux * taux + tauy * tauy + tauz * tauz;
+    const T sigma = gammap_sq - tau_sq;
+    const T ustar = upx * taux + upy * tauy + upz * tauz;
+    T gi = sqrt_(sigma * sigma + 4.0 * (tau_sq + ustar * ustar));
+    gi = sqrt_(0.5 * (sigma + gi));
+    const T tx = taux / gi, ty = tauy / gi, tz = tauz / gi;
+    const T s = 1.0 / (1.0 + tx * tx + ty * ty + tz * tz);
+    const T udott = ustar / gi;
+    const T cx = upy * tz - upz * ty, cy = upz * tx - upx * tz, cz = upx * ty - upy * tx;
+    const T ux = s * (upx + udott * tx + cx);
+    const T uy = s * (upy + udott * ty + cy);
+    const T uz = s * (upz + udott * tz + cz);
+    v[0] = ux / gi;
+    v[1] = uy / gi;
+    v[2] = uz / gi;
+    for (int a = 0; a < 3; a++) x[a] = x[a] + dt * v[a];
+    gamma = gi;
+}
+
+// Adjoint of vay_eval at inputs (f, v, gamma): lx, lv, lg hold the output
+// adjoints on entry and the input adjoints on exit; lf receives the field
+// adjoint.
+AD_HD void vay_rev(double qp, const double f[6], double dt, const double v_in[3], double g_in, double lx[3],
+                   double lv[3], double &lg, double lf[6]) {
+    const double e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
+    double vXb[3], up[3], tau[3];
+    cross3(v_in, b, vXb);
+    for (int a = 0; a < 3; a++) up[a] = g_in * v_in[a] + qp * (e[a] + vXb[a]) + qp * e[a];
+    const double gps = 1.0 + up[0] * up[0] + up[1] * up[1] + up[2] * up[2];
+    for (int a = 0; a < 3; a++) tau[a] = qp * b[a];
+    const double tsq = tau[0] * tau[0] + tau[1] * tau[1] + tau[2] * tau[2];
+    const double sigma = gps - tsq;
+    const double ustar = up[0] * tau[0] + up[1] * tau[1] + up[2] * tau[2];
+    const double gi1 = ::sqrt(sigma * sigma + 4.0 * (tsq + ustar * ustar));
+    const double gi = ::sqrt(0.5 * (sigma + gi1));
+    double tt[3];
+    for (int a = 0; a < 3; a++) tt[a] = tau[a] / gi;
+    const double s = 1.0 / (1.0 + tt[0] * tt[0] + tt[1] * tt[1] + tt[2] * tt[2]);
+    const double udott = ustar / gi;
+    double cr[3], w[3], vout[3];
+    cross3(up, tt, cr);
+    for (int a = 0; a < 3; a++) w[a] = up[a] + udott * tt[a] + cr[a];
+    for (int a = 0; a < 3; a++) vout[a] = s * w[a] / gi;
+    // reverse
+    double lvo[3];
+    for (int a = 0; a < 3; a++) lvo[a] = lv[a] + dt * lx[a];
+    double lgi = lg;
+    double luint[3];
+    for (int a = 0; a < 3; a++) luint[a] = lvo[a] / gi;
+    lgi += -(vout[0] * lvo[0] + vout[1] * lvo[1] + vout[2] * lvo[2]) / gi;
+    // uint = s w
+    const double ls = w[0] * luint[0] + w[1] * luint[1] + w[2] * luint[2];
+    double lw[3];
+    for (int a = 0; a < 3; a++) lw[a] = s * luint[a];
+    double lup[3], ltt[3], tmp[3];
+    for (int a = 0; a < 3; a++) lup[a] = lw[a];
+    const double ludott = tt[0] * lw[0] + tt[1] * lw[1] + tt[2] * lw[2];
+    for (int a = 0; a < 3; a++) ltt[a] = udott * lw[a];
+    cross3(tt, lw, tmp);
+    for (int a = 0; a < 3; a++) lup[a] += tmp[a];
+    cross3(lw, up, tmp);
+    for (int a = 0; a < 3; a++) ltt[a] += tmp[a];
+    // udott = ustar / gi
+    double lustar = ludott / gi;
+    lgi += -udott * ludott / gi;
+    // s = 1 / (1 + tt.tt)
+    for (int a = 0; a < 3; a++) ltt[a] += -2.0 * s * s * ls * tt[a];
+    // tt = tau / gi
+    double ltau[3];
+    for (int a = 0; a < 3; a++) ltau[a] = ltt[a] / gi;
+    lgi += -(tt[0] * ltt[0] + tt[1] * ltt[1] + tt[2] * ltt[2]) / gi;
+    // gi = sqrt(0.5 (sigma + gi1))
+    double lsigma = 0.25 * lgi / gi;
+    const double lgi1 = 0.25 * lgi / gi;
+    // gi1 = sqrt(sigma^2 + 4 tsq + 4 ustar^2)
+    lsigma += lgi1 * sigma / gi1;
+    double ltsq = 2.0 * lgi1 / gi1;
+    lustar += 4.0 * ustar * lgi1 / gi1;
+    // ustar = up . tau
+    for (int a = 0; a < 3; a++) {
+        lup[a] += tau[a] * lustar;
+        ltau[a] += up[a] * lustar;
+    }
+    // sigma = gps - tsq
+    const double lgps = lsigma;
+    ltsq -= lsigma;
+    for (int a = 0; a < 3; a++) ltau[a] += 2.0 * tau[a] * ltsq;
+    // gps = 1 + up.up
+    for (int a = 0; a < 3; a++) lup[a] += 2.0 * up[a] * lgps;
+    // up = g v + qp (e + v x b) + qp e
+    double lb[3], le[3], lvxb[3];
+    for (int a = 0; a < 3; a++) {
+        lb[a] = qp * ltau[a];
+        le[a] = 2.0 * qp * lup[a];
+        lvxb[a] = qp * lup[a];
+    }
+    lg = v_in[0] * lup[0] + v_in[1] * lup[1] + v_in[2] * lup[2];
+    for (int a = 0; a < 3; a++) lv[a] = g_in * lup[a];
+    cross3(b, lvxb, tmp);
+    for (int a = 0; a < 3; a++) lv[a] += tmp[a];
+    cross3(lvxb, v_in, tmp);
+    for (int a = 0; a < 3; a++) lb[a] += tmp[a];
+    for (int a = 0; a < 3; a++) {
+        lf[a] += le[a];
+        lf[3 + a] += lb[a];
+    }
+}
+
+// ---- current deposit ----------------------------------------------------
+//
+// The 12 J edge contributions of a particle at offset r from its cell's
+// vertex with velocity vv; uq = UNIT_RHOJ q.
+template <class T>
+AD_HD void jterms_eval(const CellGeo &c, double uq, const T r[3], const T vv[3], T out[12]) {
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        const double lj = c.d[j], lk = c.d[k];
+        const T cur = uq * vv[i];
+        const T ratio = (cur / c.vol) / c.area[i];
+        out[4 * i] = ratio * (lj - r[j]) * (lk - r[k]);
+        out[4 * i + 1] = ratio * r[j] * (lk - r[k]);
+        out[4 * i + 2] = ratio * r[j] * r[k];
+        out[4 * i + 3] = ratio * (lj - r[j]) * r[k];
+    }
+}
+
+// Adjoint of jterms_eval: the adjoint of each contribution is the adjoint of
+// the grid point it lands on (a gather); adds to lr[3] and lvv[3].
+AD_HD void jterms_rev(const CellGeo &c, double uq, const double r[3], const double vv[3], const double lout[12],
+                      double lr[3], double lvv[3]) {
+    for (int i = 0; i < 3; i++) {
+        const int j = (i + 1) % 3, k = (i + 2) % 3;
+        const double lj = c.d[j], lk = c.d[k];
+        const double ratio = ((uq * vv[i]) / c.vol) / c.area[i];
+        const double A = lj - r[j], Bk = lk - r[k];
+        const double l0 = lout[4 * i], l1 = lout[4 * i + 1], l2 = lout[4 * i + 2], l3 = lout[4 * i + 3];
+        const double lratio = l0 * A * Bk + l1 * r[j] * Bk + l2 * r[j] * r[k] + l3 * A * r[k];
+        lvv[i] += lratio * uq / c.vol / c.area[i];
+        lr[j] += ratio * (-l0 * Bk + l1 * Bk + l2 * r[k] - l3 * r[k]);
+        lr[k] += ratio * (-l0 * A - l1 * r[j] + l2 * r[j] + l3 * A);
+    }
+}
+
+}  // namespace ad
+}  // namespace emoo

@@ -1,0 +1,175 @@
+// Host check of apc_524_project_gb300/csrc/ad_math.cuh (built by
+// tests/test_ad_math.py with g++): for the gather, both pushers and the
+// current terms, on seeded random inputs,
+//   * the Dual (tangent-linear) derivative matches a central difference of
+//     the double evaluation;
+//   * the reverse (adjoint) function is the transpose of the Dual one:
+//     <lambda, J delta> == <J^T lambda, delta> to rounding.
+// Prints one line per check and exits non-zero if any fails.
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "ad_math.cuh"
+
+using namespace emoo::ad;
+
+static std::mt19937_64 rng(20240404);
+static double U(double a, double b) { return std::uniform_real_distribution<double>(a, b)(rng); }
+
+static int failures = 0;
+static void report(const char *what, double got, double want, double tol) {
+    double err = std::fabs(got - want) / std::fmax(std::fabs(want), 1e-300);
+    bool ok = err <= tol;
+    if (!ok) failures++;
+    std::printf("%-28s %s  got % .16e want % .16e rel %.2e\n", what, ok ? "ok  " : "FAIL", got, want, err);
+}
+
+static CellGeo geo() {
+    CellGeo c;
+    c.d[0] = U(0.5, 1.5);
+    c.d[1] = U(0.5, 1.5);
+    c.d[2] = U(0.5, 1.5);
+    for (int i = 0; i < 3; i++) c.area[i] = c.d[(i + 1) % 3] * c.d[(i + 2) % 3];
+    c.vol = c.d[0] * c.d[1] * c.d[2];
+    return c;
+}
+
+// generic check of a map R^n -> R^m given as double and Dual evaluations
+template <class FD, class FDual, class FRev>
+static void check(const char *name, int n, int m, const double *x0, FD fd, FDual fdual, FRev frev, double fd_tol) {
+    std::vector<double> dir(n), lam(m), y(m), yp(m), ym(m), xp(n), xm(n), jd(m), jtl(n, 0.0);
+    for (int i = 0; i < n; i++) dir[i] = U(-1, 1);
+    for (int i = 0; i < m; i++) lam[i] = U(-1, 1);
+    // Dual directional derivative
+    fdual(x0, dir.data(), jd.data());
+    // central difference
+    const double h = 1e-6;
+    for (int i = 0; i < n; i++) {
+        xp[i] = x0[i] + h * dir[i];
+        xm[i] = x0[i] - h * dir[i];
+    }
+    fd(xp.data(), yp.data());
+    fd(xm.data(), ym.data());
+    double num = 0, den = 0;
+    for (int i = 0; i < m; i++) {
+        double c = (yp[i] - ym[i]) / (2 * h);
+        num += (c - jd[i]) * (c - jd[i]);
+        den += jd[i] * jd[i];
+    }
+    char buf[96];
+    const double rel = std::sqrt(num / den);
+    const bool fd_ok = rel <= fd_tol;
+    if (!fd_ok) failures++;
+    std::printf("%-28s %s  relative L2 %.2e (bar %.0e)\n", (std::string(name) + " tangent vs FD").c_str(),
+                fd_ok ? "ok  " : "FAIL", rel, fd_tol);
+    // adjoint: J^T lam
+    frev(x0, lam.data(), jtl.data());
+    double lhs = 0, rhs = 0;
+    for (int i = 0; i < m; i++) lhs += lam[i] * jd[i];
+    for (int i = 0; i < n; i++) rhs += jtl[i] * dir[i];
+    std::snprintf(buf, sizeof buf, "%s <l,Jd> = <J'l,d>", name);
+    report(buf, rhs, lhs, 1e-12);
+}
+
+int main() {
+    for (int trial = 0; trial < 5; trial++) {
+        const CellGeo c = geo();
+        // ---- gather: inputs v[18], ds[3] -> out[6]
+        {
+            double x0[21];
+            for (int i = 0; i < 18; i++) x0[i] = U(-1, 1);
+            for (int a = 0; a < 3; a++) x0[18 + a] = -U(0.0, 1.0) * c.d[a];
+            auto fd = [&](const double *x, double *y) { gather_eval(c, x, x + 18, y); };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual v[18], ds[3], o[6];
+                for (int i = 0; i < 18; i++) v[i] = mk(x[i], d[i]);
+                for (int a = 0; a < 3; a++) ds[a] = mk(x[18 + a], d[18 + a]);
+                gather_eval(c, v, ds, o);
+                for (int i = 0; i < 6; i++) jd[i] = o[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                gather_rev(c, x, x + 18, l, jt, jt + 18);
+            };
+            check("gather", 21, 6, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- Boris: inputs f[6], x[3], v[3] -> x'[3], v'[3]
+        {
+            const double qp = U(-0.3, 0.3), dt = 0.5;
+            double x0[12];
+            for (int i = 0; i < 6; i++) x0[i] = U(-1, 1);
+            for (int i = 6; i < 9; i++) x0[i] = U(0, 10);
+            for (int i = 9; i < 12; i++) x0[i] = U(-0.5, 0.5);
+            auto fd = [&](const double *x, double *y) {
+                double xx[3] = {x[6], x[7], x[8]}, vv[3] = {x[9], x[10], x[11]};
+                boris_eval(qp, x, dt, xx, vv);
+                for (int a = 0; a < 3; a++) { y[a] = xx[a]; y[3 + a] = vv[a]; }
+            };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual f[6], xx[3], vv[3];
+                for (int i = 0; i < 6; i++) f[i] = mk(x[i], d[i]);
+                for (int a = 0; a < 3; a++) { xx[a] = mk(x[6 + a], d[6 + a]); vv[a] = mk(x[9 + a], d[9 + a]); }
+                boris_eval(qp, f, dt, xx, vv);
+                for (int a = 0; a < 3; a++) { jd[a] = xx[a].d; jd[3 + a] = vv[a].d; }
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                double lx[3] = {l[0], l[1], l[2]}, lv[3] = {l[3], l[4], l[5]}, lf[6] = {0, 0, 0, 0, 0, 0};
+                boris_rev(qp, x, dt, x + 9, lx, lv, lf);
+                for (int i = 0; i < 6; i++) jt[i] = lf[i];
+                for (int a = 0; a < 3; a++) { jt[6 + a] = lx[a]; jt[9 + a] = lv[a]; }
+            };
+            check("boris", 12, 6, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- Vay: inputs f[6], x[3], v[3], gamma -> x'[3], v'[3], gamma'
+        {
+            const double qp = U(-0.3, 0.3), dt = 0.5;
+            double x0[13];
+            for (int i = 0; i < 6; i++) x0[i] = U(-1, 1);
+            for (int i = 6; i < 9; i++) x0[i] = U(0, 10);
+            for (int i = 9; i < 12; i++) x0[i] = U(-0.5, 0.5);
+            x0[12] = 1.0 / std::sqrt(1.0 - (x0[9] * x0[9] + x0[10] * x0[10] + x0[11] * x0[11]));
+            auto fd = [&](const double *x, double *y) {
+                double xx[3] = {x[6], x[7], x[8]}, vv[3] = {x[9], x[10], x[11]}, g = x[12];
+                vay_eval(qp, x, dt, xx, vv, g);
+                for (int a = 0; a < 3; a++) { y[a] = xx[a]; y[3 + a] = vv[a]; }
+                y[6] = g;
+            };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual f[6], xx[3], vv[3], g = mk(x[12], d[12]);
+                for (int i = 0; i < 6; i++) f[i] = mk(x[i], d[i]);
+                for (int a = 0; a < 3; a++) { xx[a] = mk(x[6 + a], d[6 + a]); vv[a] = mk(x[9 + a], d[9 + a]); }
+                vay_eval(qp, f, dt, xx, vv, g);
+                for (int a = 0; a < 3; a++) { jd[a] = xx[a].d; jd[3 + a] = vv[a].d; }
+                jd[6] = g.d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                double lx[3] = {l[0], l[1], l[2]}, lv[3] = {l[3], l[4], l[5]}, lg = l[6], lf[6] = {0, 0, 0, 0, 0, 0};
+                vay_rev(qp, x, dt, x + 9, x[12], lx, lv, lg, lf);
+                for (int i = 0; i < 6; i++) jt[i] = lf[i];
+                for (int a = 0; a < 3; a++) { jt[6 + a] = lx[a]; jt[9 + a] = lv[a]; }
+                jt[12] = lg;
+            };
+            check("vay", 13, 7, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- J terms: inputs r[3], v[3] -> 12 contributions
+        {
+            const double uq = U(-2, 2);
+            double x0[6];
+            for (int a = 0; a < 3; a++) x0[a] = -U(0.0, 1.0) * c.d[a];
+            for (int a = 3; a < 6; a++) x0[a] = U(-0.5, 0.5);
+            auto fd = [&](const double *x, double *y) { jterms_eval(c, uq, x, x + 3, y); };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual r[3], vv[3], o[12];
+                for (int a = 0; a < 3; a++) { r[a] = mk(x[a], d[a]); vv[a] = mk(x[3 + a], d[3 + a]); }
+                jterms_eval(c, uq, r, vv, o);
+                for (int i = 0; i < 12; i++) jd[i] = o[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) { jterms_rev(c, uq, x, x + 3, l, jt, jt + 3); };
+            check("jterms", 6, 12, x0, fd, fdual, frev, 1e-7);
+        }
+    }
+    std::printf("%s (%d failures)\n", failures ? "FAILED" : "PASSED", failures);
+    return failures ? 1 : 0;
+}

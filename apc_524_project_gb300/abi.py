@@ -122,6 +122,28 @@ class Stats(C.Structure):
     ]
 
 
+AD_FORWARD, AD_TANGENT, AD_ADJOINT = 0, 1, 2
+
+
+class AdSpec(C.Structure):
+    _fields_ = [
+        ("nsteps", C.c_int),
+        ("checkpoint_every", C.c_int),
+        ("slab_lo", C.c_int),
+        ("slab_hi", C.c_int),
+    ]
+
+
+class AdResult(C.Structure):
+    _fields_ = [
+        ("objective", C.c_double),
+        ("tangent", C.c_double),
+        ("forward_ms", C.c_double),
+        ("recompute_ms", C.c_double),
+        ("reverse_ms", C.c_double),
+    ]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
@@ -166,6 +188,8 @@ PROTOTYPES = {
     "emoo_set_profiling": (C.c_int, [_P, C.c_int]),
     "emoo_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "emoo_sort_permutation_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
+    "emoo_set_waves": (C.c_int, [_P, C.c_int, _D, _D]),
+    "emoo_ad_run": (C.c_int, [_P, C.POINTER(AdSpec), C.c_int, _D, _D, C.POINTER(AdResult), _D, _D]),
 }
 
 NOALLOC_SORT_MAX = 1048576

@@ -29,6 +29,7 @@ CUDA_UNITS = [
     ("loader.cu", ["--fmad=false"]),
     ("sort.cu", []),
     ("particles_mixed.cu", ["--fmad=true"]),
+    ("adjoint_f64.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["api.cpp", "loader_host.cpp", "input_parser.cpp"]
 

@@ -254,6 +254,26 @@ def twostream(n=(256, 128, 128), steps=1000):
         relativity=1, init="constant", nstep_sort=20, seed=20240303, immobile_ions=True, b_noise=1e-4)
 
 
+def laser64(n=(64, 64, 64), steps=128, ppc=8, a0=0.5, wavelength=16.0, fwhm_steps=40):
+    """Differentiation workload: a y-polarised plane wave injected at x-left
+    (amplitude a0 omega, omega = 2 pi / wavelength, Gaussian envelope of the
+    given FWHM in steps, peak after two FWHM), reflecting particle walls in
+    x, periodic y and z, electrons and ions at ppc each (electron v_th =
+    0.05c), fields starting at zero. Objective slab x in [48, 56) of 64."""
+    dt = 0.5
+    omega = 2.0 * PI / wavelength
+    fwhm_t = fwhm_steps * dt
+    wave = Wave(side=-1, pol=2, amp=a0 * omega, omega=omega, phase_deg=0.0,
+                inv_width=math.sqrt(math.log(2.0)) / (0.5 * fwhm_t), delay=2.0 * fwhm_t)
+    return Config(
+        name="laser64", n=tuple(n), dt=dt, steps=steps, omega_pe=0.3,
+        species=[Species("e", -1.0, 1.0, ppc, 0.05), Species("i", 1.0, 1836.0, ppc, 0.05 / math.sqrt(1836.0))],
+        relativity=1, init="constant",
+        part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
+        field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
+        waves=[wave], seed=20240505)
+
+
 def tiny(name="tiny", n=(6, 5, 4), dx=(1.0, 1.0, 1.0), ppc=3, relativity=0, init="poisson", steps=4,
          part_bc=("periodic",) * 6, field_bc=("periodic",) * 6, waves=(), B0=(0.0, 0.0, 0.0), E0=(0.0, 0.0, 0.0),
          vth=0.08, nstep_sort=0, seed=7, dt=0.45, test_species=False):

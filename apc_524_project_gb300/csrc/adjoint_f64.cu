@@ -1,0 +1,901 @@
+// adjoint_f64.cu - differentiation of the FP64 time loop (no reference
+// counterpart): a tangent-linear run and an adjoint run with checkpoints.
+//
+// The differentiated step is the loop's step without sorting and without the
+// charge density: gather + push + particle boundaries + current deposit (one
+// particle kernel), the periodic J fold, the Yee update and executeBC(-1)
+// (periodic ghost copies, LightBC planes). Its parameters are the initial
+// particle velocities and the amplitude and phase of every injected wave; the
+// objective is the field energy 0.5 V sum(E^2 + B^2) over the grid points of
+// an x slab at the last step.
+//
+//  * Tangent: the particle kernel runs in dual numbers (ad_math.cuh) next to
+//    the primal one; the field part is linear, so the tangent fields go
+//    through the primal field kernels themselves (with the slot table pointed
+//    at the tangent arrays) and the planes take the derivative of their
+//    values.
+//  * Adjoint: every kernel has a transposed twin here. The deposit's adjoint
+//    is a gather of the J adjoint at the particle's 12 points, the gather's
+//    adjoint a scatter (atomics) of the field adjoint with the same weights,
+//    the Yee and ghost/fold adjoints are the transposed stencils and copies,
+//    a plane's adjoint reduces the field adjoint over the plane into the
+//    wave-parameter gradient and clears the plane. State is checkpointed
+//    every `checkpoint_every` steps; each segment is recomputed forward,
+//    storing the state before each of its steps, then reversed.
+//
+// Compiled with --fmad=false like the FP64 kernels, so the dual numbers'
+// primal values and the adjoint's recomputed forward are bit-identical to the
+// primal step, and every cell and boundary decision agrees with it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "ad_math.cuh"
+#include "dev_common.cuh"
+#include "emoo_internal.h"
+
+namespace emoo {
+
+double *role_b(emoo_handle *h, int c);
+double *role_t(emoo_handle *h, int c);
+
+namespace {
+
+using ad::CellGeo;
+using ad::Dual;
+using ad::mk;
+
+constexpr double FOURPI = 4.0 * PI_D;
+
+constexpr int NSLOT = EMOO_BZ_TM1 + 1;  // E, B, J, rho, B_tm1: the slots a step touches
+
+struct PArr {
+    double *p[7];  // x, y, z, vx, vy, vz, gamma
+};
+struct CPArr {
+    const double *p[7];
+};
+struct FPtrs {
+    const double *E[3], *B[3], *T[3];  // E, B role, B_tm1 role
+};
+struct FOut {
+    double *E[3], *B[3], *T[3];
+};
+struct JPtrs {
+    double *J[3];
+};
+
+__device__ __forceinline__ CellGeo cell_geo(const Geom &g) {
+    CellGeo c;
+    for (int a = 0; a < 3; a++) {
+        c.d[a] = g.d[a];
+        c.area[a] = g.area[a];
+    }
+    c.vol = g.vol;
+    return c;
+}
+
+// grid point of J contribution q (< 12) of cell o (Grid::addJ, the Jx quirk
+// at q = 3, src/grid/oGrid.cpp:98-111)
+__device__ __forceinline__ int64_t jpoint(const Geom &g, int64_t o, int q) {
+    const int64_t sx = g.sx, sy = g.sy;
+    switch (q) {
+        case 0: return o;
+        case 1: return o + sy;
+        case 2: return o + sy + 1;
+        case 3: return o + sy;
+        case 4: return o;
+        case 5: return o + 1;
+        case 6: return o + sx + 1;
+        case 7: return o + sx;
+        case 8: return o;
+        case 9: return o + sx;
+        case 10: return o + sx + sy;
+        default: return o + sy;
+    }
+}
+
+// the 18 gather inputs of cell o: 12 E edge points, 6 B face points
+__device__ __forceinline__ void gather_points(const Geom &g, int64_t o, int64_t pt[18]) {
+    const int64_t sx = g.sx, sy = g.sy;
+    const int64_t e[12] = {o, o + sy, o + sy + 1, o + 1, o, o + 1, o + sx + 1, o + sx, o, o + sx, o + sx + sy, o + sy};
+    for (int k = 0; k < 12; k++) pt[k] = e[k];
+    pt[12] = o;
+    pt[13] = o + sx;
+    pt[14] = o;
+    pt[15] = o + sy;
+    pt[16] = o;
+    pt[17] = o + 1;
+}
+
+// executeBC of the particles (apply_bc in particles_f64.cu) on any scalar;
+// decisions on the primal values. Returns -1 when the particle is removed,
+// else a 3-bit mask of the axes reflected an odd number of times.
+template <class T>
+__device__ __forceinline__ int bc_t(const BCTab &bc, T p[3], T v[3]) {
+    int flips = 0;
+    for (int s = 0; s < 6; s++) {
+        const int d = s >> 1;
+        const bool right = s & 1;
+        const double xmin = bc.xmin[d], xmax = bc.xmax[d];
+        const double pv = ad::val(p[d]);
+        const bool hit = right ? (pv > xmax) : (pv < xmin);
+        if (!hit) continue;
+        const int kind = bc.pbc[s];
+        if (kind == PBC_PERIODIC) {
+            if (right) p[d] = p[d] - (xmax - xmin);
+            else p[d] = p[d] + (xmax - xmin);
+        } else if (kind == PBC_REFLECTING) {
+            p[d] = right ? 2.0 * xmax - p[d] : 2.0 * xmin - p[d];
+            v[d] = -v[d];
+            flips ^= 1 << d;
+        } else {
+            return -1;
+        }
+    }
+    return flips;
+}
+
+// ---- tangent particle kernel ---------------------------------------------
+//
+// Reads the primal state before the step (P, F) and the tangents (dP, dF),
+// writes the tangents after the step and adds the tangent current to dJ.
+template <bool REL>
+__global__ void k_tlm_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs F, FPtrs dF, PArr dP, int64_t np,
+                                double dt, JPtrs dJ) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const double x = P.p[0][p];
+    if (x != x) return;  // removed
+    const int s = species_of(st, p);
+    int ix, iy, iz;
+    cell_of(g, x, P.p[1][p], P.p[2][p], ix, iy, iz);
+    if (!cell_ok(g, ix, iy, iz)) return;
+    const int64_t o = gidx(g, ix, iy, iz);
+    int64_t pt[18];
+    gather_points(g, o, pt);
+    Dual v18[18];
+    for (int k = 0; k < 12; k++) {
+        const int c = k >> 2;
+        v18[k] = mk(F.E[c][pt[k]], dF.E[c][pt[k]]);
+    }
+    for (int k = 12; k < 18; k++) {
+        const int c = (k - 12) >> 1;
+        v18[k] = mk((F.T[c][pt[k]] + F.B[c][pt[k]]) / 2, (dF.T[c][pt[k]] + dF.B[c][pt[k]]) / 2);
+    }
+    const CellGeo cg = cell_geo(g);
+    Dual pos[3], vel[3], ds[3], f[6];
+    for (int a = 0; a < 3; a++) {
+        pos[a] = mk(P.p[a][p], dP.p[a][p]);
+        vel[a] = mk(P.p[3 + a][p], dP.p[3 + a][p]);
+    }
+    const int ic[3] = {ix, iy, iz};
+    for (int a = 0; a < 3; a++) ds[a] = pos[a] - (g.x0[a] + g.d[a] * ic[a]);
+    ad::gather_eval(cg, v18, ds, f);
+    Dual gam = mk(REL ? P.p[6][p] : 1.0, REL ? dP.p[6][p] : 0.0);
+    if (REL) ad::vay_eval(st.qp[s], f, dt, pos, vel, gam);
+    else ad::boris_eval(st.qp[s], f, dt, pos, vel);
+    if (bc_t(bc, pos, vel) < 0) {
+        for (int a = 0; a < 7; a++) dP.p[a][p] = 0.0;
+        return;
+    }
+    if (st.deposit[s]) {
+        cell_of(g, pos[0].v, pos[1].v, pos[2].v, ix, iy, iz);
+        if (cell_ok(g, ix, iy, iz)) {
+            const int64_t o2 = gidx(g, ix, iy, iz);
+            const int jc[3] = {ix, iy, iz};
+            Dual r[3], c12[12];
+            for (int a = 0; a < 3; a++) r[a] = pos[a] - (g.x0[a] + g.d[a] * jc[a]);
+            ad::jterms_eval(cg, st.uq[s], r, vel, c12);
+            for (int q = 0; q < 12; q++) atomicAdd(dJ.J[q >> 2] + jpoint(g, o2, q), c12[q].d);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        dP.p[a][p] = pos[a].d;
+        dP.p[3 + a][p] = vel[a].d;
+    }
+    if (REL) dP.p[6][p] = gam.d;
+}
+
+// ---- adjoint particle kernel ---------------------------------------------
+//
+// P, F: the primal state before the step (from the tape). L: the particle
+// adjoints, after the step on entry, before it on exit. LJ: the adjoint of
+// the deposited current. LF: field adjoints that receive the gather's
+// adjoint (atomics).
+template <bool REL>
+__global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs F, PArr L, int64_t np, double dt,
+                                JPtrs LJ, FOut LF) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const double x = P.p[0][p];
+    if (x != x) return;
+    const int s = species_of(st, p);
+    int ix, iy, iz;
+    cell_of(g, x, P.p[1][p], P.p[2][p], ix, iy, iz);
+    if (!cell_ok(g, ix, iy, iz)) return;
+    const int64_t o = gidx(g, ix, iy, iz);
+    int64_t pt[18];
+    gather_points(g, o, pt);
+    double v18[18];
+    for (int k = 0; k < 12; k++) v18[k] = F.E[k >> 2][pt[k]];
+    for (int k = 12; k < 18; k++) {
+        const int c = (k - 12) >> 1;
+        v18[k] = (F.T[c][pt[k]] + F.B[c][pt[k]]) / 2;
+    }
+    const CellGeo cg = cell_geo(g);
+    const int ic[3] = {ix, iy, iz};
+    double pos[3], vel[3], ds[3], f[6];
+    for (int a = 0; a < 3; a++) {
+        pos[a] = P.p[a][p];
+        vel[a] = P.p[3 + a][p];
+        ds[a] = pos[a] - (g.x0[a] + g.d[a] * ic[a]);
+    }
+    ad::gather_eval(cg, v18, ds, f);
+    const double v_in[3] = {vel[0], vel[1], vel[2]};
+    const double g_in = REL ? P.p[6][p] : 1.0;
+    double gam = g_in;
+    if (REL) ad::vay_eval(st.qp[s], f, dt, pos, vel, gam);
+    else ad::boris_eval(st.qp[s], f, dt, pos, vel);
+    const int flips = bc_t(bc, pos, vel);
+    double lx[3], lv[3], lg = REL ? L.p[6][p] : 0.0;
+    for (int a = 0; a < 3; a++) {
+        lx[a] = L.p[a][p];
+        lv[a] = L.p[3 + a][p];
+    }
+    if (flips < 0) {  // removed: nothing after the step depends on it
+        for (int a = 0; a < 3; a++) lx[a] = lv[a] = 0.0;
+        lg = 0.0;
+    } else {
+        if (st.deposit[s]) {
+            int jx, jy, jz;
+            cell_of(g, pos[0], pos[1], pos[2], jx, jy, jz);
+            if (cell_ok(g, jx, jy, jz)) {
+                const int64_t o2 = gidx(g, jx, jy, jz);
+                const int jc[3] = {jx, jy, jz};
+                double r[3], l12[12];
+                for (int a = 0; a < 3; a++) r[a] = pos[a] - (g.x0[a] + g.d[a] * jc[a]);
+                for (int q = 0; q < 12; q++) l12[q] = LJ.J[q >> 2][jpoint(g, o2, q)];
+                ad::jterms_rev(cg, st.uq[s], r, vel, l12, lx, lv);
+            }
+        }
+        for (int a = 0; a < 3; a++)
+            if ((flips >> a) & 1) {
+                lx[a] = -lx[a];
+                lv[a] = -lv[a];
+            }
+    }
+    double lf[6] = {0, 0, 0, 0, 0, 0};
+    if (REL) ad::vay_rev(st.qp[s], f, dt, v_in, g_in, lx, lv, lg, lf);
+    else ad::boris_rev(st.qp[s], f, dt, v_in, lx, lv, lf);
+    double l18[18] = {0}, lds[3] = {0, 0, 0};
+    ad::gather_rev(cg, v18, ds, lf, l18, lds);
+    for (int k = 0; k < 12; k++)
+        if (l18[k] != 0.0) atomicAdd(LF.E[k >> 2] + pt[k], l18[k]);
+    for (int k = 12; k < 18; k++) {
+        const int c = (k - 12) >> 1;
+        if (l18[k] != 0.0) {
+            atomicAdd(LF.B[c] + pt[k], 0.5 * l18[k]);
+            atomicAdd(LF.T[c] + pt[k], 0.5 * l18[k]);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        L.p[a][p] = lx[a] + lds[a];
+        L.p[3 + a][p] = lv[a];
+    }
+    if (REL) L.p[6][p] = lg;
+}
+
+// ---- field adjoints ------------------------------------------------------
+
+__device__ __forceinline__ bool phys(const Geom &g, int i, int j, int k) {
+    return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];
+}
+
+// Adjoint of k_yee_b (B = T + dt curl E over the physical points), gather
+// form over every grid point: LT += LB (physical), LE += dt C_E^T LB.
+__global__ void k_yee_b_adj(Geom g, double dt, FOut A) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
+    const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
+    const double cx = dt / g.d[0], cy = dt / g.d[1], cz = dt / g.d[2];
+    const bool here = phys(g, i, j, k);
+    if (here)
+        for (int c = 0; c < 3; c++) A.T[c][p] += A.B[c][p];
+    const double *Bx = A.B[0], *By = A.B[1], *Bz = A.B[2];
+    // Ey: Bx(o) += cz (Ey[o+1] - Ey[o]); Bz(o) -= cx (Ey[o+sx] - Ey[o])
+    double ley = 0, lez = 0, lex = 0;
+    if (phys(g, i, j, k - 1)) ley += cz * Bx[p - 1];
+    if (here) ley += -cz * Bx[p] + cx * Bz[p];
+    if (phys(g, i - 1, j, k)) ley += -cx * Bz[p - sx];
+    // Ez: Bx(o) -= cy (Ez[o+sy] - Ez[o]); By(o) += cx (Ez[o+sx] - Ez[o])
+    if (phys(g, i, j - 1, k)) lez += -cy * Bx[p - sy];
+    if (here) lez += cy * Bx[p] - cx * By[p];
+    if (phys(g, i - 1, j, k)) lez += cx * By[p - sx];
+    // Ex: By(o) -= cz (Ex[o+1] - Ex[o]); Bz(o) += cy (Ex[o+sy] - Ex[o])
+    if (phys(g, i, j, k - 1)) lex += -cz * By[p - 1];
+    if (here) lex += cz * By[p] - cy * Bz[p];
+    if (phys(g, i, j - 1, k)) lex += cy * Bz[p - sy];
+    A.E[0][p] += lex;
+    A.E[1][p] += ley;
+    A.E[2][p] += lez;
+}
+
+// Adjoint of k_yee_e (E -= dt (curl T + 4 pi J) over the physical points):
+// LJ = -4 pi dt LE (physical, 0 elsewhere), LT += transposed curl; the B role
+// was overwritten by the step, so its physical points' adjoint is cleared.
+__global__ void k_yee_e_adj(Geom g, double dt, FOut A, JPtrs LJ) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
+    const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
+    const double cx = dt / g.d[0], cy = dt / g.d[1], cz = dt / g.d[2];
+    const bool here = phys(g, i, j, k);
+    const double *Ex = A.E[0], *Ey = A.E[1], *Ez = A.E[2];
+    for (int c = 0; c < 3; c++) LJ.J[c][p] = here ? -FOURPI * dt * A.E[c][p] : 0.0;
+    double lty = 0, ltz = 0, ltx = 0;
+    // Ty: ex(o) -= cz (Ty[o] - Ty[o-1]); ez(o) += cx (Ty[o] - Ty[o-sx])
+    if (here) lty += -cz * Ex[p] + cx * Ez[p];
+    if (phys(g, i, j, k + 1)) lty += cz * Ex[p + 1];
+    if (phys(g, i + 1, j, k)) lty += -cx * Ez[p + sx];
+    // Tz: ex(o) += cy (Tz[o] - Tz[o-sy]); ey(o) -= cx (Tz[o] - Tz[o-sx])
+    if (here) ltz += cy * Ex[p] - cx * Ey[p];
+    if (phys(g, i, j + 1, k)) ltz += -cy * Ex[p + sy];
+    if (phys(g, i + 1, j, k)) ltz += cx * Ey[p + sx];
+    // Tx: ey(o) += cz (Tx[o] - Tx[o-1]); ez(o) -= cy (Tx[o] - Tx[o-sy])
+    if (here) ltx += cz * Ey[p] - cy * Ez[p];
+    if (phys(g, i, j, k + 1)) ltx += -cz * Ey[p + 1];
+    if (phys(g, i, j + 1, k)) ltx += cy * Ez[p + sy];
+    A.T[0][p] += ltx;
+    A.T[1][p] += lty;
+    A.T[2][p] += ltz;
+    if (here)
+        for (int c = 0; c < 3; c++) A.B[c][p] = 0.0;
+}
+
+// Adjoint of k_fold (F[plane 1] += F[plane n+1], transverse physical range,
+// the two transverse J components): LF[n+1] += LF[1].
+__global__ void k_fold_adj(Geom g, int d, double *f0, double *f1) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (q > g.n[o2] || r > g.n[o1]) return;
+    int is[3], it[3];
+    is[d] = g.n[d] + 1;
+    it[d] = 1;
+    is[o1] = it[o1] = r;
+    is[o2] = it[o2] = q;
+    const int64_t s = gidx(g, is[0], is[1], is[2]), t = gidx(g, it[0], it[1], it[2]);
+    double *F = blockIdx.z == 0 ? f0 : f1;
+    F[s] += F[t];
+}
+
+struct Slots6 {
+    double *p[6];
+};
+
+// Adjoint of one side of k_ghost (ghost plane <- physical plane, transverse
+// physical range): LF[src] += LF[dst], LF[dst] = 0.
+__global__ void k_ghost_adj(Geom g, Slots6 fl, int d, int side) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (q > g.n[o2] || r > g.n[o1]) return;
+    const int nd = g.n[d];
+    const int src = side == 0 ? nd : 1, dst = side == 0 ? 0 : nd + 1;
+    int is[3], it[3];
+    is[d] = src;
+    it[d] = dst;
+    is[o1] = it[o1] = r;
+    is[o2] = it[o2] = q;
+    double *F = fl.p[blockIdx.z];
+    const int64_t ps = gidx(g, is[0], is[1], is[2]), pd = gidx(g, it[0], it[1], it[2]);
+    F[ps] += F[pd];
+    F[pd] = 0.0;
+}
+
+struct PlaneCoef {
+    int nk;
+    int kidx[2 * EMOO_NWAVE];
+    double coef[2 * EMOO_NWAVE];
+};
+
+// Adjoint of a whole-plane set: the plane's value depends only on the wave
+// parameters, so dtheta_k += coef_k sum(LF over the plane) and the plane's
+// adjoint is cleared.
+__global__ void k_plane_adj(Geom g, double *F, int d, int idx, PlaneCoef pc, double *dtheta) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    double sum = 0.0;
+    const int64_t m = (int64_t)g.tot[o1] * g.tot[o2];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        int c[3];
+        c[d] = idx;
+        c[o1] = (int)(t / g.tot[o2]);
+        c[o2] = (int)(t % g.tot[o2]);
+        const int64_t p = gidx(g, c[0], c[1], c[2]);
+        sum += F[p];
+        F[p] = 0.0;
+    }
+    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
+    if ((threadIdx.x & 31) == 0 && sum != 0.0)
+        for (int k = 0; k < pc.nk; k++) atomicAdd(dtheta + pc.kidx[k], pc.coef[k] * sum);
+}
+
+// ---- objective -----------------------------------------------------------
+
+struct Slab {
+    int lo, hi;  // grid point x index range [lo, hi)
+};
+
+// 0.5 V sum(E^2 + B^2) over the slab (and, with dE/dB, V sum(E dE + B dB)).
+__global__ void k_objective(Geom g, Slab sl, FPtrs F, FPtrs dF, int tangent, double *out2) {
+    const int64_t ny = g.n[1], nz = g.n[2];
+    const int64_t m = (int64_t)(sl.hi - sl.lo) * ny * nz;
+    double a = 0.0, b = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t % nz) + 1;
+        const int j = (int)((t / nz) % ny) + 1;
+        const int i = (int)(t / (nz * ny)) + sl.lo;
+        const int64_t p = gidx(g, i, j, k);
+        for (int c = 0; c < 3; c++) {
+            a += F.E[c][p] * F.E[c][p] + F.B[c][p] * F.B[c][p];
+            if (tangent) b += F.E[c][p] * dF.E[c][p] + F.B[c][p] * dF.B[c][p];
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out2, 0.5 * g.vol * a);
+        atomicAdd(out2 + 1, g.vol * b);
+    }
+}
+
+// Seeds the field adjoints with d objective / d(E, B role) = V (E, B) on the slab.
+__global__ void k_objective_seed(Geom g, Slab sl, FPtrs F, FOut A) {
+    const int64_t ny = g.n[1], nz = g.n[2];
+    const int64_t m = (int64_t)(sl.hi - sl.lo) * ny * nz;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t % nz) + 1;
+        const int j = (int)((t / nz) % ny) + 1;
+        const int i = (int)(t / (nz * ny)) + sl.lo;
+        const int64_t p = gidx(g, i, j, k);
+        for (int c = 0; c < 3; c++) {
+            A.E[c][p] += g.vol * F.E[c][p];
+            A.B[c][p] += g.vol * F.B[c][p];
+        }
+    }
+}
+
+int pblocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 64)); }
+
+// ---- host side -----------------------------------------------------------
+
+// The state the differentiated step reads: particles and the E / B slots.
+struct Snapshot {
+    double *buf = nullptr;
+    int bswap = 0;
+    double t = 0.0;
+    int64_t step = 0;
+};
+
+struct AdRun {
+    emoo_handle *h;
+    int64_t np, npts;
+    bool rel;
+    std::vector<double *> owned;
+
+    double *alloc(size_t n) {
+        double *p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) return nullptr;
+        owned.push_back(p);
+        return p;
+    }
+    ~AdRun() {
+        for (double *p : owned) cudaFree(p);
+    }
+    size_t snap_words() const { return 7 * (size_t)np + 9 * (size_t)npts; }
+    double **particle_ptrs(double **out7) {
+        out7[0] = h->x; out7[1] = h->y; out7[2] = h->z;
+        out7[3] = h->vx; out7[4] = h->vy; out7[5] = h->vz; out7[6] = h->gam;
+        return out7;
+    }
+    static int slot_of_snapshot(int k) {  // snapshot field k -> slot id
+        static const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1,
+                                   EMOO_BZ_TM1};
+        return ids[k];
+    }
+    int save(Snapshot &s) {
+        if (!s.buf) s.buf = alloc(snap_words());
+        if (!s.buf) return EMOO_ERR_OOM;
+        double *P[7];
+        particle_ptrs(P);
+        for (int a = 0; a < 7; a++) {
+            if (!P[a]) continue;
+            EMOO_CUDA(cudaMemcpyAsync(s.buf + a * np, P[a], sizeof(double) * np, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        for (int k = 0; k < 9; k++)
+            EMOO_CUDA(cudaMemcpyAsync(s.buf + 7 * np + k * npts, h->slot[slot_of_snapshot(k)], sizeof(double) * npts,
+                                      cudaMemcpyDeviceToDevice, h->stream));
+        s.bswap = h->bswap;
+        s.t = h->t;
+        s.step = h->step_index;
+        return EMOO_OK;
+    }
+    int restore(const Snapshot &s) {
+        double *P[7];
+        particle_ptrs(P);
+        for (int a = 0; a < 7; a++) {
+            if (!P[a]) continue;
+            EMOO_CUDA(cudaMemcpyAsync(P[a], s.buf + a * np, sizeof(double) * np, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        for (int k = 0; k < 9; k++)
+            EMOO_CUDA(cudaMemcpyAsync(h->slot[slot_of_snapshot(k)], s.buf + 7 * np + k * npts, sizeof(double) * npts,
+                                      cudaMemcpyDeviceToDevice, h->stream));
+        h->bswap = s.bswap;
+        h->t = s.t;
+        h->step_index = s.step;
+        return EMOO_OK;
+    }
+    CPArr snap_particles(const Snapshot &s) const {
+        CPArr P;
+        for (int a = 0; a < 7; a++) P.p[a] = s.buf + a * np;
+        return P;
+    }
+    FPtrs snap_fields(const Snapshot &s) const {
+        FPtrs F;
+        const double *f = s.buf + 7 * np;
+        for (int c = 0; c < 3; c++) {
+            F.E[c] = f + c * npts;
+            const double *b = f + (3 + c) * npts, *t = f + (6 + c) * npts;
+            F.B[c] = s.bswap ? t : b;  // the roles at the snapshot's bswap
+            F.T[c] = s.bswap ? b : t;
+        }
+        return F;
+    }
+};
+
+// Points the handle's slot table at other arrays for the duration of a scope
+// (the field kernels act on the slots; the tangent fields reuse them).
+struct SlotSwap {
+    emoo_handle *h;
+    double *saved[EMOO_NFIELDS];
+    int bswap;
+    SlotSwap(emoo_handle *hh, double *const *alt) : h(hh), bswap(hh->bswap) {
+        for (int k = 0; k < EMOO_NFIELDS; k++) {
+            saved[k] = h->slot[k];
+            if (k < NSLOT) h->slot[k] = alt[k];
+        }
+    }
+    ~SlotSwap() {
+        for (int k = 0; k < EMOO_NFIELDS; k++) h->slot[k] = saved[k];
+        h->bswap = bswap;
+    }
+};
+
+FPtrs field_ptrs(emoo_handle *h, double *const *slots, int bswap) {
+    FPtrs F;
+    for (int c = 0; c < 3; c++) {
+        F.E[c] = slots[EMOO_EX + c];
+        F.B[c] = bswap ? slots[EMOO_BX_TM1 + c] : slots[EMOO_BX + c];
+        F.T[c] = bswap ? slots[EMOO_BX + c] : slots[EMOO_BX_TM1 + c];
+    }
+    (void)h;
+    return F;
+}
+FOut field_out(double *const *slots, int bswap) {
+    FOut F;
+    for (int c = 0; c < 3; c++) {
+        F.E[c] = slots[EMOO_EX + c];
+        F.B[c] = bswap ? slots[EMOO_BX_TM1 + c] : slots[EMOO_BX + c];
+        F.T[c] = bswap ? slots[EMOO_BX + c] : slots[EMOO_BX_TM1 + c];
+    }
+    return F;
+}
+
+// One step of the loop without sort and charge density (the primal step the
+// tangent and adjoint runs differentiate).
+int primal_step(emoo_handle *h) {
+    EMOO_TRY(fused_step_f64(h, h->dtp, 0));
+    EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+    EMOO_TRY(yee_f64(h, h->dtp));
+    EMOO_TRY(ad_execute_bc(h, EMOO_SEND_EB));
+    h->t += h->dtp;
+    h->step_index++;
+    return EMOO_OK;
+}
+
+dim3 grid_all(const Geom &g, dim3 blk) {
+    return dim3((g.tot[2] + blk.x - 1) / blk.x, (g.tot[1] + blk.y - 1) / blk.y, g.tot[0]);
+}
+
+int objective(emoo_handle *h, const Slab &sl, double *const *dslots, double *dev2, double out2[2]) {
+    EMOO_CUDA(cudaMemsetAsync(dev2, 0, 2 * sizeof(double), h->stream));
+    FPtrs F = field_ptrs(h, h->slot, h->bswap);
+    FPtrs dF = dslots ? field_ptrs(h, dslots, h->bswap) : F;
+    h->launches++;
+    k_objective<<<pblocks((int64_t)(sl.hi - sl.lo) * h->g.n[1] * h->g.n[2]), 256, 0, h->stream>>>(
+        h->g, sl, F, dF, dslots ? 1 : 0, dev2);
+    EMOO_CUDA(cudaGetLastError());
+    EMOO_CUDA(cudaMemcpyAsync(out2, dev2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+}  // namespace
+
+// tangent step: dP, dslot advance with the primal step
+static int tlm_step(emoo_handle *h, AdRun &R, double **dP, double *const *dslot, const double *dtheta) {
+    SpeciesTab st;
+    species_tab(h, h->dtp, st);
+    const Geom &g = h->g;
+    for (int c = 0; c < 3; c++)
+        EMOO_CUDA(cudaMemsetAsync(dslot[EMOO_JX + c], 0, sizeof(double) * R.npts, h->stream));
+    CPArr P{{h->x, h->y, h->z, h->vx, h->vy, h->vz, h->gam}};
+    FPtrs F = field_ptrs(h, h->slot, h->bswap), dF = field_ptrs(h, dslot, h->bswap);
+    PArr D{{dP[0], dP[1], dP[2], dP[3], dP[4], dP[5], dP[6]}};
+    JPtrs dJ{{dslot[EMOO_JX], dslot[EMOO_JY], dslot[EMOO_JZ]}};
+    h->launches++;
+    if (R.rel)
+        k_tlm_particles<true><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, P, F, dF, D, R.np, h->dtp, dJ);
+    else
+        k_tlm_particles<false><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, P, F, dF, D, R.np, h->dtp, dJ);
+    EMOO_CUDA(cudaGetLastError());
+    // primal particle step, then the linear field part on both
+    EMOO_TRY(fused_step_f64(h, h->dtp, 0));
+    EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+    {
+        SlotSwap sw(h, dslot);
+        EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+        EMOO_TRY(yee_f64(h, h->dtp));
+    }
+    EMOO_TRY(yee_f64(h, h->dtp));
+    std::vector<AdBcOp> ops;
+    EMOO_TRY(ad_bc_ops(h, ops));
+    EMOO_TRY(ad_execute_bc(h, EMOO_SEND_EB));
+    {
+        SlotSwap sw(h, dslot);
+        static const int ids_eb[6] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ};
+        for (const AdBcOp &op : ops) {
+            if (op.kind == 0) {
+                EMOO_TRY(ghost_fill_f64(h, ids_eb, 6, op.mask));
+            } else {
+                double v = 0.0;
+                for (int k = 0; k < op.nk; k++) v += op.coef[k] * (dtheta ? dtheta[op.kidx[k]] : 0.0);
+                PlaneSet ps{dslot[op.slot], op.dim, op.idx, v};
+                EMOO_TRY(plane_set_f64(h, &ps, 1));
+            }
+        }
+    }
+    h->t += h->dtp;
+    h->step_index++;
+    return EMOO_OK;
+}
+
+// adjoint of one step, given the state before it (snapshot S)
+static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, double *const *lslot, double *dtheta) {
+    const Geom &g = h->g;
+    const int b1 = S.bswap ^ 1;  // B roles after the step's Yee update
+    // 1. executeBC(-1) at the step's time, in reverse
+    std::vector<AdBcOp> ops;
+    {
+        const double t_save = h->t;
+        const int b_save = h->bswap;
+        h->t = S.t;
+        h->bswap = b1;
+        int rc = ad_bc_ops(h, ops);
+        h->t = t_save;
+        h->bswap = b_save;
+        EMOO_TRY(rc);
+    }
+    for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
+        const AdBcOp &op = *it;
+        if (op.kind == 0) {
+            Slots6 fl{{lslot[EMOO_EX], lslot[EMOO_EY], lslot[EMOO_EZ], lslot[EMOO_BX], lslot[EMOO_BY], lslot[EMOO_BZ]}};
+            for (int d = 2; d >= 0; d--) {
+                if (!((op.mask >> d) & 1)) continue;
+                const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+                dim3 blk(32, 8);
+                dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 6);
+                for (int side = 1; side >= 0; side--) {
+                    h->launches++;
+                    k_ghost_adj<<<grd, blk, 0, h->stream>>>(g, fl, d, side);
+                }
+            }
+        } else {
+            PlaneCoef pc;
+            pc.nk = op.nk;
+            for (int k = 0; k < op.nk; k++) {
+                pc.kidx[k] = op.kidx[k];
+                pc.coef[k] = op.coef[k];
+            }
+            h->launches++;
+            k_plane_adj<<<pblocks((int64_t)g.tot[0] * g.tot[1]), 256, 0, h->stream>>>(g, lslot[op.slot], op.dim,
+                                                                                       op.idx, pc, dtheta);
+        }
+    }
+    EMOO_CUDA(cudaGetLastError());
+    // 2. Yee update, in reverse (B then E), roles after the step
+    FOut A = field_out(lslot, b1);
+    JPtrs LJ{{lslot[EMOO_JX], lslot[EMOO_JY], lslot[EMOO_JZ]}};
+    dim3 blk(32, 8);
+    h->launches += 2;
+    k_yee_b_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, h->dtp, A);
+    k_yee_e_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, h->dtp, A, LJ);
+    // 3. the J fold, in reverse
+    for (int d = 2; d >= 0; d--) {
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) continue;
+        const int f0 = (d == 0) ? EMOO_JY : EMOO_JX;
+        const int f1 = (d == 2) ? EMOO_JY : EMOO_JZ;
+        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 2);
+        h->launches++;
+        k_fold_adj<<<grd, blk, 0, h->stream>>>(g, d, lslot[f0], lslot[f1]);
+    }
+    // 4. particles: deposit, boundaries, push, gather, in reverse
+    SpeciesTab st;
+    species_tab(h, h->dtp, st);
+    PArr LP{{L[0], L[1], L[2], L[3], L[4], L[5], L[6]}};
+    FOut LF = field_out(lslot, S.bswap);
+    h->launches++;
+    if (R.rel)
+        k_adj_particles<true><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, R.snap_particles(S), R.snap_fields(S),
+                                                                   LP, R.np, h->dtp, LJ, LF);
+    else
+        k_adj_particles<false><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, R.snap_particles(S),
+                                                                    R.snap_fields(S), LP, R.np, h->dtp, LJ, LF);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+}  // namespace emoo
+
+using namespace emoo;
+
+extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
+                           emoo_ad_result *out, double *grad_theta, double *grad_v) {
+    if (!h || !spec || !out) return EMOO_ERR_ARG;
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (h->info.electrostatic == 1) return EMOO_ERR_UNSUPPORTED;
+    if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
+    if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
+        return EMOO_ERR_ARG;
+    if (mode == EMOO_AD_ADJOINT && spec->checkpoint_every < 1) return EMOO_ERR_ARG;
+    AdRun R;
+    R.h = h;
+    R.np = h->np;
+    R.npts = h->g.npts;
+    R.rel = h->info.relativity != 0;
+    if (R.rel && !h->gam) return EMOO_ERR_STATE;
+    const Slab sl{spec->slab_lo + 1, spec->slab_hi + 1};  // cells -> grid points (first physical point is 1)
+    const int ntheta = 2 * h->info.nwaves;
+    double *dev2 = R.alloc(2 + (size_t)std::max(ntheta, 1));
+    if (!dev2) return EMOO_ERR_OOM;
+    double *dth = dev2 + 2;
+    memset(out, 0, sizeof(*out));
+    cudaEvent_t ev[4];
+    for (auto &e : ev) EMOO_CUDA(cudaEventCreate(&e));
+    struct EvFree {
+        cudaEvent_t *e;
+        ~EvFree() {
+            for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]);
+        }
+    } evfree{ev};
+    double o2[2];
+
+    if (mode == EMOO_AD_FORWARD) {
+        EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
+        for (int n = 0; n < spec->nsteps; n++) EMOO_TRY(primal_step(h));
+        EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
+        EMOO_TRY(objective(h, sl, nullptr, dev2, o2));
+        float ms = 0;
+        EMOO_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        out->forward_ms = ms;
+        out->objective = o2[0];
+        return read_err(h);
+    }
+
+    if (mode == EMOO_AD_TANGENT) {
+        double *dP[7];
+        double *dslot[NSLOT];
+        for (int a = 0; a < 7; a++) {
+            if (!(dP[a] = R.alloc((size_t)std::max<int64_t>(R.np, 1)))) return EMOO_ERR_OOM;
+            EMOO_CUDA(cudaMemsetAsync(dP[a], 0, sizeof(double) * R.np, h->stream));
+        }
+        for (int k = 0; k < NSLOT; k++) {
+            if (!(dslot[k] = R.alloc((size_t)R.npts))) return EMOO_ERR_OOM;
+            EMOO_CUDA(cudaMemsetAsync(dslot[k], 0, sizeof(double) * R.npts, h->stream));
+        }
+        if (dv)
+            for (int a = 0; a < 3; a++)
+                EMOO_CUDA(cudaMemcpyAsync(dP[3 + a], dv + a * R.np, sizeof(double) * R.np, cudaMemcpyHostToDevice,
+                                          h->stream));
+        EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
+        for (int n = 0; n < spec->nsteps; n++) EMOO_TRY(tlm_step(h, R, dP, dslot, dtheta));
+        EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
+        EMOO_TRY(objective(h, sl, dslot, dev2, o2));
+        float ms = 0;
+        EMOO_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        out->forward_ms = ms;
+        out->objective = o2[0];
+        out->tangent = o2[1];
+        return read_err(h);
+    }
+
+    // ---- adjoint: forward with checkpoints
+    const int K = spec->checkpoint_every, N = spec->nsteps;
+    const int nseg = (N + K - 1) / K;
+    std::vector<Snapshot> ck(std::max(nseg, 1));
+    EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
+    for (int n = 0; n < N; n++) {
+        if (n % K == 0) EMOO_TRY(R.save(ck[n / K]));
+        EMOO_TRY(primal_step(h));
+    }
+    EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
+    EMOO_TRY(objective(h, sl, nullptr, dev2, o2));  // synchronises
+    out->objective = o2[0];
+    {
+        float ms = 0;
+        EMOO_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        out->forward_ms = ms;
+    }
+    Snapshot fin;
+    EMOO_TRY(R.save(fin));
+    // adjoint state: particles and slots, seeded from the objective
+    double *L[7];
+    double *lslot[NSLOT];
+    for (int a = 0; a < 7; a++) {
+        if (!(L[a] = R.alloc((size_t)std::max<int64_t>(R.np, 1)))) return EMOO_ERR_OOM;
+        EMOO_CUDA(cudaMemsetAsync(L[a], 0, sizeof(double) * R.np, h->stream));
+    }
+    for (int k = 0; k < NSLOT; k++) {
+        if (!(lslot[k] = R.alloc((size_t)R.npts))) return EMOO_ERR_OOM;
+        EMOO_CUDA(cudaMemsetAsync(lslot[k], 0, sizeof(double) * R.npts, h->stream));
+    }
+    EMOO_CUDA(cudaMemsetAsync(dth, 0, sizeof(double) * std::max(ntheta, 1), h->stream));
+    {
+        FPtrs F = field_ptrs(h, h->slot, h->bswap);
+        FOut A = field_out(lslot, h->bswap);
+        h->launches++;
+        k_objective_seed<<<pblocks((int64_t)(sl.hi - sl.lo) * h->g.n[1] * h->g.n[2]), 256, 0, h->stream>>>(h->g, sl,
+                                                                                                           F, A);
+        EMOO_CUDA(cudaGetLastError());
+    }
+    std::vector<Snapshot> tape(std::min(K, std::max(N, 1)));
+    float rec_ms = 0, rev_ms = 0;
+    for (int sgi = nseg - 1; sgi >= 0; sgi--) {
+        const int n0 = sgi * K, n1 = std::min(N, n0 + K);
+        EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
+        EMOO_TRY(R.restore(ck[sgi]));
+        for (int n = n0; n < n1; n++) {
+            EMOO_TRY(R.save(tape[n - n0]));
+            if (n + 1 < n1) EMOO_TRY(primal_step(h));
+        }
+        EMOO_CUDA(cudaEventRecord(ev[2], h->stream));
+        for (int n = n1 - 1; n >= n0; n--) EMOO_TRY(adj_step(h, R, tape[n - n0], L, lslot, dth));
+        EMOO_CUDA(cudaEventRecord(ev[3], h->stream));
+        EMOO_CUDA(cudaEventSynchronize(ev[3]));
+        float a = 0, b = 0;
+        EMOO_CUDA(cudaEventElapsedTime(&a, ev[1], ev[2]));
+        EMOO_CUDA(cudaEventElapsedTime(&b, ev[2], ev[3]));
+        rec_ms += a;
+        rev_ms += b;
+    }
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    out->recompute_ms = rec_ms;
+    out->reverse_ms = rev_ms;
+    if (grad_theta && ntheta)
+        EMOO_CUDA(cudaMemcpy(grad_theta, dth, sizeof(double) * ntheta, cudaMemcpyDeviceToHost));
+    if (grad_v)
+        for (int a = 0; a < 3; a++)
+            EMOO_CUDA(cudaMemcpy(grad_v + a * R.np, L[3 + a], sizeof(double) * R.np, cudaMemcpyDeviceToHost));
+    EMOO_TRY(R.restore(fin));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return read_err(h);
+}

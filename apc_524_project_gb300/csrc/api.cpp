@@ -164,9 +164,109 @@ int light_planes(emoo_handle *h, int s, PlaneSet *ps, bool slots) {
     return n;
 }
 
+// The pulses of each external side and polarisation (LightBC's constructor,
+// src/grid/lightBC.cpp:10-142).
+LightState build_light(const emoo_input_info &info) {
+    LightState L;
+    memset(&L, 0, sizeof(L));
+    for (int s = 0; s < 6; s++) {
+        int side = (s % 2 == 0) ? -(s / 2 + 1) : (s / 2 + 1);
+        for (int w = 0; w < info.nwaves && w < EMOO_NWAVE; w++) {
+            if (info.inSide[w] != side) continue;
+            int pid = info.inPolE[w] - 1;
+            if (pid < 0 || pid > 2) continue;
+            Pulses &P = L.p[s][pid];
+            P.amp[P.nw] = info.peakamps[w];
+            P.omg[P.nw] = info.omegas[w];
+            P.pha[P.nw] = info.phases[w];
+            P.del[P.nw] = info.delays[w];
+            P.iw[P.nw] = info.invWidths[w];
+            P.nw++;
+        }
+    }
+    return L;
+}
+
+// d/d(amplitude) and d/d(phase in degrees) of wave w's term
+// amp cos(omega (t + dt) + phase pi / 180) exp(-((t - delay) invW)^2).
+void pulse_derivs(const emoo_input_info &in, int w, double t, double dt, double scale, AdBcOp &op) {
+    const double arg = in.omegas[w] * (t + dt) + in.phases[w] * PI_D / 180.0;
+    const double env = exp(-pow((t - in.delays[w]) * in.invWidths[w], 2));
+    op.kidx[op.nk] = 2 * w;
+    op.coef[op.nk++] = scale * cos(arg) * env;
+    op.kidx[op.nk] = 2 * w + 1;
+    op.coef[op.nk++] = -scale * in.peakamps[w] * sin(arg) * (PI_D / 180.0) * env;
+}
+
 }  // namespace
 
 int emoo::light_planes_public(emoo_handle *h, int s, PlaneSet *ps) { return light_planes(h, s, ps, false); }
+
+namespace {
+int execute_bc(emoo_handle *h, int send_id);  // below
+}
+
+int emoo::ad_execute_bc(emoo_handle *h, int send_id) { return execute_bc(h, send_id); }
+
+// executeBC(-1) on the FP64 slots as a list of operations, at the handle's
+// current time and B roles, in the order execute_bc_slots applies them; each
+// plane carries its value's derivatives with respect to the wave parameters.
+int emoo::ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops) {
+    static const int EPOL[3][3] = {{1, 2, 0}, {2, 0, 1}, {0, 1, 2}};  // as light_planes
+    ops.clear();
+    const emoo_input_info &in = h->info;
+    int mask = 0;
+    for (int d = 0; d < 3; d++) {
+        if (h->bc.fbc[2 * d] == FBC_PERIODIC) {
+            mask |= 1 << d;
+            continue;
+        }
+        if (mask) {
+            AdBcOp g{};
+            g.kind = 0;
+            g.mask = mask;
+            ops.push_back(g);
+            mask = 0;
+        }
+        for (int r = 0; r < 2; r++) {
+            const int s = 2 * d + r;
+            if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
+            PlaneSet ps[6];
+            const int n = light_planes(h, s, ps, true);
+            const int side = (s % 2 == 0) ? -(s / 2 + 1) : (s / 2 + 1);
+            const int sign = r ? 1 : -1;
+            const double bphase = (h->g.d[d] + sign * h->dtp) / 2;
+            for (int i = 0; i < n; i++) {
+                AdBcOp op{};
+                op.kind = 1;
+                op.slot = -1;
+                for (int k = 0; k < EMOO_NFIELDS; k++)
+                    if (h->slot[k] == ps[i].f) op.slot = k;
+                if (op.slot < 0) return EMOO_ERR_STATE;
+                op.dim = ps[i].dim;
+                op.idx = ps[i].idx;
+                op.value = ps[i].v;
+                const int c = i / 2;
+                const int eid = EPOL[d][c];
+                if (eid != d) {
+                    for (int w = 0; w < in.nwaves && w < EMOO_NWAVE; w++) {
+                        if (in.inSide[w] != side || in.inPolE[w] - 1 != eid) continue;
+                        if (i % 2 == 0) pulse_derivs(in, w, h->t, 0.0, 1.0, op);
+                        else pulse_derivs(in, w, h->t, bphase, sign * (int)pow(-1, c + 1), op);
+                    }
+                }
+                ops.push_back(op);
+            }
+        }
+    }
+    if (mask) {
+        AdBcOp g{};
+        g.kind = 0;
+        g.mask = mask;
+        ops.push_back(g);
+    }
+    return EMOO_OK;
+}
 
 namespace {
 
@@ -575,24 +675,7 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
     h->t = info->t0;
     h->dtp = h->dt;
     // LightBC registry
-    LightState L;
-    memset(&L, 0, sizeof(L));
-    for (int s = 0; s < 6; s++) {
-        int side = (s % 2 == 0) ? -(s / 2 + 1) : (s / 2 + 1);
-        for (int w = 0; w < info->nwaves && w < EMOO_NWAVE; w++) {
-            if (info->inSide[w] != side) continue;
-            int pid = info->inPolE[w] - 1;
-            if (pid < 0 || pid > 2) continue;
-            Pulses &P = L.p[s][pid];
-            P.amp[P.nw] = info->peakamps[w];
-            P.omg[P.nw] = info->omegas[w];
-            P.pha[P.nw] = info->phases[w];
-            P.del[P.nw] = info->delays[w];
-            P.iw[P.nw] = info->invWidths[w];
-            P.nw++;
-        }
-    }
-    light_registry().push_back({h, L});
+    light_registry().push_back({h, build_light(*info)});
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         emoo_destroy(h);
@@ -906,6 +989,21 @@ int emoo_evolve_fields(emoo_handle *h, int electrostatic) {
     else if (electrostatic) EMOO_TRY(yee_es_f64(h, h->dtp));
     else EMOO_TRY(yee_f64(h, h->dtp));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    return EMOO_OK;
+}
+
+int emoo_set_waves(emoo_handle *h, int nwaves, const double *amp, const double *phase_deg) {
+    HANDLE_CHECK(h);
+    if (nwaves != h->info.nwaves || nwaves < 0 || nwaves > EMOO_NWAVE || (nwaves && (!amp || !phase_deg)))
+        return EMOO_ERR_ARG;
+    for (int w = 0; w < nwaves; w++) {
+        if (!std::isfinite(amp[w]) || !std::isfinite(phase_deg[w])) return EMOO_ERR_ARG;
+        h->info.peakamps[w] = amp[w];
+        h->info.phases[w] = phase_deg[w];
+    }
+    LightState *L = light_of(h);
+    if (!L) return EMOO_ERR_STATE;
+    *L = build_light(h->info);
     return EMOO_OK;
 }
 

@@ -75,6 +75,21 @@ struct PlaneSet {
     double v;
 };
 
+// One operation of executeBC(-1) on the FP64 slots, for the differentiated
+// step: a periodic ghost copy of the E / B slots over the dims in `mask`, or
+// a whole-plane set of slot `slot` to `value`, with the value's derivatives
+// with respect to the wave parameters (parameter 2 w: amplitude of wave w,
+// 2 w + 1: its phase in degrees).
+struct AdBcOp {
+    int kind;  // 0 ghost copy, 1 plane set
+    int mask;
+    int slot, dim, idx;
+    double value;
+    int nk;
+    int kidx[2 * EMOO_NWAVE];
+    double coef[2 * EMOO_NWAVE];
+};
+
 struct FieldsF32;  // mixed-form grid storage (particles_mixed.cu)
 
 }  // namespace emoo
@@ -213,6 +228,10 @@ int mixed_key_bits(emoo_handle *h);
 int cuda_status(cudaError_t e);
 int read_err(emoo_handle *h);
 int prof_accumulate(emoo_handle *h);
+
+// ---- differentiation support (api.cpp) ----
+int ad_execute_bc(emoo_handle *h, int send_id);
+int ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops);
 int light_planes_public(emoo_handle *h, int s, PlaneSet *ps);
 
 }  // namespace emoo

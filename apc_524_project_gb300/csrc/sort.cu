@@ -356,7 +356,7 @@ int count_species(emoo_handle *h, int64_t n, int64_t stride, int64_t *counts_hos
 // scratch in one file-scope device array of fixed size, and allocates nothing.
 //
 // The array is created when the library is loaded on a device and lives until
-// the process exits (12.5 MiB on every GPU that loads the library). Every call
+// the process exits (12.25 MiB on every GPU that loads the library). Every call
 // uses the same array and leaves its contents behind; nothing in it has to
 // start at zero, because each pass writes every histogram slot and every
 // buffer element it later reads. Calls whose GPU work overlaps (for example on

@@ -339,7 +339,7 @@ int emoo_get_stats(emoo_handle *h, emoo_stats *s);
  * work is queued on `stream` (a cudaStream_t, null for the default stream)
  * and the call returns without waiting for it.
  *
- * Scratch is one fixed 12.5 MiB device array in the library, held by every GPU
+ * Scratch is one fixed 12.25 MiB device array in the library, held by every GPU
  * that loads the library until the process exits; n above
  * EMOO_NOALLOC_SORT_MAX is rejected with EMOO_ERR_ARG. The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress) with the
@@ -347,6 +347,49 @@ int emoo_get_stats(emoo_handle *h, emoo_stats *s);
  * share the array and it keeps the last call's contents, so calls whose GPU
  * work overlaps race: order them (one stream, or events). */
 int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, int key_bits, uint32_t *perm, void *stream);
+
+/* ---- differentiation of the FP64 time loop ------------------------------
+ * No reference counterpart. The differentiated step is the loop's step
+ * without sorting and charge density (gather, push, particle boundaries,
+ * current deposit, J fold, Yee update, executeBC(-1) with LightBC). Its
+ * parameters are the particles' velocities at the start of the run and the
+ * amplitude and phase (degrees) of every injected wave, theta = (amp_0,
+ * phase_0, amp_1, phase_1, ...); the objective is the field energy
+ * 0.5 V sum(E^2 + B^2) over the grid points of the cells with x index in
+ * [slab_lo, slab_hi) after the run's last step (B: the current B role).
+ * The cell a particle is in and whether a boundary fires are held fixed (the
+ * step is differentiated between such events). FP64 handles only, not the
+ * electrostatic update. */
+#define EMOO_AD_FORWARD 0 /* objective only */
+#define EMOO_AD_TANGENT 1 /* objective and its derivative along (dtheta, dv) */
+#define EMOO_AD_ADJOINT 2 /* objective and its gradient */
+
+typedef struct emoo_ad_spec {
+    int nsteps;           /* steps of the run, from the handle's current state */
+    int checkpoint_every; /* adjoint: state kept every this many steps, segments recomputed (>= 1) */
+    int slab_lo, slab_hi; /* objective slab, cell x indices [slab_lo, slab_hi) */
+} emoo_ad_spec;
+
+typedef struct emoo_ad_result {
+    double objective;
+    double tangent;      /* EMOO_AD_TANGENT: d objective along (dtheta, dv) */
+    double forward_ms;   /* device time of the run's steps */
+    double recompute_ms; /* EMOO_AD_ADJOINT: re-running the segments from their checkpoints */
+    double reverse_ms;   /* EMOO_AD_ADJOINT: the adjoint steps */
+} emoo_ad_result;
+
+/* Sets the amplitude and phase (degrees) of the handle's nwaves injected
+ * waves (nwaves must equal the input's wave count); LightBC uses them from
+ * the next boundary update. */
+int emoo_set_waves(emoo_handle *h, int nwaves, const double *amp, const double *phase_deg);
+
+/* Runs spec->nsteps steps from the handle's current state and leaves it at
+ * the final state. dtheta (2 nwaves) and dv (3 np host doubles: vx of every
+ * particle, then vy, then vz, in storage order) give the tangent direction
+ * (either may be NULL: zero); grad_theta (2 nwaves) and grad_v (3 np, same
+ * layout) receive the adjoint gradient (either may be NULL). */
+int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
+                emoo_ad_result *out, double *grad_theta, double *grad_v);
 
 #ifdef __cplusplus
 }

@@ -48,6 +48,7 @@ def _args():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=6)
     return ap.parse_args()
@@ -258,7 +259,44 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
         abi.check(L.emoo_get_stats(h, C.byref(s64)))
         res["fp64"] = {"t": t64, "fused_ms": s64.timed_ms / max(1, s64.timed_launches)}
         abi.check(L.emoo_destroy(h))
+
+    # ---- differentiation: adjoint against forward cost on the laser workload
+    if not args.no_adjoint:
+        res["adjoint"] = adjoint_arm()
     return cfg, res
+
+
+def adjoint_arm():
+    """Differentiation of the FP64 loop. Cost: the laser workload at full size
+    (64^3, 2 x 8 ppc, 128 steps, objective the slab x in [48, 56),
+    checkpoints every 16 steps): one adjoint run (forward with checkpoints,
+    then recompute + reverse per segment) against its forward. Check: on a
+    16 x 8 x 8 laser case of 24 steps, where no particle changes cell within
+    the difference step, the amplitude derivative against a central
+    difference of two primal runs."""
+    from apc_524_project_gb300 import configs
+    from apc_524_project_gb300.differentiate import Problem
+
+    P = Problem(configs.laser64(), nsteps=128, slab=(48, 56), checkpoint_every=16)
+    P.gradient()  # warm-up (allocations, first launches)
+    g = P.gradient()
+    fwd = g["forward_ms"]
+    S = Problem(configs.laser64(n=(16, 8, 8), steps=24, ppc=2, wavelength=8.0, fwhm_steps=8), nsteps=24,
+                slab=(2, 8), checkpoint_every=4)
+    gs = S.gradient()["grad_theta"][0]
+    h = 1e-6 * S.theta0[0]
+    th = S.theta0.copy()
+    th[0] += h
+    lp = S.objective(th)
+    th[0] -= 2 * h
+    lm = S.objective(th)
+    fd = (lp - lm) / (2 * h)
+    return {"workload": "laser plane wave into plasma, 64^3 cells, 2 x 8 ppc = 4,194,304 particles, 128 steps, "
+                        "FP64, checkpoints every 16 steps",
+            "forward_ms": fwd, "recompute_ms": g["recompute_ms"], "reverse_ms": g["reverse_ms"],
+            "adjoint_over_forward": (g["recompute_ms"] + g["reverse_ms"]) / fwd,
+            "fd_check": {"case": "laser 16x8x8, 2 x 2 ppc, 24 steps, d objective / d amplitude",
+                         "adjoint": float(gs), "central_difference": fd, "rel_err": abs(fd - gs) / abs(fd)}}
 
 
 def _e2e(h, cfg, steps, dist_barrier, dist_max):
@@ -465,6 +503,8 @@ def main():
         line["fp64"] = {"value": v64, "unit": UNIT, "steps": args.fp64_steps,
                         "ms_per_step": f["t"] / args.fp64_steps * 1e3, "fused_kernel_ms": f["fused_ms"],
                         "mixed_over_fp64": value / v64}
+    if "adjoint" in res:
+        line["adjoint"] = res["adjoint"]
     if "e2e" in res:
         e = res["e2e"]
         line["e2e"] = {"value": N * e["steps"] * world / e["t"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

@@ -433,44 +433,24 @@ def main():
     if args.impl == "reference":
         reference_arm(args)
         return
+    from apc_524_project_gb300 import replicas
+
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu:
         # before the first GPU call (the pool is spawned, but keep it first)
         cb = cpu_baseline(args.cpu_procs, args.cpu_steps)
-    import torch
+    import torch  # noqa: F401
 
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl")
-        dev = int(os.environ.get("LOCAL_RANK", "0"))
-
-        def barrier():
-            dist.barrier(device_ids=[dev])
-
-        def dmax(x):
-            t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{dev}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-    else:
-        def barrier():
-            pass
-
-        def dmax(x):
-            return x
-
+    world, rank, barrier, dmax, close = replicas.comm("nccl", int(os.environ.get("LOCAL_RANK", "0")))
     cfg, res = run_gpu_arm(args, rank, world, barrier, dmax)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.destroy_process_group()
+    close()
     if rank != 0:
         return
     N = cfg.total_particles()
     m = res["mixed"]
-    value = N * args.steps * world / m["t"]
+    value = replicas.job_throughput(N, args.steps, world, m["t"])
     peak, peak_kind = _peaks()
     cells = cfg.n[0] * cfg.n[1] * cfg.n[2]
     # algorithmic bytes of one fused-kernel launch: every particle's 28-byte

@@ -767,6 +767,9 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
         return EMOO_ERR_ARG;
     if (mode == EMOO_AD_ADJOINT && spec->checkpoint_every < 1) return EMOO_ERR_ARG;
+    // the run moves the particles; as after emoo_step, rho is left pending
+    // (it is deposited at the final positions when read)
+    if (h->opts.deposit_rho) h->rho_stale = 1;
     AdRun R;
     R.h = h;
     R.np = h->np;

@@ -738,10 +738,27 @@ int emoo_destroy(emoo_handle *h) {
     return EMOO_OK;
 }
 
+namespace {
+// emoo_step leaves rho pending (the loop never reads it); this deposits it -
+// at the particles' current positions, folded, with the background - which
+// is what the last step's deposit and fold would have left. Called wherever
+// rho is read and before anything moves the particles.
+int materialize_rho(emoo_handle *h) {
+    if (!h->rho_stale) return EMOO_OK;
+    h->rho_stale = 0;
+    if (h->precision != EMOO_FP64) return mixed_materialize_rho(h);
+    EMOO_TRY(deposit_rho_f64(h));
+    for (int d = 0; d < 3; d++)
+        if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d, FOLD_RHO));
+    return EMOO_OK;
+}
+}  // namespace
+
 int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
                         const double *vx, const double *vy, const double *vz, const double *gamma,
                         const int64_t *ids) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     if (species < 0 || species >= h->nspec || n < 0) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
@@ -779,6 +796,7 @@ int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x,
 
 int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     if (!g || g->species < 0 || g->species >= h->nspec || n < 0) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     int64_t first_id = h->np;
@@ -868,6 +886,7 @@ int emoo_get_particle_fields(emoo_handle *h, int species, int64_t cap, double *e
 int emoo_get_field(emoo_handle *h, int id, double *out) {
     HANDLE_CHECK(h);
     if (id < 0 || id >= EMOO_NFIELDS || !out) return EMOO_ERR_ARG;
+    if (id == EMOO_RHO) EMOO_TRY(materialize_rho(h));
     size_t b = sizeof(double) * (size_t)h->g.npts;
     if (h->precision != EMOO_FP64) EMOO_TRY(mixed_get_field(h, id, h->slot[id]));
     EMOO_CUDA(cudaMemcpyAsync(out, h->slot[id], b, cudaMemcpyDeviceToHost, h->stream));
@@ -881,6 +900,7 @@ int emoo_set_field(emoo_handle *h, int id, const double *in) {
     size_t b = sizeof(double) * (size_t)h->g.npts;
     EMOO_CUDA(cudaMemcpyAsync(h->slot[id], in, b, cudaMemcpyHostToDevice, h->stream));
     if (h->precision != EMOO_FP64) EMOO_TRY(mixed_set_field(h, id, h->slot[id]));
+    if (id == EMOO_RHO) h->rho_stale = 0;
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return EMOO_OK;
 }
@@ -903,6 +923,7 @@ int emoo_init_fields(emoo_handle *h, int iters[4]) {
     h->dtp = 0.0;
     int rc = EMOO_OK;
     if (h->poisson) {
+        h->rho_stale = 0;
         rc = deposit_all(h, 1);
         if (rc == EMOO_OK) rc = execute_bc(h, EMOO_SEND_JRHO);
         // the mixed form solves in FP64 on the grid slots
@@ -921,6 +942,7 @@ int emoo_init_fields(emoo_handle *h, int iters[4]) {
 
 int emoo_poisson_init(emoo_handle *h, int iters[4]) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     double t = h->t, dtp = h->dtp;
     h->t = 0.0;
     h->dtp = 0.0;
@@ -935,6 +957,7 @@ int emoo_poisson_init(emoo_handle *h, int iters[4]) {
 
 int emoo_sort(emoo_handle *h) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     EMOO_TRY(do_sort(h));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return read_err(h);
@@ -950,6 +973,7 @@ int emoo_interpolate(emoo_handle *h) {
 
 int emoo_push(emoo_handle *h) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(push_cached_f64(h, h->dtp));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
@@ -958,6 +982,7 @@ int emoo_push(emoo_handle *h) {
 
 int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(reset_counters(h));
     EMOO_TRY(particle_bc_f64(h));
@@ -972,12 +997,14 @@ int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
 int emoo_deposit(emoo_handle *h, int with_rho) {
     HANDLE_CHECK(h);
     EMOO_TRY(deposit_all(h, with_rho));
+    if (with_rho) h->rho_stale = 0;  // else rho stays as the last deposit left it (pending or not)
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return read_err(h);
 }
 
 int emoo_execute_bc(emoo_handle *h, int send_id) {
     HANDLE_CHECK(h);
+    if (send_id == EMOO_SEND_JRHO || send_id == EMOO_RHO) EMOO_TRY(materialize_rho(h));
     EMOO_TRY(execute_bc(h, send_id));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return EMOO_OK;
@@ -1011,7 +1038,11 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
     HANDLE_CHECK(h);
     if (nsteps < 0) return EMOO_ERR_ARG;
     EMOO_TRY(reset_counters(h));
-    int with_rho = h->opts.deposit_rho ? 1 : 0;
+    // with deposit_rho the step deposits J only and leaves rho pending
+    // (materialize_rho); otherwise rho is left as it is and folded each step,
+    // as the reference does when it deposits J alone
+    const bool lazy_rho = h->opts.deposit_rho != 0;
+    const int fold_what = lazy_rho ? FOLD_J : FOLD_ALL;
     for (int it = 0; it < nsteps; it++) {
         int64_t ti = h->step_index;
         if (h->info.nstep_sort > 0 && ti % h->info.nstep_sort == 0) EMOO_TRY(do_sort(h));
@@ -1022,16 +1053,18 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
             h->next_hist += h->opts.history_every;
         }
         if (h->precision == EMOO_FP64) {
-            EMOO_TRY(fused_step_f64(h, h->dtp, with_rho));
-            EMOO_TRY(execute_bc(h, EMOO_SEND_JRHO));
+            EMOO_TRY(fused_step_f64(h, h->dtp, 0));
+            for (int d = 0; d < 3; d++)
+                if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d, fold_what));
             if (h->info.electrostatic == 1) EMOO_TRY(yee_es_f64(h, h->dtp));
             else EMOO_TRY(yee_f64(h, h->dtp));
             EMOO_TRY(execute_bc(h, EMOO_SEND_EB));
         } else {
-            EMOO_TRY(mixed_step(h, h->dtp, with_rho));
+            EMOO_TRY(mixed_step(h, h->dtp, 0, fold_what));
         }
         h->t += h->dtp;
         h->step_index++;
+        if (lazy_rho) h->rho_stale = 1;
     }
     return read_counters(h, counts6, false);
 }
@@ -1056,6 +1089,7 @@ int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n) {
 int emoo_gauss_residual(emoo_handle *h, double out2[2]) {
     HANDLE_CHECK(h);
     if (!out2) return EMOO_ERR_ARG;
+    EMOO_TRY(materialize_rho(h));
     if (h->precision != EMOO_FP64) EMOO_TRY(mixed_fields_to_slots(h));
     return gauss_residual_f64(h, out2);
 }
@@ -1075,6 +1109,7 @@ int emoo_check(emoo_handle *h) {
 int emoo_set_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
                        const double *vx, const double *vy, const double *vz, const double *gamma) {
     HANDLE_CHECK(h);
+    EMOO_TRY(materialize_rho(h));
     if (species < 0 || species >= h->nspec || n != h->count[species]) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;

@@ -151,6 +151,10 @@ struct emoo_handle {
     int64_t next_hist = 0;
     std::vector<double> hist_rows;
     int fields_initialised = 0;
+    // The loop never reads rho, so emoo_step deposits J only and leaves rho
+    // pending: it is deposited (with fold and background) at the particles'
+    // positions when something reads it or before the particles change.
+    int rho_stale = 0;
 
     // instrumentation: kernel launches issued, and CUDA-event timing of the
     // fused particle kernel (the dominant kernel of the step) when enabled
@@ -172,7 +176,8 @@ void make_geom(const emoo_input_info &in, Geom &g);
 int yee_f64(emoo_handle *h, double dt);
 int yee_es_f64(emoo_handle *h, double dt);
 int ghost_fill_f64(emoo_handle *h, const int *ids, int nids, int dims_mask);
-int fold_f64(emoo_handle *h, int dim);
+constexpr int FOLD_J = 1, FOLD_RHO = 2, FOLD_ALL = 3;
+int fold_f64(emoo_handle *h, int dim, int what = FOLD_ALL);
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
 int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);
 int phi_to_e_f64(emoo_handle *h);
@@ -189,6 +194,7 @@ int push_cached_f64(emoo_handle *h, double dtp);
 int particle_bc_f64(emoo_handle *h);
 int deposit_f64(emoo_handle *h, int with_rho);
 int fused_step_f64(emoo_handle *h, double dtp, int with_rho);
+int deposit_rho_f64(emoo_handle *h);  // rho alone at the current positions, plus the background
 int particle_moments_f64(emoo_handle *h, double out4[4]);
 int sort_keys_f64(emoo_handle *h);
 
@@ -207,7 +213,8 @@ int mixed_from_f64(emoo_handle *h, int64_t first, int64_t n, const double *x, co
                    const double *vx, const double *vy, const double *vz, const double *gam);
 int mixed_to_f64(emoo_handle *h, int64_t first, int64_t n, double *x, double *y, double *z, double *vx,
                  double *vy, double *vz, double *gam);
-int mixed_step(emoo_handle *h, double dtp, int with_rho);
+int mixed_step(emoo_handle *h, double dtp, int with_rho, int fold_what);
+int mixed_materialize_rho(emoo_handle *h);
 int mixed_sort_keys(emoo_handle *h);
 int mixed_get_field(emoo_handle *h, int id, double *out_dev);
 int mixed_set_field(emoo_handle *h, int id, const double *in_dev);

@@ -416,15 +416,23 @@ int ghost_fill_f64(emoo_handle *h, const int *ids, int nids, int dims_mask) {
     return ghost_launch(h, ids, nids, dims_mask, nullptr);
 }
 
-int fold_f64(emoo_handle *h, int d) {
+// what: FOLD_J (the two transverse J components), FOLD_RHO, or both
+int fold_f64(emoo_handle *h, int d, int what) {
     const Geom &g = h->g;
     int f0 = (d == 0) ? EMOO_JY : EMOO_JX;
     int f1 = (d == 2) ? EMOO_JY : EMOO_JZ;
     int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
     dim3 blk(32, 8);
-    dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 3);
+    double *a = h->slot[f0], *b = h->slot[f1], *r = h->slot[EMOO_RHO];
+    int nz = 3;
+    if (what == FOLD_J) nz = 2;
+    if (what == FOLD_RHO) {
+        nz = 1;
+        a = r;
+    }
+    dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, nz);
     h->launches++;
-    k_fold<<<grd, blk, 0, h->stream>>>(g, d, h->slot[f0], h->slot[f1], h->slot[EMOO_RHO]);
+    k_fold<<<grd, blk, 0, h->stream>>>(g, d, a, b, r);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }

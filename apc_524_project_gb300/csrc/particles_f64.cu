@@ -245,7 +245,7 @@ __device__ __forceinline__ int64_t deposit_point(const Geom &g, int64_t o, int q
 // cell in consecutive positions are summed in a shuffle tree, the first lane
 // of each run adds the run total to the grid with FP64 atomics.
 __device__ __forceinline__ void commit_deposit(const Geom &g, const DepositPtrs &D, bool active, int64_t cell_o,
-                                               double c[20], bool with_rho) {
+                                               double c[20], bool with_rho, int q_first = 0) {
     const int lane = threadIdx.x & 31;
     long long key = active ? (long long)cell_o : -1 - (long long)lane;
     long long prev = __shfl_up_sync(0xffffffffu, key, 1);
@@ -254,7 +254,7 @@ __device__ __forceinline__ void commit_deposit(const Geom &g, const DepositPtrs 
     int rend = run_end(heads, lane);
     const bool all_single = (heads == 0xffffffffu);
     const int nq = with_rho ? 20 : 12;
-    for (int q = 0; q < nq; q++) {
+    for (int q = q_first; q < nq; q++) {
         double v = c[q];
         if (!all_single) v = run_suffix_sum(v, lane, rend);
         if (head && active) {
@@ -354,7 +354,8 @@ __global__ void k_deposit(Geom g, SpeciesTab st, PState S, int64_t np, DepositPt
             }
         }
     }
-    commit_deposit(g, D, active, o, c, with_rho != 0);
+    // with_rho: 0 J, 1 J and rho, 2 rho only
+    commit_deposit(g, D, active, o, c, with_rho != 0, with_rho == 2 ? 12 : 0);
 }
 
 // The fused time-loop kernel: gather at the current position (what
@@ -542,6 +543,20 @@ int deposit_f64(emoo_handle *h, int with_rho) {
     k_deposit<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, pstate(h), h->np, deposit_ptrs(h), with_rho, h->ctr);
     EMOO_CUDA(cudaGetLastError());
     return rho_background_f64(h, with_rho);
+}
+
+// rho alone at the particles' current positions (J untouched), plus the
+// background: the charge density the loop's last deposit would have left.
+int deposit_rho_f64(emoo_handle *h) {
+    EMOO_CUDA(cudaMemsetAsync(h->slot[EMOO_RHO], 0, sizeof(double) * (size_t)h->g.npts, h->stream));
+    if (h->np > 0) {
+        SpeciesTab st;
+        species_tab(h, h->dtp, st);
+        h->launches++;
+        k_deposit<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, pstate(h), h->np, deposit_ptrs(h), 2, h->ctr);
+        EMOO_CUDA(cudaGetLastError());
+    }
+    return rho_background_f64(h, 1);
 }
 
 int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {

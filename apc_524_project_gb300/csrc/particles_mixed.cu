@@ -41,7 +41,8 @@ struct FieldsF32 {
     long long *J[4] = {nullptr, nullptr, nullptr, nullptr};                    // Jx, Jy, Jz, rho
     double q0 = 1.0;  // fixed-point quantum
     float4 *pack = nullptr;  // interpolation pack, 5 float4 per grid point (interior cells filled)
-    unsigned long long *wc = nullptr;  // per-cell deposit sums, 20 int64 per grid point
+    unsigned long long *wj = nullptr;  // per-cell J deposit sums, 12 int64 per grid point
+    unsigned long long *wr = nullptr;  // per-cell rho deposit sums, 8 int64 per grid point
 };
 
 namespace {
@@ -118,10 +119,12 @@ struct MGather {
 };
 
 struct MDeposit {
-    unsigned long long *wc;  // per-cell sums, 20 per cell (DEP_SLOTS)
+    unsigned long long *wj;  // per-cell J sums, DEP_JSLOTS per cell
+    unsigned long long *wr;  // per-cell rho sums, DEP_RSLOTS per cell
 };
 
-constexpr int DEP_SLOTS = 20;
+constexpr int DEP_SLOTS = 20;  // contributions per particle: J 12, rho 8
+constexpr int DEP_JSLOTS = 12, DEP_RSLOTS = 8;
 
 // Round-to-nearest-even of v as int64, the value of __float2ll_rn(v), without
 // the float-to-int64 conversion: conversions run on the FP64 pipe, which on
@@ -179,40 +182,40 @@ __host__ __device__ __forceinline__ int dep_offset(int q, int sx, int sy) {
     return (c >> 2) * sx + ((c >> 1) & 1) * sy + (c & 1);
 }
 
-// Position of contribution q in a cell's 20-slot record. Slots are grouped by
-// the point offset they feed, in the order
-//   [0,4)  offset 0          q 0 4 8 12
-//   [4,8)  offset sy         q 1 3 11 15
-//   [8,10) offset 1          q 5 19
-//   [10,12) offset sy+1      q 2 16
-//   [12,14) offset sx+1      q 6 18
-//   [14,16) offset sx+sy     q 10 14
-//   [16,19) offset sx        q 7 9 13
-//   [19]   offset sx+sy+1    q 17
-// so each point gathers a neighbour's slots with 16-byte loads. 5 bits per q.
-constexpr unsigned long long DEP_POS_LO =  // q = 0..11
-    (0ull << 0) | (4ull << 5) | (10ull << 10) | (5ull << 15) | (1ull << 20) | (8ull << 25) | (12ull << 30) |
-    (16ull << 35) | (2ull << 40) | (17ull << 45) | (14ull << 50) | (6ull << 55);
-constexpr unsigned long long DEP_POS_HI =  // q = 12..19
-    (3ull << 0) | (18ull << 5) | (15ull << 10) | (7ull << 15) | (11ull << 20) | (19ull << 25) | (13ull << 30) |
-    (9ull << 35);
+// Position of contribution q in its cell's record. J (q < 12) and rho
+// (q >= 12) have records of their own (rho is deposited only when asked
+// for), each ordered by the point offset its slots feed:
+//   J:   [0,3) offset 0: q 0 4 8 | [3,6) sy: q 1 3 11 | 6 1: q 5 | 7 sy+1: q 2
+//        | 8 sx+1: q 6 | 9 sx+sy: q 10 | [10,12) sx: q 7 9
+//   rho: 0 offset 0: q 12 | 1 sy: q 15 | 2 1: q 19 | 3 sy+1: q 16 | 4 sx+1: q 18
+//        | 5 sx+sy: q 14 | 6 sx: q 13 | 7 sx+sy+1: q 17
+// so a point gathers a neighbour's slots with few (vector) loads. 4 bits per q.
+constexpr unsigned long long DEP_JPOS =  // q = 0..11
+    (0ull << 0) | (3ull << 4) | (7ull << 8) | (4ull << 12) | (1ull << 16) | (6ull << 20) | (8ull << 24) |
+    (10ull << 28) | (2ull << 32) | (11ull << 36) | (9ull << 40) | (5ull << 44);
+constexpr unsigned long long DEP_RPOS =  // q = 12..19
+    (0ull << 0) | (6ull << 4) | (5ull << 8) | (1ull << 12) | (3ull << 16) | (7ull << 20) | (4ull << 24) |
+    (2ull << 28);
 
 __host__ __device__ __forceinline__ int dep_pos(int q) {
-    return q < 12 ? (int)((DEP_POS_LO >> (5 * q)) & 31ull) : (int)((DEP_POS_HI >> (5 * (q - 12))) & 31ull);
+    return q < 12 ? (int)((DEP_JPOS >> (4 * q)) & 15ull) : (int)((DEP_RPOS >> (4 * (q - 12))) & 15ull);
 }
 
-// The record layout and the gather in k_cells_to_points must agree with the
-// deposit table: every slot group feeds the point offset of each q placed in
-// it. Checked once per handle.
+// The record layouts and the gather in k_cells_to_points must agree with the
+// deposit table: every slot feeds the point offset of the q placed in it.
+// Checked once per handle.
 bool dep_tables_agree() {
     const int sx = 1000, sy = 30;  // distinct sums for all 8 offsets
-    const int slot_off[DEP_SLOTS] = {0,      0,      0,      0,      sy,      sy,      sy,      sy, 1, 1,
-                                     sy + 1, sy + 1, sx + 1, sx + 1, sx + sy, sx + sy, sx,      sx, sx, sx + sy + 1};
-    bool used[DEP_SLOTS] = {};
+    const int joff[DEP_JSLOTS] = {0, 0, 0, sy, sy, sy, 1, sy + 1, sx + 1, sx + sy, sx, sx};
+    const int roff[DEP_RSLOTS] = {0, sy, 1, sy + 1, sx + 1, sx + sy, sx, sx + sy + 1};
+    bool usedj[DEP_JSLOTS] = {}, usedr[DEP_RSLOTS] = {};
     for (int q = 0; q < DEP_SLOTS; q++) {
         const int pos = dep_pos(q);
-        if (pos < 0 || pos >= DEP_SLOTS || used[pos] || slot_off[pos] != dep_offset(q, sx, sy)) return false;
-        used[pos] = true;
+        const bool j = q < 12;
+        if (pos < 0 || pos >= (j ? DEP_JSLOTS : DEP_RSLOTS)) return false;
+        bool &used = j ? usedj[pos] : usedr[pos];
+        if (used || (j ? joff[pos] : roff[pos]) != dep_offset(q, sx, sy)) return false;
+        used = true;
     }
     return true;
 }
@@ -521,22 +524,52 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     if (heads == 0xffffffffu) {
         // every particle in a cell of its own (unsorted input)
         if (active) {
-            unsigned long long *dst = D.wc + (size_t)onew * DEP_SLOTS;
+            unsigned long long *dj = D.wj + (size_t)onew * DEP_JSLOTS, *dr = D.wr + (size_t)onew * DEP_RSLOTS;
 #pragma unroll
             for (int q = 0; q < DEP_SLOTS; q++) {
                 if (q >= nq) break;
                 long long fx = f2ll_rn(col[q * DEP_STRIDE + lane]);
-                if (fx != 0) atomicAdd(dst + dep_pos(q), (unsigned long long)fx);
+                if (fx != 0) atomicAdd((q < 12 ? dj : dr) + dep_pos(q), (unsigned long long)fx);
+            }
+        }
+        return;
+    }
+    const unsigned ends32 = (heads >> 1) | 0x80000000u;  // bit i: particle i ends its run
+    if (nq == DEP_JSLOTS) {
+        // J only (the time loop): lanes 0..11 walk rows 0..11 over particles
+        // 0..15 while lanes 16..27 walk them over particles 16..31, each in
+        // particle order, committing at each run end; a run that spans
+        // particles 15 and 16 is committed as two parts.
+        const int q = lane & 15, half = lane >> 4;
+        if (q < DEP_JSLOTS) {
+            unsigned long long *dst = D.wj + dep_pos(q);
+            const float *row = col + q * DEP_STRIDE + 16 * half;
+            const int *hkeys = keys + 16 * half;
+            const unsigned ends = ((ends32 >> (16 * half)) & 0xffffu) | 0x8000u;
+            float r[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) r[i] = row[i];
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+                acc += r[i];
+                if ((ends >> i) & 1u) {
+                    const int kk = hkeys[i];
+                    if (kk >= 0) atomicAdd(dst + (size_t)kk * DEP_JSLOTS, (unsigned long long)f2ll_rn(acc));
+                    acc = 0.0f;
+                }
             }
         }
         return;
     }
     if (lane < nq) {
         // row `lane`: one pass in particle order, committing at each run end;
-        // lanes 0..nq-1 commit one cell's slots together (contiguous 8-byte words)
-        unsigned long long *dst = D.wc + dep_pos(lane);
+        // lanes 0..11 commit one cell's J record together, lanes 12..19 its rho record
+        const bool jrow = lane < 12;
+        unsigned long long *dst = (jrow ? D.wj : D.wr) + dep_pos(lane);
+        const int stride = jrow ? DEP_JSLOTS : DEP_RSLOTS;
         const float *row = col + lane * DEP_STRIDE;
-        const unsigned ends = (heads >> 1) | 0x80000000u;  // bit i: particle i ends its run
+        const unsigned ends = ends32;
         float acc = 0.0f;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
@@ -550,7 +583,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                     const int kk = keys[16 * h + i];
                     if (kk >= 0) {
                         // zero totals are committed too: testing costs more than the atomic
-                        atomicAdd(dst + (size_t)kk * DEP_SLOTS, (unsigned long long)f2ll_rn(acc));
+                        atomicAdd(dst + (size_t)kk * stride, (unsigned long long)f2ll_rn(acc));
                     }
                     acc = 0.0f;
                 }
@@ -559,40 +592,47 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     }
 }
 
-// J and rho at every grid point from the per-cell sums: point p gathers slot
-// q of cell p - off(q), the inverse of the deposit table. Integer sums, so the
-// result equals committing every run total to its point directly.
-__global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned long long *__restrict__ wc,
-                                  unsigned long long *Jx, unsigned long long *Jy, unsigned long long *Jz,
-                                  unsigned long long *rho, int with_rho) {
+// J (what & 1) and rho (what & 2) at every grid point from the per-cell
+// records: point p gathers slot q of cell p - off(q), the inverse of the
+// deposit table. Integer sums, so the result equals committing every run
+// total to its point directly.
+__global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned long long *__restrict__ wj,
+                                  const unsigned long long *__restrict__ wr, unsigned long long *Jx,
+                                  unsigned long long *Jy, unsigned long long *Jz, unsigned long long *rho, int what) {
     const int64_t first = (int64_t)sx + sy + 1;  // points below have no neighbour cell with particles
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
-        unsigned long long jx = 0, jy = 0, jz = 0, r = 0;
-        if (p >= first) {
-            // record of cell c starts at wc + 20 c (160 bytes, 16-byte aligned)
-            auto rec = [&](int64_t c) { return wc + c * DEP_SLOTS; };
-            const ulonglong2 *a0 = reinterpret_cast<const ulonglong2 *>(rec(p));              // slots 0-3
-            const ulonglong2 *a2 = reinterpret_cast<const ulonglong2 *>(rec(p - sy) + 4);     // 4-7
-            const ulonglong2 g1 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - 1) + 8));             // 8-9
-            const ulonglong2 g3 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sy - 1) + 10));       // 10-11
-            const ulonglong2 g5 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx - 1) + 12));       // 12-13
-            const ulonglong2 g6 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx - sy) + 14));      // 14-15
-            const ulonglong2 g4a = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx) + 16));          // 16-17
-            const ulonglong2 g0a = __ldg(a0), g0b = __ldg(a0 + 1);
-            const ulonglong2 g2a = __ldg(a2), g2b = __ldg(a2 + 1);
-            jx = g0a.x + g2a.x + g2a.y + g3.x;  // q 0, 1, 3, 2
-            jy = g0a.y + g1.x + g5.x + g4a.x;   // q 4, 5, 6, 7
-            jz = g0b.x + g2b.x + g6.x + g4a.y;  // q 8, 11, 10, 9
-            if (with_rho) {
-                const unsigned long long g4b = __ldg(rec(p - sx) + 18);            // q 13
-                const unsigned long long g7 = __ldg(rec(p - sx - sy - 1) + 19);    // q 17
-                r = g0b.y + g2b.y + g1.y + g3.y + g5.y + g6.y + g4b + g7;  // q 12 15 19 16 18 14 13 17
+        if (what & 1) {
+            unsigned long long jx = 0, jy = 0, jz = 0;
+            if (p >= first) {
+                // J record of cell c: wj + 12 c (96 bytes, 32-byte aligned)
+                auto rec = [&](int64_t c) { return wj + c * DEP_JSLOTS; };
+                const ulonglong2 g0a = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p)));        // slots 0,1
+                const unsigned long long g0b = __ldg(rec(p) + 2);
+                const unsigned long long g2a = __ldg(rec(p - sy) + 3);
+                const ulonglong2 g2b = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sy) + 4));  // 4,5
+                const unsigned long long g1 = __ldg(rec(p - 1) + 6);
+                const unsigned long long g3 = __ldg(rec(p - sy - 1) + 7);
+                const unsigned long long g5 = __ldg(rec(p - sx - 1) + 8);
+                const unsigned long long g6 = __ldg(rec(p - sx - sy) + 9);
+                const ulonglong2 g4 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx) + 10));  // 10,11
+                jx = g0a.x + g2a + g2b.x + g3;   // q 0, 1, 3, 2
+                jy = g0a.y + g1 + g5 + g4.x;     // q 4, 5, 6, 7
+                jz = g0b + g2b.y + g6 + g4.y;    // q 8, 11, 10, 9
             }
+            Jx[p] = jx;
+            Jy[p] = jy;
+            Jz[p] = jz;
         }
-        Jx[p] = jx;
-        Jy[p] = jy;
-        Jz[p] = jz;
-        if (with_rho) rho[p] = r;
+        if (what & 2) {
+            unsigned long long r = 0;
+            if (p >= first) {
+                auto rec = [&](int64_t c) { return wr + c * DEP_RSLOTS; };
+                r = __ldg(rec(p)) + __ldg(rec(p - sy) + 1) + __ldg(rec(p - 1) + 2) + __ldg(rec(p - sy - 1) + 3) +
+                    __ldg(rec(p - sx - 1) + 4) + __ldg(rec(p - sx - sy) + 5) + __ldg(rec(p - sx) + 6) +
+                    __ldg(rec(p - sx - sy - 1) + 7);  // q 12 15 19 16 18 14 13 17
+            }
+            rho[p] = r;
+        }
     }
 }
 
@@ -974,7 +1014,8 @@ int mixed_alloc(emoo_handle *h) {
     FieldsF32 *m = h->mf;
     size_t n = (size_t)h->g.npts;
     EMOO_CUDA(cudaMalloc(&m->pack, n * PACK_F4 * sizeof(float4)));
-    EMOO_CUDA(cudaMalloc(&m->wc, n * DEP_SLOTS * sizeof(unsigned long long)));
+    EMOO_CUDA(cudaMalloc(&m->wj, n * DEP_JSLOTS * sizeof(unsigned long long)));
+    EMOO_CUDA(cudaMalloc(&m->wr, n * DEP_RSLOTS * sizeof(unsigned long long)));
     for (int c = 0; c < 3; c++) EMOO_CUDA(cudaMalloc(&m->E[c], n * sizeof(float)));
     for (int c = 0; c < 6; c++) EMOO_CUDA(cudaMalloc(&m->Bslot[c], n * sizeof(float)));
     for (int c = 0; c < 4; c++) EMOO_CUDA(cudaMalloc(&m->J[c], n * sizeof(long long)));
@@ -999,7 +1040,8 @@ void mixed_free(emoo_handle *h) {
     for (int c = 0; c < 4; c++)
         if (m->J[c]) cudaFree(m->J[c]);
     if (m->pack) cudaFree(m->pack);
-    if (m->wc) cudaFree(m->wc);
+    if (m->wj) cudaFree(m->wj);
+    if (m->wr) cudaFree(m->wr);
     if (h->g0) cudaFree(h->g0);
     h->g0 = nullptr;
     delete m;
@@ -1128,7 +1170,8 @@ int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n) {
     return EMOO_OK;
 }
 
-static int mixed_fold(emoo_handle *h) {
+// what: FOLD_J (the two transverse J components), FOLD_RHO, or both
+static int mixed_fold(emoo_handle *h, int what) {
     MGeom mg = mgeom(h, h->dtp);
     const Geom &g = h->g;
     for (int d = 0; d < 3; d++) {
@@ -1136,29 +1179,37 @@ static int mixed_fold(emoo_handle *h) {
         int f0 = (d == 0) ? 1 : 0;  // Jy for x, Jx otherwise
         int f1 = (d == 2) ? 1 : 2;  // Jy for z, Jz otherwise
         int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        long long *a = h->mf->J[f0], *b = h->mf->J[f1], *r = h->mf->J[3];
+        int nz = what == FOLD_J ? 2 : what == FOLD_RHO ? 1 : 3;
+        if (what == FOLD_RHO) a = r;
         dim3 blk(32, 8);
-        dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 3);
+        dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, nz);
         h->launches++;
-        k_fold_m<<<grd, blk, 0, h->stream>>>(mg, d, h->mf->J[f0], h->mf->J[f1], h->mf->J[3]);
+        k_fold_m<<<grd, blk, 0, h->stream>>>(mg, d, a, b, r);
     }
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
 
-// Zeroes the per-cell sums; the deposit then rewrites Jx, Jy, Jz (and rho
-// when deposited) at every point from them.
-static int mixed_deposit_zero(emoo_handle *h, int with_rho) {
-    (void)with_rho;
-    EMOO_CUDA(cudaMemsetAsync(h->mf->wc, 0, sizeof(unsigned long long) * DEP_SLOTS * (size_t)h->g.npts, h->stream));
+// Deposit modes: DEP_J (J only), DEP_J_RHO, DEP_RHO (rho only: J untouched).
+constexpr int DEP_J = 0, DEP_J_RHO = 1, DEP_RHO = 2;
+
+// Zeroes the per-cell sums the deposit mode forms its output from; the
+// deposit then rewrites Jx, Jy, Jz and / or rho at every point from them.
+static int mixed_deposit_zero(emoo_handle *h, int mode) {
+    const size_t n = (size_t)h->g.npts * sizeof(unsigned long long);
+    if (mode != DEP_RHO) EMOO_CUDA(cudaMemsetAsync(h->mf->wj, 0, n * DEP_JSLOTS, h->stream));
+    if (mode != DEP_J) EMOO_CUDA(cudaMemsetAsync(h->mf->wr, 0, n * DEP_RSLOTS, h->stream));
     return EMOO_OK;
 }
 
-static int mixed_cells_to_points(emoo_handle *h, int with_rho) {
+static int mixed_cells_to_points(emoo_handle *h, int mode) {
     FieldsF32 *m = h->mf;
+    const int what = mode == DEP_J ? 1 : mode == DEP_RHO ? 2 : 3;
     h->launches++;
     k_cells_to_points<<<nblk(h->g.npts, 152 * 8), 256, 0, h->stream>>>(
-        h->g.npts, (int)h->g.sx, (int)h->g.sy, m->wc, (unsigned long long *)m->J[0], (unsigned long long *)m->J[1],
-        (unsigned long long *)m->J[2], (unsigned long long *)m->J[3], with_rho);
+        h->g.npts, (int)h->g.sx, (int)h->g.sy, m->wj, m->wr, (unsigned long long *)m->J[0],
+        (unsigned long long *)m->J[1], (unsigned long long *)m->J[2], (unsigned long long *)m->J[3], what);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
@@ -1174,9 +1225,9 @@ __global__ void k_add_phys_i64(MGeom g, long long *f, long long v) {
 }
 
 // J and rho at the points from the per-cell records, plus the background.
-static int mixed_finish_deposit(emoo_handle *h, int with_rho) {
-    EMOO_TRY(mixed_cells_to_points(h, with_rho));
-    if (!with_rho || h->opts.rho_background == 0.0) return EMOO_OK;
+static int mixed_finish_deposit(emoo_handle *h, int mode) {
+    EMOO_TRY(mixed_cells_to_points(h, mode));
+    if (mode == DEP_J || h->opts.rho_background == 0.0) return EMOO_OK;
     const Geom &g = h->g;
     dim3 blk(32, 8);
     dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
@@ -1190,8 +1241,9 @@ static int mixed_finish_deposit(emoo_handle *h, int with_rho) {
 // Gather + push + boundaries + deposit (push = false: deposit at the current
 // state), then J and rho at the points from the per-cell sums. The per-cell
 // sums must have been zeroed (mixed_deposit_zero).
-static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = true) {
-    if (h->np == 0) return mixed_finish_deposit(h, with_rho);
+static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
+    const int with_rho = mode != DEP_J ? 1 : 0;
+    if (h->np == 0) return mixed_finish_deposit(h, mode);
     MGeom mg = mgeom(h, dtp);
     MSpecies st = mspecies(h, dtp);
     MGather P;
@@ -1201,7 +1253,8 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
         P.T[c] = mt_role(h, c);
     }
     MDeposit D;
-    D.wc = h->mf->wc;
+    D.wj = h->mf->wj;
+    D.wr = h->mf->wr;
     int64_t nb = (h->np + FUSED_BLOCK - 1) / FUSED_BLOCK;
     bool rel = h->info.relativity != 0;
     bool first = rel && h->first_push && h->g0;
@@ -1222,7 +1275,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
             k_fused_m<false, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
                                                                                with_rho, g0, h->ctr);
         EMOO_CUDA(cudaGetLastError());
-        return mixed_finish_deposit(h, with_rho);
+        return mixed_finish_deposit(h, mode);
     }
     {
         const Geom &g = h->g;
@@ -1250,7 +1303,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int with_rho, bool push = tru
     }
     // g0 stays allocated for later loads; it is read only while first_push is set
     if (first) h->first_push = 0;
-    return mixed_finish_deposit(h, with_rho);
+    return mixed_finish_deposit(h, mode);
 }
 
 static int mixed_yee(emoo_handle *h, double dtp, int es) {
@@ -1277,10 +1330,11 @@ static int mixed_yee(emoo_handle *h, double dtp, int es) {
     return EMOO_OK;
 }
 
-int mixed_step(emoo_handle *h, double dtp, int with_rho) {
-    EMOO_TRY(mixed_deposit_zero(h, with_rho));
-    EMOO_TRY(mixed_fused(h, dtp, with_rho));
-    EMOO_TRY(mixed_fold(h));
+int mixed_step(emoo_handle *h, double dtp, int with_rho, int fold_what) {
+    const int mode = with_rho ? DEP_J_RHO : DEP_J;
+    EMOO_TRY(mixed_deposit_zero(h, mode));
+    EMOO_TRY(mixed_fused(h, dtp, mode));
+    EMOO_TRY(mixed_fold(h, fold_what));
     EMOO_TRY(mixed_yee(h, dtp, h->info.electrostatic == 1));
     EMOO_TRY(mixed_ghost_fill(h));
     return EMOO_OK;
@@ -1415,11 +1469,20 @@ namespace emoo {
 // Particle_Handler::depositRhoJ for the mixed form: zero, then deposit every
 // live non-test particle at its current position (no push).
 int mixed_deposit(emoo_handle *h, int with_rho) {
-    EMOO_TRY(mixed_deposit_zero(h, with_rho));
-    return mixed_fused(h, h->dtp, with_rho, false);
+    const int mode = with_rho ? DEP_J_RHO : DEP_J;
+    EMOO_TRY(mixed_deposit_zero(h, mode));
+    return mixed_fused(h, h->dtp, mode, false);
 }
 
-int mixed_fold_public(emoo_handle *h) { return mixed_fold(h); }
+// rho alone at the particles' current positions, folded, plus the
+// background; J untouched.
+int mixed_materialize_rho(emoo_handle *h) {
+    EMOO_TRY(mixed_deposit_zero(h, DEP_RHO));
+    EMOO_TRY(mixed_fused(h, h->dtp, DEP_RHO, false));
+    return mixed_fold(h, FOLD_RHO);
+}
+
+int mixed_fold_public(emoo_handle *h) { return mixed_fold(h, FOLD_ALL); }
 
 int mixed_yee_public(emoo_handle *h, double dtp, int es) { return mixed_yee(h, dtp, es); }
 

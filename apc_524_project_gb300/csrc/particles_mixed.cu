@@ -133,8 +133,11 @@ constexpr int DEP_JSLOTS = 12, DEP_RSLOTS = 8;
 // the float spacing is 1) leaves each part's nearest integer in the low
 // mantissa bits; h 2^22 is even, so the parts round as v does. Exact for
 // |v| < 2^43; larger values (and NaN) take the conversion.
+// GUARD = false drops the range test where |v| < 2^43 is known (see the
+// relativistic deposit, where |velocity| < 1 bounds every run total).
+template <bool GUARD = true>
 __device__ __forceinline__ long long f2ll_rn(float v) {
-    if (!(fabsf(v) < 8.0e12f)) return __float2ll_rn(v);
+    if (GUARD && !(fabsf(v) < 8.0e12f)) return __float2ll_rn(v);
     const float M = 12582912.0f;                    // 1.5 * 2^23
     const float hm = v * 2.384185791015625e-07f + M;  // M + rint(v 2^-22); v 2^-22 is exact
     const float lo = fmaf(M - hm, 4194304.0f, v);   // v - rint(v 2^-22) 2^22, exact
@@ -540,12 +543,16 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
         // 0..15 while lanes 16..27 walk them over particles 16..31, each in
         // particle order, committing at each run end; a run that spans
         // particles 15 and 16 is committed as two parts.
+        // Only the ends of active runs commit: an inactive particle is a run of
+        // its own with a zero column, so skipping its end adds 0 to the next run.
+        // With |velocity| < 1 (relativistic), a run total is below 2^39 quanta.
         const int q = lane & 15, half = lane >> 4;
         if (q < DEP_JSLOTS) {
             unsigned long long *dst = D.wj + dep_pos(q);
             const float *row = col + q * DEP_STRIDE + 16 * half;
             const int *hkeys = keys + 16 * half;
-            const unsigned ends = ((ends32 >> (16 * half)) & 0xffffu) | 0x8000u;
+            const unsigned hact = (act >> (16 * half)) & 0xffffu;
+            const unsigned ends = (((ends32 >> (16 * half)) & 0xffffu) | 0x8000u) & hact;
             float r[16];
 #pragma unroll
             for (int i = 0; i < 16; i++) r[i] = row[i];
@@ -554,8 +561,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
             for (int i = 0; i < 16; i++) {
                 acc += r[i];
                 if ((ends >> i) & 1u) {
-                    const int kk = hkeys[i];
-                    if (kk >= 0) atomicAdd(dst + (size_t)kk * DEP_JSLOTS, (unsigned long long)f2ll_rn(acc));
+                    atomicAdd(dst + (size_t)hkeys[i] * DEP_JSLOTS, (unsigned long long)f2ll_rn<!REL>(acc));
                     acc = 0.0f;
                 }
             }

@@ -97,6 +97,7 @@ class Opts(C.Structure):
         ("deposit_rho", C.c_int),
         ("history_every", C.c_int),
         ("rho_background", C.c_double),
+        ("rho_background_xmin", C.c_double),
     ]
 
 
@@ -123,6 +124,8 @@ class Stats(C.Structure):
 
 
 AD_FORWARD, AD_TANGENT, AD_ADJOINT = 0, 1, 2
+AD_OBJ_FIELD, AD_OBJ_KINETIC = 0, 1
+NCOEF = 16
 
 
 class AdSpec(C.Structure):
@@ -131,6 +134,22 @@ class AdSpec(C.Structure):
         ("checkpoint_every", C.c_int),
         ("slab_lo", C.c_int),
         ("slab_hi", C.c_int),
+        ("objective", C.c_int),
+        ("species", C.c_int),
+    ]
+
+
+class WaveShape(C.Structure):
+    """emoo_wave_shape: transverse Gaussian spot and sine-series envelope of
+    one injected wave."""
+
+    _fields_ = [
+        ("waist", C.c_double),
+        ("center", C.c_double * 2),
+        ("t_start", C.c_double),
+        ("window", C.c_double),
+        ("ncoef", C.c_int),
+        ("coef", C.c_double * NCOEF),
     ]
 
 
@@ -189,6 +208,8 @@ PROTOTYPES = {
     "emoo_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "emoo_sort_permutation_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "emoo_set_waves": (C.c_int, [_P, C.c_int, _D, _D]),
+    "emoo_set_wave_shape": (C.c_int, [_P, C.c_int, C.POINTER(WaveShape)]),
+    "emoo_ad_nparams": (C.c_int, [_P]),
     "emoo_ad_run": (C.c_int, [_P, C.POINTER(AdSpec), C.c_int, _D, _D, C.POINTER(AdResult), _D, _D]),
 }
 

@@ -46,6 +46,17 @@ class Species:
 
 
 @dataclass
+class Shape:
+    """Transverse Gaussian spot and sine-series envelope of an injected wave
+    (emoo_set_wave_shape; no reference counterpart)."""
+    waist: float = 0.0                                # 0: plane wave
+    center: Optional[Tuple[float, float]] = None      # None: middle of the transverse extent
+    t_start: float = 0.0
+    window: float = 0.0
+    coef: Tuple[float, ...] = ()                      # sine-series coefficients (empty: Gaussian envelope)
+
+
+@dataclass
 class Wave:
     side: int   # -1 x left, +1 x right, ...
     pol: int    # E polarisation 1,2,3
@@ -54,6 +65,7 @@ class Wave:
     phase_deg: float = 0.0
     inv_width: float = 0.0
     delay: float = 0.0
+    shape: Optional[Shape] = None
 
 
 @dataclass
@@ -174,15 +186,65 @@ def input_info(cfg: Config) -> abi.InputInfo:
 
 def rho_background(cfg: Config) -> float:
     """Uniform immobile background (reference rho units) that neutralises the
-    deposited species on average: each macro-particle deposits
+    deposited species where they are loaded: each macro-particle deposits
     UNIT_RHOJ * charge_ratio / V = w q / V in total, so the background is
     -sum_s w q_s ppc_s / V. Zero unless cfg.immobile_ions."""
     if not cfg.immobile_ions:
         return 0.0
     w = cfg.macro_weight()
     vol = cfg.dx[0] * cfg.dx[1] * cfg.dx[2]
-    cells = cfg.n[0] * cfg.n[1] * cfg.n[2]
-    return -sum(w * s.q * cfg.count(s) / cells for s in cfg.species if not s.test) / vol
+    return -sum(w * s.q * s.ppc for s in cfg.species if not s.test) / vol
+
+
+def rho_background_xmin(cfg: Config) -> Optional[float]:
+    """Where the background starts: the lowest x the deposited species are
+    loaded from, when every one of them is loaded in an x range (None: the
+    whole box)."""
+    sp = [s for s in cfg.species if not s.test]
+    if not cfg.immobile_ions or not sp or any(s.x_range is None for s in sp):
+        return None
+    return cfg.x0[0] + min(s.x_range[0] for s in sp)
+
+
+def wave_shape(cfg: Config, w: int, coef=None) -> Optional[abi.WaveShape]:
+    """emoo_wave_shape of wave w (None when it has no shape); coef, when
+    given, replaces the shape's envelope coefficients."""
+    sh = cfg.waves[w].shape
+    if sh is None:
+        return None
+    out = abi.WaveShape()
+    out.waist = sh.waist
+    d = abs(cfg.waves[w].side) - 1
+    axes = [a for a in range(3) if a != d]
+    center = sh.center if sh.center is not None else tuple(cfg.x0[a] + 0.5 * cfg.L[a] for a in axes)
+    out.center[0], out.center[1] = center
+    out.t_start = sh.t_start
+    out.window = sh.window
+    c = list(sh.coef if coef is None else coef)
+    if len(c) > abi.NCOEF:
+        raise ValueError(f"at most {abi.NCOEF} envelope coefficients")
+    out.ncoef = len(c)
+    for k, v in enumerate(c):
+        out.coef[k] = v
+    return out
+
+
+def apply_wave_shapes(backend, cfg: Config, coefs=None):
+    """Hands every shaped wave's shape to a backend (set_wave_shape(w, shape));
+    coefs[w], when given, replaces wave w's envelope coefficients."""
+    for w, wv in enumerate(cfg.waves):
+        if wv.shape is not None:
+            backend.set_wave_shape(w, wave_shape(cfg, w, None if coefs is None else coefs[w]))
+
+
+def gaussian_sine_coefficients(window: float, fwhm: float, ncoef: int = 16):
+    """Sine-series coefficients c_k (k = 1..ncoef) of a unit-peak Gaussian
+    of the given FWHM centred in [0, window]: with a = 4 ln 2 / fwhm^2 and the
+    tails beyond the window neglected,
+    c_k = (2 / window) sin(k pi / 2) sqrt(pi / a) exp(-(k pi / window)^2 / (4 a))."""
+    a = 4.0 * math.log(2.0) / fwhm ** 2
+    return [(2.0 / window) * math.sin(k * PI / 2.0) * math.sqrt(PI / a)
+            * math.exp(-(k * PI / window) ** 2 / (4.0 * a)) for k in range(1, ncoef + 1)]
 
 
 def b_noise_fields(cfg: Config):
@@ -272,6 +334,39 @@ def laser64(n=(64, 64, 64), steps=128, ppc=8, a0=0.5, wavelength=16.0, fwhm_step
         part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
         field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
         waves=[wave], seed=20240505)
+
+
+def laser512(n=(512, 128, 128), steps=512, ppc=16, a0=1.0, wavelength=20.0, fwhm_steps=60, waist=30.0,
+             plasma_x0=64.0, density=0.01, vth=0.01, coef_sigma=0.1, seed=20240606):
+    """Laser-plasma at scale: a y-polarised pulse injected at x-left
+    (amplitude a0 omega, omega = 2 pi / wavelength) with a transverse Gaussian
+    spot of the given waist (1/e field radius) and an envelope of 16
+    sine-series coefficients over a window of four FWHM: the coefficients of
+    a unit-peak Gaussian of FWHM fwhm_steps dt centred in the window, each
+    plus seeded N(0, coef_sigma) noise. External fields and absorbing
+    particle walls in x, periodic y and z; electrons at `density` of the
+    critical density (omega_pe = sqrt(density) omega) and ppc per cell from
+    x = plasma_x0 on, over immobile ions there; relativistic push. The
+    electron temperature is not part of the workload's definition; vth sets
+    a cold plasma."""
+    import numpy as np
+
+    dt = 0.45
+    omega = 2.0 * PI / wavelength
+    fwhm_t = fwhm_steps * dt
+    window = 4.0 * fwhm_t
+    coef = gaussian_sine_coefficients(window, fwhm_t, 16)
+    rng = np.random.default_rng(seed)
+    coef = [c + coef_sigma * float(z) for c, z in zip(coef, rng.standard_normal(16))]
+    shape = Shape(waist=waist, t_start=0.0, window=window, coef=tuple(coef))
+    wave = Wave(side=-1, pol=2, amp=a0 * omega, omega=omega, phase_deg=0.0, shape=shape)
+    return Config(
+        name="laser512", n=tuple(n), dt=dt, steps=steps, omega_pe=math.sqrt(density) * omega,
+        species=[Species("e", -1.0, 1.0, ppc, vth, x_range=(plasma_x0, n[0] * 1.0))],
+        relativity=1, init="constant",
+        part_bc=("absorbing", "absorbing", "periodic", "periodic", "periodic", "periodic"),
+        field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
+        waves=[wave], seed=seed, immobile_ions=True)
 
 
 def tiny(name="tiny", n=(6, 5, 4), dx=(1.0, 1.0, 1.0), ppc=3, relativity=0, init="poisson", steps=4,

@@ -5,9 +5,10 @@
 // charge density: gather + push + particle boundaries + current deposit (one
 // particle kernel), the periodic J fold, the Yee update and executeBC(-1)
 // (periodic ghost copies, LightBC planes). Its parameters are the initial
-// particle velocities and the amplitude and phase of every injected wave; the
-// objective is the field energy 0.5 V sum(E^2 + B^2) over the grid points of
-// an x slab at the last step.
+// particle velocities, the amplitude and phase of every injected wave and the
+// coefficients of sine-series envelopes; the objective is the field energy
+// 0.5 V sum(E^2 + B^2) over the grid points of an x slab, or the kinetic
+// energy of the particles in an x range, at the last step.
 //
 //  * Tangent: the particle kernel runs in dual numbers (ad_math.cuh) next to
 //    the primal one; the field part is linear, so the tangent fields go
@@ -18,8 +19,9 @@
 //    is a gather of the J adjoint at the particle's 12 points, the gather's
 //    adjoint a scatter (atomics) of the field adjoint with the same weights,
 //    the Yee and ghost/fold adjoints are the transposed stencils and copies,
-//    a plane's adjoint reduces the field adjoint over the plane into the
-//    wave-parameter gradient and clears the plane. State is checkpointed
+//    a plane's adjoint reduces the field adjoint over the plane (plain and
+//    weighted by the transverse spot) and clears the plane; the host forms
+//    the wave-parameter gradient from those sums. State is checkpointed
 //    every `checkpoint_every` steps; each segment is recomputed forward,
 //    storing the state before each of its steps, then reversed.
 //
@@ -399,31 +401,45 @@ __global__ void k_ghost_adj(Geom g, Slots6 fl, int d, int side) {
     F[pd] = 0.0;
 }
 
-struct PlaneCoef {
-    int nk;
-    int kidx[2 * EMOO_NWAVE];
-    double coef[2 * EMOO_NWAVE];
-};
-
-// Adjoint of a whole-plane set: the plane's value depends only on the wave
-// parameters, so dtheta_k += coef_k sum(LF over the plane) and the plane's
-// adjoint is cleared.
-__global__ void k_plane_adj(Geom g, double *F, int d, int idx, PlaneCoef pc, double *dtheta) {
+// Adjoint of a plane set v + vs t1[p] t2[q]: the plane's values depend only
+// on the wave parameters, so the step needs sum(LF) and sum(LF t1 t2) over
+// the plane (one block, fixed order); the host turns them into the
+// parameter gradient. The plane's adjoint is cleared.
+__global__ void k_plane_adj(Geom g, double *F, int d, int idx, const double *t1, const double *t2, double *sums2) {
+    __shared__ double s_u[8], s_s[8];
     const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-    double sum = 0.0;
+    double su = 0.0, ss = 0.0;
     const int64_t m = (int64_t)g.tot[o1] * g.tot[o2];
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = threadIdx.x; t < m; t += blockDim.x) {
         int c[3];
         c[d] = idx;
         c[o1] = (int)(t / g.tot[o2]);
         c[o2] = (int)(t % g.tot[o2]);
         const int64_t p = gidx(g, c[0], c[1], c[2]);
-        sum += F[p];
+        const double l = F[p];
+        su += l;
+        if (t1) ss += l * t1[c[o1]] * t2[c[o2]];
         F[p] = 0.0;
     }
-    for (int off = 16; off > 0; off >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, off);
-    if ((threadIdx.x & 31) == 0 && sum != 0.0)
-        for (int k = 0; k < pc.nk; k++) atomicAdd(dtheta + pc.kidx[k], pc.coef[k] * sum);
+    for (int off = 16; off > 0; off >>= 1) {
+        su += __shfl_down_sync(0xffffffffu, su, off);
+        ss += __shfl_down_sync(0xffffffffu, ss, off);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_u[w] = su;
+        s_s[w] = ss;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            a += s_u[i];
+            b += s_s[i];
+        }
+        sums2[0] = a;
+        sums2[1] = b;
+    }
 }
 
 // ---- objective -----------------------------------------------------------
@@ -469,6 +485,63 @@ __global__ void k_objective_seed(Geom g, Slab sl, FPtrs F, FOut A) {
         for (int c = 0; c < 3; c++) {
             A.E[c][p] += g.vol * F.E[c][p];
             A.B[c][p] += g.vol * F.B[c][p];
+        }
+    }
+}
+
+// Selection of the kinetic objective: particles of `species` (-1: all),
+// alive, with x in [xlo, xhi).
+struct KinSel {
+    int species;
+    double xlo, xhi;
+};
+
+__device__ __forceinline__ bool kin_selected(const SpeciesTab &st, const KinSel &ks, int64_t p, double x, int &s) {
+    if (x != x) return false;  // removed
+    s = species_of(st, p);
+    return (ks.species < 0 || s == ks.species) && x >= ks.xlo && x < ks.xhi;
+}
+
+// sum m (gamma - 1) (REL) or 0.5 m v^2 over the selected particles; with
+// tangent, also its derivative along dP: m dgamma, or m v . dv.
+template <bool REL>
+__global__ void k_objective_kin(SpeciesTab st, CPArr P, CPArr dP, int64_t np, KinSel ks, int tangent, double *out2) {
+    double a = 0.0, b = 0.0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        int s;
+        if (!kin_selected(st, ks, p, P.p[0][p], s)) continue;
+        const double m = st.m[s];
+        if (REL) {
+            a += m * (P.p[6][p] - 1.0);
+            if (tangent) b += m * dP.p[6][p];
+        } else {
+            const double vx = P.p[3][p], vy = P.p[4][p], vz = P.p[5][p];
+            a += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+            if (tangent) b += m * (vx * dP.p[3][p] + vy * dP.p[4][p] + vz * dP.p[5][p]);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out2, a);
+        atomicAdd(out2 + 1, b);
+    }
+}
+
+// Seeds the particle adjoints with d objective / d(gamma) = m (REL) or
+// d objective / d v = m v on the selected particles.
+template <bool REL>
+__global__ void k_objective_kin_seed(SpeciesTab st, CPArr P, PArr L, int64_t np, KinSel ks) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        int s;
+        if (!kin_selected(st, ks, p, P.p[0][p], s)) continue;
+        const double m = st.m[s];
+        if (REL) {
+            L.p[6][p] += m;
+        } else {
+            for (int c = 0; c < 3; c++) L.p[3 + c][p] += m * P.p[3 + c][p];
         }
     }
 }
@@ -615,13 +688,36 @@ dim3 grid_all(const Geom &g, dim3 blk) {
     return dim3((g.tot[2] + blk.x - 1) / blk.x, (g.tot[1] + blk.y - 1) / blk.y, g.tot[0]);
 }
 
-int objective(emoo_handle *h, const Slab &sl, double *const *dslots, double *dev2, double out2[2]) {
+struct ObjSpec {
+    int kind;  // EMOO_AD_OBJ_FIELD or EMOO_AD_OBJ_KINETIC
+    Slab sl;
+    KinSel ks;
+};
+
+CPArr particle_arrays(emoo_handle *h) { return CPArr{{h->x, h->y, h->z, h->vx, h->vy, h->vz, h->gam}}; }
+
+// The objective (out2[0]) and, with tangent states dslots / dP, its
+// derivative along them (out2[1]).
+int objective(emoo_handle *h, const ObjSpec &os, double *const *dslots, double *const *dP, double *dev2,
+              double out2[2]) {
     EMOO_CUDA(cudaMemsetAsync(dev2, 0, 2 * sizeof(double), h->stream));
-    FPtrs F = field_ptrs(h, h->slot, h->bswap);
-    FPtrs dF = dslots ? field_ptrs(h, dslots, h->bswap) : F;
     h->launches++;
-    k_objective<<<pblocks((int64_t)(sl.hi - sl.lo) * h->g.n[1] * h->g.n[2]), 256, 0, h->stream>>>(
-        h->g, sl, F, dF, dslots ? 1 : 0, dev2);
+    if (os.kind == EMOO_AD_OBJ_FIELD) {
+        const Slab &sl = os.sl;
+        FPtrs F = field_ptrs(h, h->slot, h->bswap);
+        FPtrs dF = dslots ? field_ptrs(h, dslots, h->bswap) : F;
+        k_objective<<<pblocks((int64_t)(sl.hi - sl.lo) * h->g.n[1] * h->g.n[2]), 256, 0, h->stream>>>(
+            h->g, sl, F, dF, dslots ? 1 : 0, dev2);
+    } else {
+        SpeciesTab st;
+        species_tab(h, h->dtp, st);
+        const CPArr P = particle_arrays(h);
+        const CPArr D = dP ? CPArr{{dP[0], dP[1], dP[2], dP[3], dP[4], dP[5], dP[6]}} : P;
+        if (h->info.relativity)
+            k_objective_kin<true><<<pblocks(h->np), 256, 0, h->stream>>>(st, P, D, h->np, os.ks, dP ? 1 : 0, dev2);
+        else
+            k_objective_kin<false><<<pblocks(h->np), 256, 0, h->stream>>>(st, P, D, h->np, os.ks, dP ? 1 : 0, dev2);
+    }
     EMOO_CUDA(cudaGetLastError());
     EMOO_CUDA(cudaMemcpyAsync(out2, dev2, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
@@ -666,9 +762,12 @@ static int tlm_step(emoo_handle *h, AdRun &R, double **dP, double *const *dslot,
             if (op.kind == 0) {
                 EMOO_TRY(ghost_fill_f64(h, ids_eb, 6, op.mask));
             } else {
-                double v = 0.0;
-                for (int k = 0; k < op.nk; k++) v += op.coef[k] * (dtheta ? dtheta[op.kidx[k]] : 0.0);
-                PlaneSet ps{dslot[op.slot], op.dim, op.idx, v};
+                double v = 0.0, vs = 0.0;
+                if (dtheta) {
+                    for (size_t k = 0; k < op.ku.size(); k++) v += op.cu[k] * dtheta[op.ku[k]];
+                    for (size_t k = 0; k < op.ks.size(); k++) vs += op.cs[k] * dtheta[op.ks[k]];
+                }
+                PlaneSet ps{dslot[op.slot], op.dim, op.idx, v, vs, op.t1, op.t2, nullptr, nullptr};
                 EMOO_TRY(plane_set_f64(h, &ps, 1));
             }
         }
@@ -678,8 +777,17 @@ static int tlm_step(emoo_handle *h, AdRun &R, double **dP, double *const *dslot,
     return EMOO_OK;
 }
 
+// The plane sets met by the adjoint steps, in reverse order, with the
+// device sums (sum LF, sum LF t1 t2) each one left in `sums`; the wave
+// parameter gradient is formed from them on the host at the end.
+struct PlaneLedger {
+    std::vector<AdBcOp> ops;
+    double *sums = nullptr;
+    size_t cap = 0;
+};
+
 // adjoint of one step, given the state before it (snapshot S)
-static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, double *const *lslot, double *dtheta) {
+static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, double *const *lslot, PlaneLedger &pl) {
     const Geom &g = h->g;
     const int b1 = S.bswap ^ 1;  // B roles after the step's Yee update
     // 1. executeBC(-1) at the step's time, in reverse
@@ -709,15 +817,11 @@ static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, dou
                 }
             }
         } else {
-            PlaneCoef pc;
-            pc.nk = op.nk;
-            for (int k = 0; k < op.nk; k++) {
-                pc.kidx[k] = op.kidx[k];
-                pc.coef[k] = op.coef[k];
-            }
+            if (pl.ops.size() >= pl.cap) return EMOO_ERR_STATE;
+            double *sums = pl.sums + 2 * pl.ops.size();
+            pl.ops.push_back(op);
             h->launches++;
-            k_plane_adj<<<pblocks((int64_t)g.tot[0] * g.tot[1]), 256, 0, h->stream>>>(g, lslot[op.slot], op.dim,
-                                                                                       op.idx, pc, dtheta);
+            k_plane_adj<<<1, 256, 0, h->stream>>>(g, lslot[op.slot], op.dim, op.idx, op.t1, op.t2, sums);
         }
     }
     EMOO_CUDA(cudaGetLastError());
@@ -766,21 +870,31 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
     if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
         return EMOO_ERR_ARG;
+    if (spec->objective != EMOO_AD_OBJ_FIELD && spec->objective != EMOO_AD_OBJ_KINETIC) return EMOO_ERR_ARG;
+    if (spec->objective == EMOO_AD_OBJ_KINETIC && (spec->species < -1 || spec->species >= h->nspec))
+        return EMOO_ERR_ARG;
     if (mode == EMOO_AD_ADJOINT && spec->checkpoint_every < 1) return EMOO_ERR_ARG;
     // the run moves the particles; as after emoo_step, rho is left pending
-    // (it is deposited at the final positions when read)
+    // (it is deposited at the final positions when read), and particles that
+    // absorbing walls remove leave the store when it is next read
     if (h->opts.deposit_rho) h->rho_stale = 1;
+    for (int s = 0; s < 6; s++)
+        if (h->bc.pbc[s] == PBC_ABSORBING) h->dead_pending = 1;
     AdRun R;
     R.h = h;
     R.np = h->np;
     R.npts = h->g.npts;
     R.rel = h->info.relativity != 0;
     if (R.rel && !h->gam) return EMOO_ERR_STATE;
-    const Slab sl{spec->slab_lo + 1, spec->slab_hi + 1};  // cells -> grid points (first physical point is 1)
-    const int ntheta = 2 * h->info.nwaves;
-    double *dev2 = R.alloc(2 + (size_t)std::max(ntheta, 1));
+    ObjSpec os;
+    os.kind = spec->objective;
+    os.sl = Slab{spec->slab_lo + 1, spec->slab_hi + 1};  // cells -> grid points (first physical point is 1)
+    os.ks.species = spec->species;
+    os.ks.xlo = h->info.xyz0[0] + spec->slab_lo * h->g.d[0];
+    os.ks.xhi = h->info.xyz0[0] + spec->slab_hi * h->g.d[0];
+    const int ntheta = emoo_ad_nparams(h);
+    double *dev2 = R.alloc(2);
     if (!dev2) return EMOO_ERR_OOM;
-    double *dth = dev2 + 2;
     memset(out, 0, sizeof(*out));
     cudaEvent_t ev[4];
     for (auto &e : ev) EMOO_CUDA(cudaEventCreate(&e));
@@ -796,7 +910,7 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
         EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
         for (int n = 0; n < spec->nsteps; n++) EMOO_TRY(primal_step(h));
         EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
-        EMOO_TRY(objective(h, sl, nullptr, dev2, o2));
+        EMOO_TRY(objective(h, os, nullptr, nullptr, dev2, o2));
         float ms = 0;
         EMOO_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
         out->forward_ms = ms;
@@ -822,7 +936,7 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
         EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
         for (int n = 0; n < spec->nsteps; n++) EMOO_TRY(tlm_step(h, R, dP, dslot, dtheta));
         EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
-        EMOO_TRY(objective(h, sl, dslot, dev2, o2));
+        EMOO_TRY(objective(h, os, dslot, dP, dev2, o2));
         float ms = 0;
         EMOO_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
         out->forward_ms = ms;
@@ -841,7 +955,7 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
         EMOO_TRY(primal_step(h));
     }
     EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
-    EMOO_TRY(objective(h, sl, nullptr, dev2, o2));  // synchronises
+    EMOO_TRY(objective(h, os, nullptr, nullptr, dev2, o2));  // synchronises
     out->objective = o2[0];
     {
         float ms = 0;
@@ -861,14 +975,33 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
         if (!(lslot[k] = R.alloc((size_t)R.npts))) return EMOO_ERR_OOM;
         EMOO_CUDA(cudaMemsetAsync(lslot[k], 0, sizeof(double) * R.npts, h->stream));
     }
-    EMOO_CUDA(cudaMemsetAsync(dth, 0, sizeof(double) * std::max(ntheta, 1), h->stream));
-    {
+    h->launches++;
+    if (os.kind == EMOO_AD_OBJ_FIELD) {
         FPtrs F = field_ptrs(h, h->slot, h->bswap);
         FOut A = field_out(lslot, h->bswap);
-        h->launches++;
+        const Slab &sl = os.sl;
         k_objective_seed<<<pblocks((int64_t)(sl.hi - sl.lo) * h->g.n[1] * h->g.n[2]), 256, 0, h->stream>>>(h->g, sl,
                                                                                                            F, A);
-        EMOO_CUDA(cudaGetLastError());
+    } else {
+        SpeciesTab st;
+        species_tab(h, h->dtp, st);
+        PArr LP{{L[0], L[1], L[2], L[3], L[4], L[5], L[6]}};
+        if (R.rel)
+            k_objective_kin_seed<true><<<pblocks(R.np), 256, 0, h->stream>>>(st, particle_arrays(h), LP, R.np, os.ks);
+        else
+            k_objective_kin_seed<false><<<pblocks(R.np), 256, 0, h->stream>>>(st, particle_arrays(h), LP, R.np, os.ks);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    // plane sums of every adjoint step (the plane sets per step do not change)
+    PlaneLedger pl;
+    {
+        std::vector<AdBcOp> ops;
+        EMOO_TRY(ad_bc_ops(h, ops));
+        size_t per = 0;
+        for (const AdBcOp &op : ops) per += op.kind == 1;
+        pl.cap = per * (size_t)N;
+        if (pl.cap && !(pl.sums = R.alloc(2 * pl.cap))) return EMOO_ERR_OOM;
+        pl.ops.reserve(pl.cap);
     }
     std::vector<Snapshot> tape(std::min(K, std::max(N, 1)));
     float rec_ms = 0, rev_ms = 0;
@@ -881,7 +1014,7 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
             if (n + 1 < n1) EMOO_TRY(primal_step(h));
         }
         EMOO_CUDA(cudaEventRecord(ev[2], h->stream));
-        for (int n = n1 - 1; n >= n0; n--) EMOO_TRY(adj_step(h, R, tape[n - n0], L, lslot, dth));
+        for (int n = n1 - 1; n >= n0; n--) EMOO_TRY(adj_step(h, R, tape[n - n0], L, lslot, pl));
         EMOO_CUDA(cudaEventRecord(ev[3], h->stream));
         EMOO_CUDA(cudaEventSynchronize(ev[3]));
         float a = 0, b = 0;
@@ -893,8 +1026,17 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     out->recompute_ms = rec_ms;
     out->reverse_ms = rev_ms;
-    if (grad_theta && ntheta)
-        EMOO_CUDA(cudaMemcpy(grad_theta, dth, sizeof(double) * ntheta, cudaMemcpyDeviceToHost));
+    if (grad_theta && ntheta) {
+        std::vector<double> sums(2 * pl.ops.size());
+        if (!sums.empty())
+            EMOO_CUDA(cudaMemcpy(sums.data(), pl.sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < ntheta; k++) grad_theta[k] = 0.0;
+        for (size_t i = 0; i < pl.ops.size(); i++) {
+            const AdBcOp &op = pl.ops[i];
+            for (size_t k = 0; k < op.ku.size(); k++) grad_theta[op.ku[k]] += op.cu[k] * sums[2 * i];
+            for (size_t k = 0; k < op.ks.size(); k++) grad_theta[op.ks[k]] += op.cs[k] * sums[2 * i + 1];
+        }
+    }
     if (grad_v)
         for (int a = 0; a < 3; a++)
             EMOO_CUDA(cudaMemcpy(grad_v + a * R.np, L[3 + a], sizeof(double) * R.np, cudaMemcpyDeviceToHost));

@@ -89,6 +89,7 @@ namespace {
 struct Pulses {
     int nw;
     double amp[EMOO_NWAVE], omg[EMOO_NWAVE], pha[EMOO_NWAVE], del[EMOO_NWAVE], iw[EMOO_NWAVE];
+    int wid[EMOO_NWAVE];  // input index of each wave
 };
 
 // LightBC host state per handle (src/grid/lightBC.cpp:10-142), computed on
@@ -108,14 +109,42 @@ LightState *light_of(emoo_handle *h) {
     return nullptr;
 }
 
-// GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30
-double gaussian_pulses(double t, double dt, const Pulses &P) {
-    double val = 0.0;
+// Sine-series envelope of a shaped wave: sum_k coef[k-1] sin(k pi a),
+// a = (t - t_start) / window, inside the window and 0 outside.
+double sine_envelope(const emoo_wave_shape &sh, double t) {
+    if (!(t >= sh.t_start && t <= sh.t_start + sh.window)) return 0.0;
+    const double a = (t - sh.t_start) / sh.window;
+    double e = 0.0;
+    for (int k = 1; k <= sh.ncoef; k++) e += sh.coef[k - 1] * sin(k * PI_D * a);
+    return e;
+}
+
+const emoo_wave_shape *shape_of(const emoo_handle *h, int w) { return h->wshaped[w] ? &h->wshape[w] : nullptr; }
+
+// GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30, over the waves of
+// one side and polarisation; a shaped wave takes its sine-series envelope in
+// place of the Gaussian. Terms of waves with a transverse spot are summed
+// into *spot, the others into the return value (so that without spots the
+// sum is the reference's, term by term).
+double light_sum(const emoo_handle *h, const Pulses &P, double t, double dt, double *spot) {
+    double val = 0.0, sv = 0.0;
     for (int i = 0; i < P.nw; i++) {
+        const emoo_wave_shape *sh = shape_of(h, P.wid[i]);
         double tmp = P.amp[i] * cos(P.omg[i] * (t + dt) + P.pha[i] * PI_D / 180.0);
-        val += tmp * exp(-pow((t - P.del[i]) * P.iw[i], 2));
+        const double env = (sh && sh->ncoef > 0) ? sine_envelope(*sh, t) : exp(-pow((t - P.del[i]) * P.iw[i], 2));
+        if (sh && sh->waist > 0) sv += tmp * env;
+        else val += tmp * env;
     }
+    *spot = sv;
     return val;
+}
+
+// Spot factor tables of side s, E component p (null when it has no spot).
+const double *spot_table(const emoo_handle *h, int s, int p, int a) {
+    return h->wspot[s][p] ? h->wprof + (size_t)((3 * s + p) * 2 + a) * h->wprof_stride : nullptr;
+}
+const float *spot_table_f(const emoo_handle *h, int s, int p, int a) {
+    return h->wspot[s][p] ? h->wproff + (size_t)((3 * s + p) * 2 + a) * h->wprof_stride : nullptr;
 }
 
 int edge_plane(const Geom &g, bool isB, int comp, int dim, bool right) {
@@ -144,21 +173,32 @@ int light_planes(emoo_handle *h, int s, PlaneSet *ps, bool slots) {
     int n = 0;
     for (int i = 0; i < 3; i++) {
         int eid = EPOL[dim][i], bid = BPOL[dim][i];
+        double es = 0.0, bs = 0.0;  // spot parts
         if (L && L->p[s][eid].nw > 0 && eid != dim) {
-            double ev = gaussian_pulses(h->t, 0.0, L->p[s][eid]);
+            double ev = light_sum(h, L->p[s][eid], h->t, 0.0, &es);
             E1[eid] += ev;
             int bsign = sign * (int)pow(-1, i + 1);
-            double bv = bsign * gaussian_pulses(h->t, bphase, L->p[s][eid]);
+            double bsp;
+            double bv = bsign * light_sum(h, L->p[s][eid], h->t, bphase, &bsp);
             B1[bid] += bv;
+            bs = bsign * bsp;
         }
+        // the B component paired with E component eid sits at the same
+        // transverse offsets, so both take side s / component eid's factors
+        const int sp = eid != dim ? eid : -1;
+        const double *t1 = sp >= 0 ? spot_table(h, s, sp, 0) : nullptr;
+        const double *t2 = sp >= 0 ? spot_table(h, s, sp, 1) : nullptr;
+        const float *t1f = sp >= 0 ? spot_table_f(h, s, sp, 0) : nullptr;
+        const float *t2f = sp >= 0 ? spot_table_f(h, s, sp, 1) : nullptr;
+        const int ie = edge_plane(h->g, false, eid, dim, right), ib = edge_plane(h->g, true, bid, dim, right);
         if (slots) {
-            ps[n++] = PlaneSet{h->slot[EMOO_EX + eid], dim, edge_plane(h->g, false, eid, dim, right), E1[eid]};
+            ps[n++] = PlaneSet{h->slot[EMOO_EX + eid], dim, ie, E1[eid], es, t1, t2, t1f, t2f};
             double *bp = h->bswap ? h->slot[EMOO_BX_TM1 + bid] : h->slot[EMOO_BX + bid];
-            ps[n++] = PlaneSet{bp, dim, edge_plane(h->g, true, bid, dim, right), B1[bid]};
+            ps[n++] = PlaneSet{bp, dim, ib, B1[bid], bs, t1, t2, t1f, t2f};
         } else {
             // mixed form: slot index in f, resolved by the mixed plane-set launcher
-            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_EX + eid), dim, edge_plane(h->g, false, eid, dim, right), E1[eid]};
-            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_BX + bid), dim, edge_plane(h->g, true, bid, dim, right), B1[bid]};
+            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_EX + eid), dim, ie, E1[eid], es, t1, t2, t1f, t2f};
+            ps[n++] = PlaneSet{(double *)(intptr_t)(EMOO_BX + bid), dim, ib, B1[bid], bs, t1, t2, t1f, t2f};
         }
     }
     return n;
@@ -181,21 +221,37 @@ LightState build_light(const emoo_input_info &info) {
             P.pha[P.nw] = info.phases[w];
             P.del[P.nw] = info.delays[w];
             P.iw[P.nw] = info.invWidths[w];
+            P.wid[P.nw] = w;
             P.nw++;
         }
     }
     return L;
 }
 
-// d/d(amplitude) and d/d(phase in degrees) of wave w's term
-// amp cos(omega (t + dt) + phase pi / 180) exp(-((t - delay) invW)^2).
-void pulse_derivs(const emoo_input_info &in, int w, double t, double dt, double scale, AdBcOp &op) {
+// d/d(amplitude), d/d(phase in degrees) and, for a sine-series envelope,
+// d/d(coef[k]) of wave w's term amp cos(omega (t + dt) + phase pi / 180)
+// env(t), times scale; appended to the op's spot list when the wave has a
+// spot, to its uniform list otherwise.
+void pulse_derivs(const emoo_handle *h, int w, double t, double dt, double scale, AdBcOp &op) {
+    const emoo_input_info &in = h->info;
+    const emoo_wave_shape *sh = shape_of(h, w);
+    const bool series = sh && sh->ncoef > 0;
     const double arg = in.omegas[w] * (t + dt) + in.phases[w] * PI_D / 180.0;
-    const double env = exp(-pow((t - in.delays[w]) * in.invWidths[w], 2));
-    op.kidx[op.nk] = 2 * w;
-    op.coef[op.nk++] = scale * cos(arg) * env;
-    op.kidx[op.nk] = 2 * w + 1;
-    op.coef[op.nk++] = -scale * in.peakamps[w] * sin(arg) * (PI_D / 180.0) * env;
+    const double env = series ? sine_envelope(*sh, t) : exp(-pow((t - in.delays[w]) * in.invWidths[w], 2));
+    const bool spot = sh && sh->waist > 0;
+    std::vector<int> &K = spot ? op.ks : op.ku;
+    std::vector<double> &C = spot ? op.cs : op.cu;
+    K.push_back(2 * w);
+    C.push_back(scale * cos(arg) * env);
+    K.push_back(2 * w + 1);
+    C.push_back(-scale * in.peakamps[w] * sin(arg) * (PI_D / 180.0) * env);
+    if (series && t >= sh->t_start && t <= sh->t_start + sh->window) {
+        const double a = (t - sh->t_start) / sh->window;
+        for (int k = 1; k <= sh->ncoef; k++) {
+            K.push_back(2 * in.nwaves + EMOO_NCOEF * w + k - 1);
+            C.push_back(scale * in.peakamps[w] * cos(arg) * sin(k * PI_D * a));
+        }
+    }
 }
 
 }  // namespace
@@ -246,13 +302,16 @@ int emoo::ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops) {
                 op.dim = ps[i].dim;
                 op.idx = ps[i].idx;
                 op.value = ps[i].v;
+                op.vs = ps[i].vs;
+                op.t1 = ps[i].t1;
+                op.t2 = ps[i].t2;
                 const int c = i / 2;
                 const int eid = EPOL[d][c];
                 if (eid != d) {
                     for (int w = 0; w < in.nwaves && w < EMOO_NWAVE; w++) {
                         if (in.inSide[w] != side || in.inPolE[w] - 1 != eid) continue;
-                        if (i % 2 == 0) pulse_derivs(in, w, h->t, 0.0, 1.0, op);
-                        else pulse_derivs(in, w, h->t, bphase, sign * (int)pow(-1, c + 1), op);
+                        if (i % 2 == 0) pulse_derivs(h, w, h->t, 0.0, 1.0, op);
+                        else pulse_derivs(h, w, h->t, bphase, sign * (int)pow(-1, c + 1), op);
                     }
                 }
                 ops.push_back(op);
@@ -412,8 +471,43 @@ int do_sort(emoo_handle *h) {
     }
     h->off[h->nspec] = off;
     h->np = off;
+    h->dead_pending = 0;
     dfree(h->fcache);
     return EMOO_OK;
+}
+
+// Drops the particles absorbing walls removed since the last sort, keeping
+// each species' order: a stable sort by (species, removed) keys.
+int compact(emoo_handle *h) {
+    if (!h->dead_pending || h->np == 0) {
+        h->dead_pending = 0;
+        return EMOO_OK;
+    }
+    if (h->precision == EMOO_FP64) EMOO_TRY(compact_keys_f64(h));
+    else EMOO_TRY(mixed_compact_keys(h));
+    int bits = 1;
+    while ((1 << bits) <= h->nspec) bits++;
+    EMOO_TRY(radix_sort_perm(h, h->np, bits));
+    EMOO_TRY(gather_payload(h, h->np));
+    int64_t cnt[EMOO_NSPEC];
+    EMOO_TRY(count_species(h, h->np, 1, cnt));
+    int64_t off = 0;
+    for (int s = 0; s < h->nspec; s++) {
+        h->off[s] = off;
+        h->count[s] = cnt[s];
+        off += cnt[s];
+    }
+    h->off[h->nspec] = off;
+    h->np = off;
+    h->dead_pending = 0;
+    dfree(h->fcache);
+    return EMOO_OK;
+}
+
+bool has_absorbing(const emoo_handle *h) {
+    for (int s = 0; s < 6; s++)
+        if (h->bc.pbc[s] == PBC_ABSORBING) return true;
+    return false;
 }
 
 int execute_bc(emoo_handle *h, int send_id);
@@ -607,6 +701,7 @@ int emoo_default_opts(emoo_opts *o) {
     o->deposit_rho = 1;
     o->history_every = 10;
     o->rho_background = 0.0;
+    o->rho_background_xmin = -HUGE_VAL;
     return EMOO_OK;
 }
 
@@ -633,7 +728,7 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
     if (opts) o = *opts;
     else emoo_default_opts(&o);
     if (o.precision != EMOO_FP64 && o.precision != EMOO_MIXED) return EMOO_ERR_ARG;
-    if (!std::isfinite(o.rho_background)) return EMOO_ERR_ARG;
+    if (!std::isfinite(o.rho_background) || std::isnan(o.rho_background_xmin)) return EMOO_ERR_ARG;
     if (info->nspecies < 0 || info->nspecies > EMOO_NSPEC) return EMOO_ERR_ARG;
     for (int d = 0; d < 3; d++)
         if (info->nCell[d] < 1 || !(info->Lxyz[d] > 0)) return EMOO_ERR_ARG;
@@ -669,6 +764,13 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
         h->bc.xmax[d] = h->bc.xmin[d] + info->Lxyz[d];
     }
     h->poisson = info->restart == 0 && strcmp(info->fields_init, "poisson") == 0;
+    // first physical x index (grid point x0 + (i - 1) dx) the background covers
+    h->rho_bg_first = h->g.n[0] + 1;
+    for (int i = 1; i <= h->g.n[0]; i++)
+        if (info->xyz0[0] + (i - 1) * h->g.d[0] >= o.rho_background_xmin) {
+            h->rho_bg_first = i;
+            break;
+        }
     h->nspec = info->nspecies;
     double mindx = std::min(std::min(h->g.d[0], h->g.d[1]), h->g.d[2]);
     h->dt = o.dt > 0 ? o.dt : (mindx / 1) / 100.0;  // src/main.cpp:213-214
@@ -722,6 +824,8 @@ int emoo_destroy(emoo_handle *h) {
     dfree(h->d_spec_count);
     dfree(h->ctr);
     dfree(h->red);
+    dfree(h->wprof);
+    dfree(h->wproff);
     if (h->jacobi_state) cudaFree(h->jacobi_state);
     for (int i = 0; i < 2; i++)
         if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
@@ -759,6 +863,7 @@ int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x,
                         const int64_t *ids) {
     HANDLE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
+    EMOO_TRY(compact(h));
     if (species < 0 || species >= h->nspec || n < 0) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
@@ -797,6 +902,7 @@ int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x,
 int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n) {
     HANDLE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
+    EMOO_TRY(compact(h));
     if (!g || g->species < 0 || g->species >= h->nspec || n < 0) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     int64_t first_id = h->np;
@@ -831,6 +937,7 @@ int emoo_num_particles(emoo_handle *h, int species, int64_t *n) {
     HANDLE_CHECK(h);
     if (!n) return EMOO_ERR_ARG;
     if (species >= h->nspec) return EMOO_ERR_ARG;
+    EMOO_TRY(compact(h));
     *n = species < 0 ? h->np : h->count[species];
     return EMOO_OK;
 }
@@ -839,6 +946,7 @@ int emoo_get_particles(emoo_handle *h, int species, int64_t cap, double *x, doub
                        double *vy, double *vz, double *gamma, int64_t *ids, int64_t *n) {
     HANDLE_CHECK(h);
     if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
+    EMOO_TRY(compact(h));
     int64_t cnt = h->count[species];
     *n = cnt;
     if (cap < cnt) return EMOO_ERR_ARG;
@@ -868,6 +976,7 @@ int emoo_get_particle_fields(emoo_handle *h, int species, int64_t cap, double *e
                              double *b2, double *b3, int64_t *n) {
     HANDLE_CHECK(h);
     if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
+    EMOO_TRY(compact(h));  // a compaction drops the cache: it no longer matches the store
     if (!h->fcache) return EMOO_ERR_STATE;
     int64_t cnt = h->count[species];
     *n = cnt;
@@ -966,6 +1075,7 @@ int emoo_sort(emoo_handle *h) {
 int emoo_interpolate(emoo_handle *h) {
     HANDLE_CHECK(h);
     if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    EMOO_TRY(compact(h));
     EMOO_TRY(interpolate_f64(h));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return read_err(h);
@@ -987,8 +1097,7 @@ int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
     EMOO_TRY(reset_counters(h));
     EMOO_TRY(particle_bc_f64(h));
     int rc = read_counters(h, counts6, false);
-    bool absorbing = false;
-    for (int s = 0; s < 6; s++) absorbing |= h->bc.pbc[s] == PBC_ABSORBING;
+    const bool absorbing = has_absorbing(h);
     // clearGhosts: removed particles leave the store (compaction by the sort)
     if (rc == EMOO_OK && absorbing) rc = do_sort(h);
     return rc;
@@ -1034,6 +1143,118 @@ int emoo_set_waves(emoo_handle *h, int nwaves, const double *amp, const double *
     return EMOO_OK;
 }
 
+namespace {
+// Side index (0..5: x-left, x-right, y-left, ...) of an input wave side
+// (-1 x left, +1 x right, -2 y left, ...), or -1.
+int side_index(int side) {
+    if (side == 0 || side < -3 || side > 3) return -1;
+    return 2 * (std::abs(side) - 1) + (side > 0 ? 1 : 0);
+}
+
+// Recomputes the spot factor tables from the handle's wave shapes; returns
+// EMOO_ERR_ARG when two spotted waves of one side and polarisation differ in
+// waist or centre.
+int build_spots(emoo_handle *h) {
+    const emoo_input_info &in = h->info;
+    int spot_w[6][3];
+    for (auto &r : spot_w)
+        for (int &v : r) v = -1;
+    for (int w = 0; w < in.nwaves && w < EMOO_NWAVE; w++) {
+        const emoo_wave_shape *sh = shape_of(h, w);
+        if (!sh || !(sh->waist > 0)) continue;
+        const int s = side_index(in.inSide[w]), p = in.inPolE[w] - 1;
+        if (s < 0 || p < 0 || p > 2) continue;
+        const int o = spot_w[s][p];
+        if (o >= 0) {
+            const emoo_wave_shape &a = h->wshape[o];
+            if (a.waist != sh->waist || a.center[0] != sh->center[0] || a.center[1] != sh->center[1])
+                return EMOO_ERR_ARG;
+        } else {
+            spot_w[s][p] = w;
+        }
+    }
+    const Geom &g = h->g;
+    const int stride = std::max(std::max(g.tot[0], g.tot[1]), g.tot[2]);
+    std::vector<double> tab((size_t)36 * stride, 0.0);
+    std::vector<float> tabf((size_t)36 * stride, 0.0f);
+    bool any = false;
+    for (int s = 0; s < 6; s++) {
+        const int d = s / 2, o[2] = {(d == 0) ? 1 : 0, (d == 2) ? 1 : 2};
+        for (int p = 0; p < 3; p++) {
+            const int w = spot_w[s][p];
+            if (w < 0) continue;
+            any = true;
+            const emoo_wave_shape &sh = h->wshape[w];
+            for (int a = 0; a < 2; a++) {
+                const int ax = o[a];
+                const double hh = ax == p ? 0.5 : 0.0;
+                const double x0 = in.xyz0[ax], dd = g.d[ax];
+                const size_t base = (size_t)((3 * s + p) * 2 + a) * stride;
+                for (int j = 0; j < g.tot[ax]; j++) {
+                    const double pos = x0 + (j - 1 + hh) * dd;
+                    const double r = (pos - sh.center[a]) / sh.waist;
+                    tab[base + j] = exp(-(r * r));
+                    tabf[base + j] = (float)tab[base + j];
+                }
+            }
+        }
+    }
+    if (any && !h->wprof) {
+        EMOO_TRY(dalloc(h->wprof, tab.size()));
+        EMOO_TRY(dalloc(h->wproff, tabf.size()));
+    }
+    if (any) {
+        EMOO_CUDA(cudaMemcpyAsync(h->wprof, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaMemcpyAsync(h->wproff, tabf.data(), sizeof(float) * tabf.size(), cudaMemcpyHostToDevice,
+                                  h->stream));
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    h->wprof_stride = stride;
+    for (int s = 0; s < 6; s++)
+        for (int p = 0; p < 3; p++) h->wspot[s][p] = spot_w[s][p] >= 0;
+    return EMOO_OK;
+}
+}  // namespace
+
+int emoo_set_wave_shape(emoo_handle *h, int wave, const emoo_wave_shape *shape) {
+    HANDLE_CHECK(h);
+    if (wave < 0 || wave >= h->info.nwaves || wave >= EMOO_NWAVE) return EMOO_ERR_ARG;
+    if (shape) {
+        const emoo_wave_shape &sh = *shape;
+        if (!std::isfinite(sh.waist) || sh.waist < 0 || !std::isfinite(sh.center[0]) || !std::isfinite(sh.center[1]))
+            return EMOO_ERR_ARG;
+        if (sh.ncoef < 0 || sh.ncoef > EMOO_NCOEF) return EMOO_ERR_ARG;
+        if (sh.ncoef > 0 && !(std::isfinite(sh.t_start) && std::isfinite(sh.window) && sh.window > 0))
+            return EMOO_ERR_ARG;
+        for (int k = 0; k < sh.ncoef; k++)
+            if (!std::isfinite(sh.coef[k])) return EMOO_ERR_ARG;
+    }
+    const emoo_wave_shape old = h->wshape[wave];
+    const int old_on = h->wshaped[wave];
+    if (shape) {
+        h->wshape[wave] = *shape;
+        for (int k = shape->ncoef; k < EMOO_NCOEF; k++) h->wshape[wave].coef[k] = 0.0;
+        h->wshaped[wave] = 1;
+    } else {
+        h->wshape[wave] = emoo_wave_shape{};
+        h->wshaped[wave] = 0;
+    }
+    const int rc = build_spots(h);
+    if (rc != EMOO_OK) {
+        h->wshape[wave] = old;
+        h->wshaped[wave] = old_on;
+        build_spots(h);
+    }
+    return rc;
+}
+
+int emoo_ad_nparams(const emoo_handle *h) {
+    if (!h) return EMOO_ERR_ARG;
+    bool series = false;
+    for (int w = 0; w < h->info.nwaves && w < EMOO_NWAVE; w++) series |= h->wshaped[w] && h->wshape[w].ncoef > 0;
+    return 2 * h->info.nwaves + (series ? EMOO_NCOEF * h->info.nwaves : 0);
+}
+
 int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
     HANDLE_CHECK(h);
     if (nsteps < 0) return EMOO_ERR_ARG;
@@ -1066,7 +1287,13 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
         h->step_index++;
         if (lazy_rho) h->rho_stale = 1;
     }
-    return read_counters(h, counts6, false);
+    int64_t c6[6];
+    const int rc = read_counters(h, c6, false);
+    for (int s = 0; s < 6; s++)
+        if (h->bc.pbc[s] == PBC_ABSORBING && c6[s] > 0) h->dead_pending = 1;
+    if (counts6)
+        for (int s = 0; s < 6; s++) counts6[s] = c6[s];
+    return rc;
 }
 
 int emoo_history(emoo_handle *h, double out8[8]) {
@@ -1110,6 +1337,7 @@ int emoo_set_particles(emoo_handle *h, int species, int64_t n, const double *x, 
                        const double *vx, const double *vy, const double *vz, const double *gamma) {
     HANDLE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
+    EMOO_TRY(compact(h));
     if (species < 0 || species >= h->nspec || n != h->count[species]) return EMOO_ERR_ARG;
     if (n == 0) return EMOO_OK;
     if (!x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;

@@ -68,26 +68,33 @@ struct DevCounters {
     unsigned long long pad;
 };
 
-// One LightBC plane write (src/grid/lightBC.cpp:196-197).
+// One LightBC plane write (src/grid/lightBC.cpp:196-197). With a transverse
+// profile (shaped waves with a spot) the value at transverse point (p, q) of
+// the plane is v + vs t1[p] t2[q]; t1 / t2 (t1f / t2f for the FP32 grid) are
+// the spot's per-axis factors, null for the reference's uniform plane.
 struct PlaneSet {
-    double *f;
-    int dim, idx;
-    double v;
+    double *f = nullptr;
+    int dim = 0, idx = 0;
+    double v = 0.0;
+    double vs = 0.0;
+    const double *t1 = nullptr, *t2 = nullptr;
+    const float *t1f = nullptr, *t2f = nullptr;
 };
 
 // One operation of executeBC(-1) on the FP64 slots, for the differentiated
 // step: a periodic ghost copy of the E / B slots over the dims in `mask`, or
-// a whole-plane set of slot `slot` to `value`, with the value's derivatives
-// with respect to the wave parameters (parameter 2 w: amplitude of wave w,
-// 2 w + 1: its phase in degrees).
+// a plane set of slot `slot` to value + vs t1[p] t2[q], with the derivatives
+// of value (ku, cu) and of vs (ks, cs) with respect to the wave parameters
+// (parameter 2 w: amplitude of wave w, 2 w + 1: its phase in degrees,
+// 2 nwaves + EMOO_NCOEF w + k: its envelope coefficient k).
 struct AdBcOp {
     int kind;  // 0 ghost copy, 1 plane set
     int mask;
     int slot, dim, idx;
-    double value;
-    int nk;
-    int kidx[2 * EMOO_NWAVE];
-    double coef[2 * EMOO_NWAVE];
+    double value, vs;
+    const double *t1, *t2;
+    std::vector<int> ku, ks;
+    std::vector<double> cu, cs;
 };
 
 struct FieldsF32;  // mixed-form grid storage (particles_mixed.cu)
@@ -151,10 +158,25 @@ struct emoo_handle {
     int64_t next_hist = 0;
     std::vector<double> hist_rows;
     int fields_initialised = 0;
+    // shaped injected waves (emoo_set_wave_shape) and the transverse spot
+    // factors of each external side and polarisation: for side s and E
+    // component p, wprof + ((3 s + p) 2 + a) wprof_stride holds the factor
+    // along the plane's first (a = 0) or second (a = 1) transverse axis
+    emoo_wave_shape wshape[EMOO_NWAVE] = {};
+    int wshaped[EMOO_NWAVE] = {};
+    int wspot[6][3] = {};
+    double *wprof = nullptr;
+    float *wproff = nullptr;
+    int wprof_stride = 0;
     // The loop never reads rho, so emoo_step deposits J only and leaves rho
     // pending: it is deposited (with fold and background) at the particles'
     // positions when something reads it or before the particles change.
     int rho_stale = 0;
+    int rho_bg_first = 1;  // first physical x index the immobile background covers
+    // Absorbing walls mark removed particles (FP64: x = NaN, mixed: cell < 0)
+    // and the loop skips them; they leave the store at the next sort, or at
+    // the next call that reads or changes the particle store (compaction).
+    int dead_pending = 0;
 
     // instrumentation: kernel launches issued, and CUDA-event timing of the
     // fused particle kernel (the dominant kernel of the step) when enabled
@@ -197,6 +219,7 @@ int fused_step_f64(emoo_handle *h, double dtp, int with_rho);
 int deposit_rho_f64(emoo_handle *h);  // rho alone at the current positions, plus the background
 int particle_moments_f64(emoo_handle *h, double out4[4]);
 int sort_keys_f64(emoo_handle *h);
+int compact_keys_f64(emoo_handle *h);  // species index, nspec for removed particles
 
 // ---- sort (sort.cu) ----
 int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits);
@@ -216,6 +239,7 @@ int mixed_to_f64(emoo_handle *h, int64_t first, int64_t n, double *x, double *y,
 int mixed_step(emoo_handle *h, double dtp, int with_rho, int fold_what);
 int mixed_materialize_rho(emoo_handle *h);
 int mixed_sort_keys(emoo_handle *h);
+int mixed_compact_keys(emoo_handle *h);
 int mixed_get_field(emoo_handle *h, int id, double *out_dev);
 int mixed_set_field(emoo_handle *h, int id, const double *in_dev);
 int mixed_moments(emoo_handle *h, double out4[4]);

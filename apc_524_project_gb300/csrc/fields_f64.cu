@@ -155,7 +155,9 @@ __global__ void k_plane_set(Geom g, PlaneList pl, const int *skip) {
     ii[d] = ps.idx;
     ii[o1] = p;
     ii[o2] = q;
-    ps.f[gidx(g, ii[0], ii[1], ii[2])] = ps.v;
+    double v = ps.v;
+    if (ps.t1) v = __dadd_rn(v, __dmul_rn(__dmul_rn(ps.vs, ps.t1[p]), ps.t2[q]));  // v + (vs t1) t2
+    ps.f[gidx(g, ii[0], ii[1], ii[2])] = v;
 }
 
 __global__ void k_fill(double *p, int64_t n, double v) {
@@ -455,23 +457,23 @@ static int plane_launch(emoo_handle *h, const PlaneSet *ps, int n, const int *sk
 
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n) { return plane_launch(h, ps, n, nullptr); }
 
-// rho += background at every physical point (immobile neutralising ions of
-// the C3 / C5 workloads; no reference counterpart).
-__global__ void k_add_phys(Geom g, double *f, double v) {
+// rho += background at the physical points with x index >= i0 (immobile
+// neutralising ions; no reference counterpart).
+__global__ void k_add_phys(Geom g, double *f, double v, int i0) {
     int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    int i = blockIdx.z + 1;
+    int i = blockIdx.z + i0;
     if (k > g.n[2] || j > g.n[1]) return;
     f[(int64_t)i * g.sx + (int64_t)j * g.sy + k] += v;
 }
 
 int rho_background_f64(emoo_handle *h, int with_rho) {
-    if (!with_rho || h->opts.rho_background == 0.0) return EMOO_OK;
+    if (!with_rho || h->opts.rho_background == 0.0 || h->rho_bg_first > h->g.n[0]) return EMOO_OK;
     const Geom &g = h->g;
     dim3 blk(32, 8);
-    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0] - h->rho_bg_first + 1);
     h->launches++;
-    k_add_phys<<<grd, blk, 0, h->stream>>>(g, h->slot[EMOO_RHO], h->opts.rho_background);
+    k_add_phys<<<grd, blk, 0, h->stream>>>(g, h->slot[EMOO_RHO], h->opts.rho_background, h->rho_bg_first);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
@@ -503,7 +505,7 @@ static int single_field_bc(emoo_handle *h, int id, const int *skip) {
             mask_run = 0;
         }
         if (!h->poisson || id <= 0) continue;
-        PlaneSet ps[2];
+        PlaneSet ps[2] = {};
         int np = 0;
         for (int r = 0; r < 2; r++) {
             int s = 2 * d + r;

@@ -604,6 +604,23 @@ int particle_moments_f64(emoo_handle *h, double out4[4]) {
     return EMOO_OK;
 }
 
+// Compaction keys: the species index, nspec for removed particles (a stable
+// sort by them drops the removed particles and keeps every species' order).
+__global__ void k_compact_keys(SpeciesTab st, const double *x, int64_t np, uint32_t *key) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    key[p] = alive(x[p]) ? (uint32_t)species_of(st, p) : (uint32_t)st.nspec;
+}
+
+int compact_keys_f64(emoo_handle *h) {
+    SpeciesTab st;
+    species_tab(h, h->dtp, st);
+    h->launches++;
+    k_compact_keys<<<blocks_for(h->np), 256, 0, h->stream>>>(st, h->x, h->np, h->key[0]);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 int sort_keys_f64(emoo_handle *h) {
     SpeciesTab st;
     species_tab(h, h->dtp, st);

@@ -840,7 +840,8 @@ __global__ void k_fold_m(MGeom g, int d, long long *f0, long long *f1, long long
 struct MPlane {
     float *f;
     int dim, idx;
-    float v;
+    float v, vs;
+    const float *t1, *t2;  // transverse spot factors, or null (PlaneSet)
 };
 struct MPlaneList {
     MPlane s[12];
@@ -861,7 +862,9 @@ __global__ void k_plane_m(MGeom g, MPlaneList pl, int tot0, int tot1, int tot2) 
     ii[d] = ps.idx;
     ii[o1] = p;
     ii[o2] = q;
-    ps.f[(int64_t)ii[0] * g.sx + (int64_t)ii[1] * g.sy + ii[2]] = ps.v;
+    float v = ps.v;
+    if (ps.t1) v += ps.vs * ps.t1[p] * ps.t2[q];
+    ps.f[(int64_t)ii[0] * g.sx + (int64_t)ii[1] * g.sy + ii[2]] = v;
 }
 
 // ---- reductions (FP64 accumulation) -------------------------------------
@@ -961,6 +964,13 @@ __global__ void k_keys_m(MSpecies st, MState S, int64_t np, int64_t npts, uint32
     if (p >= np) return;
     int32_t c = S.cell[p];
     key[p] = c < 0 ? dead : (uint32_t)((int64_t)species_of_m(st, p) * npts + c);
+}
+
+// Compaction keys: species index, nspec for removed particles (cell < 0).
+__global__ void k_compact_keys_m(MSpecies st, const int32_t *cell, int64_t np, int nspec, uint32_t *key) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    key[p] = cell[p] < 0 ? (uint32_t)nspec : (uint32_t)species_of_m(st, p);
 }
 
 // ---- host helpers ----------------------------------------------------------
@@ -1164,7 +1174,7 @@ int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n) {
     for (int i = 0; i < n; i++) {
         int id = (int)(intptr_t)ps[i].f;
         float *f = id < EMOO_BX ? h->mf->E[id] : mb_role(h, id - EMOO_BX);
-        pl.s[i] = MPlane{f, ps[i].dim, ps[i].idx, (float)ps[i].v};
+        pl.s[i] = MPlane{f, ps[i].dim, ps[i].idx, (float)ps[i].v, (float)ps[i].vs, ps[i].t1f, ps[i].t2f};
     }
     const Geom &g = h->g;
     int m = std::max(std::max(g.tot[0], g.tot[1]), g.tot[2]);
@@ -1220,12 +1230,12 @@ static int mixed_cells_to_points(emoo_handle *h, int mode) {
     return EMOO_OK;
 }
 
-// rho += background (fixed point) at every physical point: immobile
-// neutralising ions (C3 / C5 workloads), no reference counterpart.
-__global__ void k_add_phys_i64(MGeom g, long long *f, long long v) {
+// rho += background (fixed point) at the physical points with x index >= i0:
+// immobile neutralising ions, no reference counterpart.
+__global__ void k_add_phys_i64(MGeom g, long long *f, long long v, int i0) {
     int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    int i = blockIdx.z + 1;
+    int i = blockIdx.z + i0;
     if (k > g.n[2] || j > g.n[1]) return;
     f[(int64_t)i * g.sx + (int64_t)j * g.sy + k] += v;
 }
@@ -1233,13 +1243,14 @@ __global__ void k_add_phys_i64(MGeom g, long long *f, long long v) {
 // J and rho at the points from the per-cell records, plus the background.
 static int mixed_finish_deposit(emoo_handle *h, int mode) {
     EMOO_TRY(mixed_cells_to_points(h, mode));
-    if (mode == DEP_J || h->opts.rho_background == 0.0) return EMOO_OK;
+    if (mode == DEP_J || h->opts.rho_background == 0.0 || h->rho_bg_first > h->g.n[0]) return EMOO_OK;
     const Geom &g = h->g;
     dim3 blk(32, 8);
-    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    dim3 grd((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0] - h->rho_bg_first + 1);
     h->launches++;
     k_add_phys_i64<<<grd, blk, 0, h->stream>>>(mgeom(h, h->dtp), h->mf->J[3],
-                                               (long long)llrint(h->opts.rho_background / h->mf->q0));
+                                               (long long)llrint(h->opts.rho_background / h->mf->q0),
+                                               h->rho_bg_first);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
@@ -1351,6 +1362,14 @@ int mixed_sort_keys(emoo_handle *h) {
     uint32_t dead = (uint32_t)((int64_t)h->nspec * h->g.npts + 1);
     h->launches++;
     k_keys_m<<<(unsigned)((h->np + 255) / 256), 256, 0, h->stream>>>(st, mstate(h), h->np, h->g.npts, h->key[0], dead);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int mixed_compact_keys(emoo_handle *h) {
+    MSpecies st = mspecies(h, h->dtp);
+    h->launches++;
+    k_compact_keys_m<<<(unsigned)((h->np + 255) / 256), 256, 0, h->stream>>>(st, h->cell, h->np, h->nspec, h->key[0]);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }

@@ -2,15 +2,19 @@
 
 A Problem holds a workload and its initial particles. Every evaluation
 builds a fresh FP64 handle, loads the particles with the velocity
-perturbation dv added (gamma kept), sets the wave amplitudes and phases,
-starts the fields and runs emoo_ad_run:
+perturbation dv added (gamma kept), sets the wave amplitudes and phases and
+the wave shapes (with the envelope coefficients from theta), starts the
+fields and runs emoo_ad_run:
 
   * objective(theta, dv)            the objective alone (the primal loop)
   * tangent(theta, dv, dtheta, ddv) the objective's derivative along a direction
   * gradient(theta, dv)             the objective and its adjoint gradient
 
-theta = (amp_0, phase_0 [degrees], amp_1, phase_1, ...); dv has shape
-(3, N) in the particles' load order. PicObjective wraps gradient() as a
+theta = (amp_0, phase_0 [degrees], amp_1, phase_1, ...), followed, when a
+wave has a sine-series envelope, by 16 envelope coefficients per wave;
+dv has shape (3, N) in the particles' load order. The objective is the
+field energy of the x slab `slab` (cells), or with objective="kinetic" the
+kinetic energy of the particles of `species` (-1: all) in that x range. PicObjective wraps gradient() as a
 torch.autograd.Function for optimisation loops; the C++ driver reaches the
 same kernels through include/emoo.h."""
 import ctypes as C
@@ -21,15 +25,27 @@ from . import abi, configs, loading
 
 
 class Problem:
-    def __init__(self, cfg, nsteps=None, slab=(48, 56), checkpoint_every=16, parts=None):
+    def __init__(self, cfg, nsteps=None, slab=(48, 56), checkpoint_every=16, parts=None, objective="field",
+                 species=-1):
         self.cfg = cfg
         self.info0 = configs.input_info(cfg)
         self.nsteps = cfg.steps if nsteps is None else nsteps
         self.slab = slab
         self.every = checkpoint_every
+        self.kind = {"field": abi.AD_OBJ_FIELD, "kinetic": abi.AD_OBJ_KINETIC}[objective]
+        self.species = species
         self.parts = parts if parts is not None else loading.sample_all(cfg)
         self.np = sum(len(p["x"]) for p in self.parts)
-        self.theta0 = np.array([v for w in cfg.waves for v in (w.amp, w.phase_deg)], dtype=np.float64)
+        nw = len(cfg.waves)
+        self.series = any(w.shape is not None and len(w.shape.coef) > 0 for w in cfg.waves)
+        th = [v for w in cfg.waves for v in (w.amp, w.phase_deg)]
+        if self.series:
+            for w in cfg.waves:
+                c = list(w.shape.coef) if w.shape is not None else []
+                th += c + [0.0] * (abi.NCOEF - len(c))
+        self.theta0 = np.array(th, dtype=np.float64)
+        self.ntheta = len(th)
+        self.nwaves = nw
 
     # ---- one run on a fresh handle
     def _run(self, mode, theta, dv, dtheta=None, ddv=None, want_grad=False):
@@ -40,6 +56,10 @@ class Problem:
         o.precision = abi.FP64
         o.dt = self.cfg.dt
         o.capacity = self.np
+        o.rho_background = configs.rho_background(self.cfg)
+        xmin = configs.rho_background_xmin(self.cfg)
+        if xmin is not None:
+            o.rho_background_xmin = xmin
         h = C.c_void_p()
         abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
         try:
@@ -58,13 +78,23 @@ class Problem:
             nw = len(self.cfg.waves)
             if nw:
                 th = np.asarray(theta, dtype=np.float64)
-                amp = np.ascontiguousarray(th[0::2])
-                pha = np.ascontiguousarray(th[1::2])
+                amp = np.ascontiguousarray(th[0:2 * nw:2])
+                pha = np.ascontiguousarray(th[1:2 * nw:2])
                 abi.check(L.emoo_set_waves(h, nw, amp.ctypes.data_as(C.POINTER(C.c_double)),
                                            pha.ctypes.data_as(C.POINTER(C.c_double))), "emoo_set_waves")
+                for w, wv in enumerate(self.cfg.waves):
+                    if wv.shape is None:
+                        continue
+                    coef = None
+                    if self.series and len(wv.shape.coef):
+                        base = 2 * nw + abi.NCOEF * w
+                        coef = th[base:base + len(wv.shape.coef)]
+                    shape = configs.wave_shape(self.cfg, w, coef)
+                    abi.check(L.emoo_set_wave_shape(h, w, C.byref(shape)), "emoo_set_wave_shape")
+            assert L.emoo_ad_nparams(h) == self.ntheta
             it = (C.c_int * 4)()
             abi.check(L.emoo_init_fields(h, it), "emoo_init_fields")
-            spec = abi.AdSpec(self.nsteps, self.every, self.slab[0], self.slab[1])
+            spec = abi.AdSpec(self.nsteps, self.every, self.slab[0], self.slab[1], self.kind, self.species)
             res = abi.AdResult()
             dp = C.POINTER(C.c_double)
             dth = ddvp = None
@@ -74,7 +104,7 @@ class Problem:
             if ddv is not None:
                 ddv_arr = np.ascontiguousarray(ddv, dtype=np.float64).reshape(3, self.np)
                 ddvp = ddv_arr.ctypes.data_as(dp)
-            gth = np.zeros(max(1, 2 * nw))
+            gth = np.zeros(max(1, self.ntheta))
             gv = np.zeros((3, self.np))
             abi.check(L.emoo_ad_run(h, C.byref(spec), mode, dth, ddvp, C.byref(res),
                                     gth.ctypes.data_as(dp) if want_grad else None,
@@ -82,7 +112,7 @@ class Problem:
             out = {"objective": res.objective, "tangent": res.tangent, "forward_ms": res.forward_ms,
                    "recompute_ms": res.recompute_ms, "reverse_ms": res.reverse_ms}
             if want_grad:
-                out["grad_theta"] = gth[:2 * nw]
+                out["grad_theta"] = gth[:self.ntheta]
                 out["grad_v"] = gv
             return out
         finally:

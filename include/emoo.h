@@ -138,6 +138,8 @@ typedef struct emoo_opts {
     int deposit_rho;       /* 1 = deposit rho every step as the reference does (src/main.cpp:245) */
     int history_every;     /* history cadence in steps; the reference hard-codes 10 (src/IO/output.cpp:46) */
     double rho_background; /* uniform immobile background charge density added to rho, reference units */
+    double rho_background_xmin; /* the background covers the physical points with x >= this
+                                   (emoo_default_opts: -HUGE_VAL, every point) */
 } emoo_opts;
 
 /* Seeded sampler of one species (no reference counterpart: replaces the
@@ -357,18 +359,35 @@ int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, int key_bits,
  * phase_0, amp_1, phase_1, ...); the objective is the field energy
  * 0.5 V sum(E^2 + B^2) over the grid points of the cells with x index in
  * [slab_lo, slab_hi) after the run's last step (B: the current B role).
+ * When a wave has a sine-series envelope (emoo_set_wave_shape), theta goes
+ * on with the envelope coefficients, EMOO_NCOEF per wave: theta[2 nwaves +
+ * EMOO_NCOEF w + k] = coef[k] of wave w (emoo_ad_nparams gives the length).
+ * The objective is either the field energy above, or (EMOO_AD_OBJ_KINETIC)
+ * the kinetic energy sum m (gamma - 1) (relativistic; 0.5 m v^2 otherwise,
+ * m the species' mass_ratio) of the particles of one species (or all) whose
+ * x lies in [xyz0 + slab_lo dx, xyz0 + slab_hi dx) after the last step.
  * The cell a particle is in and whether a boundary fires are held fixed (the
- * step is differentiated between such events). FP64 handles only, not the
+ * step is differentiated between such events), and so is whether a particle
+ * is inside the kinetic objective's range. FP64 handles only, not the
  * electrostatic update. */
 #define EMOO_AD_FORWARD 0 /* objective only */
 #define EMOO_AD_TANGENT 1 /* objective and its derivative along (dtheta, dv) */
 #define EMOO_AD_ADJOINT 2 /* objective and its gradient */
 
+#define EMOO_AD_OBJ_FIELD 0   /* field energy over the slab's grid points */
+#define EMOO_AD_OBJ_KINETIC 1 /* kinetic energy of the particles in the slab */
+
 typedef struct emoo_ad_spec {
     int nsteps;           /* steps of the run, from the handle's current state */
     int checkpoint_every; /* adjoint: state kept every this many steps, segments recomputed (>= 1) */
     int slab_lo, slab_hi; /* objective slab, cell x indices [slab_lo, slab_hi) */
+    int objective;        /* EMOO_AD_OBJ_FIELD or EMOO_AD_OBJ_KINETIC */
+    int species;          /* EMOO_AD_OBJ_KINETIC: the species counted, -1 for all */
 } emoo_ad_spec;
+
+/* Length of theta for emoo_ad_run: 2 nwaves, plus EMOO_NCOEF nwaves when a
+ * wave has a sine-series envelope. */
+int emoo_ad_nparams(const emoo_handle *h);
 
 typedef struct emoo_ad_result {
     double objective;
@@ -383,11 +402,45 @@ typedef struct emoo_ad_result {
  * the next boundary update. */
 int emoo_set_waves(emoo_handle *h, int nwaves, const double *amp, const double *phase_deg);
 
+/* ---- shaped injected waves ------------------------------------------------
+ * No reference counterpart: LightBC (src/grid/lightBC.cpp:165-200) writes one
+ * value over a whole plane, with the Gaussian envelope of
+ * src/utils/evaluateGaussianPulse.cpp:7-30. A shape gives injected wave
+ * `wave` (input order) a transverse Gaussian spot, an envelope made of a
+ * sine series, or both; its term of the LightBC sum becomes
+ *
+ *   amp cos(omega (t + dt) + phase pi / 180) env(t) S(a, b)
+ *   env(t)  = sum_{k=1..ncoef} coef[k-1] sin(k pi (t - t_start) / window)
+ *             for t_start <= t <= t_start + window, 0 elsewhere
+ *             (ncoef = 0: the reference's exp(-((t - delay) invWidth)^2))
+ *   S(a, b) = exp(-((a - center[0]) / waist)^2) exp(-((b - center[1]) / waist)^2)
+ *             (waist = 0: S = 1, the reference's plane wave)
+ *
+ * a and b are the positions of a point of the written plane along the two
+ * axes other than the side's, in axis order: xyz0 + (j - 1 + h) d for grid
+ * index j, with h = 1/2 along the wave's E polarisation and 0 across it
+ * (where that E component, and the B component LightBC pairs with it, sit).
+ * The envelope is evaluated at t, the carrier at t + dt, as the reference's
+ * Gaussian. Waves of one side and polarisation whose shapes have spots must
+ * share the waist and centre. shape NULL restores the plain wave. */
+#define EMOO_NCOEF 16
+
+typedef struct emoo_wave_shape {
+    double waist;          /* transverse 1/e field radius (length units); 0: plane wave */
+    double center[2];      /* spot centre on the two transverse axes, in axis order */
+    double t_start, window;  /* envelope window [t_start, t_start + window] (time units) */
+    int ncoef;             /* sine-series coefficients used, 0..EMOO_NCOEF */
+    double coef[EMOO_NCOEF];
+} emoo_wave_shape;
+
+int emoo_set_wave_shape(emoo_handle *h, int wave, const emoo_wave_shape *shape);
+
 /* Runs spec->nsteps steps from the handle's current state and leaves it at
- * the final state. dtheta (2 nwaves) and dv (3 np host doubles: vx of every
- * particle, then vy, then vz, in storage order) give the tangent direction
- * (either may be NULL: zero); grad_theta (2 nwaves) and grad_v (3 np, same
- * layout) receive the adjoint gradient (either may be NULL). */
+ * the final state. dtheta (emoo_ad_nparams) and dv (3 np host doubles: vx of
+ * every particle, then vy, then vz, in storage order) give the tangent
+ * direction (either may be NULL: zero); grad_theta (emoo_ad_nparams) and
+ * grad_v (3 np, same layout) receive the adjoint gradient (either may be
+ * NULL). */
 int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
                 emoo_ad_result *out, double *grad_theta, double *grad_v);
 

@@ -60,6 +60,7 @@ enum { BC_PERIODIC = 0, BC_REFLECTING = 1, BC_ABSORBING = 2, BC_EXTERNAL = 3 };
 typedef struct {
     int nw;
     double amp[EMOO_NWAVE], omg[EMOO_NWAVE], pha[EMOO_NWAVE], del[EMOO_NWAVE], iw[EMOO_NWAVE];
+    int wid[EMOO_NWAVE]; /* input index of each wave */
 } pulses_t;
 
 typedef struct {
@@ -85,6 +86,13 @@ typedef struct {
     double t, dtp; /* the reference's globals time_phys and dt_phys */
     long next_hist;
     double rho_bg; /* immobile uniform background charge density (no reference counterpart) */
+    int rho_bg_i0; /* first physical x index it covers */
+    /* shaped injected waves (no reference counterpart): shape per wave, and
+     * per side and E component the spot's factors along the plane's two
+     * transverse axes (NULL: no spot) */
+    emoo_wave_shape wshape[EMOO_NWAVE];
+    int wshaped[EMOO_NWAVE];
+    double *spot[6][3][2];
 } orc_t;
 
 /* ------------------------------------------------------------------ */
@@ -168,6 +176,7 @@ static void setup_pulses(orc_t *c) {
             P->pha[P->nw] = in->phases[w];
             P->del[P->nw] = in->delays[w];
             P->iw[P->nw] = in->invWidths[w];
+            P->wid[P->nw] = w;
             P->nw++;
         }
     }
@@ -231,6 +240,8 @@ void orc_destroy(void *h) {
     free(c->x); free(c->y); free(c->z); free(c->vx); free(c->vy); free(c->vz); free(c->g);
     free(c->fe1); free(c->fe2); free(c->fe3); free(c->fb1); free(c->fb2); free(c->fb3);
     free(c->type); free(c->pid); free(c->ghost);
+    for (int s = 0; s < 6; s++)
+        for (int p = 0; p < 3; p++) { free(c->spot[s][p][0]); free(c->spot[s][p][1]); }
     free(c);
 }
 
@@ -348,14 +359,98 @@ static void plane_set(orc_t *c, double *f, int dim, int idx, double v) {
         }
 }
 
-/* GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30 */
-static double gaussian_pulses(double t, double dt, const pulses_t *P) {
-    double val = 0.0;
+/* Sine-series envelope of a shaped wave (no reference counterpart):
+ * sum_k coef[k-1] sin(k pi a), a = (t - t_start) / window, inside the window,
+ * 0 outside. */
+static double sine_envelope(const emoo_wave_shape *sh, double t) {
+    if (!(t >= sh->t_start && t <= sh->t_start + sh->window)) return 0.0;
+    double a = (t - sh->t_start) / sh->window;
+    double e = 0.0;
+    for (int k = 1; k <= sh->ncoef; k++) e += sh->coef[k - 1] * sin(k * PI_D * a);
+    return e;
+}
+
+/* GaussianPulses, src/utils/evaluateGaussianPulse.cpp:7-30. A shaped wave
+ * takes its sine-series envelope in place of the Gaussian; terms of waves
+ * with a transverse spot go to *spot, the rest to the return value. */
+static double gaussian_pulses(const orc_t *c, double t, double dt, const pulses_t *P, double *spot) {
+    double val = 0.0, sv = 0.0;
     for (int i = 0; i < P->nw; i++) {
+        const emoo_wave_shape *sh = c->wshaped[P->wid[i]] ? &c->wshape[P->wid[i]] : NULL;
         double tmp = P->amp[i] * cos(P->omg[i] * (t + dt) + P->pha[i] * PI_D / 180.0);
-        val += tmp * exp(-pow((t - P->del[i]) * P->iw[i], 2));
+        double env = (sh && sh->ncoef > 0) ? sine_envelope(sh, t) : exp(-pow((t - P->del[i]) * P->iw[i], 2));
+        if (sh && sh->waist > 0) sv += tmp * env;
+        else val += tmp * env;
     }
+    *spot = sv;
     return val;
+}
+
+/* Plane set with a transverse spot: v + (vs t1[p]) t2[q]. */
+static void plane_set_spot(orc_t *c, double *f, int dim, int idx, double v, double vs, const double *t1,
+                           const double *t2) {
+    if (!t1) { plane_set(c, f, dim, idx, v); return; }
+    int o1 = (dim == 0) ? 1 : 0;
+    int o2 = (dim == 2) ? 1 : 2;
+    for (int p = 0; p < c->tot[o1]; p++)
+        for (int q = 0; q < c->tot[o2]; q++) {
+            int ii[3];
+            ii[dim] = idx; ii[o1] = p; ii[o2] = q;
+            f[IDX(c, ii[0], ii[1], ii[2])] = v + vs * t1[p] * t2[q];
+        }
+}
+
+/* Shape of wave w (NULL: plain). Spots of one side and E component must
+ * share waist and centre (else -1 and nothing changes). The spot factor
+ * along transverse axis a of the plane at grid index j is
+ * exp(-(r r)), r = (xyz0 + (j - 1 + h) d - center) / waist, h = 1/2 along
+ * the wave's E polarisation, 0 across it. */
+int orc_set_wave_shape(void *h, int w, const emoo_wave_shape *sh) {
+    orc_t *c = (orc_t *)h;
+    if (w < 0 || w >= c->info.nwaves || w >= EMOO_NWAVE) return -1;
+    emoo_wave_shape old = c->wshape[w];
+    int old_on = c->wshaped[w];
+    if (sh) { c->wshape[w] = *sh; c->wshaped[w] = 1; }
+    else { memset(&c->wshape[w], 0, sizeof(emoo_wave_shape)); c->wshaped[w] = 0; }
+    int owner[6][3];
+    for (int s = 0; s < 6; s++) for (int p = 0; p < 3; p++) owner[s][p] = -1;
+    for (int v = 0; v < c->info.nwaves && v < EMOO_NWAVE; v++) {
+        if (!c->wshaped[v] || !(c->wshape[v].waist > 0)) continue;
+        int side = c->info.inSide[v], p = c->info.inPolE[v] - 1;
+        if (side == 0 || side < -3 || side > 3 || p < 0 || p > 2) continue;
+        int s = 2 * (abs(side) - 1) + (side > 0 ? 1 : 0);
+        int o = owner[s][p];
+        if (o >= 0) {
+            const emoo_wave_shape *a = &c->wshape[o], *b = &c->wshape[v];
+            if (a->waist != b->waist || a->center[0] != b->center[0] || a->center[1] != b->center[1]) {
+                c->wshape[w] = old;
+                c->wshaped[w] = old_on;
+                return -1;
+            }
+        } else {
+            owner[s][p] = v;
+        }
+    }
+    for (int s = 0; s < 6; s++) {
+        int d = s / 2, ax[2] = {(d == 0) ? 1 : 0, (d == 2) ? 1 : 2};
+        for (int p = 0; p < 3; p++)
+            for (int a = 0; a < 2; a++) {
+                free(c->spot[s][p][a]);
+                c->spot[s][p][a] = NULL;
+                if (owner[s][p] < 0) continue;
+                const emoo_wave_shape *ws = &c->wshape[owner[s][p]];
+                int n = c->tot[ax[a]];
+                double hh = ax[a] == p ? 0.5 : 0.0;
+                double *t = (double *)malloc(sizeof(double) * n);
+                for (int j = 0; j < n; j++) {
+                    double pos = c->x0[ax[a]] + (j - 1 + hh) * c->d[ax[a]];
+                    double r = (pos - ws->center[a]) / ws->waist;
+                    t[j] = exp(-(r * r));
+                }
+                c->spot[s][p][a] = t;
+            }
+    }
+    return 0;
 }
 
 /* setFieldAlongEdge plane index, src/grid/oGrid.cpp:291-431: left = first
@@ -382,15 +477,22 @@ static void light_bc(orc_t *c, int s, double t, double dt) {
     double bphase = (dx + sign * dt) / 2;
     for (int i = 0; i < 3; i++) {
         int eid = EPOL[dim][i], bid = BPOL[dim][i];
+        double es = 0.0, bs = 0.0;
         if (c->pulse[s][eid].nw > 0 && eid != dim) {
-            double ev = gaussian_pulses(t, 0.0, &c->pulse[s][eid]);
+            double ev = gaussian_pulses(c, t, 0.0, &c->pulse[s][eid], &es);
             E1[eid] += ev;
             int bsign = sign * (int)pow(-1, i + 1);
-            double bv = bsign * gaussian_pulses(t, bphase, &c->pulse[s][eid]);
+            double bsp;
+            double bv = bsign * gaussian_pulses(c, t, bphase, &c->pulse[s][eid], &bsp);
             B1[bid] += bv;
+            bs = bsign * bsp;
         }
-        plane_set(c, c->slot[EMOO_EX + eid], dim, edge_plane(c, 0, eid, dim, right), E1[eid]);
-        plane_set(c, role_B(c, bid), dim, edge_plane(c, 1, bid, dim, right), B1[bid]);
+        /* the B component paired with E component eid sits at the same
+         * transverse offsets: both take the spot of (s, eid) */
+        const double *t1 = eid != dim ? c->spot[s][eid][0] : NULL;
+        const double *t2 = eid != dim ? c->spot[s][eid][1] : NULL;
+        plane_set_spot(c, c->slot[EMOO_EX + eid], dim, edge_plane(c, 0, eid, dim, right), E1[eid], es, t1, t2);
+        plane_set_spot(c, role_B(c, bid), dim, edge_plane(c, 1, bid, dim, right), B1[bid], bs, t1, t2);
     }
 }
 
@@ -768,7 +870,7 @@ static void deposit(orc_t *c, int with_rho) {
     if (with_rho && c->rho_bg != 0.0) {
         /* the immobile background sits on the physical points */
         double *rho = c->slot[EMOO_RHO];
-        for (int i = 1; i <= c->n[0]; i++)
+        for (int i = c->rho_bg_i0 > 1 ? c->rho_bg_i0 : 1; i <= c->n[0]; i++)
             for (int j = 1; j <= c->n[1]; j++)
                 for (int k = 1; k <= c->n[2]; k++) rho[IDX(c, i, j, k)] += c->rho_bg;
     }
@@ -777,6 +879,15 @@ static void deposit(orc_t *c, int with_rho) {
 /* Uniform immobile background charge density added to rho at every deposit
  * (the C3 and C5 workloads' neutralising ions; the reference has none). */
 void orc_set_rho_background(void *h, double v) { ((orc_t *)h)->rho_bg = v; }
+
+/* Restricts the background to the physical points with x >= xmin (grid point
+ * x index i at xyz0 + (i - 1) dx). */
+void orc_set_rho_background_xmin(void *h, double xmin) {
+    orc_t *c = (orc_t *)h;
+    c->rho_bg_i0 = c->n[0] + 1;
+    for (int i = 1; i <= c->n[0]; i++)
+        if (c->x0[0] + (i - 1) * c->d[0] >= xmin) { c->rho_bg_i0 = i; break; }
+}
 
 int orc_deposit(void *h, int with_rho) {
     deposit((orc_t *)h, with_rho);

@@ -71,6 +71,8 @@ def _load_cpu_lib(path, prefix):
         f("time", C.c_double, [P])
         f("gauss_residual", C.c_int, [P, _D])
         f("set_rho_background", None, [P, C.c_double])
+        f("set_wave_shape", C.c_int, [P, C.c_int, C.POINTER(abi.WaveShape)])
+        f("set_rho_background_xmin", None, [P, C.c_double])
     return L
 
 
@@ -233,14 +235,22 @@ class OracleBackend(CpuBackend):
         self._f("gauss_residual")(self.h, out)
         return list(out)
 
-    def set_rho_background(self, v):
+    def set_rho_background(self, v, xmin=None):
         self._f("set_rho_background")(self.h, C.c_double(v))
+        if xmin is not None:
+            self._f("set_rho_background_xmin")(self.h, C.c_double(xmin))
+
+    def set_wave_shape(self, w, shape):
+        rc = self._f("set_wave_shape")(self.h, w, C.byref(shape) if shape is not None else None)
+        if rc != 0:
+            raise ValueError("orc_set_wave_shape refused the shape")
 
 
 class GpuBackend:
     """The product, through include/emoo.h."""
 
-    def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0, rho_background=0.0):
+    def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0, rho_background=0.0,
+                 rho_background_xmin=None):
         self.L = abi.lib()
         self.info = info
         self.n = [info.nCell[d] for d in range(3)]
@@ -253,6 +263,8 @@ class GpuBackend:
         o.track_ids = track_ids
         o.device = device
         o.rho_background = rho_background
+        if rho_background_xmin is not None:
+            o.rho_background_xmin = rho_background_xmin
         h = C.c_void_p()
         abi.check(self.L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
         self.h = h
@@ -320,6 +332,10 @@ class GpuBackend:
         c = C.c_int()
         abi.check(self.L.emoo_cell_id(self.h, x, y, z, C.byref(c)))
         return c.value
+
+    def set_wave_shape(self, w, shape):
+        abi.check(self.L.emoo_set_wave_shape(self.h, w, C.byref(shape) if shape is not None else None),
+                  "emoo_set_wave_shape")
 
     def init_fields(self):
         it = (C.c_int * 4)()

@@ -1,0 +1,373 @@
+"""Shaped injected waves (transverse Gaussian spot, sine-series envelope),
+the immobile background restricted to an x range, and the laser-plasma
+workload (512 x 128^2, absorbing x walls, electrons from x = 64) built on
+them. None of these has a reference counterpart; they are pinned against
+their stated definitions (restated here in numpy), against the oracle's
+independent C restatement, and - for the gradients with respect to the
+envelope coefficients and the kinetic-energy objective - against the
+tangent-linear run and central finite differences.
+
+CPU tests: the oracle's plane values against the definition, the Gaussian's
+sine-series coefficients, the workload's numbers, the background's x range.
+GPU tests: the FP64 form against the oracle (bit-exact planes without
+particles, FP64_RTOL with them), the mixed form against the FP64 form, a
+scaled-down laser-plasma run against the oracle, and the derivatives."""
+import math
+
+import numpy as np
+import pytest
+
+from apc_524_project_gb300 import abi, configs, loading
+from backends import OracleBackend, by_id, rel_l2
+
+FP64_RTOL = 1e-9
+DEF_RTOL = 1e-13   # oracle plane values against the numpy restatement (evaluation order)
+MIXED_RTOL = 2e-5  # FP32 plane values against FP64 ones
+FD_RTOL = 1e-5
+DOT_RTOL = 1e-9
+
+
+def _shaped_cfg():
+    """A tiny box with x and z external sides and four injected waves that
+    take every path: spot + sine series (x-left Ey), spot with the Gaussian
+    envelope (x-left Ez), a plain wave (x-right Ey) and a series without a
+    spot (z-left Ex)."""
+    W = configs.Wave
+    S = configs.Shape
+    waves = [
+        W(-1, 2, 0.5, 0.7, 20.0, shape=S(waist=2.5, center=(2.0, 1.5), t_start=0.1, window=3.0,
+                                           coef=(0.9, -0.2, 0.3, 0.05))),
+        W(-1, 3, 0.3, 0.9, 10.0, 0.4, 1.0, shape=S(waist=2.5, center=(2.0, 1.5))),
+        W(1, 2, 0.2, 0.8, 0.0, 0.3, 0.5),
+        W(-3, 1, 0.25, 0.6, 45.0, shape=S(t_start=0.0, window=4.0, coef=(1.0, 0.5))),
+    ]
+    return configs.tiny("shape", n=(6, 5, 4), init="constant", E0=(0.0, 0.01, 0.0), B0=(0.0, 0.0, 0.02),
+                        part_bc=("reflecting", "reflecting", "periodic", "periodic", "reflecting", "reflecting"),
+                        field_bc=("external", "external", "periodic", "periodic", "external", "external"),
+                        waves=waves, dt=0.35)
+
+
+# ---- the definition, restated in numpy -----------------------------------
+
+def _env(wv, t):
+    sh = wv.shape
+    if sh is not None and len(sh.coef):
+        if not (sh.t_start <= t <= sh.t_start + sh.window):
+            return 0.0
+        a = (t - sh.t_start) / sh.window
+        return sum(c * math.sin(k * math.pi * a) for k, c in enumerate(sh.coef, start=1))
+    return math.exp(-((t - wv.delay) * wv.inv_width) ** 2)
+
+
+def _spot(cfg, wv, d, pol):
+    """Spot factor on the (n+3)^2 plane of side dimension d (1 without a spot)."""
+    o1, o2 = [a for a in range(3) if a != d]
+    tot = [v + 3 for v in cfg.n]
+    if wv.shape is None or wv.shape.waist <= 0:
+        return np.ones((tot[o1], tot[o2]))
+    c = wv.shape.center if wv.shape.center is not None else tuple(cfg.x0[a] + 0.5 * cfg.L[a] for a in (o1, o2))
+    f = []
+    for a, ax in enumerate((o1, o2)):
+        h = 0.5 if ax == pol else 0.0
+        pos = cfg.x0[ax] + (np.arange(tot[ax]) - 1 + h) * cfg.dx[ax]
+        f.append(np.exp(-((pos - c[a]) / wv.shape.waist) ** 2))
+    return np.outer(f[0], f[1])
+
+
+def _planes(cfg, t, dt):
+    """Expected E and B plane values of every external side at time t (dt:
+    the step, for the B phase shift), as {(field id, dim, index): array}."""
+    EPOL = ((1, 2, 0), (2, 0, 1), (0, 1, 2))
+    BPOL = ((2, 1, 0), (0, 2, 1), (1, 0, 2))
+    out = {}
+    for s in range(6):
+        if cfg.field_bc[s] != "external":
+            continue
+        d, right = s // 2, s % 2
+        sign = 1 if right else -1
+        side = sign * (d + 1)
+        bphase = (cfg.dx[d] + sign * dt) / 2
+        for i in range(3):
+            eid, bid = EPOL[d][i], BPOL[d][i]
+            tot = [v + 3 for v in cfg.n]
+            o1, o2 = [a for a in range(3) if a != d]
+            E = np.full((tot[o1], tot[o2]), cfg.E0[eid])
+            B = np.full((tot[o1], tot[o2]), cfg.B0[bid])
+            if eid != d:
+                bsign = sign * (-1) ** (i + 1)
+                for wv in cfg.waves:
+                    if wv.side != side or wv.pol - 1 != eid:
+                        continue
+                    S = _spot(cfg, wv, d, eid)
+                    env = _env(wv, t)
+                    E = E + wv.amp * math.cos(wv.omega * t + wv.phase_deg * math.pi / 180) * env * S
+                    B = B + bsign * wv.amp * math.cos(wv.omega * (t + bphase) + wv.phase_deg * math.pi / 180) * env * S
+            n = cfg.n[d]
+            ie = 1 if not right else (n if eid == d else n + 1)
+            ib = 1 if not right else (n + 1 if bid == d else n)
+            out[(abi.EX + eid, d, ie)] = E
+            out[(abi.BX + bid, d, ib)] = B
+    return out
+
+
+def _plane(field, d, idx):
+    return np.take(field, idx, axis=d)
+
+
+# ---- CPU ------------------------------------------------------------------
+
+@pytest.mark.parametrize("t", [0.0, 0.7, 1.9, 3.5])
+def test_oracle_shaped_planes_match_definition(t):
+    cfg = _shaped_cfg()
+    dt = cfg.dt
+    o = OracleBackend(configs.input_info(cfg), dt)
+    configs.apply_wave_shapes(o, cfg)
+    o.init_fields()
+    o.set_time(t, dt)
+    o.execute_bc(abi.SEND_EB)
+    # executeBC(-1) works in dimension order: the periodic y ghost copy and
+    # the z planes later overwrite lines of the x planes, so the x planes are
+    # compared on physical y rows away from the z planes, the z planes in full
+    nz = cfg.n[2]
+    for (fid, d, idx), want in _planes(cfg, t, dt).items():
+        got = _plane(o.get_field(fid), d, idx)
+        if d == 0:
+            got, want = got[1:cfg.n[1] + 1, 2:nz], want[1:cfg.n[1] + 1, 2:nz]
+        np.testing.assert_allclose(got, want, rtol=DEF_RTOL, atol=1e-15, err_msg=f"{abi.FIELD_NAMES[fid]} {d} {idx}")
+    o.close()
+
+
+def test_oracle_rejects_two_spots_of_one_side_and_polarisation():
+    cfg = _shaped_cfg()
+    cfg.waves.append(configs.Wave(-1, 2, 0.1, 0.5, shape=configs.Shape(waist=4.0)))  # a second x-left Ey spot
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    o.set_wave_shape(0, configs.wave_shape(cfg, 0))
+    with pytest.raises(ValueError):
+        o.set_wave_shape(4, configs.wave_shape(cfg, 4))
+    same = configs.wave_shape(cfg, 4)
+    same.waist = 2.5
+    same.center[0], same.center[1] = 2.0, 1.5
+    o.set_wave_shape(4, same)  # the same spot is accepted
+    o.close()
+
+
+def test_gaussian_sine_coefficients_rebuild_the_gaussian():
+    window, fwhm = 108.0, 27.0
+    c = configs.gaussian_sine_coefficients(window, fwhm, 16)
+    t = np.linspace(0.0, window, 2001)
+    env = sum(ck * np.sin(k * np.pi * t / window) for k, ck in enumerate(c, start=1))
+    g = np.exp(-4.0 * np.log(2.0) * (t - window / 2) ** 2 / fwhm ** 2)
+    assert np.abs(env - g).max() < 1e-4
+    assert all(abs(ck) < 1e-12 for ck in c[1::2])  # even terms vanish for a centred Gaussian
+
+
+def test_laser512_workload():
+    cfg = configs.laser512()
+    assert cfg.n == (512, 128, 128) and cfg.dt == 0.45 and cfg.steps == 512
+    assert cfg.total_particles() == 16 * 448 * 128 * 128 == 117_440_512
+    assert cfg.part_bc[:2] == ("absorbing", "absorbing") and cfg.field_bc[:2] == ("external", "external")
+    assert configs.rho_background_xmin(cfg) == 64.0
+    wv = cfg.waves[0]
+    sh = configs.wave_shape(cfg, 0)
+    assert sh.waist == 30.0 and tuple(sh.center) == (64.0, 64.0) and sh.ncoef == 16
+    assert math.isclose(sh.window, 4 * 60 * 0.45)
+    assert math.isclose(wv.amp, 2 * math.pi / 20)  # a0 = 1
+    # omega_pe^2 = 0.01 omega^2 (0.01 critical density)
+    assert math.isclose(cfg.omega_pe ** 2, 0.01 * wv.omega ** 2)
+    # seeded coefficients: reproducible, and 0.1-sized noise around the Gaussian's
+    assert configs.laser512().waves[0].shape.coef == wv.shape.coef
+    dev = np.array(wv.shape.coef) - np.array(configs.gaussian_sine_coefficients(sh.window, 60 * 0.45))
+    assert 0.02 < np.std(dev) < 0.3
+
+
+def test_oracle_background_x_range():
+    cfg = configs.tiny("bg", n=(8, 4, 4), init="constant")
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    o.set_rho_background(-0.25, xmin=3.0)  # grid point i sits at x = i - 1
+    o.deposit(True)
+    rho = o.get_field(abi.RHO)
+    assert np.all(rho[1:4, 1:5, 1:5] == 0.0)
+    assert np.all(rho[4:9, 1:5, 1:5] == -0.25)
+    o.close()
+
+
+# ---- GPU ------------------------------------------------------------------
+
+def _load(b, parts):
+    nid = 0
+    for si, p in enumerate(parts):
+        n = len(p["x"])
+        b.add_species(si, p, ids=np.arange(nid, nid + n))
+        nid += n
+
+
+@pytest.mark.gpu
+def test_gpu_shaped_planes_bit_exact_without_particles():
+    from backends import GpuBackend
+
+    cfg = _shaped_cfg()
+    info = configs.input_info(cfg)
+    g = GpuBackend(info, cfg.dt)
+    o = OracleBackend(info, cfg.dt)
+    for b in (g, o):
+        configs.apply_wave_shapes(b, cfg)
+        b.init_fields()
+    for ti in range(12):  # t crosses both windows
+        g.step(1)
+        o.step(ti)
+    for i in range(13):
+        np.testing.assert_array_equal(g.get_field(i), o.get_field(i), err_msg=abi.FIELD_NAMES[i])
+    g.close()
+    o.close()
+
+
+@pytest.mark.gpu
+def test_gpu_shaped_waves_with_particles_match_oracle():
+    from backends import GpuBackend
+
+    cfg = _shaped_cfg()
+    info = configs.input_info(cfg)
+    parts = loading.sample_all(cfg)
+    g = GpuBackend(info, cfg.dt)
+    o = OracleBackend(info, cfg.dt)
+    for b in (g, o):
+        _load(b, parts)
+        configs.apply_wave_shapes(b, cfg)
+        b.init_fields()
+    for ti in range(10):
+        assert g.step(1) == o.step(ti)[0]
+    for i in range(13):
+        assert rel_l2(g.get_field(i), o.get_field(i)) <= FP64_RTOL, i
+    pg, po = by_id(g.particles()), by_id(o.particles())
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert rel_l2(pg[k], po[k]) <= FP64_RTOL, k
+    g.close()
+    o.close()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_shaped_planes_match_fp64():
+    from backends import GpuBackend
+
+    cfg = _shaped_cfg()
+    info = configs.input_info(cfg)
+    g = GpuBackend(info, cfg.dt)
+    m = GpuBackend(info, cfg.dt, precision=abi.MIXED)
+    for b in (g, m):
+        configs.apply_wave_shapes(b, cfg)
+        b.init_fields()
+    for _ in range(8):
+        g.step(1)
+        m.step(1)
+    for i in range(6):
+        assert rel_l2(m.get_field(i), g.get_field(i)) <= MIXED_RTOL, i
+    g.close()
+    m.close()
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_bad_shapes():
+    from backends import GpuBackend
+
+    cfg = _shaped_cfg()
+    cfg.waves.append(configs.Wave(-1, 2, 0.1, 0.5, shape=configs.Shape(waist=4.0)))
+    g = GpuBackend(configs.input_info(cfg), cfg.dt)
+    g.set_wave_shape(0, configs.wave_shape(cfg, 0))
+    with pytest.raises(RuntimeError):
+        g.set_wave_shape(4, configs.wave_shape(cfg, 4))  # second x-left Ey spot, other waist
+    bad = configs.wave_shape(cfg, 3)
+    bad.window = 0.0
+    with pytest.raises(RuntimeError):
+        g.set_wave_shape(3, bad)
+    g.close()
+
+
+def _small_laser(steps=30, ppc=2):
+    """The laser-plasma workload scaled down: 40 x 16^2 cells, plasma from x = 8,
+    pulse of wavelength 8, FWHM 6 steps, waist 5."""
+    return configs.laser512(n=(40, 16, 16), steps=steps, ppc=ppc, wavelength=8.0, fwhm_steps=6, waist=5.0,
+                            plasma_x0=8.0, vth=0.02, seed=11)
+
+
+@pytest.mark.gpu
+def test_gpu_small_laser_plasma_matches_oracle():
+    """Absorbing walls, x-limited plasma over an x-limited background, shaped
+    pulse: FP64 form against the oracle, crossings bit-exact; the mixed form
+    within its tolerance of the FP64 form."""
+    from backends import GpuBackend
+
+    cfg = _small_laser(steps=40)
+    info = configs.input_info(cfg)
+    parts = loading.sample_all(cfg)
+    bg, xmin = configs.rho_background(cfg), configs.rho_background_xmin(cfg)
+    g = GpuBackend(info, cfg.dt, rho_background=bg, rho_background_xmin=xmin)
+    m = GpuBackend(info, cfg.dt, precision=abi.MIXED, rho_background=bg, rho_background_xmin=xmin)
+    o = OracleBackend(info, cfg.dt)
+    o.set_rho_background(bg, xmin=xmin)
+    for b in (g, m, o):
+        _load(b, parts)
+        configs.apply_wave_shapes(b, cfg)
+        b.init_fields()
+    for ti in range(cfg.steps):
+        cg = g.step(1)
+        assert cg == o.step(ti)[0], ti
+        m.step(1)
+    for i in range(10):
+        assert rel_l2(g.get_field(i), o.get_field(i)) <= FP64_RTOL, i
+    assert g.num_particles() == o.num_particles() < cfg.total_particles()  # some were absorbed
+    pg, po = by_id(g.particles()), by_id(o.particles())
+    np.testing.assert_array_equal(pg["id"], po["id"])
+    for k in ("x", "y", "z", "vx", "vy", "vz", "gamma"):
+        assert rel_l2(pg[k], po[k]) <= FP64_RTOL, k
+    assert m.num_particles() == g.num_particles()
+    # mixed against FP64 over the E / B vector (the small components - By, Ex
+    # - carry only the spot's transverse structure and the plasma response,
+    # and their own relative error is larger)
+    num = sum(float(np.sum((m.get_field(i) - g.get_field(i)) ** 2)) for i in range(6))
+    den = sum(float(np.sum(g.get_field(i) ** 2)) for i in range(6))
+    assert math.sqrt(num / den) <= 1e-4, math.sqrt(num / den)
+    # no electron reaches x < 4 and the background starts at x = 8
+    rho = g.get_field(abi.RHO)
+    assert np.all(rho[1:5] == 0.0)
+    for b in (g, m, o):
+        b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("objective", ["field", "kinetic"])
+def test_envelope_gradient_is_transpose_of_tangent(objective):
+    from apc_524_project_gb300.differentiate import Problem
+
+    cfg = _small_laser()
+    P = Problem(cfg, nsteps=30, slab=(8, 16), checkpoint_every=6, objective=objective, species=0)
+    assert P.ntheta == 2 + abi.NCOEF
+    gr = P.gradient()
+    assert gr["objective"] > 0
+    rng = np.random.default_rng(4)
+    dth = rng.uniform(-1, 1, P.ntheta)
+    dth[1] *= 10.0
+    ddv = 1e-3 * rng.uniform(-1, 1, (3, P.np))
+    t = P.tangent(dth, ddv)
+    adj = float(np.dot(gr["grad_theta"], dth) + np.sum(gr["grad_v"] * ddv))
+    assert abs(adj - t["tangent"]) <= DOT_RTOL * abs(t["tangent"]), (adj, t["tangent"])
+    # every envelope coefficient reaches the objective
+    assert np.all(np.abs(gr["grad_theta"][2:]) > 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("objective", ["field", "kinetic"])
+def test_envelope_gradient_matches_central_differences(objective):
+    from apc_524_project_gb300.differentiate import Problem
+
+    cfg = _small_laser()
+    P = Problem(cfg, nsteps=30, slab=(8, 16), checkpoint_every=10, objective=objective, species=0)
+    g = P.gradient()["grad_theta"]
+    for k in (2, 3, 5, 9):  # coefficients 1, 2, 4, 8
+        h = 1e-6
+        th = P.theta0.copy()
+        th[k] += h
+        lp = P.objective(th)
+        th[k] -= 2 * h
+        lm = P.objective(th)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[k]) <= FD_RTOL * abs(g[k]), (k, fd, g[k])

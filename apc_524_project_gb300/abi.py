@@ -120,6 +120,7 @@ class Stats(C.Structure):
         ("launches", C.c_int64),
         ("timed_launches", C.c_int64),
         ("timed_ms", C.c_double),
+        ("ad_cell_mismatch", C.c_int64),
     ]
 
 

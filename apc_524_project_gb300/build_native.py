@@ -30,6 +30,7 @@ CUDA_UNITS = [
     ("sort.cu", []),
     ("particles_mixed.cu", ["--fmad=true"]),
     ("adjoint_f64.cu", ["--fmad=false"]),
+    ("adjoint_mixed.cu", []),
 ]
 HOST_UNITS = ["api.cpp", "loader_host.cpp", "input_parser.cpp"]
 

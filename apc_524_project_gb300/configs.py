@@ -346,9 +346,9 @@ def laser512(n=(512, 128, 128), steps=512, ppc=16, a0=1.0, wavelength=20.0, fwhm
     plus seeded N(0, coef_sigma) noise. External fields and absorbing
     particle walls in x, periodic y and z; electrons at `density` of the
     critical density (omega_pe = sqrt(density) omega) and ppc per cell from
-    x = plasma_x0 on, over immobile ions there; relativistic push. The
-    electron temperature is not part of the workload's definition; vth sets
-    a cold plasma."""
+    x = plasma_x0 on, over immobile ions there; relativistic push; sorted by
+    cell every 20 steps. The electron temperature is not part of the
+    workload's definition; vth sets a cold plasma."""
     import numpy as np
 
     dt = 0.45
@@ -366,7 +366,7 @@ def laser512(n=(512, 128, 128), steps=512, ppc=16, a0=1.0, wavelength=20.0, fwhm
         relativity=1, init="constant",
         part_bc=("absorbing", "absorbing", "periodic", "periodic", "periodic", "periodic"),
         field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
-        waves=[wave], seed=seed, immobile_ions=True)
+        waves=[wave], seed=seed, immobile_ions=True, nstep_sort=20)
 
 
 def tiny(name="tiny", n=(6, 5, 4), dx=(1.0, 1.0, 1.0), ppc=3, relativity=0, init="poisson", steps=4,

@@ -158,52 +158,56 @@ AD_HD void boris_eval(double qp, const T f[6], double dt, T x[3], T v[3]) {
     for (int a = 0; a < 3; a++) x[a] = x[a] + dt * v[a];
 }
 
-AD_HD void cross3(const double a[3], const double b[3], double o[3]) {
+template <class R>
+AD_HD void cross3t(const R a[3], const R b[3], R o[3]) {
     o[0] = a[1] * b[2] - a[2] * b[1];
     o[1] = a[2] * b[0] - a[0] * b[2];
     o[2] = a[0] * b[1] - a[1] * b[0];
 }
+AD_HD void cross3(const double a[3], const double b[3], double o[3]) { cross3t(a, b, o); }
 
 // Adjoint of boris_eval at inputs (f, v): lx, lv hold the adjoints of the
 // outputs on entry and of the inputs on exit; lf receives the field adjoint.
-AD_HD void boris_rev(double qp, const double f[6], double dt, const double v_in[3], double lx[3], double lv[3],
-                     double lf[6]) {
-    const double e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
-    double t[3], s[3], vm[3], vi[3];
+// R: double (FP64 form) or float (mixed form, with dt = 0 and the position
+// adjoint folded into lv by the caller).
+template <class R>
+AD_HD void boris_rev(R qp, const R f[6], R dt, const R v_in[3], R lx[3], R lv[3], R lf[6]) {
+    const R e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
+    R t[3], s[3], vm[3], vi[3];
     for (int a = 0; a < 3; a++) t[a] = qp * b[a];
-    const double bsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
-    const double tsq = 2.0 / (1.0 + qp * qp * bsq);
+    const R bsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    const R tsq = R(2) / (R(1) + qp * qp * bsq);
     for (int a = 0; a < 3; a++) s[a] = tsq * t[a];
     for (int a = 0; a < 3; a++) vm[a] = v_in[a] + qp * e[a];
-    double c[3];
-    cross3(vm, t, c);
+    R c[3];
+    cross3t(vm, t, c);
     for (int a = 0; a < 3; a++) vi[a] = vm[a] + c[a];
     // x' = x + dt v': the adjoint of v' collects dt lx
-    double lvp[3], le[3] = {0, 0, 0}, lb[3] = {0, 0, 0}, lvm[3], lvi[3], ls[3], lt[3];
+    R lvp[3], le[3] = {0, 0, 0}, lb[3] = {0, 0, 0}, lvm[3], lvi[3], ls[3], lt[3];
     for (int a = 0; a < 3; a++) {
         lvp[a] = lv[a] + dt * lx[a];
         le[a] += qp * lvp[a];  // v' = vp + qp e
     }
     // vp = vm + vi x s
-    double tmp[3];
+    R tmp[3];
     for (int a = 0; a < 3; a++) lvm[a] = lvp[a];
-    cross3(s, lvp, lvi);
-    cross3(lvp, vi, ls);
+    cross3t(s, lvp, lvi);
+    cross3t(lvp, vi, ls);
     // vi = vm + vm x t
-    cross3(t, lvi, tmp);
+    cross3t(t, lvi, tmp);
     for (int a = 0; a < 3; a++) lvm[a] += lvi[a] + tmp[a];
-    cross3(lvi, vm, lt);
+    cross3t(lvi, vm, lt);
     // vm = v + qp e
     for (int a = 0; a < 3; a++) {
         lv[a] = lvm[a];
         le[a] += qp * lvm[a];
     }
     // s = tsq t
-    const double ltsq = ls[0] * t[0] + ls[1] * t[1] + ls[2] * t[2];
+    const R ltsq = ls[0] * t[0] + ls[1] * t[1] + ls[2] * t[2];
     for (int a = 0; a < 3; a++) lt[a] += tsq * ls[a];
     // tsq = 2 / (1 + qp^2 bsq)
-    const double lbsq = ltsq * (-0.5 * tsq * tsq * qp * qp);
-    for (int a = 0; a < 3; a++) lb[a] += 2.0 * b[a] * lbsq + qp * lt[a];
+    const R lbsq = ltsq * (R(-0.5) * tsq * tsq * qp * qp);
+    for (int a = 0; a < 3; a++) lb[a] += R(2) * b[a] * lbsq + qp * lt[a];
     for (int a = 0; a < 3; a++) {
         lf[a] += le[a];
         lf[3 + a] += lb[a];

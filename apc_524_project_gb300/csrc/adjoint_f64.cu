@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "ad_math.cuh"
+#include "adjoint_fields.cuh"
 #include "dev_common.cuh"
 #include "emoo_internal.h"
 
@@ -49,8 +50,6 @@ using ad::CellGeo;
 using ad::Dual;
 using ad::mk;
 
-constexpr double FOURPI = 4.0 * PI_D;
-
 constexpr int NSLOT = EMOO_BZ_TM1 + 1;  // E, B, J, rho, B_tm1: the slots a step touches
 
 struct PArr {
@@ -62,12 +61,14 @@ struct CPArr {
 struct FPtrs {
     const double *E[3], *B[3], *T[3];  // E, B role, B_tm1 role
 };
-struct FOut {
-    double *E[3], *B[3], *T[3];
-};
-struct JPtrs {
-    double *J[3];
-};
+using FOut = adf::FOutT<double>;
+using JPtrs = adf::JPtrsT<double>;
+using Slots6 = adf::Slots6T<double>;
+using adf::k_fold_adj;
+using adf::k_ghost_adj;
+using adf::k_plane_adj;
+using adf::k_yee_b_adj;
+using adf::k_yee_e_adj;
 
 __device__ __forceinline__ CellGeo cell_geo(const Geom &g) {
     CellGeo c;
@@ -288,158 +289,6 @@ __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
         L.p[3 + a][p] = lv[a];
     }
     if (REL) L.p[6][p] = lg;
-}
-
-// ---- field adjoints ------------------------------------------------------
-
-__device__ __forceinline__ bool phys(const Geom &g, int i, int j, int k) {
-    return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];
-}
-
-// Adjoint of k_yee_b (B = T + dt curl E over the physical points), gather
-// form over every grid point: LT += LB (physical), LE += dt C_E^T LB.
-__global__ void k_yee_b_adj(Geom g, double dt, FOut A) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
-    const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
-    const double cx = dt / g.d[0], cy = dt / g.d[1], cz = dt / g.d[2];
-    const bool here = phys(g, i, j, k);
-    if (here)
-        for (int c = 0; c < 3; c++) A.T[c][p] += A.B[c][p];
-    const double *Bx = A.B[0], *By = A.B[1], *Bz = A.B[2];
-    // Ey: Bx(o) += cz (Ey[o+1] - Ey[o]); Bz(o) -= cx (Ey[o+sx] - Ey[o])
-    double ley = 0, lez = 0, lex = 0;
-    if (phys(g, i, j, k - 1)) ley += cz * Bx[p - 1];
-    if (here) ley += -cz * Bx[p] + cx * Bz[p];
-    if (phys(g, i - 1, j, k)) ley += -cx * Bz[p - sx];
-    // Ez: Bx(o) -= cy (Ez[o+sy] - Ez[o]); By(o) += cx (Ez[o+sx] - Ez[o])
-    if (phys(g, i, j - 1, k)) lez += -cy * Bx[p - sy];
-    if (here) lez += cy * Bx[p] - cx * By[p];
-    if (phys(g, i - 1, j, k)) lez += cx * By[p - sx];
-    // Ex: By(o) -= cz (Ex[o+1] - Ex[o]); Bz(o) += cy (Ex[o+sy] - Ex[o])
-    if (phys(g, i, j, k - 1)) lex += -cz * By[p - 1];
-    if (here) lex += cz * By[p] - cy * Bz[p];
-    if (phys(g, i, j - 1, k)) lex += cy * Bz[p - sy];
-    A.E[0][p] += lex;
-    A.E[1][p] += ley;
-    A.E[2][p] += lez;
-}
-
-// Adjoint of k_yee_e (E -= dt (curl T + 4 pi J) over the physical points):
-// LJ = -4 pi dt LE (physical, 0 elsewhere), LT += transposed curl; the B role
-// was overwritten by the step, so its physical points' adjoint is cleared.
-__global__ void k_yee_e_adj(Geom g, double dt, FOut A, JPtrs LJ) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = blockIdx.z;
-    if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
-    const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
-    const double cx = dt / g.d[0], cy = dt / g.d[1], cz = dt / g.d[2];
-    const bool here = phys(g, i, j, k);
-    const double *Ex = A.E[0], *Ey = A.E[1], *Ez = A.E[2];
-    for (int c = 0; c < 3; c++) LJ.J[c][p] = here ? -FOURPI * dt * A.E[c][p] : 0.0;
-    double lty = 0, ltz = 0, ltx = 0;
-    // Ty: ex(o) -= cz (Ty[o] - Ty[o-1]); ez(o) += cx (Ty[o] - Ty[o-sx])
-    if (here) lty += -cz * Ex[p] + cx * Ez[p];
-    if (phys(g, i, j, k + 1)) lty += cz * Ex[p + 1];
-    if (phys(g, i + 1, j, k)) lty += -cx * Ez[p + sx];
-    // Tz: ex(o) += cy (Tz[o] - Tz[o-sy]); ey(o) -= cx (Tz[o] - Tz[o-sx])
-    if (here) ltz += cy * Ex[p] - cx * Ey[p];
-    if (phys(g, i, j + 1, k)) ltz += -cy * Ex[p + sy];
-    if (phys(g, i + 1, j, k)) ltz += cx * Ey[p + sx];
-    // Tx: ey(o) += cz (Tx[o] - Tx[o-1]); ez(o) -= cy (Tx[o] - Tx[o-sy])
-    if (here) ltx += cz * Ey[p] - cy * Ez[p];
-    if (phys(g, i, j, k + 1)) ltx += -cz * Ey[p + 1];
-    if (phys(g, i, j + 1, k)) ltx += cy * Ez[p + sy];
-    A.T[0][p] += ltx;
-    A.T[1][p] += lty;
-    A.T[2][p] += ltz;
-    if (here)
-        for (int c = 0; c < 3; c++) A.B[c][p] = 0.0;
-}
-
-// Adjoint of k_fold (F[plane 1] += F[plane n+1], transverse physical range,
-// the two transverse J components): LF[n+1] += LF[1].
-__global__ void k_fold_adj(Geom g, int d, double *f0, double *f1) {
-    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int r = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (q > g.n[o2] || r > g.n[o1]) return;
-    int is[3], it[3];
-    is[d] = g.n[d] + 1;
-    it[d] = 1;
-    is[o1] = it[o1] = r;
-    is[o2] = it[o2] = q;
-    const int64_t s = gidx(g, is[0], is[1], is[2]), t = gidx(g, it[0], it[1], it[2]);
-    double *F = blockIdx.z == 0 ? f0 : f1;
-    F[s] += F[t];
-}
-
-struct Slots6 {
-    double *p[6];
-};
-
-// Adjoint of one side of k_ghost (ghost plane <- physical plane, transverse
-// physical range): LF[src] += LF[dst], LF[dst] = 0.
-__global__ void k_ghost_adj(Geom g, Slots6 fl, int d, int side) {
-    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int r = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (q > g.n[o2] || r > g.n[o1]) return;
-    const int nd = g.n[d];
-    const int src = side == 0 ? nd : 1, dst = side == 0 ? 0 : nd + 1;
-    int is[3], it[3];
-    is[d] = src;
-    it[d] = dst;
-    is[o1] = it[o1] = r;
-    is[o2] = it[o2] = q;
-    double *F = fl.p[blockIdx.z];
-    const int64_t ps = gidx(g, is[0], is[1], is[2]), pd = gidx(g, it[0], it[1], it[2]);
-    F[ps] += F[pd];
-    F[pd] = 0.0;
-}
-
-// Adjoint of a plane set v + vs t1[p] t2[q]: the plane's values depend only
-// on the wave parameters, so the step needs sum(LF) and sum(LF t1 t2) over
-// the plane (one block, fixed order); the host turns them into the
-// parameter gradient. The plane's adjoint is cleared.
-__global__ void k_plane_adj(Geom g, double *F, int d, int idx, const double *t1, const double *t2, double *sums2) {
-    __shared__ double s_u[8], s_s[8];
-    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-    double su = 0.0, ss = 0.0;
-    const int64_t m = (int64_t)g.tot[o1] * g.tot[o2];
-    for (int64_t t = threadIdx.x; t < m; t += blockDim.x) {
-        int c[3];
-        c[d] = idx;
-        c[o1] = (int)(t / g.tot[o2]);
-        c[o2] = (int)(t % g.tot[o2]);
-        const int64_t p = gidx(g, c[0], c[1], c[2]);
-        const double l = F[p];
-        su += l;
-        if (t1) ss += l * t1[c[o1]] * t2[c[o2]];
-        F[p] = 0.0;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        su += __shfl_down_sync(0xffffffffu, su, off);
-        ss += __shfl_down_sync(0xffffffffu, ss, off);
-    }
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_u[w] = su;
-        s_s[w] = ss;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-            a += s_u[i];
-            b += s_s[i];
-        }
-        sums2[0] = a;
-        sums2[1] = b;
-    }
 }
 
 // ---- objective -----------------------------------------------------------
@@ -865,7 +714,6 @@ using namespace emoo;
 extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
                            emoo_ad_result *out, double *grad_theta, double *grad_v) {
     if (!h || !spec || !out) return EMOO_ERR_ARG;
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     if (h->info.electrostatic == 1) return EMOO_ERR_UNSUPPORTED;
     if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
@@ -874,6 +722,8 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
     if (spec->objective == EMOO_AD_OBJ_KINETIC && (spec->species < -1 || spec->species >= h->nspec))
         return EMOO_ERR_ARG;
     if (mode == EMOO_AD_ADJOINT && spec->checkpoint_every < 1) return EMOO_ERR_ARG;
+    EMOO_CUDA(cudaSetDevice(h->dev));
+    if (h->precision == EMOO_MIXED) return ad_run_mixed(h, spec, mode, out, grad_theta, grad_v);
     // the run moves the particles; as after emoo_step, rho is left pending
     // (it is deposited at the final positions when read), and particles that
     // absorbing walls remove leave the store when it is next read

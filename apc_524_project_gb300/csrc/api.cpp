@@ -1396,6 +1396,7 @@ int emoo_get_stats(emoo_handle *h, emoo_stats *s) {
     s->launches = h->launches;
     s->timed_launches = h->prof_count;
     s->timed_ms = h->prof_ms;
+    s->ad_cell_mismatch = h->ad_cell_mismatch;
     return EMOO_OK;
 }
 

@@ -177,6 +177,10 @@ struct emoo_handle {
     // and the loop skips them; they leave the store at the next sort, or at
     // the next call that reads or changes the particle store (compaction).
     int dead_pending = 0;
+    // last mixed-form adjoint run: particles whose recomputed cell after a
+    // step disagreed with the recorded one (0 when the recomputation is the
+    // primal's, as it is by construction)
+    int64_t ad_cell_mismatch = 0;
 
     // instrumentation: kernel launches issued, and CUDA-event timing of the
     // fused particle kernel (the dominant kernel of the step) when enabled
@@ -240,6 +244,25 @@ int mixed_step(emoo_handle *h, double dtp, int with_rho, int fold_what);
 int mixed_materialize_rho(emoo_handle *h);
 int mixed_sort_keys(emoo_handle *h);
 int mixed_compact_keys(emoo_handle *h);
+
+// ---- differentiation of the mixed step (particles_mixed.cu) ----
+// A particle and field state of the mixed form (a snapshot, or the handle's
+// own arrays): cell, offsets, momenta; E and the B / B_tm1 roles.
+struct MSnapView {
+    const int32_t *cell;
+    const float *o[3], *u[3];
+    const float *E[3], *B[3], *T[3];
+};
+void mixed_field_arrays(emoo_handle *h, float *E[3], float *Bslot[6]);
+int mixed_ad_momentum_from_velocity(emoo_handle *h);
+int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_after, float *const lo[3],
+                       float *const lu[3], const float *const lj[3], float *const lE[3], float *const lB[3],
+                       float *const lT[3], unsigned long long *mismatch);
+int mixed_ad_kinetic(emoo_handle *h, const MSnapView &S, int species, double xlo, double xhi, double *dev_out,
+                     float *const lu[3]);
+// the mixed form's differentiated run (adjoint_mixed.cu), behind emoo_ad_run
+int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_result *out, double *grad_theta,
+                 double *grad_v);
 int mixed_get_field(emoo_handle *h, int id, double *out_dev);
 int mixed_set_field(emoo_handle *h, int id, const double *in_dev);
 int mixed_moments(emoo_handle *h, double out4[4]);

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "dev_common.cuh"
+#include "ad_mixed.cuh"
 #include "emoo_internal.h"
 
 namespace emoo {
@@ -342,6 +343,70 @@ __device__ __forceinline__ int axis_bc(const BCTab &bc, int d, int n, int &i, fl
     return mask;
 }
 
+// The push of k_fused_m on one particle: Vay's pusher (REL) on u = gamma v,
+// or Boris's; u is updated in place and v receives the new velocity. The
+// adjoint kernel recomputes the step with this same function.
+template <bool REL, bool FIRST>
+__device__ __forceinline__ void push_m(const float f[6], const float qp, const float *g0, int64_t p, float &ux,
+                                       float &uy, float &uz, float &vx, float &vy, float &vz) {
+    if (REL) {
+        // Vay's pusher (src/pusher/relativisticBoris.cpp:53-140) on
+        // u = gamma v. Before the first push u holds the loaded v and
+        // g0 the loaded gamma, which the reference multiplies in.
+        float v0x, v0y, v0z, mx0, my0, mz0;
+        if (FIRST) {
+            v0x = ux; v0y = uy; v0z = uz;
+            float g = g0[p];
+            mx0 = g * ux; my0 = g * uy; mz0 = g * uz;
+        } else {
+            float iv = rsqrtf(1.0f + ux * ux + uy * uy + uz * uz);
+            v0x = ux * iv; v0y = uy * iv; v0z = uz * iv;
+            mx0 = ux; my0 = uy; mz0 = uz;
+        }
+        float vXbx = v0y * f[5] - v0z * f[4];
+        float vXby = v0z * f[3] - v0x * f[5];
+        float vXbz = v0x * f[4] - v0y * f[3];
+        float upx = mx0 + qp * (f[0] + vXbx) + qp * f[0];
+        float upy = my0 + qp * (f[1] + vXby) + qp * f[1];
+        float upz = mz0 + qp * (f[2] + vXbz) + qp * f[2];
+        float gps = 1.0f + upx * upx + upy * upy + upz * upz;
+        float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
+        float tau2 = tx * tx + ty * ty + tz * tz;
+        float sigma = gps - tau2;
+        float ust = upx * tx + upy * ty + upz * tz;
+        // sigma >= 1 (gps >= 1 + tau2), so both radicands are >= 1
+        float rad = sigma * sigma + 4.0f * (tau2 + ust * ust);
+        float igi = rsqrtf(0.5f * (sigma + rad * rsqrtf(rad)));
+        tx *= igi;
+        ty *= igi;
+        tz *= igi;
+        float sfac = __fdividef(1.0f, 1.0f + tx * tx + ty * ty + tz * tz);
+        float ud = ust * igi;
+        ux = sfac * (upx + ud * tx + (upy * tz - upz * ty));
+        uy = sfac * (upy + ud * ty + (upz * tx - upx * tz));
+        uz = sfac * (upz + ud * tz + (upx * ty - upy * tx));
+        vx = ux * igi;
+        vy = uy * igi;
+        vz = uz * igi;
+    } else {
+        // Boris (src/pusher/boris.cpp:33-85)
+        float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
+        float b2 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
+        float ts = __fdividef(2.0f, 1.0f + qp * qp * b2);
+        float sx = ts * tx, sy = ts * ty, sz = ts * tz;
+        float mx = ux + qp * f[0], my = uy + qp * f[1], mz = uz + qp * f[2];
+        float ix_ = mx + my * tz - mz * ty;
+        float iy_ = my + mz * tx - mx * tz;
+        float iz_ = mz + mx * ty - my * tx;
+        ux = mx + iy_ * sz - iz_ * sy + qp * f[0];
+        uy = my + iz_ * sx - ix_ * sz + qp * f[1];
+        uz = mz + ix_ * sy - iy_ * sx + qp * f[2];
+        vx = ux;
+        vy = uy;
+        vz = uz;
+    }
+}
+
 constexpr int FUSED_BLOCK = 256;
 constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
 constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: conflict-free both ways)
@@ -391,63 +456,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
             } else {
             float f[6];
             gather_pack(pack + (int64_t)c * PACK_F4, ox, oy, oz, f);
-            const float qp = st.qp[s];
-            if (REL) {
-                // Vay's pusher (src/pusher/relativisticBoris.cpp:53-140) on
-                // u = gamma v. Before the first push u holds the loaded v and
-                // g0 the loaded gamma, which the reference multiplies in.
-                float v0x, v0y, v0z, mx0, my0, mz0;
-                if (FIRST) {
-                    v0x = ux; v0y = uy; v0z = uz;
-                    float g = g0[p];
-                    mx0 = g * ux; my0 = g * uy; mz0 = g * uz;
-                } else {
-                    float iv = rsqrtf(1.0f + ux * ux + uy * uy + uz * uz);
-                    v0x = ux * iv; v0y = uy * iv; v0z = uz * iv;
-                    mx0 = ux; my0 = uy; mz0 = uz;
-                }
-                float vXbx = v0y * f[5] - v0z * f[4];
-                float vXby = v0z * f[3] - v0x * f[5];
-                float vXbz = v0x * f[4] - v0y * f[3];
-                float upx = mx0 + qp * (f[0] + vXbx) + qp * f[0];
-                float upy = my0 + qp * (f[1] + vXby) + qp * f[1];
-                float upz = mz0 + qp * (f[2] + vXbz) + qp * f[2];
-                float gps = 1.0f + upx * upx + upy * upy + upz * upz;
-                float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
-                float tau2 = tx * tx + ty * ty + tz * tz;
-                float sigma = gps - tau2;
-                float ust = upx * tx + upy * ty + upz * tz;
-                // sigma >= 1 (gps >= 1 + tau2), so both radicands are >= 1
-                float rad = sigma * sigma + 4.0f * (tau2 + ust * ust);
-                float igi = rsqrtf(0.5f * (sigma + rad * rsqrtf(rad)));
-                tx *= igi;
-                ty *= igi;
-                tz *= igi;
-                float sfac = __fdividef(1.0f, 1.0f + tx * tx + ty * ty + tz * tz);
-                float ud = ust * igi;
-                ux = sfac * (upx + ud * tx + (upy * tz - upz * ty));
-                uy = sfac * (upy + ud * ty + (upz * tx - upx * tz));
-                uz = sfac * (upz + ud * tz + (upx * ty - upy * tx));
-                vx = ux * igi;
-                vy = uy * igi;
-                vz = uz * igi;
-            } else {
-                // Boris (src/pusher/boris.cpp:33-85)
-                float tx = qp * f[3], ty = qp * f[4], tz = qp * f[5];
-                float b2 = f[3] * f[3] + f[4] * f[4] + f[5] * f[5];
-                float ts = __fdividef(2.0f, 1.0f + qp * qp * b2);
-                float sx = ts * tx, sy = ts * ty, sz = ts * tz;
-                float mx = ux + qp * f[0], my = uy + qp * f[1], mz = uz + qp * f[2];
-                float ix_ = mx + my * tz - mz * ty;
-                float iy_ = my + mz * tx - mx * tz;
-                float iz_ = mz + mx * ty - my * tx;
-                ux = mx + iy_ * sz - iz_ * sy + qp * f[0];
-                uy = my + iz_ * sx - ix_ * sz + qp * f[1];
-                uz = mz + ix_ * sy - iy_ * sx + qp * f[2];
-                vx = ux;
-                vy = uy;
-                vz = uz;
-            }
+            push_m<REL, FIRST>(f, st.qp[s], g0, p, ux, uy, uz, vx, vy, vz);
             // position update in cell units, then the boundaries per axis
             float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
             cell_step(nx, ix, ox);
@@ -971,6 +980,197 @@ __global__ void k_compact_keys_m(MSpecies st, const int32_t *cell, int64_t np, i
     int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (p >= np) return;
     key[p] = cell[p] < 0 ? (uint32_t)nspec : (uint32_t)species_of_m(st, p);
+}
+
+// ---- differentiation of the mixed step --------------------------------------
+//
+// The adjoint of one step of the loop (k_fused_m<REL, false, true> with J
+// only, then fold, Yee, executeBC(-1)) for one particle, given the particle
+// state before the step (S) and the pack built from the fields before it.
+// The forward is recomputed with k_fused_m's own functions (gather_pack,
+// push_m, cell_step, axis_bc), so the cell after the step and the boundary
+// events are the primal's; cell_after (the state after the step) checks that,
+// counting disagreements. L: offset and momentum adjoints, after the step on
+// entry, before it on exit. LJ: adjoint of the current at the points (physical
+// units; the deposited fixed-point sums are J / q0). LF: the field adjoints,
+// which receive the gather's adjoint (atomics; B and B_tm1 each half).
+struct MAdjState {
+    float *o[3], *u[3];
+};
+struct MAdjFields {
+    float *E[3], *B[3], *T[3];
+};
+struct MAdjJ {
+    const float *J[3];
+};
+struct MSnapC {
+    const int32_t *cell;
+    const float *o[3], *u[3];
+};
+
+template <bool REL>
+__global__ void k_adj_particles_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MSnapC S,
+                                  const int32_t *cell_after, int64_t np, float q0, MAdjState L, MAdjJ LJ,
+                                  MAdjFields LF, unsigned long long *mismatch) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int32_t c = S.cell[p];
+    if (c < 0) return;  // removed before the step: its adjoint stays 0
+    const int s = species_of_m(st, p);
+    const float o_in[3] = {S.o[0][p], S.o[1][p], S.o[2][p]};
+    const float u_in[3] = {S.u[0][p], S.u[1][p], S.u[2][p]};
+    int ic[3];
+    split_cell(g, dv, c, ic[0], ic[1], ic[2]);
+    const float4 *pk = pack + (int64_t)c * PACK_F4;
+    float f[6];
+    gather_pack(pk, o_in[0], o_in[1], o_in[2], f);
+    float u[3] = {u_in[0], u_in[1], u_in[2]}, v[3];
+    push_m<REL, false>(f, st.qp[s], nullptr, p, u[0], u[1], u[2], v[0], v[1], v[2]);
+    float o[3];
+    int ii[3] = {ic[0], ic[1], ic[2]};
+    for (int a = 0; a < 3; a++) cell_step(o_in[a] + v[a] * g.dtid[a], ii[a], o[a]);
+    // bit a: axis a reflected (u, v -> -u, -v); bit 3 + a: its offset mapped
+    // to 1 - o (axis_bc keeps an offset of exactly 0)
+    int mask = 0, flip = 0;
+    for (int a = 0; a < 3; a++) {
+        if (mask & 64) break;
+        const float o_pre = o[a];
+        const int m = axis_bc(bc, a, g.n[a], ii[a], o[a], u[a], v[a]);
+        const int side = ((m >> (2 * a + 1)) & 1) ? 2 * a + 1 : 2 * a;
+        if ((m & 63) && !(m & 64) && bc.pbc[side] == PBC_REFLECTING) {
+            flip |= 1 << a;
+            if (o_pre != 0.0f) flip |= 8 << a;
+        }
+        mask |= m;
+    }
+    if (mask & 64) {  // removed in this step: nothing after it depends on the particle
+        for (int a = 0; a < 3; a++) {
+            L.o[a][p] = 0.0f;
+            L.u[a][p] = 0.0f;
+        }
+        return;
+    }
+    const int32_t onew = ii[0] * (int)g.sx + ii[1] * (int)g.sy + ii[2];
+    if (cell_after && cell_after[p] != onew) atomicAdd(mismatch, 1ull);
+    float lo[3], lu[3], lv[3] = {0.0f, 0.0f, 0.0f};
+    for (int a = 0; a < 3; a++) {
+        lo[a] = L.o[a][p];
+        lu[a] = L.u[a][p];
+    }
+    if (st.deposit[s]) {
+        float l12[12];
+#pragma unroll
+        for (int q = 0; q < 12; q++) l12[q] = q0 * LJ.J[q >> 2][onew + dep_offset(q, (int)g.sx, (int)g.sy)];
+        ad::jterms_m_rev(st.qdep[s], o, v, l12, lo, lv);
+    }
+    // boundaries: a reflection maps u -> -u, v -> -v and o -> 1 - o
+    for (int a = 0; a < 3; a++) {
+        if (!(flip & (1 << a))) continue;
+        lu[a] = -lu[a];
+        lv[a] = -lv[a];
+        if (flip & (8 << a)) lo[a] = -lo[a];
+    }
+    // offset update o' = o + v dt / d (cell held)
+    for (int a = 0; a < 3; a++) lv[a] += lo[a] * g.dtid[a];
+    float lf[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (REL) {
+        ad::vay_u_rev(st.qp[s], f, u_in, lu, lv, lf);
+    } else {
+        float lx[3] = {0.0f, 0.0f, 0.0f}, lvb[3] = {lu[0] + lv[0], lu[1] + lv[1], lu[2] + lv[2]};
+        ad::boris_rev(st.qp[s], f, 0.0f, u_in, lx, lvb, lf);
+        for (int a = 0; a < 3; a++) lu[a] = lvb[a];
+    }
+    // gather: offsets through the pack polynomial, fields through the weights
+    float pkf[18];
+    {
+        const float4 ex = pk[0], ey = pk[1], ez = pk[2], bxy = pk[3], bz = pk[4];
+        const float t[18] = {ex.x, ex.y, ex.z, ex.w, ey.x, ey.y, ey.z, ey.w, ez.x, ez.y, ez.z, ez.w,
+                             bxy.x, bxy.y, bxy.z, bxy.w, bz.x, bz.y};
+#pragma unroll
+        for (int k = 0; k < 18; k++) pkf[k] = t[k];
+    }
+    ad::gather_m_rev_offsets(pkf, o_in, lf, lo);
+    float we[12], wb[6];
+    ad::gather_m_weights(o_in, we, wb);
+    const int64_t sx = g.sx, sy = g.sy, o0 = c;
+    const int64_t pe[12] = {o0, o0 + sy, o0 + sy + 1, o0 + 1,        // Ex: F00 F10 F11 F01 over (y, z)
+                            o0, o0 + 1, o0 + sx + 1, o0 + sx,        // Ey over (z, x)
+                            o0, o0 + sx, o0 + sx + sy, o0 + sy};     // Ez over (x, y)
+    const int64_t pb[6] = {o0, o0 + sx, o0, o0 + sy, o0, o0 + 1};
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        const float l = we[k] * lf[k >> 2];
+        if (l != 0.0f) atomicAdd(LF.E[k >> 2] + pe[k], l);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const float l = wb[k] * lf[3 + (k >> 1)];
+        if (l != 0.0f) {
+            atomicAdd(LF.B[k >> 1] + pb[k], l);
+            atomicAdd(LF.T[k >> 1] + pb[k], l);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        L.o[a][p] = lo[a];
+        L.u[a][p] = lu[a];
+    }
+}
+
+// Selection of the kinetic objective: particles of `species` (-1: all) whose
+// x = xyz0 + ((i - 1) + o) dx lies in [xlo, xhi).
+struct MKinSel {
+    int species;
+    double x0, dx, xlo, xhi;
+    double m[EMOO_NSPEC];
+};
+
+__device__ __forceinline__ bool kin_selected_m(const MGeom &g, const Div3 &dv, const MSpecies &st, const MKinSel &ks,
+                                               MSnapC S, int64_t p, int &s) {
+    const int32_t c = S.cell[p];
+    if (c < 0) return false;
+    s = species_of_m(st, p);
+    if (ks.species >= 0 && s != ks.species) return false;
+    int ix, iy, iz;
+    split_cell(g, dv, c, ix, iy, iz);
+    const double x = ks.x0 + ((double)(ix - 1) + (double)S.o[0][p]) * ks.dx;
+    return x >= ks.xlo && x < ks.xhi;
+}
+
+// sum m (gamma - 1) (REL, gamma = sqrt(1 + u^2)) or 0.5 m u^2 over the
+// selected particles, in FP64; or, with L, the seed d objective / d u.
+template <bool REL>
+__global__ void k_kinetic_m(MGeom g, Div3 dv, MSpecies st, MKinSel ks, MSnapC S, int64_t np, double *out,
+                            MAdjState L) {
+    double a = 0.0;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        int s;
+        if (!kin_selected_m(g, dv, st, ks, S, p, s)) continue;
+        const double ux = S.u[0][p], uy = S.u[1][p], uz = S.u[2][p];
+        const double u2 = ux * ux + uy * uy + uz * uz, m = ks.m[s];
+        if (out) {
+            a += REL ? m * (sqrt(1.0 + u2) - 1.0) : 0.5 * m * u2;
+        } else {
+            const double k = REL ? m / sqrt(1.0 + u2) : m;
+            L.u[0][p] += (float)(k * ux);
+            L.u[1][p] += (float)(k * uy);
+            L.u[2][p] += (float)(k * uz);
+        }
+    }
+    if (!out) return;
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, a);
+}
+
+// Before the first push the momentum slots hold the loaded velocity and g0
+// the loaded gamma; this stores u = gamma v, the state every later push
+// starts from.
+__global__ void k_momentum_from_velocity(MState S, const float *g0, int64_t np) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const float g = g0[p];
+    S.ux[p] *= g;
+    S.uy[p] *= g;
+    S.uz[p] *= g;
 }
 
 // ---- host helpers ----------------------------------------------------------
@@ -1515,6 +1715,93 @@ int mixed_yee_public(emoo_handle *h, double dtp, int es) { return mixed_yee(h, d
 // diagnostics: Gauss-law residual).
 int mixed_fields_to_slots(emoo_handle *h) {
     for (int id = 0; id <= EMOO_BZ_TM1; id++) EMOO_TRY(mixed_get_field(h, id, h->slot[id]));
+    return EMOO_OK;
+}
+
+// ---- differentiation of the mixed step (driven from adjoint_mixed.cu) ----
+
+// The FP32 field storage: E, and the B slots (BX..BZ, BX_TM1..BZ_TM1 storage).
+void mixed_field_arrays(emoo_handle *h, float *E[3], float *Bslot[6]) {
+    for (int c = 0; c < 3; c++) E[c] = h->mf->E[c];
+    for (int c = 0; c < 6; c++) Bslot[c] = h->mf->Bslot[c];
+}
+
+// Before the first relativistic push the momentum slots hold the loaded
+// velocity (and g0 the loaded gamma); store u = gamma v so that every step
+// of a differentiated run is the same function.
+int mixed_ad_momentum_from_velocity(emoo_handle *h) {
+    if (!(h->info.relativity && h->first_push && h->g0)) return EMOO_OK;
+    if (h->np) {
+        h->launches++;
+        k_momentum_from_velocity<<<(unsigned)((h->np + 255) / 256), 256, 0, h->stream>>>(mstate(h), h->g0, h->np);
+        EMOO_CUDA(cudaGetLastError());
+    }
+    h->first_push = 0;
+    return EMOO_OK;
+}
+
+int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_after, float *const lo[3],
+                       float *const lu[3], const float *const lj[3], float *const lE[3], float *const lB[3],
+                       float *const lT[3], unsigned long long *mismatch) {
+    if (h->np == 0) return EMOO_OK;
+    MGeom mg = mgeom(h, h->dtp);
+    {
+        MGather P;
+        for (int c = 0; c < 3; c++) {
+            P.E[c] = S.E[c];
+            P.B[c] = S.B[c];
+            P.T[c] = S.T[c];
+        }
+        const Geom &g = h->g;
+        dim3 blk(32, 8);
+        dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+        h->launches++;
+        k_pack_m<<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        EMOO_CUDA(cudaGetLastError());
+    }
+    MSnapC SC{S.cell, {S.o[0], S.o[1], S.o[2]}, {S.u[0], S.u[1], S.u[2]}};
+    MAdjState L{{lo[0], lo[1], lo[2]}, {lu[0], lu[1], lu[2]}};
+    MAdjJ LJ{{lj[0], lj[1], lj[2]}};
+    MAdjFields LF{{lE[0], lE[1], lE[2]}, {lB[0], lB[1], lB[2]}, {lT[0], lT[1], lT[2]}};
+    MSpecies st = mspecies(h, h->dtp);
+    Div3 dv = div3(h);
+    const float q0 = (float)h->mf->q0;
+    const unsigned nb = (unsigned)((h->np + 255) / 256);
+    h->launches++;
+    if (h->info.relativity)
+        k_adj_particles_m<true><<<nb, 256, 0, h->stream>>>(mg, dv, st, h->bc, h->mf->pack, SC, cell_after, h->np, q0, L,
+                                                           LJ, LF, mismatch);
+    else
+        k_adj_particles_m<false><<<nb, 256, 0, h->stream>>>(mg, dv, st, h->bc, h->mf->pack, SC, cell_after, h->np, q0,
+                                                            L, LJ, LF, mismatch);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// The kinetic objective of the particles in state S (dev_out: += its value)
+// or its seed (lu += d objective / d u).
+int mixed_ad_kinetic(emoo_handle *h, const MSnapView &S, int species, double xlo, double xhi, double *dev_out,
+                     float *const lu[3]) {
+    if (h->np == 0) return EMOO_OK;
+    MKinSel ks;
+    ks.species = species;
+    ks.x0 = h->info.xyz0[0];
+    ks.dx = h->g.d[0];
+    ks.xlo = xlo;
+    ks.xhi = xhi;
+    for (int s = 0; s < EMOO_NSPEC; s++) ks.m[s] = h->info.mass_ratio[s];
+    MSnapC SC{S.cell, {S.o[0], S.o[1], S.o[2]}, {S.u[0], S.u[1], S.u[2]}};
+    MAdjState L{{nullptr, nullptr, nullptr}, {lu ? lu[0] : nullptr, lu ? lu[1] : nullptr, lu ? lu[2] : nullptr}};
+    MGeom mg = mgeom(h, h->dtp);
+    MSpecies st = mspecies(h, h->dtp);
+    Div3 dv = div3(h);
+    const int nb = nblk(h->np);
+    h->launches++;
+    if (h->info.relativity)
+        k_kinetic_m<true><<<nb, 256, 0, h->stream>>>(mg, dv, st, ks, SC, h->np, lu ? nullptr : dev_out, L);
+    else
+        k_kinetic_m<false><<<nb, 256, 0, h->stream>>>(mg, dv, st, ks, SC, h->np, lu ? nullptr : dev_out, L);
+    EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
 

@@ -1,7 +1,8 @@
-"""Differentiation of the FP64 time loop: a thin harness over emoo_ad_run.
+"""Differentiation of the time loop: a thin harness over emoo_ad_run.
 
 A Problem holds a workload and its initial particles. Every evaluation
-builds a fresh FP64 handle, loads the particles with the velocity
+builds a fresh handle (FP64, or the mixed-precision form: objective and
+adjoint only), loads the particles with the velocity
 perturbation dv added (gamma kept), sets the wave amplitudes and phases and
 the wave shapes (with the envelope coefficients from theta), starts the
 fields and runs emoo_ad_run:
@@ -14,9 +15,9 @@ theta = (amp_0, phase_0 [degrees], amp_1, phase_1, ...), followed, when a
 wave has a sine-series envelope, by 16 envelope coefficients per wave;
 dv has shape (3, N) in the particles' load order. The objective is the
 field energy of the x slab `slab` (cells), or with objective="kinetic" the
-kinetic energy of the particles of `species` (-1: all) in that x range. PicObjective wraps gradient() as a
-torch.autograd.Function for optimisation loops; the C++ driver reaches the
-same kernels through include/emoo.h."""
+kinetic energy of the particles of `species` (-1: all) in that x range.
+PicObjective wraps gradient() as a torch.autograd.Function for optimisation
+loops; the C++ driver reaches the same kernels through include/emoo.h."""
 import ctypes as C
 
 import numpy as np
@@ -26,7 +27,7 @@ from . import abi, configs, loading
 
 class Problem:
     def __init__(self, cfg, nsteps=None, slab=(48, 56), checkpoint_every=16, parts=None, objective="field",
-                 species=-1):
+                 species=-1, precision=abi.FP64):
         self.cfg = cfg
         self.info0 = configs.input_info(cfg)
         self.nsteps = cfg.steps if nsteps is None else nsteps
@@ -34,6 +35,7 @@ class Problem:
         self.every = checkpoint_every
         self.kind = {"field": abi.AD_OBJ_FIELD, "kinetic": abi.AD_OBJ_KINETIC}[objective]
         self.species = species
+        self.precision = precision
         self.parts = parts if parts is not None else loading.sample_all(cfg)
         self.np = sum(len(p["x"]) for p in self.parts)
         nw = len(cfg.waves)
@@ -53,7 +55,7 @@ class Problem:
         info = configs.input_info(self.cfg)
         o = abi.Opts()
         L.emoo_default_opts(C.byref(o))
-        o.precision = abi.FP64
+        o.precision = self.precision
         o.dt = self.cfg.dt
         o.capacity = self.np
         o.rho_background = configs.rho_background(self.cfg)
@@ -111,6 +113,10 @@ class Problem:
                                     gv.ctypes.data_as(dp) if want_grad else None), "emoo_ad_run")
             out = {"objective": res.objective, "tangent": res.tangent, "forward_ms": res.forward_ms,
                    "recompute_ms": res.recompute_ms, "reverse_ms": res.reverse_ms}
+            if self.precision == abi.MIXED and mode == abi.AD_ADJOINT:
+                st = abi.Stats()
+                abi.check(L.emoo_get_stats(h, C.byref(st)), "emoo_get_stats")
+                out["cell_mismatch"] = st.ad_cell_mismatch
             if want_grad:
                 out["grad_theta"] = gth[:self.ntheta]
                 out["grad_v"] = gv

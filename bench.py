@@ -49,6 +49,7 @@ def _args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-laser512", action="store_true")
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=6)
     return ap.parse_args()
@@ -158,8 +159,16 @@ def _make_handle(cfg, precision, capacity, device):
     o.capacity = capacity
     o.track_ids = 0
     o.device = device
+    o.rho_background = configs.rho_background(cfg)
+    xmin = configs.rho_background_xmin(cfg)
+    if xmin is not None:
+        o.rho_background_xmin = xmin
     h = C.c_void_p()
     abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
+    for w in range(len(cfg.waves)):
+        shape = configs.wave_shape(cfg, w)
+        if shape is not None:
+            abi.check(L.emoo_set_wave_shape(h, w, C.byref(shape)), "emoo_set_wave_shape")
     for si in range(len(cfg.species)):
         g = configs.gen_params(cfg, si)
         abi.check(L.emoo_load_generated(h, C.byref(g), cfg.count(cfg.species[si])), "emoo_load_generated")
@@ -269,7 +278,54 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
     # ---- differentiation: adjoint against forward cost on the laser workload
     if not args.no_adjoint:
         res["adjoint"] = adjoint_arm()
+    if not args.no_laser512:
+        res["laser512"] = laser512_arm(device)
     return cfg, res
+
+
+def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_steps=64, ad_every=8):
+    """The laser-plasma workload at full size (512 x 128^2 cells, 117,440,512
+    electrons, shaped pulse, absorbing x walls, sort every 20 steps): loop
+    throughput of the mixed and FP64 forms, and the FP64 adjoint of the named
+    objective (electron kinetic energy at x in [448, 512)) with respect to the
+    16 envelope coefficients over the first ad_steps steps, checkpoints every
+    ad_every steps (FP64 snapshots take 7.2 GB each; the full 512 steps with
+    sqrt(N) checkpoints would need 46 of them)."""
+    import torch
+    from apc_524_project_gb300 import abi, configs
+
+    L = abi.lib()
+    cfg = configs.laser512()
+    N = cfg.total_particles()
+    out = {"workload": "laser-plasma 512x128x128 cells, 117,440,512 electrons from x = 64 at 0.01 n_c, a0 = 1 "
+                       "pulse with waist 30 and a 16-coefficient sine envelope, absorbing x, sort every 20"}
+    cnt = (C.c_int64 * 6)()
+    n = C.c_int64()
+    for prec, name, k in ((abi.MIXED, "mixed", steps), (abi.FP64, "fp64", fp64_steps)):
+        h = _make_handle(cfg, prec, N, device)
+        for _ in range(warmup if prec == abi.MIXED else 1):
+            abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
+        t = _timed_steps(h, k, lambda: None)
+        abi.check(L.emoo_num_particles(h, -1, C.byref(n)), "emoo_num_particles")
+        out[name] = {"value": n.value * k / t, "unit": UNIT, "steps": k, "ms_per_step": t / k * 1e3,
+                     "particles": n.value}
+        abi.check(L.emoo_destroy(h))
+        torch.cuda.synchronize()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    h = _make_handle(cfg, abi.FP64, N, device)
+    nth = L.emoo_ad_nparams(h)
+    spec = abi.AdSpec(ad_steps, ad_every, 448, 512, abi.AD_OBJ_KINETIC, 0)
+    res = abi.AdResult()
+    g = (C.c_double * nth)()
+    abi.check(L.emoo_ad_run(h, C.byref(spec), abi.AD_ADJOINT, None, None, C.byref(res), g, None), "emoo_ad_run")
+    abi.check(L.emoo_destroy(h))
+    coef = list(g)[2:]
+    out["adjoint"] = {"form": "FP64", "steps": ad_steps, "checkpoint_every": ad_every,
+                      "objective": "electron kinetic energy, x in [448, 512)", "value": res.objective,
+                      "forward_ms": res.forward_ms, "recompute_ms": res.recompute_ms, "reverse_ms": res.reverse_ms,
+                      "adjoint_over_forward": (res.recompute_ms + res.reverse_ms) / res.forward_ms,
+                      "max_abs_coef_gradient": max(abs(v) for v in coef)}
+    return out
 
 
 def adjoint_arm():
@@ -491,6 +547,8 @@ def main():
                         "mixed_over_fp64": value / v64}
     if "adjoint" in res:
         line["adjoint"] = res["adjoint"]
+    if "laser512" in res:
+        line["laser512"] = res["laser512"]
     if "e2e" in res:
         e = res["e2e"]
         line["e2e"] = {"value": N * e["steps"] * world / e["t"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

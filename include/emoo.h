@@ -316,6 +316,7 @@ typedef struct emoo_stats {
     int64_t launches;       /* kernels launched by the handle so far */
     int64_t timed_launches; /* launches of the fused particle kernel timed since profiling was enabled */
     double timed_ms;        /* their summed CUDA-event durations */
+    int64_t ad_cell_mismatch; /* last mixed-form adjoint run: particles whose recomputed cell disagreed (0) */
 } emoo_stats;
 
 /* Enables (1) or disables (0) CUDA-event timing of every fused particle

@@ -1,6 +1,8 @@
-// Host check of apc_524_project_gb300/csrc/ad_math.cuh (built by
-// tests/test_ad_math.py with g++): for the gather, both pushers and the
-// current terms, on seeded random inputs,
+// Host check of apc_524_project_gb300/csrc/ad_math.cuh and ad_mixed.cuh
+// (built by tests/test_ad_math.py with g++): for the gather, both pushers and
+// the current terms of the FP64 form, and the pack gather, the u-form Vay
+// pusher and the cell-unit current terms of the mixed form, on seeded random
+// inputs,
 //   * the Dual (tangent-linear) derivative matches a central difference of
 //     the double evaluation;
 //   * the reverse (adjoint) function is the transpose of the Dual one:
@@ -13,6 +15,7 @@
 #include <vector>
 
 #include "ad_math.cuh"
+#include "ad_mixed.cuh"
 
 using namespace emoo::ad;
 
@@ -168,6 +171,92 @@ int main() {
             };
             auto frev = [&](const double *x, const double *l, double *jt) { jterms_rev(c, uq, x, x + 3, l, jt, jt + 3); };
             check("jterms", 6, 12, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- mixed pack gather: inputs F[12] (E edge values), S[6] (B + B_tm1
+        // face values), o[3] -> f[6], through the pack coefficients
+        {
+            double x0[21];
+            for (int i = 0; i < 18; i++) x0[i] = U(-1, 1);
+            for (int a = 0; a < 3; a++) x0[18 + a] = U(0.0, 1.0);
+            auto pack = [](const auto *x, auto *pk) {
+                for (int i = 0; i < 3; i++) {  // edge_coef of (F00, F10, F11, F01)
+                    const auto f00 = x[4 * i], f10 = x[4 * i + 1], f11 = x[4 * i + 2], f01 = x[4 * i + 3];
+                    pk[4 * i] = (4.0 * f00 - 2.0 * f01) + (f11 - 2.0 * f10);
+                    pk[4 * i + 1] = (2.0 * f10 - 2.0 * f00) + (f01 - f11);
+                    pk[4 * i + 2] = (2.0 * f01 - 2.0 * f00) + (f10 - f11);
+                    pk[4 * i + 3] = (f00 - f10) + (f11 - f01);
+                    const auto s0 = x[12 + 2 * i], s1 = x[12 + 2 * i + 1];
+                    pk[12 + 2 * i] = s0 - 0.5 * s1;
+                    pk[12 + 2 * i + 1] = 0.5 * (s1 - s0);
+                }
+            };
+            auto fd = [&](const double *x, double *y) {
+                double pk[18];
+                pack(x, pk);
+                gather_m_eval(pk, x + 18, y);
+            };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual xx[21], pk[18], o[6];
+                for (int i = 0; i < 21; i++) xx[i] = mk(x[i], d[i]);
+                pack(xx, pk);
+                gather_m_eval(pk, xx + 18, o);
+                for (int i = 0; i < 6; i++) jd[i] = o[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                double pk[18], we[12], wb[6];
+                pack(x, pk);
+                gather_m_weights(x + 18, we, wb);
+                for (int k = 0; k < 12; k++) jt[k] = we[k] * l[k >> 2];
+                for (int k = 0; k < 6; k++) jt[12 + k] = wb[k] * l[3 + (k >> 1)];
+                for (int a = 0; a < 3; a++) jt[18 + a] = 0.0;
+                gather_m_rev_offsets(pk, x + 18, l, jt + 18);
+            };
+            check("mixed gather", 21, 6, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- mixed Vay: inputs f[6], u[3] -> u'[3], v'[3]
+        {
+            const double qp = U(-0.3, 0.3);
+            double x0[9];
+            for (int i = 0; i < 6; i++) x0[i] = U(-1, 1);
+            for (int i = 6; i < 9; i++) x0[i] = U(-2, 2);
+            auto fd = [&](const double *x, double *y) {
+                double u[3] = {x[6], x[7], x[8]}, v[3];
+                vay_u_eval(qp, x, u, v);
+                for (int a = 0; a < 3; a++) { y[a] = u[a]; y[3 + a] = v[a]; }
+            };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual f[6], u[3], v[3];
+                for (int i = 0; i < 6; i++) f[i] = mk(x[i], d[i]);
+                for (int a = 0; a < 3; a++) u[a] = mk(x[6 + a], d[6 + a]);
+                vay_u_eval(qp, f, u, v);
+                for (int a = 0; a < 3; a++) { jd[a] = u[a].d; jd[3 + a] = v[a].d; }
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                double lu[3] = {l[0], l[1], l[2]}, lv[3] = {l[3], l[4], l[5]}, lf[6] = {0, 0, 0, 0, 0, 0};
+                vay_u_rev(qp, x, x + 6, lu, lv, lf);
+                for (int i = 0; i < 6; i++) jt[i] = lf[i];
+                for (int a = 0; a < 3; a++) jt[6 + a] = lu[a];
+            };
+            check("mixed vay", 9, 6, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- mixed J terms: inputs o[3], v[3] -> 12 contributions
+        {
+            const double qd = U(-2, 2);
+            double x0[6];
+            for (int a = 0; a < 3; a++) x0[a] = U(0.0, 1.0);
+            for (int a = 3; a < 6; a++) x0[a] = U(-0.5, 0.5);
+            auto fd = [&](const double *x, double *y) { jterms_m_eval(qd, x, x + 3, y); };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual o[3], vv[3], out[12];
+                for (int a = 0; a < 3; a++) { o[a] = mk(x[a], d[a]); vv[a] = mk(x[3 + a], d[3 + a]); }
+                jterms_m_eval(qd, o, vv, out);
+                for (int i = 0; i < 12; i++) jd[i] = out[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                for (int i = 0; i < 6; i++) jt[i] = 0.0;
+                jterms_m_rev(qd, x, x + 3, l, jt, jt + 3);
+            };
+            check("mixed jterms", 6, 12, x0, fd, fdual, frev, 1e-7);
         }
     }
     std::printf("%s (%d failures)\n", failures ? "FAILED" : "PASSED", failures);

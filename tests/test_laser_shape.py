@@ -371,3 +371,42 @@ def test_envelope_gradient_matches_central_differences(objective):
         lm = P.objective(th)
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[k]) <= FD_RTOL * abs(g[k]), (k, fd, g[k])
+
+
+# ---- the mixed-precision adjoint ----------------------------------------------
+
+MIXED_GRAD_RTOL = 2e-3  # mixed-form gradient against the FP64 form's (FP32 forward and adjoint)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("objective", ["field", "kinetic"])
+def test_mixed_adjoint_matches_fp64_gradient(objective):
+    """The mixed-precision run (FP32 state, checkpoints and adjoint) gives the
+    FP64 run's objective and envelope gradient to FP32 accuracy, and
+    recomputes every step's cells exactly."""
+    from apc_524_project_gb300.differentiate import Problem
+
+    cfg = _small_laser()
+    kw = dict(nsteps=30, slab=(8, 16), checkpoint_every=6, objective=objective, species=0)
+    f = Problem(cfg, **kw).gradient()
+    m = Problem(cfg, precision=abi.MIXED, **kw).gradient()
+    assert m["cell_mismatch"] == 0
+    assert abs(m["objective"] - f["objective"]) <= 1e-4 * abs(f["objective"])
+    gf, gm = f["grad_theta"], m["grad_theta"]
+    err = np.linalg.norm(gm - gf) / np.linalg.norm(gf)
+    assert err <= MIXED_GRAD_RTOL, (err, gf[:6], gm[:6])
+    vf, vm = f["grad_v"], m["grad_v"]
+    assert np.linalg.norm(vm - vf) / np.linalg.norm(vf) <= 10 * MIXED_GRAD_RTOL
+
+
+@pytest.mark.gpu
+def test_mixed_adjoint_checkpoint_spacing():
+    from apc_524_project_gb300.differentiate import Problem
+
+    cfg = _small_laser()
+    a = Problem(cfg, nsteps=30, slab=(8, 16), checkpoint_every=5, objective="kinetic", species=0,
+                precision=abi.MIXED).gradient()
+    b = Problem(cfg, nsteps=30, slab=(8, 16), checkpoint_every=30, objective="kinetic", species=0,
+                precision=abi.MIXED).gradient()
+    # same forward and reverse arithmetic; only the FP32 atomics' order differs
+    assert np.linalg.norm(a["grad_theta"] - b["grad_theta"]) <= 1e-4 * np.linalg.norm(b["grad_theta"])

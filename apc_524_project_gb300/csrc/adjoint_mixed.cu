@@ -16,8 +16,11 @@
 //
 // Before the first push the relativistic mixed state holds the loaded
 // velocity; the run first stores u = gamma v (the first push's own input), so
-// every step of the run is the same function. The velocity gradient is
-// d objective / d v with gamma held, gamma d objective / d u.
+// every step of the run is the same function. The run then sorts the store
+// by cell once (the deposit's run sums and the gather's locality depend on
+// it; the loop's periodic re-sorts are left out of the differentiated
+// steps). The velocity gradient is d objective / d v with gamma held,
+// gamma d objective / d u, returned in the store's order before the run.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -308,6 +311,10 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
     EMOO_TRY(mixed_ad_momentum_from_velocity(h));
     AdRunM R;
     R.h = h;
+    const int64_t np0 = h->np;
+    uint32_t *perm0 = (uint32_t *)R.alloc(sizeof(uint32_t) * (size_t)std::max<int64_t>(np0, 1));
+    if (!perm0) return EMOO_ERR_OOM;
+    EMOO_TRY(sort_with_permutation(h, perm0));
     R.np = h->np;
     R.npts = h->g.npts;
     ObjM os;
@@ -440,19 +447,26 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
             for (size_t k = 0; k < op.ks.size(); k++) grad_theta[op.ks[k]] += op.cs[k] * sums[2 * i + 1];
         }
     }
-    if (grad_v && R.np) {
-        // d objective / d v (gamma held) = gamma d objective / d u, gamma from the run's start
-        const MSnapView v0 = R.view(ck[0]);
-        std::vector<float> u(R.np), l(R.np);
-        std::vector<double> g2(R.np, 0.0);
-        const bool rel = h->info.relativity != 0;
-        for (int a = 0; a < 3; a++) {
-            EMOO_CUDA(cudaMemcpy(u.data(), v0.u[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
-            for (int64_t p = 0; p < R.np; p++) g2[p] += (double)u[p] * (double)u[p];
-        }
-        for (int a = 0; a < 3; a++) {
-            EMOO_CUDA(cudaMemcpy(l.data(), lu[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
-            for (int64_t p = 0; p < R.np; p++) grad_v[a * R.np + p] = (rel ? std::sqrt(1.0 + g2[p]) : 1.0) * l[p];
+    if (grad_v && np0) {
+        // d objective / d v (gamma held) = gamma d objective / d u, gamma from
+        // the run's start; particle i of the sorted store was perm0[i] before
+        for (int64_t k = 0; k < 3 * np0; k++) grad_v[k] = 0.0;
+        std::vector<uint32_t> perm(R.np);
+        if (R.np) {
+            EMOO_CUDA(cudaMemcpy(perm.data(), perm0, sizeof(uint32_t) * R.np, cudaMemcpyDeviceToHost));
+            const MSnapView v0 = R.view(ck[0]);
+            std::vector<float> u(R.np), l(R.np);
+            std::vector<double> g2(R.np, 0.0);
+            const bool rel = h->info.relativity != 0;
+            for (int a = 0; a < 3; a++) {
+                EMOO_CUDA(cudaMemcpy(u.data(), v0.u[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
+                for (int64_t p = 0; p < R.np; p++) g2[p] += (double)u[p] * (double)u[p];
+            }
+            for (int a = 0; a < 3; a++) {
+                EMOO_CUDA(cudaMemcpy(l.data(), lu[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
+                for (int64_t p = 0; p < R.np; p++)
+                    grad_v[a * np0 + perm[p]] = (rel ? std::sqrt(1.0 + g2[p]) : 1.0) * l[p];
+            }
         }
     }
     EMOO_TRY(R.restore(fin));

@@ -259,6 +259,20 @@ void pulse_derivs(const emoo_handle *h, int w, double t, double dt, double scale
 int emoo::light_planes_public(emoo_handle *h, int s, PlaneSet *ps) { return light_planes(h, s, ps, false); }
 
 namespace {
+int do_sort(emoo_handle *h);  // below
+}
+
+// Sorts the store by cell (dropping removed particles); perm_out (device,
+// the store's size before the call) receives perm[i] = the index before the
+// sort of the i-th particle after it.
+int emoo::sort_with_permutation(emoo_handle *h, uint32_t *perm_out) {
+    const int64_t n = h->np;
+    EMOO_TRY(do_sort(h));
+    if (n) EMOO_CUDA(cudaMemcpyAsync(perm_out, h->perm[0], sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, h->stream));
+    return EMOO_OK;
+}
+
+namespace {
 int execute_bc(emoo_handle *h, int send_id);  // below
 }
 

@@ -287,6 +287,7 @@ int prof_accumulate(emoo_handle *h);
 int ad_execute_bc(emoo_handle *h, int send_id);
 int ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops);
 int light_planes_public(emoo_handle *h, int s, PlaneSet *ps);
+int sort_with_permutation(emoo_handle *h, uint32_t *perm_out);
 
 }  // namespace emoo
 

@@ -283,16 +283,19 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
     return cfg, res
 
 
-def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_steps=64, ad_every=8):
+def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
     """The laser-plasma workload at full size (512 x 128^2 cells, 117,440,512
     electrons, shaped pulse, absorbing x walls, sort every 20 steps): loop
-    throughput of the mixed and FP64 forms, and the FP64 adjoint of the named
-    objective (electron kinetic energy at x in [448, 512)) with respect to the
-    16 envelope coefficients over the first ad_steps steps, checkpoints every
-    ad_every steps (FP64 snapshots take 7.2 GB each; the full 512 steps with
-    sqrt(N) checkpoints would need 46 of them)."""
+    throughput of the mixed and FP64 forms, and the mixed-precision adjoint
+    of the named objective (electron kinetic energy at x in [448, 512) after
+    512 steps) with respect to the 16 envelope coefficients, checkpoints
+    every 23 steps (sqrt(512); 47 mixed snapshots of 3.6 GB). Check: on the
+    workload scaled to 40 x 16^2 cells (30 steps, objective x in [8, 16)),
+    the mixed adjoint's derivative for envelope coefficient 1 against a
+    central difference of two FP64 primal runs."""
     import torch
     from apc_524_project_gb300 import abi, configs
+    from apc_524_project_gb300.differentiate import Problem
 
     L = abi.lib()
     cfg = configs.laser512()
@@ -312,19 +315,38 @@ def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_steps=64, ad_every
         abi.check(L.emoo_destroy(h))
         torch.cuda.synchronize()
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    h = _make_handle(cfg, abi.FP64, N, device)
+    h = _make_handle(cfg, abi.MIXED, N, device)
     nth = L.emoo_ad_nparams(h)
-    spec = abi.AdSpec(ad_steps, ad_every, 448, 512, abi.AD_OBJ_KINETIC, 0)
+    spec = abi.AdSpec(cfg.steps, ad_every, 448, 512, abi.AD_OBJ_KINETIC, 0)
     res = abi.AdResult()
     g = (C.c_double * nth)()
     abi.check(L.emoo_ad_run(h, C.byref(spec), abi.AD_ADJOINT, None, None, C.byref(res), g, None), "emoo_ad_run")
+    st = abi.Stats()
+    abi.check(L.emoo_get_stats(h, C.byref(st)), "emoo_get_stats")
     abi.check(L.emoo_destroy(h))
     coef = list(g)[2:]
-    out["adjoint"] = {"form": "FP64", "steps": ad_steps, "checkpoint_every": ad_every,
+    small = configs.laser512(n=(40, 16, 16), steps=30, ppc=2, wavelength=8.0, fwhm_steps=6, waist=5.0,
+                             plasma_x0=8.0, vth=0.02, seed=11)
+    kw = dict(nsteps=30, slab=(8, 16), checkpoint_every=6, objective="kinetic", species=0)
+    gm = Problem(small, precision=abi.MIXED, **kw).gradient()["grad_theta"]
+    P = Problem(small, **kw)
+    k = 2  # envelope coefficient 1
+    hstep = 1e-6
+    th = P.theta0.copy()
+    th[k] += hstep
+    lp = P.objective(th)
+    th[k] -= 2 * hstep
+    lm = P.objective(th)
+    fd = (lp - lm) / (2 * hstep)
+    out["adjoint"] = {"form": "mixed", "steps": cfg.steps, "checkpoint_every": ad_every,
                       "objective": "electron kinetic energy, x in [448, 512)", "value": res.objective,
                       "forward_ms": res.forward_ms, "recompute_ms": res.recompute_ms, "reverse_ms": res.reverse_ms,
                       "adjoint_over_forward": (res.recompute_ms + res.reverse_ms) / res.forward_ms,
-                      "max_abs_coef_gradient": max(abs(v) for v in coef)}
+                      "max_abs_coef_gradient": max(abs(v) for v in coef), "cell_mismatch": st.ad_cell_mismatch,
+                      "fd_check": {"case": "laser-plasma 40x16x16, 2 ppc, 30 steps, kinetic energy x in [8, 16), "
+                                           "d objective / d envelope coefficient 1",
+                                   "mixed_adjoint": float(gm[k]), "fp64_central_difference": fd,
+                                   "rel_err": abs(fd - gm[k]) / abs(fd)}}
     return out
 
 

@@ -28,6 +28,13 @@
 #else
 #define AD_HD inline
 #endif
+// full unrolling of the 3- and 6-long loops on the device (their index
+// arithmetic then folds into register names instead of local arrays)
+#if defined(__CUDA_ARCH__)
+#define AD_UNROLL _Pragma("unroll")
+#else
+#define AD_UNROLL
+#endif
 
 namespace emoo {
 namespace ad {

@@ -22,12 +22,33 @@ namespace ad {
 
 AD_HD float sqrt_(float a) { return ::sqrtf(a); }
 
+// 1 / x and 1 / sqrt(x): the hardware approximations for float on the device
+// (relative error a few 2^-24, the mixed form's own accuracy), exact
+// arithmetic for double and on the host.
+AD_HD float rcp_(float x) {
+#if defined(__CUDA_ARCH__)
+    return __fdividef(1.0f, x);
+#else
+    return 1.0f / x;
+#endif
+}
+AD_HD float rsq_(float x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrtf(x);
+#else
+    return 1.0f / ::sqrtf(x);
+#endif
+}
+AD_HD double rcp_(double x) { return 1.0 / x; }
+AD_HD double rsq_(double x) { return 1.0 / ::sqrt(x); }
+
 // ---- gather from the pack ------------------------------------------------
 //
 // pk[18]: Ex (c0 ct cr ctr; t = y, r = z), Ey (t = z, r = x), Ez (t = x,
 // r = y), then Bx (d0 d1), By (d0 d1), Bz (d0 d1). o: in-cell offsets.
 template <class T, class P>
 AD_HD void gather_m_eval(const P pk[18], const T o[3], T f[6]) {
+    AD_UNROLL
     for (int i = 0; i < 3; i++) {
         const T &t = o[(i + 1) % 3], &r = o[(i + 2) % 3];
         f[i] = t * (r * pk[4 * i + 3] + pk[4 * i + 1]) + (r * pk[4 * i + 2] + pk[4 * i]);
@@ -38,6 +59,7 @@ AD_HD void gather_m_eval(const P pk[18], const T o[3], T f[6]) {
 // Adjoint with respect to the offsets: lo += (df/do)^T lf.
 template <class R>
 AD_HD void gather_m_rev_offsets(const R pk[18], const R o[3], const R lf[6], R lo[3]) {
+    AD_UNROLL
     for (int i = 0; i < 3; i++) {
         const int jt = (i + 1) % 3, jr = (i + 2) % 3;
         lo[jt] += lf[i] * (pk[4 * i + 1] + pk[4 * i + 3] * o[jr]);
@@ -53,10 +75,12 @@ AD_HD void gather_m_rev_offsets(const R pk[18], const R o[3], const R lf[6], R l
 template <class R>
 AD_HD void gather_m_weights(const R o[3], R we[12], R wb[6]) {
     R a[3], b[3];
+    AD_UNROLL
     for (int k = 0; k < 3; k++) {
         a[k] = R(2) - o[k];
         b[k] = o[k] - R(1);
     }
+    AD_UNROLL
     for (int i = 0; i < 3; i++) {
         const int jt = (i + 1) % 3, jr = (i + 2) % 3;
         we[4 * i] = a[jt] * a[jr];
@@ -78,6 +102,7 @@ AD_HD void vay_u_eval(double qp, const T f[6], T u[3], T v[3]) {
     const T bx = f[3], by = f[4], bz = f[5];
     const T vxb[3] = {v0[1] * bz - v0[2] * by, v0[2] * bx - v0[0] * bz, v0[0] * by - v0[1] * bx};
     T up[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) up[a] = u[a] + qp * (f[a] + vxb[a]) + qp * f[a];
     const T gps = 1.0 + up[0] * up[0] + up[1] * up[1] + up[2] * up[2];
     const T tau[3] = {qp * bx, qp * by, qp * bz};
@@ -89,6 +114,7 @@ AD_HD void vay_u_eval(double qp, const T f[6], T u[3], T v[3]) {
     const T s = 1.0 / (1.0 + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
     const T ud = ust / gi;
     const T c[3] = {up[1] * t[2] - up[2] * t[1], up[2] * t[0] - up[0] * t[2], up[0] * t[1] - up[1] * t[0]};
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         u[a] = s * (up[a] + ud * t[a] + c[a]);
         v[a] = u[a] / gi;
@@ -100,72 +126,90 @@ AD_HD void vay_u_eval(double qp, const T f[6], T u[3], T v[3]) {
 template <class R>
 AD_HD void vay_u_rev(R qp, const R f[6], const R u_in[3], R lu[3], const R lv[3], R lf[6]) {
     const R e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
-    const R g0 = sqrt_(R(1) + u_in[0] * u_in[0] + u_in[1] * u_in[1] + u_in[2] * u_in[2]);
+    const R ig0 = rsq_(R(1) + u_in[0] * u_in[0] + u_in[1] * u_in[1] + u_in[2] * u_in[2]);  // 1 / gamma_in
     R v0[3], vxb[3], up[3], tau[3];
-    for (int a = 0; a < 3; a++) v0[a] = u_in[a] / g0;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) v0[a] = u_in[a] * ig0;
     cross3t(v0, b, vxb);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) up[a] = u_in[a] + qp * (e[a] + vxb[a]) + qp * e[a];
     const R gps = R(1) + up[0] * up[0] + up[1] * up[1] + up[2] * up[2];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) tau[a] = qp * b[a];
     const R tau2 = tau[0] * tau[0] + tau[1] * tau[1] + tau[2] * tau[2];
     const R sigma = gps - tau2;
     const R ust = up[0] * tau[0] + up[1] * tau[1] + up[2] * tau[2];
-    const R g1 = sqrt_(sigma * sigma + R(4) * (tau2 + ust * ust));
-    const R gi = sqrt_(R(0.5) * (sigma + g1));
+    const R rad = sigma * sigma + R(4) * (tau2 + ust * ust);
+    const R ig1 = rsq_(rad), g1 = rad * ig1;
+    const R hg = R(0.5) * (sigma + g1);
+    const R igi = rsq_(hg);  // 1 / gamma'
     R t[3];
-    for (int a = 0; a < 3; a++) t[a] = tau[a] / gi;
-    const R s = R(1) / (R(1) + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
-    const R ud = ust / gi;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) t[a] = tau[a] * igi;
+    const R s = rcp_(R(1) + t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    const R ud = ust * igi;
     R c[3], w[3], uo[3];
     cross3t(up, t, c);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         w[a] = up[a] + ud * t[a] + c[a];
         uo[a] = s * w[a];
     }
     // v' = u' / gi
     R luo[3];
-    for (int a = 0; a < 3; a++) luo[a] = lu[a] + lv[a] / gi;
-    R lgi = -(uo[0] * lv[0] + uo[1] * lv[1] + uo[2] * lv[2]) / (gi * gi);
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) luo[a] = lu[a] + lv[a] * igi;
+    R lgi = -(uo[0] * lv[0] + uo[1] * lv[1] + uo[2] * lv[2]) * (igi * igi);
     // u' = s w
     const R ls = w[0] * luo[0] + w[1] * luo[1] + w[2] * luo[2];
     R lw[3], lup[3], lt[3], tmp[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lw[a] = s * luo[a];
     // w = up + ud t + up x t
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lup[a] = lw[a];
     cross3t(t, lw, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lup[a] += tmp[a];
     const R lud = t[0] * lw[0] + t[1] * lw[1] + t[2] * lw[2];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lt[a] = ud * lw[a];
     cross3t(lw, up, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lt[a] += tmp[a];
     // ud = ust / gi
-    R lust = lud / gi;
-    lgi += -ud * lud / gi;
+    R lust = lud * igi;
+    lgi += -ud * lud * igi;
     // s = 1 / (1 + t.t)
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lt[a] += R(-2) * s * s * ls * t[a];
     // t = tau / gi
     R ltau[3];
-    for (int a = 0; a < 3; a++) ltau[a] = lt[a] / gi;
-    lgi += -(t[0] * lt[0] + t[1] * lt[1] + t[2] * lt[2]) / gi;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) ltau[a] = lt[a] * igi;
+    lgi += -(t[0] * lt[0] + t[1] * lt[1] + t[2] * lt[2]) * igi;
     // gi = sqrt(0.5 (sigma + g1)), g1 = sqrt(sigma^2 + 4 tau2 + 4 ust^2)
-    R lsigma = R(0.25) * lgi / gi;
-    const R lg1 = R(0.25) * lgi / gi;
-    lsigma += lg1 * sigma / g1;
-    R ltau2 = R(2) * lg1 / g1;
-    lust += R(4) * ust * lg1 / g1;
+    R lsigma = R(0.25) * lgi * igi;
+    const R lg1 = R(0.25) * lgi * igi;
+    lsigma += lg1 * sigma * ig1;
+    R ltau2 = R(2) * lg1 * ig1;
+    lust += R(4) * ust * lg1 * ig1;
     // ust = up . tau
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         lup[a] += tau[a] * lust;
         ltau[a] += up[a] * lust;
     }
     // sigma = gps - tau2; tau2 = tau.tau; gps = 1 + up.up
     ltau2 -= lsigma;
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         ltau[a] += R(2) * tau[a] * ltau2;
         lup[a] += R(2) * up[a] * lsigma;
     }
     // up = u + qp (e + v0 x b) + qp e; tau = qp b
     R lvxb[3], lv0[3], lb[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         lvxb[a] = qp * lup[a];
         lb[a] = qp * ltau[a];
@@ -173,10 +217,14 @@ AD_HD void vay_u_rev(R qp, const R f[6], const R u_in[3], R lu[3], const R lv[3]
     }
     cross3t(b, lvxb, lv0);
     cross3t(lvxb, v0, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lb[a] += tmp[a];
     // v0 = u / g0, g0 = sqrt(1 + u.u)
     const R uv = u_in[0] * lv0[0] + u_in[1] * lv0[1] + u_in[2] * lv0[2];
-    for (int a = 0; a < 3; a++) lu[a] = lup[a] + lv0[a] / g0 - u_in[a] * uv / (g0 * g0 * g0);
+    const R ig03 = ig0 * ig0 * ig0;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) lu[a] = lup[a] + lv0[a] * ig0 - u_in[a] * uv * ig03;
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lf[3 + a] += lb[a];
 }
 
@@ -186,6 +234,7 @@ AD_HD void vay_u_rev(R qp, const R f[6], const R u_in[3], R lu[3], const R lv[3]
 // k = i + 2 (mod 3), a = 2 - o, b = o - 1.
 template <class T>
 AD_HD void jterms_m_eval(double qd, const T o[3], const T v[3], T out[12]) {
+    AD_UNROLL
     for (int i = 0; i < 3; i++) {
         const int j = (i + 1) % 3, k = (i + 2) % 3;
         const T J = qd * v[i];
@@ -200,6 +249,7 @@ AD_HD void jterms_m_eval(double qd, const T o[3], const T v[3], T out[12]) {
 // Adjoint of jterms_m_eval: adds to lo[3] and lv[3].
 template <class R>
 AD_HD void jterms_m_rev(R qd, const R o[3], const R v[3], const R l[12], R lo[3], R lv[3]) {
+    AD_UNROLL
     for (int i = 0; i < 3; i++) {
         const int j = (i + 1) % 3, k = (i + 2) % 3;
         const R J = qd * v[i];

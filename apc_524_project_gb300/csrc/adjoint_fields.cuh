@@ -35,16 +35,28 @@ __device__ __forceinline__ bool phys(const Geom &g, int i, int j, int k) {
     return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];
 }
 
+// The stencil coefficients dt / d (and -4 pi dt), computed once on the host:
+// per-thread FP64 divisions would run on this GPU's narrow FP64 pipe.
+template <class R>
+struct YeeCoef {
+    R cx, cy, cz, cj;
+};
+
+template <class R>
+YeeCoef<R> yee_coef(const Geom &g, double dt) {
+    return YeeCoef<R>{(R)(dt / g.d[0]), (R)(dt / g.d[1]), (R)(dt / g.d[2]), (R)(-FOURPI * dt)};
+}
+
 // Adjoint of the B update (B = T + dt curl E over the physical points),
 // gather form over every grid point: LT += LB (physical), LE += dt C_E^T LB.
 template <class R>
-__global__ void k_yee_b_adj(Geom g, double dt, FOutT<R> A) {
+__global__ void k_yee_b_adj(Geom g, YeeCoef<R> yc, FOutT<R> A) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
     const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
-    const R cx = (R)(dt / g.d[0]), cy = (R)(dt / g.d[1]), cz = (R)(dt / g.d[2]);
+    const R cx = yc.cx, cy = yc.cy, cz = yc.cz;
     const bool here = phys(g, i, j, k);
     if (here)
         for (int c = 0; c < 3; c++) A.T[c][p] += A.B[c][p];
@@ -72,14 +84,13 @@ __global__ void k_yee_b_adj(Geom g, double dt, FOutT<R> A) {
 // the B role was overwritten by the step, so its physical points' adjoint is
 // cleared.
 template <class R>
-__global__ void k_yee_e_adj(Geom g, double dt, FOutT<R> A, JPtrsT<R> LJ) {
+__global__ void k_yee_e_adj(Geom g, YeeCoef<R> yc, FOutT<R> A, JPtrsT<R> LJ) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
     if (k >= g.tot[2] || j >= g.tot[1] || i >= g.tot[0]) return;
     const int64_t p = gidx(g, i, j, k), sx = g.sx, sy = g.sy;
-    const R cx = (R)(dt / g.d[0]), cy = (R)(dt / g.d[1]), cz = (R)(dt / g.d[2]);
-    const R cj = (R)(-FOURPI * dt);
+    const R cx = yc.cx, cy = yc.cy, cz = yc.cz, cj = yc.cj;
     const bool here = phys(g, i, j, k);
     const R *Ex = A.E[0], *Ey = A.E[1], *Ez = A.E[2];
     for (int c = 0; c < 3; c++) LJ.J[c][p] = here ? cj * A.E[c][p] : (R)0;
@@ -144,15 +155,19 @@ __global__ void k_ghost_adj(Geom g, Slots6T<R> fl, int d, int side) {
 
 // Adjoint of a plane set v + vs t1[p] t2[q]: the plane's values depend only
 // on the wave parameters, so the step needs sum(LF) and sum(LF t1 t2) over
-// the plane (one block, fixed order, FP64 sums); the host turns them into
-// the parameter gradient. The plane's adjoint is cleared.
+// the plane; the host turns them into the parameter gradient. Block b of the
+// PLANE_BLOCKS launched writes its partial pair to sums2[2 b], sums2[2 b + 1]
+// (FP64, fixed order within the block; the host adds the blocks in order).
+// The plane's adjoint is cleared.
+constexpr int PLANE_BLOCKS = 64;
+
 template <class R>
 __global__ void k_plane_adj(Geom g, R *F, int d, int idx, const double *t1, const double *t2, double *sums2) {
     __shared__ double s_u[32], s_s[32];
     const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
     double su = 0.0, ss = 0.0;
     const int64_t m = (int64_t)g.tot[o1] * g.tot[o2];
-    for (int64_t t = threadIdx.x; t < m; t += blockDim.x) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
         int c[3];
         c[d] = idx;
         c[o1] = (int)(t / g.tot[o2]);
@@ -179,8 +194,8 @@ __global__ void k_plane_adj(Geom g, R *F, int d, int idx, const double *t1, cons
             a += s_u[i];
             b += s_s[i];
         }
-        sums2[0] = a;
-        sums2[1] = b;
+        sums2[2 * blockIdx.x] = a;
+        sums2[2 * blockIdx.x + 1] = b;
     }
 }
 

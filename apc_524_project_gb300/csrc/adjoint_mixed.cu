@@ -270,10 +270,11 @@ int adj_step_m(emoo_handle *h, AdRunM &R, const MSnap &S, const int32_t *cell_af
             }
         } else {
             if (pl.ops.size() >= pl.cap) return EMOO_ERR_STATE;
-            double *sums = pl.sums + 2 * pl.ops.size();
+            double *sums = pl.sums + 2 * adf::PLANE_BLOCKS * pl.ops.size();
             pl.ops.push_back(op);
             h->launches++;
-            adf::k_plane_adj<float><<<1, 256, 0, h->stream>>>(g, lslot[op.slot], op.dim, op.idx, op.t1, op.t2, sums);
+            adf::k_plane_adj<float><<<adf::PLANE_BLOCKS, 256, 0, h->stream>>>(g, lslot[op.slot], op.dim, op.idx, op.t1,
+                                                                              op.t2, sums);
         }
     }
     EMOO_CUDA(cudaGetLastError());
@@ -281,8 +282,9 @@ int adj_step_m(emoo_handle *h, AdRunM &R, const MSnap &S, const int32_t *cell_af
     JPtrsF LJ{{lslot[EMOO_JX], lslot[EMOO_JY], lslot[EMOO_JZ]}};
     dim3 blk(32, 8);
     h->launches += 2;
-    adf::k_yee_b_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, h->dtp, A);
-    adf::k_yee_e_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, h->dtp, A, LJ);
+    const adf::YeeCoef<float> yc = adf::yee_coef<float>(g, h->dtp);
+    adf::k_yee_b_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, yc, A);
+    adf::k_yee_e_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, yc, A, LJ);
     for (int d = 2; d >= 0; d--) {
         if (h->bc.fbc[2 * d] != FBC_PERIODIC) continue;
         const int f0 = (d == 0) ? EMOO_JY : EMOO_JX;
@@ -402,7 +404,8 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
         size_t per = 0;
         for (const AdBcOp &op : ops) per += op.kind == 1;
         pl.cap = per * (size_t)N;
-        if (pl.cap && !(pl.sums = (double *)R.alloc(sizeof(double) * 2 * pl.cap))) return EMOO_ERR_OOM;
+        if (pl.cap && !(pl.sums = (double *)R.alloc(sizeof(double) * 2 * adf::PLANE_BLOCKS * pl.cap)))
+            return EMOO_ERR_OOM;
         pl.ops.reserve(pl.cap);
     }
     std::vector<MSnap> tape(std::min(K, std::max(N, 1)));
@@ -437,14 +440,19 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
         h->ad_cell_mismatch = (int64_t)m;
     }
     if (grad_theta && ntheta) {
-        std::vector<double> sums(2 * pl.ops.size());
-        if (!sums.empty())
-            EMOO_CUDA(cudaMemcpy(sums.data(), pl.sums, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost));
+        std::vector<double> part(2 * adf::PLANE_BLOCKS * pl.ops.size());
+        if (!part.empty())
+            EMOO_CUDA(cudaMemcpy(part.data(), pl.sums, sizeof(double) * part.size(), cudaMemcpyDeviceToHost));
         for (int k = 0; k < ntheta; k++) grad_theta[k] = 0.0;
         for (size_t i = 0; i < pl.ops.size(); i++) {
             const AdBcOp &op = pl.ops[i];
-            for (size_t k = 0; k < op.ku.size(); k++) grad_theta[op.ku[k]] += op.cu[k] * sums[2 * i];
-            for (size_t k = 0; k < op.ks.size(); k++) grad_theta[op.ks[k]] += op.cs[k] * sums[2 * i + 1];
+            double su = 0.0, ss = 0.0;
+            for (int b = 0; b < adf::PLANE_BLOCKS; b++) {
+                su += part[2 * (adf::PLANE_BLOCKS * i + b)];
+                ss += part[2 * (adf::PLANE_BLOCKS * i + b) + 1];
+            }
+            for (size_t k = 0; k < op.ku.size(); k++) grad_theta[op.ku[k]] += op.cu[k] * su;
+            for (size_t k = 0; k < op.ks.size(); k++) grad_theta[op.ks[k]] += op.cs[k] * ss;
         }
     }
     if (grad_v && np0) {

@@ -1008,111 +1008,189 @@ struct MSnapC {
     const float *o[3], *u[3];
 };
 
+// Grid point, relative to the cell, of each of the 18 gather inputs in the
+// order of gather_m_weights: Ex F00 F10 F11 F01 over (y, z), Ey over (z, x),
+// Ez over (x, y), then the two faces of Bx, By, Bz; 3 bits each (x 4, y 2,
+// z 1), input k at bits 3k..3k+2.
+constexpr unsigned long long GATHER_CODE =
+    (0ull << 0) | (2ull << 3) | (3ull << 6) | (1ull << 9) |       // Ex: o, o+sy, o+sy+1, o+1
+    (0ull << 12) | (1ull << 15) | (5ull << 18) | (4ull << 21) |   // Ey: o, o+1, o+sx+1, o+sx
+    (0ull << 24) | (4ull << 27) | (6ull << 30) | (2ull << 33) |   // Ez: o, o+sx, o+sx+sy, o+sy
+    (0ull << 36) | (4ull << 39) | (0ull << 42) | (2ull << 45) |   // Bx: o, o+sx; By: o, o+sy
+    (0ull << 48) | (1ull << 51);                                  // Bz: o, o+1
+
+__device__ __forceinline__ int gather_offset(int k, int sx, int sy) {
+    const int c = (int)((GATHER_CODE >> (3 * k)) & 7ull);
+    return (c >> 2) * sx + ((c >> 1) & 1) * sy + (c & 1);
+}
+
+constexpr int ADJ_BLOCK = 256;
+constexpr int ADJ_WARPS = ADJ_BLOCK / 32;
+constexpr int GATHER_IN = 18;
+
 template <bool REL>
-__global__ void k_adj_particles_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MSnapC S,
-                                  const int32_t *cell_after, int64_t np, float q0, MAdjState L, MAdjJ LJ,
-                                  MAdjFields LF, unsigned long long *mismatch) {
+__global__ void __launch_bounds__(ADJ_BLOCK)
+    k_adj_particles_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MSnapC S,
+                      const int32_t *cell_after, int64_t np, float q0, MAdjState L, MAdjJ LJ, MAdjFields LF,
+                      unsigned long long *mismatch) {
+    // per warp: the 18 gather-input adjoints of each lane's particle (a
+    // column each), reduced over runs of equal cells before the atomics
+    __shared__ float s_g[ADJ_WARPS][GATHER_IN * DEP_STRIDE];
+    __shared__ int s_c[ADJ_WARPS][32];
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= np) return;
-    const int32_t c = S.cell[p];
-    if (c < 0) return;  // removed before the step: its adjoint stays 0
-    const int s = species_of_m(st, p);
-    const float o_in[3] = {S.o[0][p], S.o[1][p], S.o[2][p]};
-    const float u_in[3] = {S.u[0][p], S.u[1][p], S.u[2][p]};
-    int ic[3];
-    split_cell(g, dv, c, ic[0], ic[1], ic[2]);
-    const float4 *pk = pack + (int64_t)c * PACK_F4;
-    float f[6];
-    gather_pack(pk, o_in[0], o_in[1], o_in[2], f);
-    float u[3] = {u_in[0], u_in[1], u_in[2]}, v[3];
-    push_m<REL, false>(f, st.qp[s], nullptr, p, u[0], u[1], u[2], v[0], v[1], v[2]);
-    float o[3];
-    int ii[3] = {ic[0], ic[1], ic[2]};
-    for (int a = 0; a < 3; a++) cell_step(o_in[a] + v[a] * g.dtid[a], ii[a], o[a]);
-    // bit a: axis a reflected (u, v -> -u, -v); bit 3 + a: its offset mapped
-    // to 1 - o (axis_bc keeps an offset of exactly 0)
-    int mask = 0, flip = 0;
-    for (int a = 0; a < 3; a++) {
-        if (mask & 64) break;
-        const float o_pre = o[a];
-        const int m = axis_bc(bc, a, g.n[a], ii[a], o[a], u[a], v[a]);
-        const int side = ((m >> (2 * a + 1)) & 1) ? 2 * a + 1 : 2 * a;
-        if ((m & 63) && !(m & 64) && bc.pbc[side] == PBC_REFLECTING) {
-            flip |= 1 << a;
-            if (o_pre != 0.0f) flip |= 8 << a;
-        }
-        mask |= m;
-    }
-    if (mask & 64) {  // removed in this step: nothing after it depends on the particle
-        for (int a = 0; a < 3; a++) {
-            L.o[a][p] = 0.0f;
-            L.u[a][p] = 0.0f;
-        }
-        return;
-    }
-    const int32_t onew = ii[0] * (int)g.sx + ii[1] * (int)g.sy + ii[2];
-    if (cell_after && cell_after[p] != onew) atomicAdd(mismatch, 1ull);
-    float lo[3], lu[3], lv[3] = {0.0f, 0.0f, 0.0f};
-    for (int a = 0; a < 3; a++) {
-        lo[a] = L.o[a][p];
-        lu[a] = L.u[a][p];
-    }
-    if (st.deposit[s]) {
-        float l12[12];
-#pragma unroll
-        for (int q = 0; q < 12; q++) l12[q] = q0 * LJ.J[q >> 2][onew + dep_offset(q, (int)g.sx, (int)g.sy)];
-        ad::jterms_m_rev(st.qdep[s], o, v, l12, lo, lv);
-    }
-    // boundaries: a reflection maps u -> -u, v -> -v and o -> 1 - o
-    for (int a = 0; a < 3; a++) {
-        if (!(flip & (1 << a))) continue;
-        lu[a] = -lu[a];
-        lv[a] = -lv[a];
-        if (flip & (8 << a)) lo[a] = -lo[a];
-    }
-    // offset update o' = o + v dt / d (cell held)
-    for (int a = 0; a < 3; a++) lv[a] += lo[a] * g.dtid[a];
+    const int lane = threadIdx.x & 31;
+    float *col = s_g[threadIdx.x >> 5];
+    int *keys = s_c[threadIdx.x >> 5];
+    int32_t c = -1;
     float lf[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (REL) {
-        ad::vay_u_rev(st.qp[s], f, u_in, lu, lv, lf);
-    } else {
-        float lx[3] = {0.0f, 0.0f, 0.0f}, lvb[3] = {lu[0] + lv[0], lu[1] + lv[1], lu[2] + lv[2]};
-        ad::boris_rev(st.qp[s], f, 0.0f, u_in, lx, lvb, lf);
-        for (int a = 0; a < 3; a++) lu[a] = lvb[a];
-    }
-    // gather: offsets through the pack polynomial, fields through the weights
-    float pkf[18];
-    {
-        const float4 ex = pk[0], ey = pk[1], ez = pk[2], bxy = pk[3], bz = pk[4];
-        const float t[18] = {ex.x, ex.y, ex.z, ex.w, ey.x, ey.y, ey.z, ey.w, ez.x, ez.y, ez.z, ez.w,
-                             bxy.x, bxy.y, bxy.z, bxy.w, bz.x, bz.y};
+    float o_in[3] = {0.0f, 0.0f, 0.0f};
+    if (p < np) c = S.cell[p];
+    bool zero = false;
+    if (c >= 0 && cell_after) {
+        // every adjoint this particle's step reads is 0 (its offsets and
+        // momenta after the step, the current adjoint where it deposited):
+        // then so are all it writes, and the recorded cell after the step
+        // locates the deposit without recomputing it
+        const int32_t ca = cell_after[p];
+        zero = ca >= 0;
+        if (zero) {
 #pragma unroll
-        for (int k = 0; k < 18; k++) pkf[k] = t[k];
-    }
-    ad::gather_m_rev_offsets(pkf, o_in, lf, lo);
-    float we[12], wb[6];
-    ad::gather_m_weights(o_in, we, wb);
-    const int64_t sx = g.sx, sy = g.sy, o0 = c;
-    const int64_t pe[12] = {o0, o0 + sy, o0 + sy + 1, o0 + 1,        // Ex: F00 F10 F11 F01 over (y, z)
-                            o0, o0 + 1, o0 + sx + 1, o0 + sx,        // Ey over (z, x)
-                            o0, o0 + sx, o0 + sx + sy, o0 + sy};     // Ez over (x, y)
-    const int64_t pb[6] = {o0, o0 + sx, o0, o0 + sy, o0, o0 + 1};
+            for (int a = 0; a < 3; a++) zero = zero && L.o[a][p] == 0.0f && L.u[a][p] == 0.0f;
+        }
+        if (zero && st.deposit[species_of_m(st, p)]) {
 #pragma unroll
-    for (int k = 0; k < 12; k++) {
-        const float l = we[k] * lf[k >> 2];
-        if (l != 0.0f) atomicAdd(LF.E[k >> 2] + pe[k], l);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const float l = wb[k] * lf[3 + (k >> 1)];
-        if (l != 0.0f) {
-            atomicAdd(LF.B[k >> 1] + pb[k], l);
-            atomicAdd(LF.T[k >> 1] + pb[k], l);
+            for (int q = 0; q < 12; q++)
+                zero = zero && LJ.J[q >> 2][ca + dep_offset(q, (int)g.sx, (int)g.sy)] == 0.0f;
         }
     }
-    for (int a = 0; a < 3; a++) {
-        L.o[a][p] = lo[a];
-        L.u[a][p] = lu[a];
+    if (c >= 0 && !zero) {
+        const int s = species_of_m(st, p);
+        o_in[0] = S.o[0][p];
+        o_in[1] = S.o[1][p];
+        o_in[2] = S.o[2][p];
+        const float u_in[3] = {S.u[0][p], S.u[1][p], S.u[2][p]};
+        int ic[3];
+        split_cell(g, dv, c, ic[0], ic[1], ic[2]);
+        const float4 *pk = pack + (int64_t)c * PACK_F4;
+        float f[6];
+        gather_pack(pk, o_in[0], o_in[1], o_in[2], f);
+        float u[3] = {u_in[0], u_in[1], u_in[2]}, v[3];
+        push_m<REL, false>(f, st.qp[s], nullptr, p, u[0], u[1], u[2], v[0], v[1], v[2]);
+        float o[3];
+        int ii[3] = {ic[0], ic[1], ic[2]};
+#pragma unroll
+        for (int a = 0; a < 3; a++) cell_step(o_in[a] + v[a] * g.dtid[a], ii[a], o[a]);
+        // bit a: axis a reflected (u, v -> -u, -v); bit 3 + a: its offset mapped
+        // to 1 - o (axis_bc keeps an offset of exactly 0)
+        int mask = 0, flip = 0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (mask & 64) break;
+            const float o_pre = o[a];
+            const int m = axis_bc(bc, a, g.n[a], ii[a], o[a], u[a], v[a]);
+            // static indices into the parameter (a dynamic one copies it to local memory)
+            const int kind = ((m >> (2 * a + 1)) & 1) ? bc.pbc[2 * a + 1] : bc.pbc[2 * a];
+            if ((m & 63) && !(m & 64) && kind == PBC_REFLECTING) {
+                flip |= 1 << a;
+                if (o_pre != 0.0f) flip |= 8 << a;
+            }
+            mask |= m;
+        }
+        float lo[3] = {0.0f, 0.0f, 0.0f}, lu[3] = {0.0f, 0.0f, 0.0f};
+        if (!(mask & 64)) {  // a particle removed in this step leaves nothing after it
+            const int32_t onew = ii[0] * (int)g.sx + ii[1] * (int)g.sy + ii[2];
+            if (cell_after && cell_after[p] != onew) atomicAdd(mismatch, 1ull);
+            float lv[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                lo[a] = L.o[a][p];
+                lu[a] = L.u[a][p];
+            }
+            if (st.deposit[s]) {
+                float l12[12];
+#pragma unroll
+                for (int q = 0; q < 12; q++)
+                    l12[q] = q0 * LJ.J[q >> 2][onew + dep_offset(q, (int)g.sx, (int)g.sy)];
+                ad::jterms_m_rev(st.qdep[s], o, v, l12, lo, lv);
+            }
+            // boundaries: a reflection maps u -> -u, v -> -v and o -> 1 - o
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (!(flip & (1 << a))) continue;
+                lu[a] = -lu[a];
+                lv[a] = -lv[a];
+                if (flip & (8 << a)) lo[a] = -lo[a];
+            }
+            // offset update o' = o + v dt / d (cell held)
+#pragma unroll
+            for (int a = 0; a < 3; a++) lv[a] += lo[a] * g.dtid[a];
+            if (REL) {
+                ad::vay_u_rev(st.qp[s], f, u_in, lu, lv, lf);
+            } else {
+                float lx[3] = {0.0f, 0.0f, 0.0f}, lvb[3] = {lu[0] + lv[0], lu[1] + lv[1], lu[2] + lv[2]};
+                ad::boris_rev(st.qp[s], f, 0.0f, u_in, lx, lvb, lf);
+#pragma unroll
+                for (int a = 0; a < 3; a++) lu[a] = lvb[a];
+            }
+            // gather: the offsets through the pack polynomial
+            float pkf[18];
+            {
+                const float4 ex = pk[0], ey = pk[1], ez = pk[2], bxy = pk[3], bz = pk[4];
+                pkf[0] = ex.x; pkf[1] = ex.y; pkf[2] = ex.z; pkf[3] = ex.w;
+                pkf[4] = ey.x; pkf[5] = ey.y; pkf[6] = ey.z; pkf[7] = ey.w;
+                pkf[8] = ez.x; pkf[9] = ez.y; pkf[10] = ez.z; pkf[11] = ez.w;
+                pkf[12] = bxy.x; pkf[13] = bxy.y; pkf[14] = bxy.z; pkf[15] = bxy.w;
+                pkf[16] = bz.x; pkf[17] = bz.y;
+            }
+            ad::gather_m_rev_offsets(pkf, o_in, lf, lo);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            L.o[a][p] = lo[a];
+            L.u[a][p] = lu[a];
+        }
+    }
+    // the fields through the gather weights, summed over runs of equal cells
+    {
+        float we[12], wb[6];
+        ad::gather_m_weights(o_in, we, wb);
+        float *w = col + lane;
+#pragma unroll
+        for (int k = 0; k < 12; k++) w[k * DEP_STRIDE] = we[k] * lf[k >> 2];
+#pragma unroll
+        for (int k = 0; k < 6; k++) w[(12 + k) * DEP_STRIDE] = wb[k] * lf[3 + (k >> 1)];
+    }
+    const bool active = c >= 0;
+    if (__ballot_sync(0xffffffffu, active) == 0u) return;
+    const int key = active ? c : -1 - lane;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+    const unsigned ends = (heads >> 1) | 0x80000000u;  // bit i: particle i ends its run
+    keys[lane] = active ? c : -1;
+    __syncwarp();
+    if (lane < GATHER_IN) {
+        const int q = lane;
+        const int off = gather_offset(q, (int)g.sx, (int)g.sy);
+        // pointer choice by static indices (a dynamic one copies LF to local memory)
+        const int cq = q < 12 ? q >> 2 : (q - 12) >> 1;
+        float *e = cq == 0 ? LF.E[0] : (cq == 1 ? LF.E[1] : LF.E[2]);
+        float *b = cq == 0 ? LF.B[0] : (cq == 1 ? LF.B[1] : LF.B[2]);
+        float *t = cq == 0 ? LF.T[0] : (cq == 1 ? LF.T[1] : LF.T[2]);
+        float *d0 = q < 12 ? e : b;
+        float *d1 = q < 12 ? nullptr : t;
+        const float *row = col + q * DEP_STRIDE;
+        float acc = 0.0f;
+        for (int i = 0; i < 32; i++) {
+            acc += row[i];
+            if ((ends >> i) & 1u) {
+                const int kc = keys[i];
+                if (kc >= 0 && acc != 0.0f) {
+                    atomicAdd(d0 + (int64_t)kc + off, acc);
+                    if (d1) atomicAdd(d1 + (int64_t)kc + off, acc);
+                }
+                acc = 0.0f;
+            }
+        }
     }
 }
 

@@ -16,11 +16,12 @@
 //
 // Before the first push the relativistic mixed state holds the loaded
 // velocity; the run first stores u = gamma v (the first push's own input), so
-// every step of the run is the same function. The run then sorts the store
-// by cell once (the deposit's run sums and the gather's locality depend on
-// it; the loop's periodic re-sorts are left out of the differentiated
-// steps). The velocity gradient is d objective / d v with gamma held,
-// gamma d objective / d u, returned in the store's order before the run.
+// every step of the run is the same function. The store is sorted by cell at
+// the start of every segment (the deposit's run sums and the gather's
+// locality depend on it); a sort is a permutation, whose adjoint maps the
+// particle adjoints back through it. The velocity gradient is d objective /
+// d v with gamma held, gamma d objective / d u, returned in the store's order
+// before the run.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -105,11 +106,14 @@ struct MSnap {
     int bswap = 0;
     double t = 0.0;
     int64_t step = 0;
+    int64_t np = 0;  // the store's size and species segments at the snapshot
+    int64_t off[EMOO_NSPEC + 1] = {};
+    int64_t count[EMOO_NSPEC] = {};
 };
 
 struct AdRunM {
     emoo_handle *h = nullptr;
-    int64_t np = 0, npts = 0;
+    int64_t cap = 0, npts = 0;  // particle capacity of the buffers (the store's size at the start)
     std::vector<void *> owned;
 
     void *alloc(size_t bytes) {
@@ -121,14 +125,16 @@ struct AdRunM {
     ~AdRunM() {
         for (void *p : owned) cudaFree(p);
     }
-    // layout: cell int32[np] | ox oy oz ux uy uz float[np] | E xyz, B slots (B, B_tm1 storage) float[npts]
-    size_t snap_bytes() const { return (size_t)np * 28 + (size_t)npts * 36; }
-    float *pf(const MSnap &s, int k) const { return (float *)(s.buf + (size_t)np * 4) + (size_t)k * np; }
-    float *ff(const MSnap &s, int k) const { return (float *)(s.buf + (size_t)np * 28) + (size_t)k * npts; }
+    // layout (capacity cap): cell int32[cap] | ox oy oz ux uy uz float[cap] | E xyz, B slots (B, B_tm1
+    // storage) float[npts]
+    size_t snap_bytes() const { return (size_t)cap * 28 + (size_t)npts * 36; }
+    float *pf(const MSnap &s, int k) const { return (float *)(s.buf + (size_t)cap * 4) + (size_t)k * cap; }
+    float *ff(const MSnap &s, int k) const { return (float *)(s.buf + (size_t)cap * 28) + (size_t)k * npts; }
     int save(MSnap &s) {
         if (!s.buf) s.buf = (char *)alloc(snap_bytes());
         if (!s.buf) return EMOO_ERR_OOM;
         cudaStream_t st = h->stream;
+        const int64_t np = h->np;
         if (np) {
             EMOO_CUDA(cudaMemcpyAsync(s.buf, h->cell, sizeof(int32_t) * np, cudaMemcpyDeviceToDevice, st));
             const float *P[6] = {h->ox, h->oy, h->oz, h->ux, h->uy, h->uz};
@@ -144,10 +150,14 @@ struct AdRunM {
         s.bswap = h->bswap;
         s.t = h->t;
         s.step = h->step_index;
+        s.np = np;
+        for (int k = 0; k <= EMOO_NSPEC; k++) s.off[k] = h->off[k];
+        for (int k = 0; k < EMOO_NSPEC; k++) s.count[k] = h->count[k];
         return EMOO_OK;
     }
     int restore(const MSnap &s) {
         cudaStream_t st = h->stream;
+        const int64_t np = s.np;
         if (np) {
             EMOO_CUDA(cudaMemcpyAsync(h->cell, s.buf, sizeof(int32_t) * np, cudaMemcpyDeviceToDevice, st));
             float *P[6] = {h->ox, h->oy, h->oz, h->ux, h->uy, h->uz};
@@ -163,6 +173,9 @@ struct AdRunM {
         h->bswap = s.bswap;
         h->t = s.t;
         h->step_index = s.step;
+        h->np = np;
+        for (int k = 0; k <= EMOO_NSPEC; k++) h->off[k] = s.off[k];
+        for (int k = 0; k < EMOO_NSPEC; k++) h->count[k] = s.count[k];
         return EMOO_OK;
     }
     MSnapView view(const MSnap &s) const {
@@ -178,6 +191,20 @@ struct AdRunM {
         return v;
     }
 };
+
+// The adjoint of a sort: the particle adjoints after it (order of the sorted
+// store, n_after entries) go back to the order before it: dst[perm[i]] =
+// src[i]; particles the sort dropped (removed earlier) keep 0.
+struct Lam6 {
+    float *p[6];
+};
+__global__ void k_unsort_adjoint(Lam6 src, Lam6 dst, const uint32_t *perm, int64_t n_after) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n_after) return;
+    const uint32_t j = perm[i];
+#pragma unroll
+    for (int k = 0; k < 6; k++) dst.p[k][j] = src.p[k][i];
+}
 
 MSnapView handle_view(emoo_handle *h) {
     MSnapView v;
@@ -314,10 +341,7 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
     AdRunM R;
     R.h = h;
     const int64_t np0 = h->np;
-    uint32_t *perm0 = (uint32_t *)R.alloc(sizeof(uint32_t) * (size_t)std::max<int64_t>(np0, 1));
-    if (!perm0) return EMOO_ERR_OOM;
-    EMOO_TRY(sort_with_permutation(h, perm0));
-    R.np = h->np;
+    R.cap = std::max<int64_t>(np0, 1);
     R.npts = h->g.npts;
     ObjM os;
     os.kind = spec->objective;
@@ -339,10 +363,27 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
             for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]);
         }
     } evfree{ev};
+    // The store is sorted by cell at the start of every segment of
+    // checkpoint_every steps (the whole run is one segment without
+    // checkpoints); sort s leaves perm[s] (perm[s][i]: the index before the
+    // sort of particle i after it) and the store's size before it.
+    const int N = spec->nsteps;
+    const int K = spec->checkpoint_every >= 1 ? spec->checkpoint_every : std::max(N, 1);
+    const int nseg = std::max((N + K - 1) / K, 1);
+    std::vector<uint32_t *> perm(nseg, nullptr);
+    std::vector<int64_t> np_before(nseg, 0);
+    auto segment_start = [&](int sgi) -> int {
+        if (!perm[sgi] && !(perm[sgi] = (uint32_t *)R.alloc(sizeof(uint32_t) * (size_t)R.cap))) return EMOO_ERR_OOM;
+        np_before[sgi] = h->np;
+        return sort_with_permutation(h, perm[sgi]);
+    };
 
     if (mode == EMOO_AD_FORWARD) {
         EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
-        for (int n = 0; n < spec->nsteps; n++) EMOO_TRY(primal_step_m(h));
+        for (int n = 0; n < N; n++) {
+            if (n % K == 0) EMOO_TRY(segment_start(n / K));
+            EMOO_TRY(primal_step_m(h));
+        }
         EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
         EMOO_TRY(objective_m(h, os, dev, &out->objective));
         float ms = 0;
@@ -351,14 +392,19 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
         return read_err(h);
     }
 
-    // ---- adjoint: forward with checkpoints
-    const int K = spec->checkpoint_every, N = spec->nsteps;
-    const int nseg = (N + K - 1) / K;
-    std::vector<MSnap> ck(std::max(nseg, 1));
+    // ---- adjoint: forward with checkpoints (after each segment's sort)
+    std::vector<MSnap> ck(nseg);
     EMOO_CUDA(cudaEventRecord(ev[0], h->stream));
     for (int n = 0; n < N; n++) {
-        if (n % K == 0) EMOO_TRY(R.save(ck[n / K]));
+        if (n % K == 0) {
+            EMOO_TRY(segment_start(n / K));
+            EMOO_TRY(R.save(ck[n / K]));
+        }
         EMOO_TRY(primal_step_m(h));
+    }
+    if (N == 0) {
+        EMOO_TRY(segment_start(0));
+        EMOO_TRY(R.save(ck[0]));
     }
     EMOO_CUDA(cudaEventRecord(ev[1], h->stream));
     EMOO_TRY(objective_m(h, os, dev, &out->objective));
@@ -369,14 +415,14 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
     }
     MSnap fin;
     EMOO_TRY(R.save(fin));
-    // adjoint state: offsets and momenta per particle, the 13 field slots
-    float *lo[3], *lu[3], *lslot[NSLOT];
-    for (int a = 0; a < 3; a++) {
-        lo[a] = (float *)R.alloc(sizeof(float) * std::max<int64_t>(R.np, 1));
-        lu[a] = (float *)R.alloc(sizeof(float) * std::max<int64_t>(R.np, 1));
-        if (!lo[a] || !lu[a]) return EMOO_ERR_OOM;
-        EMOO_CUDA(cudaMemsetAsync(lo[a], 0, sizeof(float) * R.np, h->stream));
-        EMOO_CUDA(cudaMemsetAsync(lu[a], 0, sizeof(float) * R.np, h->stream));
+    // adjoint state: offsets and momenta per particle (two sets, for the
+    // sorts' adjoints), the 13 field slots
+    float *lam[6], *lam2[6], *lslot[NSLOT];
+    for (int a = 0; a < 6; a++) {
+        lam[a] = (float *)R.alloc(sizeof(float) * (size_t)R.cap);
+        lam2[a] = (float *)R.alloc(sizeof(float) * (size_t)R.cap);
+        if (!lam[a] || !lam2[a]) return EMOO_ERR_OOM;
+        EMOO_CUDA(cudaMemsetAsync(lam[a], 0, sizeof(float) * R.cap, h->stream));
     }
     for (int k = 0; k < NSLOT; k++) {
         if (!(lslot[k] = (float *)R.alloc(sizeof(float) * (size_t)R.npts))) return EMOO_ERR_OOM;
@@ -395,6 +441,7 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
                                    h->stream>>>(h->g, os.sl, field_out_f(sl, h->bswap), field_out_f(lslot, h->bswap));
         EMOO_CUDA(cudaGetLastError());
     } else {
+        float *lu[3] = {lam[3], lam[4], lam[5]};
         EMOO_TRY(mixed_ad_kinetic(h, handle_view(h), os.species, os.xlo, os.xhi, nullptr, lu));
     }
     LedgerM pl;
@@ -420,9 +467,25 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
         }
         EMOO_CUDA(cudaEventRecord(ev[2], h->stream));
         for (int n = n1 - 1; n >= n0; n--) {
-            const MSnap &after = n + 1 < n1 ? tape[n + 1 - n0] : (sgi + 1 < nseg ? ck[sgi + 1] : fin);
-            EMOO_TRY(adj_step_m(h, R, tape[n - n0], (const int32_t *)after.buf, lo, lu, lslot, pl, mism));
+            // the recorded next state, in this segment's order (the next
+            // checkpoint follows a sort, so the last step of a segment has none)
+            const int32_t *after = n + 1 < n1 ? (const int32_t *)tape[n + 1 - n0].buf
+                                              : (sgi + 1 == nseg ? (const int32_t *)fin.buf : nullptr);
+            float *lo[3] = {lam[0], lam[1], lam[2]}, *lu[3] = {lam[3], lam[4], lam[5]};
+            EMOO_TRY(adj_step_m(h, R, tape[n - n0], after, lo, lu, lslot, pl, mism));
         }
+        // the adjoint of the segment's sort
+        for (int a = 0; a < 6; a++)
+            EMOO_CUDA(cudaMemsetAsync(lam2[a], 0, sizeof(float) * (size_t)np_before[sgi], h->stream));
+        if (ck[sgi].np) {
+            Lam6 src{{lam[0], lam[1], lam[2], lam[3], lam[4], lam[5]}};
+            Lam6 dst{{lam2[0], lam2[1], lam2[2], lam2[3], lam2[4], lam2[5]}};
+            h->launches++;
+            k_unsort_adjoint<<<(unsigned)((ck[sgi].np + 255) / 256), 256, 0, h->stream>>>(src, dst, perm[sgi],
+                                                                                            ck[sgi].np);
+            EMOO_CUDA(cudaGetLastError());
+        }
+        for (int a = 0; a < 6; a++) std::swap(lam[a], lam2[a]);
         EMOO_CUDA(cudaEventRecord(ev[3], h->stream));
         EMOO_CUDA(cudaEventSynchronize(ev[3]));
         float a = 0, b = 0;
@@ -457,24 +520,26 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
     }
     if (grad_v && np0) {
         // d objective / d v (gamma held) = gamma d objective / d u, gamma from
-        // the run's start; particle i of the sorted store was perm0[i] before
-        for (int64_t k = 0; k < 3 * np0; k++) grad_v[k] = 0.0;
-        std::vector<uint32_t> perm(R.np);
-        if (R.np) {
-            EMOO_CUDA(cudaMemcpy(perm.data(), perm0, sizeof(uint32_t) * R.np, cudaMemcpyDeviceToHost));
+        // the run's start; the adjoints are in the store's order before the
+        // run, the first checkpoint in the order after the first sort
+        const int64_t n = ck[0].np;
+        std::vector<uint32_t> p0(n);
+        std::vector<float> u(n), l(np0);
+        std::vector<double> g(np0, 1.0);
+        const bool rel = h->info.relativity != 0;
+        if (n) EMOO_CUDA(cudaMemcpy(p0.data(), perm[0], sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        if (rel && n) {
             const MSnapView v0 = R.view(ck[0]);
-            std::vector<float> u(R.np), l(R.np);
-            std::vector<double> g2(R.np, 0.0);
-            const bool rel = h->info.relativity != 0;
+            std::vector<double> g2(n, 0.0);
             for (int a = 0; a < 3; a++) {
-                EMOO_CUDA(cudaMemcpy(u.data(), v0.u[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
-                for (int64_t p = 0; p < R.np; p++) g2[p] += (double)u[p] * (double)u[p];
+                EMOO_CUDA(cudaMemcpy(u.data(), v0.u[a], sizeof(float) * n, cudaMemcpyDeviceToHost));
+                for (int64_t i = 0; i < n; i++) g2[i] += (double)u[i] * (double)u[i];
             }
-            for (int a = 0; a < 3; a++) {
-                EMOO_CUDA(cudaMemcpy(l.data(), lu[a], sizeof(float) * R.np, cudaMemcpyDeviceToHost));
-                for (int64_t p = 0; p < R.np; p++)
-                    grad_v[a * np0 + perm[p]] = (rel ? std::sqrt(1.0 + g2[p]) : 1.0) * l[p];
-            }
+            for (int64_t i = 0; i < n; i++) g[p0[i]] = std::sqrt(1.0 + g2[i]);
+        }
+        for (int a = 0; a < 3; a++) {
+            EMOO_CUDA(cudaMemcpy(l.data(), lam[3 + a], sizeof(float) * np0, cudaMemcpyDeviceToHost));
+            for (int64_t q = 0; q < np0; q++) grad_v[a * np0 + q] = g[q] * l[q];
         }
     }
     EMOO_TRY(R.restore(fin));

@@ -1029,7 +1029,7 @@ constexpr int ADJ_WARPS = ADJ_BLOCK / 32;
 constexpr int GATHER_IN = 18;
 
 template <bool REL>
-__global__ void __launch_bounds__(ADJ_BLOCK)
+__global__ void __launch_bounds__(ADJ_BLOCK, 4)
     k_adj_particles_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MSnapC S,
                       const int32_t *cell_after, int64_t np, float q0, MAdjState L, MAdjJ LJ, MAdjFields LF,
                       unsigned long long *mismatch) {

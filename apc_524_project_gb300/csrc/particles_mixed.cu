@@ -1342,12 +1342,40 @@ void mixed_free(emoo_handle *h) {
     h->mf = nullptr;
 }
 
-// n > 0: host FP64 arrays (copied through the payload scratch in chunks);
-// n < 0: |n| particles already staged on the device at the given pointers.
+// Whether kernels on the handle's device can read and write host array p
+// in place: pinned (registered) memory mapped at the same address, device
+// or managed memory, or any host memory on a device that uses the host's
+// page tables (a coherent CPU-GPU link). Then the conversion kernels move
+// the caller's arrays themselves, at the link's bandwidth, without staging.
+static bool device_accessible(const emoo_handle *h, const void *p) {
+    if (!p) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return a.device == h->dev;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+    int pt = 0;
+    if (cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return pt != 0;
+}
+
+// n > 0: host FP64 arrays (read in place where the device can, else copied
+// through the payload scratch in chunks); n < 0: |n| particles already
+// staged on the device at the given pointers.
 int mixed_from_f64(emoo_handle *h, int64_t at, int64_t n, const double *x, const double *y, const double *z,
                    const double *vx, const double *vy, const double *vz, const double *gam) {
     bool dev = n < 0;
     if (dev) n = -n;
+    if (!dev) {
+        const void *src[7] = {x, y, z, vx, vy, vz, gam};
+        dev = true;
+        for (const void *q : src) dev = dev && device_accessible(h, q);
+    }
     int rel = h->info.relativity != 0;
     if (rel && !h->g0) {
         EMOO_CUDA(cudaMalloc(&h->g0, sizeof(float) * (size_t)h->cap));
@@ -1359,6 +1387,7 @@ int mixed_from_f64(emoo_handle *h, int64_t at, int64_t n, const double *x, const
         k_from_f64<<<nblk(n), 256, 0, h->stream>>>(h->g, mstate(h), at, n, x, y, z, vx, vy, vz, gam, rel, vmode,
                                                    h->g0, h->ctr);
         EMOO_CUDA(cudaGetLastError());
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
         return EMOO_OK;
     }
     int64_t chunk = (int64_t)(h->pay_bytes / (7 * sizeof(double)));
@@ -1384,9 +1413,20 @@ int mixed_from_f64(emoo_handle *h, int64_t at, int64_t n, const double *x, const
 int mixed_to_f64(emoo_handle *h, int64_t at, int64_t n, double *x, double *y, double *z, double *vx, double *vy,
                  double *vz, double *gam) {
     int rel = h->info.relativity != 0;
+    const float *g0 = (h->first_push && h->g0) ? h->g0 : nullptr;
+    bool direct = true;
+    for (const void *q : {(const void *)x, (const void *)y, (const void *)z, (const void *)vx, (const void *)vy,
+                          (const void *)vz, (const void *)gam})
+        direct = direct && device_accessible(h, q);
+    if (direct) {  // written in place (see device_accessible)
+        h->launches++;
+        k_to_f64<<<nblk(n), 256, 0, h->stream>>>(h->g, mstate(h), at, n, x, y, z, vx, vy, vz, gam, rel, g0);
+        EMOO_CUDA(cudaGetLastError());
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+        return EMOO_OK;
+    }
     int64_t chunk = (int64_t)(h->pay_bytes / (7 * sizeof(double)));
     double *s = (double *)h->pay;
-    const float *g0 = (h->first_push && h->g0) ? h->g0 : nullptr;
     for (int64_t b = 0; b < n; b += chunk) {
         int64_t m = std::min(chunk, n - b);
         h->launches++;

@@ -93,7 +93,7 @@ class Config:
     zero_mean: Optional[bool] = None  # default: Poisson start with all-periodic fields
     x0: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     immobile_ions: bool = False  # uniform neutralising background instead of ion particles
-    b_noise: float = 0.0         # seeded white-noise amplitude on every B component (C3)
+    b_noise: float = 0.0         # seeded white-noise amplitude on every B component (two-stream start)
 
     @property
     def L(self):
@@ -250,7 +250,7 @@ def gaussian_sine_coefficients(window: float, fwhm: float, ncoef: int = 16):
 def b_noise_fields(cfg: Config):
     """Seeded white noise of amplitude cfg.b_noise on Bx, By, Bz at the
     physical points ((n+3)^3 arrays, ghosts zero), the same values for B and
-    B_tm1 (the C3 start). Returns None when cfg.b_noise is 0."""
+    B_tm1 (the two-stream workload's start). Returns None when cfg.b_noise is 0."""
     if not cfg.b_noise:
         return None
     import numpy as np

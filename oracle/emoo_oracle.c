@@ -877,7 +877,7 @@ static void deposit(orc_t *c, int with_rho) {
 }
 
 /* Uniform immobile background charge density added to rho at every deposit
- * (the C3 and C5 workloads' neutralising ions; the reference has none). */
+ * (the neutralising ions of the two-stream and laser-plasma workloads; the reference has none). */
 void orc_set_rho_background(void *h, double v) { ((orc_t *)h)->rho_bg = v; }
 
 /* Restricts the background to the physical points with x >= xmin (grid point

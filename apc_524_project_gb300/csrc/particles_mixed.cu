@@ -454,17 +454,17 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 vy = uy * iga;
                 vz = uz * iga;
             } else {
-            float f[6];
-            gather_pack(pack + (int64_t)c * PACK_F4, ox, oy, oz, f);
-            push_m<REL, FIRST>(f, st.qp[s], g0, p, ux, uy, uz, vx, vy, vz);
-            // position update in cell units, then the boundaries per axis
-            float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
-            cell_step(nx, ix, ox);
-            cell_step(ny, iy, oy);
-            cell_step(nz, iz, oz);
-            mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
-            if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
-            if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
+                float f[6];
+                gather_pack(pack + (int64_t)c * PACK_F4, ox, oy, oz, f);
+                push_m<REL, FIRST>(f, st.qp[s], g0, p, ux, uy, uz, vx, vy, vz);
+                // position update in cell units, then the boundaries per axis
+                float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
+                cell_step(nx, ix, ox);
+                cell_step(ny, iy, oy);
+                cell_step(nz, iz, oz);
+                mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
+                if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
+                if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
             }
             if (mask & 64) {
                 S.cell[p] = -1;

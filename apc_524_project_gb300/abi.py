@@ -126,6 +126,7 @@ class Stats(C.Structure):
 
 AD_FORWARD, AD_TANGENT, AD_ADJOINT = 0, 1, 2
 AD_OBJ_FIELD, AD_OBJ_KINETIC = 0, 1
+FIELDS_RHO, FIELDS_E, FIELDS_J, FIELDS_B, FIELDS_ALL = 0, 1, 2, 3, 4
 NCOEF = 16
 
 
@@ -211,6 +212,9 @@ PROTOTYPES = {
     "emoo_set_waves": (C.c_int, [_P, C.c_int, _D, _D]),
     "emoo_set_wave_shape": (C.c_int, [_P, C.c_int, C.POINTER(WaveShape)]),
     "emoo_ad_nparams": (C.c_int, [_P]),
+    "emoo_write_fields": (C.c_int, [_P, C.c_char_p, C.c_int]),
+    "emoo_write_restart": (C.c_int, [_P, C.c_char_p]),
+    "emoo_read_restart": (C.c_int, [_P, C.c_char_p]),
     "emoo_ad_run": (C.c_int, [_P, C.POINTER(AdSpec), C.c_int, _D, _D, C.POINTER(AdResult), _D, _D]),
 }
 

@@ -32,7 +32,7 @@ CUDA_UNITS = [
     ("adjoint_f64.cu", ["--fmad=false"]),
     ("adjoint_mixed.cu", []),
 ]
-HOST_UNITS = ["api.cpp", "loader_host.cpp", "input_parser.cpp"]
+HOST_UNITS = ["api.cpp", "loader_host.cpp", "input_parser.cpp", "io.cpp"]
 
 
 def _nvcc():

@@ -428,6 +428,12 @@ int reserve(emoo_handle *h, int64_t cap) {
     return EMOO_OK;
 }
 
+}  // namespace
+
+int emoo::reserve_store(emoo_handle *h, int64_t cap) { return reserve(h, cap); }
+
+namespace {
+
 // Opens a gap of n particles at the end of species s's segment and returns
 // its start index.
 int make_room(emoo_handle *h, int s, int64_t n, int64_t *at) {

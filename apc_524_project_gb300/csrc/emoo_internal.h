@@ -254,6 +254,7 @@ struct MSnapView {
     const float *E[3], *B[3], *T[3];
 };
 void mixed_field_arrays(emoo_handle *h, float *E[3], float *Bslot[6]);
+void mixed_point_arrays(emoo_handle *h, long long *J[4], double *q0);
 int mixed_ad_momentum_from_velocity(emoo_handle *h);
 int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_after, float *const lo[3],
                        float *const lu[3], const float *const lj[3], float *const lE[3], float *const lB[3],
@@ -288,6 +289,7 @@ int ad_execute_bc(emoo_handle *h, int send_id);
 int ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops);
 int light_planes_public(emoo_handle *h, int s, PlaneSet *ps);
 int sort_with_permutation(emoo_handle *h, uint32_t *perm_out);
+int reserve_store(emoo_handle *h, int64_t cap);  // particle capacity, contents kept
 
 }  // namespace emoo
 

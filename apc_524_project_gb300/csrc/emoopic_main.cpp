@@ -4,8 +4,14 @@
 //
 //   emoopic_gpu <input.txt> [--mixed] [--dt DT]
 //
-// Writes history.dat next to the input file like the reference. The HDF5 field
-// writer and particle tracks of the reference are not part of this program.
+// Writes history.dat next to the input file like the reference, and the field
+// time series at the reference's cadence (t = 0, every nstep_fields steps, the
+// last step) into output.fields/ there: the reference's HDF5 datasets as raw
+// files (emoo_write_fields; HDF5 is not available). With nstep_restart > 0 it
+// writes restart.emoo there every nstep_restart steps; with restart = 1 in the
+// input it continues from that file when present. Particle tracks of the
+// reference are not part of this program.
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -53,18 +59,42 @@ int main(int argc, char **argv) {
         std::string inputname = argv[1];
         std::string dir = inputname.substr(0, inputname.find_last_of('/') + 1);
         OutputBoxQuantities box((dir + "history.dat").c_str(), grids, &part_handler, info);
+        emoo_handle *h = grids->handle();
         double t = info->t0, dt = 0.0;
-        emoo_time(grids->handle(), nullptr, &dt);
+        emoo_time(h, nullptr, &dt);
+        const std::string fields_dir = dir + "output.fields", restart = dir + "restart.emoo";
+        int t0 = 0;
+        if (info->restart) {
+            FILE *rf = fopen(restart.c_str(), "rb");
+            if (rf) {
+                fclose(rf);
+                emoopic::check(emoo_read_restart(h, restart.c_str()), "emoo_read_restart");
+                emoo_time(h, &t, nullptr);
+                t0 = (int)llround((t - info->t0) / dt);
+                printf("Continuing from %s at step %d\n", restart.c_str(), t0);
+            }
+        }
+        const int nstep_fields = info->nstep_fields > 0 ? info->nstep_fields : 1;
+        if (info->which_fields >= 0 && t0 == 0)
+            emoopic::check(emoo_write_fields(h, fields_dir.c_str(), info->which_fields), "emoo_write_fields");
         printf("Advancing %d time steps with dt = %f\n", info->nt, dt);
         int64_t cross[6];
-        for (int ti = 0; ti < info->nt; ti++) {
+        for (int ti = t0; ti < info->nt; ti++) {
             box.output(t, ti);
             // sort (every nstep_sort) + fused push / boundaries / deposit +
             // fold + Yee update + E/B boundaries, src/main.cpp:225-272
-            emoopic::check(emoo_step(grids->handle(), 1, cross), "emoo_step");
+            emoopic::check(emoo_step(h, 1, cross), "emoo_step");
             t += dt;
+            // output, src/main.cpp:277-283
+            if ((ti + 1) % nstep_fields == 0 && info->which_fields >= 0)
+                emoopic::check(emoo_write_fields(h, fields_dir.c_str(), info->which_fields), "emoo_write_fields");
+            if (info->nstep_restart > 0 && (ti + 1) % info->nstep_restart == 0)
+                emoopic::check(emoo_write_restart(h, restart.c_str()), "emoo_write_restart");
         }
         printf("***Timestep loop complete***\n");
+        // final output, src/main.cpp:295-300
+        if (info->nt % nstep_fields != 0 && info->which_fields >= 0)
+            emoopic::check(emoo_write_fields(h, fields_dir.c_str(), info->which_fields), "emoo_write_fields");
         delete grids;
         for (int i = 0; i < 6; i++) delete bc[i];
         delete[] bc;

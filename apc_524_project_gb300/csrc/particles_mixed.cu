@@ -1844,6 +1844,12 @@ void mixed_field_arrays(emoo_handle *h, float *E[3], float *Bslot[6]) {
     for (int c = 0; c < 6; c++) Bslot[c] = h->mf->Bslot[c];
 }
 
+// The fixed-point J and rho at the points (Jx, Jy, Jz, rho) and their quantum.
+void mixed_point_arrays(emoo_handle *h, long long *J[4], double *q0) {
+    for (int c = 0; c < 4; c++) J[c] = h->mf->J[c];
+    *q0 = h->mf->q0;
+}
+
 // Before the first relativistic push the momentum slots hold the loaded
 // velocity (and g0 the loaded gamma); store u = gamma v so that every step
 // of a differentiated run is the same function.

@@ -436,6 +436,41 @@ typedef struct emoo_wave_shape {
 
 int emoo_set_wave_shape(emoo_handle *h, int wave, const emoo_wave_shape *shape);
 
+/* ---- output files ----------------------------------------------------------
+ * Field time series, replacing Hdf5IO (src/IO/hdf5io.cpp:6-72, 108-141,
+ * 169-350). The reference writes per field a 4-D dataset of the physical
+ * points, dims [nx][ny][nz][time], chunked one snapshot per chunk, with the
+ * point coordinates as attributes x, y, z, and a /time dataset. HDF5 is not
+ * available to this library, so the same data go to raw little-endian files
+ * in directory `dir` (created if missing): time.f64 (one double per
+ * snapshot), per field <name>.f64 (the snapshots in order, each the physical
+ * points as doubles in C order [i][j][k]: the reference dataset's chunks in
+ * file order) and <name>.xyz (x[nx], y[ny], z[nz], written at the first
+ * snapshot: xyz0 + offset + d (i - 1), the offset d/2 along an E or J
+ * component's own axis and across a B component's two others, Grid::getGridPhys
+ * src/grid/grid.cpp:415-466). The first call on a directory without
+ * time.f64 starts the series; later calls append. which: the reference's
+ * fields_to_write (src/IO/hdf5io.hpp:14-20): 0 rho, 1 E, 2 J, 3 B, 4 all;
+ * names Ex Ey Ez Bx By Bz Jx Jy Jz rho; B is (B + B_tm1) / 2 (Grid::AvgB,
+ * src/grid/grid.cpp:495-506). */
+#define EMOO_FIELDS_RHO 0
+#define EMOO_FIELDS_E 1
+#define EMOO_FIELDS_J 2
+#define EMOO_FIELDS_B 3
+#define EMOO_FIELDS_ALL 4
+int emoo_write_fields(emoo_handle *h, const char *dir, int which);
+
+/* Restart files (the reference parses nstep_restart, src/IO/readinfo.cpp:706-711,
+ * and writes none): the whole state the loop continues from - time and step,
+ * B roles, the fields the loop reads and writes, the particle store in the
+ * handle's precision (with ids when tracked), the history rows - in one file.
+ * emoo_read_restart restores it into a handle created from the same input and
+ * options (same grid, species and precision; EMOO_ERR_STATE otherwise); wave
+ * shapes and other emoo_set_* settings are configuration and are set again by
+ * the caller. Continuing from a restart reproduces the uninterrupted run. */
+int emoo_write_restart(emoo_handle *h, const char *path);
+int emoo_read_restart(emoo_handle *h, const char *path);
+
 /* Runs spec->nsteps steps from the handle's current state and leaves it at
  * the final state. dtheta (emoo_ad_nparams) and dv (3 np host doubles: vx of
  * every particle, then vy, then vz, in storage order) give the tangent

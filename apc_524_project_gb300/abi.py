@@ -98,6 +98,7 @@ class Opts(C.Structure):
         ("history_every", C.c_int),
         ("rho_background", C.c_double),
         ("rho_background_xmin", C.c_double),
+        ("policy", C.c_int),
     ]
 
 
@@ -127,6 +128,7 @@ class Stats(C.Structure):
 AD_FORWARD, AD_TANGENT, AD_ADJOINT = 0, 1, 2
 AD_OBJ_FIELD, AD_OBJ_KINETIC = 0, 1
 FIELDS_RHO, FIELDS_E, FIELDS_J, FIELDS_B, FIELDS_ALL = 0, 1, 2, 3, 4
+POLICY_REFERENCE, POLICY_CORRECTED = 0, 1
 NCOEF = 16
 
 

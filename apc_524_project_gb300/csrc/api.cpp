@@ -619,6 +619,8 @@ int execute_bc(emoo_handle *h, int send_id) {
 
 // executeBC on the FP64 grid slots.
 int execute_bc_slots(emoo_handle *h, int send_id) {
+    if (h->policy == EMOO_POLICY_CORRECTED && send_id == EMOO_SEND_JRHO) return fold_full_f64(h, FOLD_ALL);
+    if (h->policy == EMOO_POLICY_CORRECTED && send_id == EMOO_SEND_EB) return ghost_full_f64(h);
     if (send_id == EMOO_SEND_JRHO) {
         for (int d = 0; d < 3; d++)
             if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d));
@@ -784,6 +786,22 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
         h->bc.xmax[d] = h->bc.xmin[d] + info->Lxyz[d];
     }
     h->poisson = info->restart == 0 && strcmp(info->fields_init, "poisson") == 0;
+    {
+        int prc = EMOO_OK;
+        if (o.policy != EMOO_POLICY_REFERENCE && o.policy != EMOO_POLICY_CORRECTED) prc = EMOO_ERR_ARG;
+        if (o.policy == EMOO_POLICY_CORRECTED) {
+            // the FP64 form with periodic particles and fields on every side
+            if (h->precision != EMOO_FP64) prc = EMOO_ERR_UNSUPPORTED;
+            for (int s = 0; s < 6; s++)
+                if (h->bc.pbc[s] != PBC_PERIODIC || h->bc.fbc[s] != FBC_PERIODIC) prc = EMOO_ERR_UNSUPPORTED;
+            h->policy = o.policy;
+            h->g.vshift = 1;
+        }
+        if (prc != EMOO_OK) {
+            emoo_destroy(h);
+            return prc;
+        }
+    }
     // first physical x index (grid point x0 + (i - 1) dx) the background covers
     h->rho_bg_first = h->g.n[0] + 1;
     for (int i = 1; i <= h->g.n[0]; i++)
@@ -872,6 +890,7 @@ int materialize_rho(emoo_handle *h) {
     h->rho_stale = 0;
     if (h->precision != EMOO_FP64) return mixed_materialize_rho(h);
     EMOO_TRY(deposit_rho_f64(h));
+    if (h->policy == EMOO_POLICY_CORRECTED) return fold_full_f64(h, FOLD_RHO);
     for (int d = 0; d < 3; d++)
         if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d, FOLD_RHO));
     return EMOO_OK;
@@ -1295,8 +1314,10 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
         }
         if (h->precision == EMOO_FP64) {
             EMOO_TRY(fused_step_f64(h, h->dtp, 0));
-            for (int d = 0; d < 3; d++)
-                if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d, fold_what));
+            if (h->policy == EMOO_POLICY_CORRECTED) EMOO_TRY(fold_full_f64(h, fold_what));
+            else
+                for (int d = 0; d < 3; d++)
+                    if (h->bc.fbc[2 * d] == FBC_PERIODIC) EMOO_TRY(fold_f64(h, d, fold_what));
             if (h->info.electrostatic == 1) EMOO_TRY(yee_es_f64(h, h->dtp));
             else EMOO_TRY(yee_f64(h, h->dtp));
             EMOO_TRY(execute_bc(h, EMOO_SEND_EB));

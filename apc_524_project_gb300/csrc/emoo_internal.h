@@ -41,6 +41,9 @@ struct Geom {
     int vol_p2;
     double area[3], iarea[3];  // area[i] = d[j] * d[k], j,k the other two axes in cyclic order
     int area_p2[3];
+    // gather / deposit vertex of cell i: x0 + d (i - vshift); 0 the reference's
+    // ghost-offset vertex, 1 the cell's own lower corner (corrected policy)
+    int vshift = 0;
 };
 
 // Per-species constants, precomputed on the host in the reference's order of
@@ -181,6 +184,7 @@ struct emoo_handle {
     // step disagreed with the recorded one (0 when the recomputation is the
     // primal's, as it is by construction)
     int64_t ad_cell_mismatch = 0;
+    int policy = EMOO_POLICY_REFERENCE;
 
     // instrumentation: kernel launches issued, and CUDA-event timing of the
     // fused particle kernel (the dominant kernel of the step) when enabled
@@ -204,6 +208,10 @@ int yee_es_f64(emoo_handle *h, double dt);
 int ghost_fill_f64(emoo_handle *h, const int *ids, int nids, int dims_mask);
 constexpr int FOLD_J = 1, FOLD_RHO = 2, FOLD_ALL = 3;
 int fold_f64(emoo_handle *h, int dim, int what = FOLD_ALL);
+// corrected policy: periodic folds (J and rho) and ghost copies (E, B, B_tm1)
+// over the whole transverse range, dimension by dimension
+int fold_full_f64(emoo_handle *h, int what);
+int ghost_full_f64(emoo_handle *h);
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
 int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);
 int phi_to_e_f64(emoo_handle *h);

@@ -439,6 +439,71 @@ int fold_f64(emoo_handle *h, int d, int what) {
     return EMOO_OK;
 }
 
+// ---- corrected policy: periodic copies and folds over the whole range ----
+
+struct Slots9 {
+    double *p[9];
+};
+
+// Along dim d, for every transverse point of the whole (n+3)^2 plane:
+// fold = 1: f[n] += f[0], f[1] += f[n+1], f[2] += f[n+2] (the ghost planes'
+// deposits to their periodic images); fold = 0: f[0] = f[n], f[n+1] = f[1],
+// f[n+2] = f[2] (the ghost planes refreshed). One field per blockIdx.z.
+__global__ void k_periodic_full(Geom g, Slots9 fl, int d, int fold) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= g.tot[o2] || r >= g.tot[o1]) return;
+    double *F = fl.p[blockIdx.z];
+    const int n = g.n[d];
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    auto at = [&](int i) -> double & {
+        c[d] = i;
+        return F[gidx(g, c[0], c[1], c[2])];
+    };
+    if (fold) {
+        at(n) += at(0);
+        at(1) += at(n + 1);
+        at(2) += at(n + 2);
+    } else {
+        at(0) = at(n);
+        at(n + 1) = at(1);
+        at(n + 2) = at(2);
+    }
+}
+
+static int periodic_full(emoo_handle *h, const int *ids, int nids, int fold) {
+    const Geom &g = h->g;
+    Slots9 fl;
+    for (int k = 0; k < nids; k++) fl.p[k] = h->slot[ids[k]];
+    dim3 blk(32, 8);
+    for (int d = 0; d < 3; d++) {  // dimension by dimension: edge and corner lines follow
+        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, nids);
+        h->launches++;
+        k_periodic_full<<<grd, blk, 0, h->stream>>>(g, fl, d, fold);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// what: FOLD_J (the three J components), FOLD_RHO, or both
+int fold_full_f64(emoo_handle *h, int what) {
+    int ids[4], n = 0;
+    if (what & FOLD_J)
+        for (int c = 0; c < 3; c++) ids[n++] = EMOO_JX + c;
+    if (what & FOLD_RHO) ids[n++] = EMOO_RHO;
+    return periodic_full(h, ids, n, 1);
+}
+
+int ghost_full_f64(emoo_handle *h) {
+    static const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1,
+                               EMOO_BZ_TM1};
+    return periodic_full(h, ids, 9, 0);
+}
+
 static int plane_launch(emoo_handle *h, const PlaneSet *ps, int n, const int *skip) {
     const Geom &g = h->g;
     for (int b = 0; b < n; b += 12) {

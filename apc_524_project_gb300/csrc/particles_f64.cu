@@ -46,9 +46,9 @@ __device__ __forceinline__ void gather_cell(const Geom &g, const GatherPtrs &P, 
     int64_t o = gidx(g, ix, iy, iz);
     const int64_t sx = g.sx, sy = g.sy;
     double v[21];
-    v[0] = g.x0[0] + g.d[0] * ix;
-    v[1] = g.x0[1] + g.d[1] * iy;
-    v[2] = g.x0[2] + g.d[2] * iz;
+    v[0] = g.x0[0] + g.d[0] * (ix - g.vshift);
+    v[1] = g.x0[1] + g.d[1] * (iy - g.vshift);
+    v[2] = g.x0[2] + g.d[2] * (iz - g.vshift);
     v[3] = P.E[0][o];
     v[4] = P.E[0][o + sy];
     v[5] = P.E[0][o + sy + 1];
@@ -183,9 +183,9 @@ __device__ __forceinline__ void deposit_terms(const Geom &g, double uq, double c
                                               double py, double pz, double vx, double vy, double vz, bool with_rho,
                                               double c[20]) {
     double r[3];
-    r[0] = px - (g.x0[0] + g.d[0] * ix);
-    r[1] = py - (g.x0[1] + g.d[1] * iy);
-    r[2] = pz - (g.x0[2] + g.d[2] * iz);
+    r[0] = px - (g.x0[0] + g.d[0] * (ix - g.vshift));
+    r[1] = py - (g.x0[1] + g.d[1] * (iy - g.vshift));
+    r[2] = pz - (g.x0[2] + g.d[2] * (iz - g.vshift));
     const double *l = g.d;
     double vv[3] = {vx, vy, vz};
 #pragma unroll
@@ -221,7 +221,7 @@ __device__ __forceinline__ int64_t deposit_point(const Geom &g, int64_t o, int q
         case 0: return o;
         case 1: return o + sy;
         case 2: return o + sy + 1;
-        case 3: return o + sy;  // Jx[ix][iy+1][iz] (src/grid/oGrid.cpp:101)
+        case 3: return g.vshift ? o + 1 : o + sy;  // reference: Jx[ix][iy+1][iz] (src/grid/oGrid.cpp:101)
         case 4: return o;
         case 5: return o + 1;
         case 6: return o + sx + 1;
@@ -356,6 +356,109 @@ __global__ void k_deposit(Geom g, SpeciesTab st, PState S, int64_t np, DepositPt
     }
     // with_rho: 0 J, 1 J and rho, 2 rho only
     commit_deposit(g, D, active, o, c, with_rho != 0, with_rho == 2 ? 12 : 0);
+}
+
+// Villasenor-Buneman current (J. Villasenor and O. Buneman, Comput. Phys.
+// Commun. 69 (1992) 306) of a particle moving in a straight line from p0 to
+// p1 (unwrapped, at most one cell face per axis), for the corrected policy:
+// the path is split at the faces it crosses; a piece with offsets a -> b in a
+// cell (cell units, m = (a + b) / 2, D = b - a) adds to the cell's four x
+// edges coef dx Dx ((1-my)(1-mz) + Dy Dz / 12), (my (1-mz) - ..),
+// ((1-my) mz - ..), (my mz + ..), and likewise for y and z; with the linear
+// charge assignment, rho(t + dt) - rho(t) + dt div J = 0 at every point.
+// coef = UNIT_RHOJ q / V / dt. Pieces outside the box land in the ghost
+// planes, which the periodic fold adds back.
+__device__ void vb_deposit(const Geom &g, const DepositPtrs &D, const double p0[3], const double p1[3], double coef) {
+    double u0[3], u1[3], ts[5];
+    int nt = 0;
+    ts[nt++] = 0.0;
+    for (int a = 0; a < 3; a++) {
+        u0[a] = (p0[a] - g.x0[a]) * g.id[a];
+        u1[a] = (p1[a] - g.x0[a]) * g.id[a];
+        const double f0 = floor(u0[a]), f1 = floor(u1[a]);
+        if (f0 != f1) {
+            const double b = f0 > f1 ? f0 : f1;
+            ts[nt++] = (b - u0[a]) / (u1[a] - u0[a]);
+        }
+    }
+    ts[nt++] = 1.0;
+    for (int i = 2; i < nt - 1; i++)
+        for (int j = i; j > 1 && ts[j] < ts[j - 1]; j--) {
+            const double t = ts[j];
+            ts[j] = ts[j - 1];
+            ts[j - 1] = t;
+        }
+    for (int sgi = 0; sgi + 1 < nt; sgi++) {
+        const double ta = ts[sgi], tb = ts[sgi + 1];
+        if (!(tb > ta)) continue;
+        double m[3], Dd[3];
+        int cell[3];
+        for (int a = 0; a < 3; a++) {
+            const double ua = u0[a] + ta * (u1[a] - u0[a]), ub = u0[a] + tb * (u1[a] - u0[a]);
+            cell[a] = (int)floor(0.5 * (ua + ub));
+            const double aa = ua - cell[a], bb = ub - cell[a];
+            Dd[a] = bb - aa;
+            m[a] = 0.5 * (aa + bb);
+        }
+        // every point of the piece's cell exists: cells -1..n (the path moves less
+        // than a cell per axis from a physical position); out of range is recorded
+        bool ok = true;
+        for (int a = 0; a < 3; a++) ok = ok && cell[a] >= -1 && cell[a] + 2 < g.tot[a];
+        if (!ok) continue;
+        for (int a = 0; a < 3; a++) {
+            const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+            const double w = coef * g.d[a] * Dd[a];
+            const double cr = Dd[jb] * Dd[kb] / 12.0;
+            const double W[4] = {w * ((1.0 - m[jb]) * (1.0 - m[kb]) + cr), w * (m[jb] * (1.0 - m[kb]) - cr),
+                                 w * ((1.0 - m[jb]) * m[kb] - cr), w * (m[jb] * m[kb] + cr)};
+            for (int e = 0; e < 4; e++) {
+                int ii[3] = {cell[0] + 1, cell[1] + 1, cell[2] + 1};
+                ii[jb] += e & 1;
+                ii[kb] += e >> 1;
+                atomicAdd(D.J[a] + gidx(g, ii[0], ii[1], ii[2]), W[e]);
+            }
+        }
+    }
+}
+
+// The corrected policy's time-loop kernel: gather at the current position
+// (the cell's own vertex), push, the charge-conserving current of the move,
+// then the (periodic) boundaries.
+template <bool REL>
+__global__ void __launch_bounds__(256) k_fused_vb(Geom g, SpeciesTab st, BCTab bc, GatherPtrs P, PState S, int64_t np,
+                                                  DepositPtrs D, double dt, DevCounters *ctr) {
+    int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int mask = 0;
+    if (p < np) {
+        double x = S.x[p], y = S.y[p], z = S.z[p];
+        if (alive(x)) {
+            int s = species_of(st, p);
+            int ix, iy, iz;
+            cell_of(g, x, y, z, ix, iy, iz);
+            if (!cell_ok(g, ix, iy, iz)) {
+                atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
+            } else {
+                const double p0[3] = {x, y, z};
+                double f[6];
+                gather_cell(g, P, ix, iy, iz, x, y, z, f);
+                double vx = S.vx[p], vy = S.vy[p], vz = S.vz[p];
+                if (REL) {
+                    double ga = S.g[p];
+                    vay_push(st.qp[s], f, dt, x, y, z, vx, vy, vz, ga);
+                    S.g[p] = ga;
+                } else {
+                    boris_push(st.qp[s], f, dt, x, y, z, vx, vy, vz);
+                }
+                double pos[3] = {x, y, z}, v[3] = {vx, vy, vz};
+                if (st.deposit[s] && dt > 0.0) vb_deposit(g, D, p0, pos, st.uq[s] / g.vol / dt);
+                mask = apply_bc(bc, pos, v);
+                if (mask & 64) pos[0] = __longlong_as_double(0x7ff8000000000000LL);
+                S.x[p] = pos[0]; S.y[p] = pos[1]; S.z[p] = pos[2];
+                S.vx[p] = v[0]; S.vy[p] = v[1]; S.vz[p] = v[2];
+            }
+        }
+    }
+    count_crossings(ctr, mask);
 }
 
 // The fused time-loop kernel: gather at the current position (what
@@ -566,6 +669,19 @@ int fused_step_f64(emoo_handle *h, double dtp, int with_rho) {
     if (h->np == 0) return rho_background_f64(h, with_rho);
     SpeciesTab st;
     species_tab(h, dtp, st);
+    if (h->policy == EMOO_POLICY_CORRECTED) {
+        // current along the paths; rho (when asked for) at the new positions
+        h->launches++;
+        if (h->info.relativity)
+            k_fused_vb<true><<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, h->bc, gather_ptrs(h), pstate(h),
+                                                                      h->np, deposit_ptrs(h), dtp, h->ctr);
+        else
+            k_fused_vb<false><<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, st, h->bc, gather_ptrs(h), pstate(h),
+                                                                       h->np, deposit_ptrs(h), dtp, h->ctr);
+        EMOO_CUDA(cudaGetLastError());
+        if (!with_rho) return EMOO_OK;
+        return deposit_rho_f64(h);
+    }
     h->launches++;
     if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
     if (h->info.relativity)

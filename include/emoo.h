@@ -140,7 +140,21 @@ typedef struct emoo_opts {
     double rho_background; /* uniform immobile background charge density added to rho, reference units */
     double rho_background_xmin; /* the background covers the physical points with x >= this
                                    (emoo_default_opts: -HUGE_VAL, every point) */
+    int policy;            /* EMOO_POLICY_REFERENCE (default) or EMOO_POLICY_CORRECTED */
 } emoo_opts;
+
+/* Physics policies. REFERENCE reproduces the reference's arithmetic with its
+ * quirks (ghost-offset gather / deposit vertex, the Jx index of Grid::addJ,
+ * src/grid/oGrid.cpp:101, ghost copies and folds over the physical
+ * transverse range only, current from the velocity at the new position).
+ * CORRECTED (no reference counterpart; FP64 form, periodic boundaries on
+ * every side, EMOO_ERR_UNSUPPORTED otherwise): the cell's own lower corner
+ * as vertex, the fixed Jx index, Villasenor and Buneman's charge-conserving
+ * current along each particle's path (so rho(t + dt) - rho(t) + dt div J = 0
+ * and the Gauss-law residual stays at its initial value), and periodic
+ * copies and folds of every component over the whole range. */
+#define EMOO_POLICY_REFERENCE 0
+#define EMOO_POLICY_CORRECTED 1
 
 /* Seeded sampler of one species (no reference counterpart: replaces the
  * sequential ran2 loader of src/particles/particle_handler.cpp:47-84 with

@@ -93,6 +93,9 @@ typedef struct {
     emoo_wave_shape wshape[EMOO_NWAVE];
     int wshaped[EMOO_NWAVE];
     double *spot[6][3][2];
+    /* 1: the corrected-physics policy (no reference counterpart; see
+     * orc_set_policy), 0: the reference's arithmetic */
+    int policy;
 } orc_t;
 
 /* ------------------------------------------------------------------ */
@@ -515,8 +518,19 @@ static void poisson_bc(orc_t *c, int s, int id) {
 /* Grid::executeBC(sendID), src/grid/grid.cpp:577-585, dispatching to
  * BC_F_Periodic::completeBC (src/boundaries/b_fields/bc_f_periodic.cpp:34-57)
  * and BC_F_External::completeBC (src/boundaries/b_fields/bc_f_external.cpp:45-58). */
+static void corrected_fold(orc_t *c);
+static void corrected_ghosts(orc_t *c);
+
 int orc_execute_bc(void *h, int send_id) {
     orc_t *c = (orc_t *)h;
+    if (c->policy && send_id == EMOO_SEND_JRHO) {
+        corrected_fold(c);
+        return 0;
+    }
+    if (c->policy && send_id == EMOO_SEND_EB) {
+        corrected_ghosts(c);
+        return 0;
+    }
     for (int dim = 0; dim < 3; dim++) {
         for (int r = 0; r < 2; r++) {
             int s = 2 * dim + r;
@@ -558,9 +572,12 @@ static void gather(orc_t *c, double px, double py, double pz, double out[6]) {
     int cid = cell_id(c, px, py, pz, NULL, NULL, NULL);
     cell_split(c, cid, &ix, &iy, &iz);
     double v[21];
-    v[0] = c->x0[0] + c->d[0] * ix;
-    v[1] = c->x0[1] + c->d[1] * iy;
-    v[2] = c->x0[2] + c->d[2] * iz;
+    /* the reference's ghost-offset vertex (a); the corrected policy's is the
+     * cell's own lower corner, grid point i at x0 + (i - 1) d */
+    const int vs = c->policy;
+    v[0] = c->x0[0] + c->d[0] * (ix - vs);
+    v[1] = c->x0[1] + c->d[1] * (iy - vs);
+    v[2] = c->x0[2] + c->d[2] * (iz - vs);
     const double *Ex = c->slot[EMOO_EX], *Ey = c->slot[EMOO_EY], *Ez = c->slot[EMOO_EZ];
     v[3] = Ex[IDX(c, ix, iy, iz)];
     v[4] = Ex[IDX(c, ix, iy + 1, iz)];
@@ -777,7 +794,8 @@ static void add_j(orc_t *c, int cid, const double *J) {
     Jx[IDX(c, ix, iy, iz)] += J[0];
     Jx[IDX(c, ix, iy + 1, iz)] += J[1];
     Jx[IDX(c, ix, iy + 1, iz + 1)] += J[2];
-    Jx[IDX(c, ix, iy + 1, iz)] += J[3];
+    if (c->policy) Jx[IDX(c, ix, iy, iz + 1)] += J[3]; /* corrected: the cell's own 4th x-edge */
+    else Jx[IDX(c, ix, iy + 1, iz)] += J[3];
     Jy[IDX(c, ix, iy, iz)] += J[4];
     Jy[IDX(c, ix, iy, iz + 1)] += J[5];
     Jy[IDX(c, ix + 1, iy, iz + 1)] += J[6];
@@ -832,9 +850,9 @@ static void deposit(orc_t *c, int with_rho) {
             cellID = tmp;
             int ix, iy, iz;
             cell_split(c, tmp, &ix, &iy, &iz);
-            verts[0] = c->x0[0] + c->d[0] * ix;
-            verts[1] = c->x0[1] + c->d[1] * iy;
-            verts[2] = c->x0[2] + c->d[2] * iz;
+            verts[0] = c->x0[0] + c->d[0] * (ix - c->policy);
+            verts[1] = c->x0[1] + c->d[1] * (iy - c->policy);
+            verts[2] = c->x0[2] + c->d[2] * (iz - c->policy);
         }
         double q = c->info.charge_ratio[s];
         double xp[3] = {c->x[p], c->y[p], c->z[p]};
@@ -1198,10 +1216,183 @@ int orc_gauss_residual(void *h, double *out2) {
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* the corrected-physics policy (no reference counterpart)              */
+
+/* Selects the corrected-physics policy (1) or the reference's arithmetic
+ * (0). The corrected policy needs periodic particle and field boundaries on
+ * every side (-1 otherwise): gather and deposit use the cell's own lower
+ * corner as vertex, the current comes from Villasenor and Buneman's
+ * charge-conserving deposit along each particle's straight path, and ghost
+ * copies and folds cover the whole transverse range of every component. */
+int orc_set_policy(void *h, int policy) {
+    orc_t *c = (orc_t *)h;
+    if (policy != 0 && policy != 1) return -1;
+    if (policy)
+        for (int s = 0; s < 6; s++)
+            if (c->pbc[s] != BC_PERIODIC || c->fbc[s] != BC_PERIODIC) return -1;
+    c->policy = policy;
+    return 0;
+}
+
+/* Villasenor-Buneman current (J. Villasenor and O. Buneman, Comput. Phys.
+ * Commun. 69 (1992) 306) of one particle moving in a straight line from p0
+ * to p1 (unwrapped, at most one cell face per axis): the path is split at
+ * the faces it crosses; a piece with offsets a -> b inside a cell (cell
+ * units, m = (a + b) / 2, D = b - a) adds to the cell's four x edges
+ * coef dx Dx ((1-my)(1-mz) + Dy Dz / 12), (my (1-mz) - ..), ((1-my) mz - ..),
+ * (my mz + ..) (edges at y, y+1 / z, z+1), and likewise for y and z. With the
+ * linear charge assignment this makes rho(t + dt) - rho(t) + dt div J = 0
+ * exactly at every point. coef = UNIT_RHOJ q / V / dt. */
+static void vb_deposit(orc_t *c, const double p0[3], const double p1[3], double coef) {
+    double u0[3], u1[3], ts[5];
+    int nt = 0;
+    ts[nt++] = 0.0;
+    for (int a = 0; a < 3; a++) {
+        u0[a] = (p0[a] - c->x0[a]) * c->id[a];
+        u1[a] = (p1[a] - c->x0[a]) * c->id[a];
+        double f0 = floor(u0[a]), f1 = floor(u1[a]);
+        if (f0 != f1) {
+            double b = f0 > f1 ? f0 : f1;
+            ts[nt++] = (b - u0[a]) / (u1[a] - u0[a]);
+        }
+    }
+    ts[nt++] = 1.0;
+    for (int i = 2; i < nt - 1; i++) /* insertion sort of the crossings */
+        for (int j = i; j > 1 && ts[j] < ts[j - 1]; j--) {
+            double t = ts[j]; ts[j] = ts[j - 1]; ts[j - 1] = t;
+        }
+    double *J[3] = {c->slot[EMOO_JX], c->slot[EMOO_JY], c->slot[EMOO_JZ]};
+    for (int sgi = 0; sgi + 1 < nt; sgi++) {
+        double ta = ts[sgi], tb = ts[sgi + 1];
+        if (!(tb > ta)) continue;
+        double a_[3], b_[3], m[3], D[3];
+        int cell[3];
+        for (int a = 0; a < 3; a++) {
+            double ua = u0[a] + ta * (u1[a] - u0[a]), ub = u0[a] + tb * (u1[a] - u0[a]);
+            cell[a] = (int)floor(0.5 * (ua + ub));
+            a_[a] = ua - cell[a];
+            b_[a] = ub - cell[a];
+            D[a] = b_[a] - a_[a];
+            m[a] = 0.5 * (a_[a] + b_[a]);
+        }
+        for (int a = 0; a < 3; a++) {
+            int jb = (a + 1) % 3, kb = (a + 2) % 3;
+            double w = coef * c->d[a] * D[a];
+            double cr = D[jb] * D[kb] / 12.0;
+            double W[4] = {w * ((1.0 - m[jb]) * (1.0 - m[kb]) + cr), w * (m[jb] * (1.0 - m[kb]) - cr),
+                           w * ((1.0 - m[jb]) * m[kb] - cr), w * (m[jb] * m[kb] + cr)};
+            for (int e = 0; e < 4; e++) {
+                int ii[3] = {cell[0] + 1, cell[1] + 1, cell[2] + 1};
+                ii[jb] += e & 1;
+                ii[kb] += e >> 1;
+                J[a][IDX(c, ii[0], ii[1], ii[2])] += W[e];
+            }
+        }
+    }
+}
+
+/* Push with the cached fields and the charge-conserving current of the
+ * move (before the boundaries wrap the particle). */
+static void push_vb(orc_t *c, double dt) {
+    long npts = c->npts;
+    for (int a = 0; a < 3; a++) memset(c->slot[EMOO_JX + a], 0, sizeof(double) * (size_t)npts);
+    double vol = c->d[0] * c->d[1] * c->d[2];
+    for (long p = 0; p < c->np; p++) {
+        int s = c->type[p];
+        double p0[3] = {c->x[p], c->y[p], c->z[p]};
+        double st[7] = {c->x[p], c->y[p], c->z[p], c->vx[p], c->vy[p], c->vz[p], c->g[p]};
+        double f[6] = {c->fe1[p], c->fe2[p], c->fe3[p], c->fb1[p], c->fb2[p], c->fb3[p]};
+        if (c->info.relativity == 0) boris(st, c->info.charge_ratio[s], c->info.mass_ratio[s], f, dt);
+        else vay(st, c->info.charge_ratio[s], c->info.mass_ratio[s], f, dt);
+        c->x[p] = st[0]; c->y[p] = st[1]; c->z[p] = st[2];
+        c->vx[p] = st[3]; c->vy[p] = st[4]; c->vz[p] = st[5]; c->g[p] = st[6];
+        if (c->info.isTestParticle[s] || !(dt > 0)) continue;
+        double p1[3] = {st[0], st[1], st[2]};
+        vb_deposit(c, p0, p1, UNIT_RHOJ * c->info.charge_ratio[s] / vol / dt);
+    }
+}
+
+/* rho alone at the particles' positions (the deposit's charge part). */
+static void deposit_rho_only(orc_t *c) {
+    double *save[3];
+    double *tmp = (double *)malloc(sizeof(double) * 3 * (size_t)c->npts);
+    for (int a = 0; a < 3; a++) {
+        save[a] = c->slot[EMOO_JX + a];
+        c->slot[EMOO_JX + a] = tmp + (size_t)a * c->npts;
+    }
+    deposit(c, 1);
+    for (int a = 0; a < 3; a++) c->slot[EMOO_JX + a] = save[a];
+    free(tmp);
+}
+
+/* Periodic copies and folds over the whole transverse range, dimension by
+ * dimension (so edge and corner lines follow): the ghost planes 0, n+1, n+2
+ * are the images of n, 1, 2. */
+static void full_plane(orc_t *c, double *f, int dim, int src, int dst, int sum) {
+    int o1 = (dim == 0) ? 1 : 0;
+    int o2 = (dim == 2) ? 1 : 2;
+    for (int p = 0; p < c->tot[o1]; p++)
+        for (int q = 0; q < c->tot[o2]; q++) {
+            int is[3], id_[3];
+            is[dim] = src; id_[dim] = dst;
+            is[o1] = id_[o1] = p;
+            is[o2] = id_[o2] = q;
+            if (sum) f[IDX(c, id_[0], id_[1], id_[2])] += f[IDX(c, is[0], is[1], is[2])];
+            else f[IDX(c, id_[0], id_[1], id_[2])] = f[IDX(c, is[0], is[1], is[2])];
+        }
+}
+
+static void corrected_fold(orc_t *c) {
+    const int ids[4] = {EMOO_JX, EMOO_JY, EMOO_JZ, EMOO_RHO};
+    for (int dim = 0; dim < 3; dim++) {
+        int n = c->n[dim];
+        for (int k = 0; k < 4; k++) {
+            double *f = c->slot[ids[k]];
+            full_plane(c, f, dim, 0, n, 1);
+            full_plane(c, f, dim, n + 1, 1, 1);
+            full_plane(c, f, dim, n + 2, 2, 1);
+        }
+    }
+}
+
+static void corrected_ghosts(orc_t *c) {
+    const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
+    for (int dim = 0; dim < 3; dim++) {
+        int n = c->n[dim];
+        for (int k = 0; k < 9; k++) {
+            double *f = c->slot[ids[k]];
+            full_plane(c, f, dim, n, 0, 0);
+            full_plane(c, f, dim, 1, n + 1, 0);
+            full_plane(c, f, dim, 2, n + 2, 0);
+        }
+    }
+}
+
 /* One pass of the driver loop, src/main.cpp:221-287 (history cadence of
  * src/IO/output.cpp:46,68-71: every 10 steps from step 0). */
 int orc_step(void *h, int ti, long *counts6, double *hist8, int *hist_written) {
     orc_t *c = (orc_t *)h;
+    if (c->policy) {
+        if (c->info.nstep_sort > 0 && ti % c->info.nstep_sort == 0) orc_sort(c);
+        *hist_written = 0;
+        if (ti >= c->next_hist) {
+            orc_history(c, c->t, hist8);
+            c->next_hist += 10;
+            *hist_written = 1;
+        }
+        push_vb(c, c->dtp);
+        if (orc_particle_bc(c, counts6)) return -2;
+        orc_clear_ghosts(c);
+        deposit_rho_only(c);
+        corrected_fold(c);
+        if (c->info.electrostatic == 1) evolve_es(c, c->dtp);
+        else evolve(c, c->dtp);
+        corrected_ghosts(c);
+        orc_interpolate(c);
+        c->t += c->dtp;
+        return 0;
+    }
     if (c->info.nstep_sort > 0 && ti % c->info.nstep_sort == 0) orc_sort(c);
     *hist_written = 0;
     if (ti >= c->next_hist) {

@@ -73,6 +73,7 @@ def _load_cpu_lib(path, prefix):
         f("set_rho_background", None, [P, C.c_double])
         f("set_wave_shape", C.c_int, [P, C.c_int, C.POINTER(abi.WaveShape)])
         f("set_rho_background_xmin", None, [P, C.c_double])
+        f("set_policy", C.c_int, [P, C.c_int])
     return L
 
 
@@ -245,12 +246,16 @@ class OracleBackend(CpuBackend):
         if rc != 0:
             raise ValueError("orc_set_wave_shape refused the shape")
 
+    def set_policy(self, policy):
+        if self._f("set_policy")(self.h, policy) != 0:
+            raise ValueError("orc_set_policy refused the policy")
+
 
 class GpuBackend:
     """The product, through include/emoo.h."""
 
     def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0, rho_background=0.0,
-                 rho_background_xmin=None):
+                 rho_background_xmin=None, policy=abi.POLICY_REFERENCE):
         self.L = abi.lib()
         self.info = info
         self.n = [info.nCell[d] for d in range(3)]
@@ -265,6 +270,7 @@ class GpuBackend:
         o.rho_background = rho_background
         if rho_background_xmin is not None:
             o.rho_background_xmin = rho_background_xmin
+        o.policy = policy
         h = C.c_void_p()
         abi.check(self.L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
         self.h = h

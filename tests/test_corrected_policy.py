@@ -1,0 +1,188 @@
+"""The corrected-physics policy (no reference counterpart): the cell's own
+lower corner as gather / deposit vertex, the Villasenor-Buneman
+charge-conserving current, ghost copies and folds over the whole range of
+every component; periodic boundaries only.
+
+CPU (oracle): the discrete continuity equation rho(t + dt) - rho(t) + dt div J
+= 0 holds at every point to rounding, so the Gauss-law residual div E - 4 pi
+rho keeps its initial value step after step; the policy refuses walls.
+GPU: the FP64 form against the oracle, and the residual's conservation."""
+import numpy as np
+import pytest
+
+from apc_524_project_gb300 import abi, configs, loading
+from backends import OracleBackend, by_id, rel_l2
+
+FP64_RTOL = 1e-9
+
+
+def _cfg(relativity=1, n=(6, 5, 4), dx=(0.9, 1.2, 0.7), steps=6, vth=0.15, nstep_sort=0):
+    return configs.tiny("corr", n=n, dx=dx, relativity=relativity, init="poisson", vth=vth, steps=steps,
+                        nstep_sort=nstep_sort, dt=0.3)
+
+
+def _load(b, parts):
+    nid = 0
+    for si, p in enumerate(parts):
+        b.add_species(si, p, ids=np.arange(nid, nid + len(p["x"])))
+        nid += len(p["x"])
+
+
+def _periodic(f, n):
+    """The ghost planes 0 and n+1 set to their periodic images n and 1 (a fold
+    leaves J's ghost planes holding their own deposits only)."""
+    g = f.copy()
+    for d in range(3):
+        src, dst = [slice(None)] * 3, [slice(None)] * 3
+        src[d], dst[d] = n[d], 0
+        g[tuple(dst)] = g[tuple(src)]
+        src[d], dst[d] = 1, n[d] + 1
+        g[tuple(dst)] = g[tuple(src)]
+    return g
+
+
+def _div(f, dx, n):
+    """Backward-difference divergence at the physical points, periodic."""
+    Ex, Ey, Ez = (_periodic(a, n) for a in f)
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    return ((Ex[P] - Ex[0:n[0], 1:n[1] + 1, 1:n[2] + 1]) / dx[0] + (Ey[P] - Ey[1:n[0] + 1, 0:n[1], 1:n[2] + 1]) / dx[1]
+            + (Ez[P] - Ez[1:n[0] + 1, 1:n[1] + 1, 0:n[2]]) / dx[2])
+
+
+def _oracle(cfg, policy=1):
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    o.set_policy(policy)
+    _load(o, loading.sample_all(cfg))
+    return o
+
+
+@pytest.mark.parametrize("relativity", [0, 1])
+def test_oracle_continuity_and_gauss_law(relativity):
+    cfg = _cfg(relativity)
+    n = cfg.n
+    o = _oracle(cfg)
+    o.init_fields()
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    rho0 = o.get_field(abi.RHO)[P].copy()
+    res0 = _div([o.get_field(i) for i in (abi.EX, abi.EY, abi.EZ)], cfg.dx, n) - 4 * np.pi * rho0
+    scale = np.abs(rho0).max()
+    for ti in range(cfg.steps):
+        o.step(ti)
+        rho1 = o.get_field(abi.RHO)[P]
+        divj = _div([o.get_field(i) for i in (abi.JX, abi.JY, abi.JZ)], cfg.dx, n)
+        cont = (rho1 - rho0) + cfg.dt * divj
+        assert np.abs(cont).max() <= 1e-12 * scale, (ti, np.abs(cont).max(), scale)
+        rho0 = rho1.copy()
+    res = _div([o.get_field(i) for i in (abi.EX, abi.EY, abi.EZ)], cfg.dx, n) - 4 * np.pi * rho0
+    assert np.abs(res - res0).max() <= 1e-10 * 4 * np.pi * scale
+    o.close()
+
+
+def test_oracle_refuses_walls():
+    cfg = configs.tiny("walls", part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
+                       field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
+                       init="constant")
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    with pytest.raises(ValueError):
+        o.set_policy(1)
+    o.close()
+
+
+def test_reference_policy_does_not_conserve_charge():
+    """The reference's deposit (ghost-offset vertex, current at the new
+    position) breaks the continuity equation: what the corrected policy fixes."""
+    cfg = _cfg(1)
+    n = cfg.n
+    o = _oracle(cfg, policy=0)
+    o.init_fields()
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    rho0 = o.get_field(abi.RHO)[P].copy()
+    o.step(0)
+    rho1 = o.get_field(abi.RHO)[P]
+    divj = _div([o.get_field(i) for i in (abi.JX, abi.JY, abi.JZ)], cfg.dx, n)
+    assert np.abs(rho1 - rho0 + cfg.dt * divj).max() > 1e-3 * np.abs(rho0).max()
+    o.close()
+
+
+# ---- GPU -------------------------------------------------------------------
+
+def _gpu(cfg, precision=abi.FP64, policy=abi.POLICY_CORRECTED):
+    from backends import GpuBackend
+
+    g = GpuBackend(configs.input_info(cfg), cfg.dt, precision=precision, policy=policy)
+    _load(g, loading.sample_all(cfg))
+    return g
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("relativity", [0, 1])
+def test_gpu_corrected_policy_matches_oracle(relativity):
+    cfg = _cfg(relativity, nstep_sort=3)
+    g = _gpu(cfg)
+    o = _oracle(cfg)
+    rg, _ = g.init_fields()
+    ro, _ = o.init_fields()
+    assert rg == ro
+    for ti in range(cfg.steps):
+        assert g.step(1) == o.step(ti)[0], ti
+    for i in range(13):
+        assert rel_l2(g.get_field(i), o.get_field(i)) <= FP64_RTOL, abi.FIELD_NAMES[i]
+    pg, po = by_id(g.particles()), by_id(o.particles())
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert rel_l2(pg[k], po[k]) <= FP64_RTOL, k
+    g.close()
+    o.close()
+
+
+@pytest.mark.gpu
+def test_gpu_corrected_policy_keeps_gauss_law():
+    cfg = _cfg(1, n=(8, 6, 5), steps=10)
+    n = cfg.n
+    g = _gpu(cfg)
+    g.init_fields()
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+
+    def residual():
+        return _div([g.get_field(i) for i in (abi.EX, abi.EY, abi.EZ)], cfg.dx, n) - 4 * np.pi * g.get_field(abi.RHO)[P]
+
+    r0 = residual()
+    scale = 4 * np.pi * np.abs(g.get_field(abi.RHO)[P]).max()
+    g.step(cfg.steps)
+    assert np.abs(residual() - r0).max() <= 1e-10 * scale
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_corrected_policy_refuses_what_it_does_not_cover():
+    with pytest.raises(Exception):
+        _gpu(_cfg(1), precision=abi.MIXED)
+    walls = configs.tiny("walls", part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
+                         field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
+                         init="constant")
+    with pytest.raises(Exception):
+        _gpu(walls)
+
+
+@pytest.mark.gpu
+def test_gpu_corrected_policy_is_stable_where_the_reference_is_not():
+    """Thermal plasma 16^3, 2 x 16 ppc, v_th 0.1c, dt 0.125, 600 steps: the
+    reference's arithmetic heats the plasma (total energy grows several-fold);
+    the corrected policy keeps it within a few per cent."""
+    from backends import GpuBackend
+
+    cfg = configs.thermal256(16)
+    cfg.dt = 0.125
+
+    def history(policy):
+        g = GpuBackend(configs.input_info(cfg), cfg.dt, policy=policy, track_ids=0)
+        for si, p in enumerate(loading.sample_all(cfg)):
+            g.add_species(si, p)
+        g.init_fields()
+        g.step(600)
+        rows = g.history_rows()
+        g.close()
+        return rows[:, 7] / rows[0, 7]
+
+    ref, cor = history(abi.POLICY_REFERENCE), history(abi.POLICY_CORRECTED)
+    assert ref[-1] > 2.0, ref[-1]
+    assert np.abs(cor - 1.0).max() < 0.1, np.abs(cor - 1.0).max()

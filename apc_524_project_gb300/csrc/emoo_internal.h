@@ -212,6 +212,7 @@ int fold_f64(emoo_handle *h, int dim, int what = FOLD_ALL);
 // over the whole transverse range, dimension by dimension
 int fold_full_f64(emoo_handle *h, int what);
 int ghost_full_f64(emoo_handle *h);
+int ghost_e_full_f64(emoo_handle *h);
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
 int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);
 int phi_to_e_f64(emoo_handle *h);

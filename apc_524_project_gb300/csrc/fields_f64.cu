@@ -380,6 +380,11 @@ int yee_f64(emoo_handle *h, double dt) {
     CF3 J = {{h->slot[EMOO_JX], h->slot[EMOO_JY], h->slot[EMOO_JZ]}};
     h->launches++;
     k_yee_e<<<grd, blk, 0, h->stream>>>(g, dt, E, T, J);
+    // The B half reads E one plane past the high faces. The reference refreshes
+    // those ghosts only after both halves, so at the periodic wrap B sees the
+    // previous step's E: the leapfrog loses its time centring there and vacuum
+    // fields grow without bound at dt 0.5. The corrected policy refreshes them.
+    if (h->policy == EMOO_POLICY_CORRECTED) EMOO_TRY(ghost_e_full_f64(h));
     F3 B = {{role_b(h, 0), role_b(h, 1), role_b(h, 2)}};
     CF3 Ec = {{E.p[0], E.p[1], E.p[2]}};
     h->launches++;
@@ -496,6 +501,11 @@ int fold_full_f64(emoo_handle *h, int what) {
         for (int c = 0; c < 3; c++) ids[n++] = EMOO_JX + c;
     if (what & FOLD_RHO) ids[n++] = EMOO_RHO;
     return periodic_full(h, ids, n, 1);
+}
+
+int ghost_e_full_f64(emoo_handle *h) {
+    static const int ids[3] = {EMOO_EX, EMOO_EY, EMOO_EZ};
+    return periodic_full(h, ids, 3, 0);
 }
 
 int ghost_full_f64(emoo_handle *h) {

@@ -518,6 +518,7 @@ static void poisson_bc(orc_t *c, int s, int id) {
 /* Grid::executeBC(sendID), src/grid/grid.cpp:577-585, dispatching to
  * BC_F_Periodic::completeBC (src/boundaries/b_fields/bc_f_periodic.cpp:34-57)
  * and BC_F_External::completeBC (src/boundaries/b_fields/bc_f_external.cpp:45-58). */
+static void full_plane(orc_t *c, double *f, int dim, int src, int dst, int sum);
 static void corrected_fold(orc_t *c);
 static void corrected_ghosts(orc_t *c);
 
@@ -959,6 +960,16 @@ static void evolve(orc_t *c, double dt) {
                                       4 * PI_D * Jy[o]);
                 Ez[o] = Ez[o] - dt * ((Tx[o] - Tx[IDX(c, i, j - 1, k)]) / dy - (Ty[o] - Ty[IDX(c, i - 1, j, k)]) / dx +
                                       4 * PI_D * Jz[o]);
+            }
+    /* corrected policy: the B half below reads E at plane n+1, so refresh
+     * E's periodic ghosts first (time-centred leapfrog at the wrap) */
+    if (c->policy)
+        for (int dim = 0; dim < 3; dim++)
+            for (int a = 0; a < 3; a++) {
+                double *f = c->slot[EMOO_EX + a];
+                full_plane(c, f, dim, c->n[dim], 0, 0);
+                full_plane(c, f, dim, 1, c->n[dim] + 1, 0);
+                full_plane(c, f, dim, 2, c->n[dim] + 2, 0);
             }
     for (int i = 1; i <= nx; i++)
         for (int j = 1; j <= ny; j++)

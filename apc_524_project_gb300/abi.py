@@ -99,6 +99,8 @@ class Opts(C.Structure):
         ("rho_background", C.c_double),
         ("rho_background_xmin", C.c_double),
         ("policy", C.c_int),
+        ("poisson_solver", C.c_int),
+        ("poisson_rtol", C.c_double),
     ]
 
 
@@ -129,6 +131,7 @@ AD_FORWARD, AD_TANGENT, AD_ADJOINT = 0, 1, 2
 AD_OBJ_FIELD, AD_OBJ_KINETIC = 0, 1
 FIELDS_RHO, FIELDS_E, FIELDS_J, FIELDS_B, FIELDS_ALL = 0, 1, 2, 3, 4
 POLICY_REFERENCE, POLICY_CORRECTED = 0, 1
+POISSON_JACOBI, POISSON_MULTIGRID = 0, 1
 NCOEF = 16
 
 

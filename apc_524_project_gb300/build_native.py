@@ -25,6 +25,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + I
 # (source, extra nvcc flags)
 CUDA_UNITS = [
     ("fields_f64.cu", ["--fmad=false"]),
+    ("multigrid.cu", []),
     ("particles_f64.cu", ["--fmad=false"]),
     ("loader.cu", ["--fmad=false"]),
     ("sort.cu", []),

@@ -562,6 +562,21 @@ int poisson_init(emoo_handle *h, int iters[4]) {
     double mult = -4 * PI_D;
     double tol = std::max(conv_phi * CONV_RATIO, CONV_CRIT);
     int it[4] = {0, 0, 0, 0}, cv, ok = 1;
+    if (h->poisson_solver == EMOO_POISSON_MULTIGRID) {
+        // the same four solves, phiToE after the first and AToB after the last
+        for (int q = 0; q < 4; q++) {
+            EMOO_TRY(multigrid_f64(h, q == 0 ? EMOO_PHI1 : EMOO_AX1 + (q - 1), q == 0 ? EMOO_PHI2 : EMOO_AX2 + (q - 1),
+                                   q == 0 ? EMOO_RHO : EMOO_JX + (q - 1), mult, &it[q], &cv));
+            ok &= cv;
+            if (q == 0) EMOO_TRY(phi_to_e_f64(h));
+        }
+        EMOO_TRY(a_to_b_f64(h));
+        EMOO_TRY(execute_bc_slots(h, EMOO_SEND_EB));
+        if (h->precision != EMOO_FP64) EMOO_TRY(mixed_fields_from_slots(h));
+        if (iters)
+            for (int q = 0; q < 4; q++) iters[q] = it[q];
+        return ok ? EMOO_OK : EMOO_ERR_NOT_CONVERGED;
+    }
     EMOO_TRY(jacobi_f64(h, EMOO_PHI1, EMOO_PHI2, EMOO_RHO, tol, mult, &it[0], &cv));
     ok &= it[0] < ITER_MAX;
     EMOO_TRY(phi_to_e_f64(h));
@@ -724,6 +739,8 @@ int emoo_default_opts(emoo_opts *o) {
     o->history_every = 10;
     o->rho_background = 0.0;
     o->rho_background_xmin = -HUGE_VAL;
+    o->poisson_solver = EMOO_POISSON_JACOBI;
+    o->poisson_rtol = 1e-10;
     return EMOO_OK;
 }
 
@@ -732,7 +749,7 @@ const char *emoo_strerror(int s) {
         case EMOO_OK: return "ok";
         case EMOO_ERR_ARG: return "bad argument";
         case EMOO_ERR_OOM: return "out of memory or capacity";
-        case EMOO_ERR_NOT_CONVERGED: return "Jacobi Poisson solve did not converge";
+        case EMOO_ERR_NOT_CONVERGED: return "Poisson solve did not converge (Jacobi iteration cap or multigrid cycle cap)";
         case EMOO_ERR_FIXED_OVERFLOW: return "fixed-point accumulator saturated";
         case EMOO_ERR_BOUNDS: return "device bounds check failed";
         case EMOO_ERR_CUDA: return "CUDA runtime error";
@@ -796,6 +813,15 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
                 if (h->bc.pbc[s] != PBC_PERIODIC || h->bc.fbc[s] != FBC_PERIODIC) prc = EMOO_ERR_UNSUPPORTED;
             h->policy = o.policy;
             h->g.vshift = 1;
+        }
+        if (o.poisson_solver != EMOO_POISSON_JACOBI && o.poisson_solver != EMOO_POISSON_MULTIGRID) prc = EMOO_ERR_ARG;
+        if (o.poisson_solver == EMOO_POISSON_MULTIGRID) {
+            for (int d = 0; d < 3; d++) {
+                int a = h->bc.fbc[2 * d], b = h->bc.fbc[2 * d + 1];
+                if (a != b || (a != FBC_PERIODIC && a != FBC_EXTERNAL)) prc = EMOO_ERR_UNSUPPORTED;
+            }
+            h->poisson_solver = o.poisson_solver;
+            h->poisson_rtol = o.poisson_rtol > 0 ? o.poisson_rtol : 1e-10;
         }
         if (prc != EMOO_OK) {
             emoo_destroy(h);
@@ -865,6 +891,7 @@ int emoo_destroy(emoo_handle *h) {
     dfree(h->wprof);
     dfree(h->wproff);
     if (h->jacobi_state) cudaFree(h->jacobi_state);
+    multigrid_free(h);
     for (int i = 0; i < 2; i++)
         if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
     for (cudaEvent_t e : h->prof_pending) cudaEventDestroy(e);

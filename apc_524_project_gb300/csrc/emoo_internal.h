@@ -153,6 +153,9 @@ struct emoo_handle {
     double *red = nullptr;  // reduction partials
     size_t red_cap = 0;
     void *jacobi_state = nullptr;
+    int poisson_solver = 0;      // EMOO_POISSON_JACOBI / EMOO_POISSON_MULTIGRID
+    double poisson_rtol = 1e-10; // multigrid stop, relative to the start residual
+    void *mg = nullptr;          // multigrid levels (multigrid.cu), kept between solves
 
     double dt = 0.0;    // configured step
     double t = 0.0;     // time_phys
@@ -213,6 +216,9 @@ int fold_f64(emoo_handle *h, int dim, int what = FOLD_ALL);
 int fold_full_f64(emoo_handle *h, int what);
 int ghost_full_f64(emoo_handle *h);
 int ghost_e_full_f64(emoo_handle *h);
+int poisson_field_bc(emoo_handle *h, int id);
+int multigrid_f64(emoo_handle *h, int id1, int id2, int rid, double mult, int *cycles, int *converged);
+void multigrid_free(emoo_handle *h);
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
 int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);
 int phi_to_e_f64(emoo_handle *h);

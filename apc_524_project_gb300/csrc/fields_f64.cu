@@ -602,6 +602,10 @@ static int single_field_bc(emoo_handle *h, int id, const int *skip) {
     return EMOO_OK;
 }
 
+// The Poisson fields' boundary fill (executeBC(fieldID)) as the Jacobi loop
+// applies it, for the multigrid's start and result.
+int poisson_field_bc(emoo_handle *h, int id) { return single_field_bc(h, id, nullptr); }
+
 // Poisson_Solver::run_poisson_solver_, src/poisson/poisson.cpp:172-287, with
 // the iteration control on the device: iterations are queued in batches and
 // become no-ops once the stop test of the reference has fired.

@@ -50,6 +50,9 @@ def _args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-laser512", action="store_true")
+    ap.add_argument("--no-poisson", action="store_true")
+    ap.add_argument("--only", choices=["poisson"], default=None,
+                    help="run one side measurement alone and print its JSON line")
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=6)
     return ap.parse_args()
@@ -147,7 +150,7 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ GPU arms
 
-def _make_handle(cfg, precision, capacity, device):
+def _make_handle(cfg, precision, capacity, device, poisson_solver=0):
     from apc_524_project_gb300 import abi, configs
 
     L = abi.lib()
@@ -155,6 +158,7 @@ def _make_handle(cfg, precision, capacity, device):
     o = abi.Opts()
     L.emoo_default_opts(C.byref(o))
     o.precision = precision
+    o.poisson_solver = poisson_solver
     o.dt = cfg.dt
     o.capacity = capacity
     o.track_ids = 0
@@ -280,7 +284,86 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
         res["adjoint"] = adjoint_arm()
     if not args.no_laser512:
         res["laser512"] = laser512_arm(device)
+    if not args.no_poisson:
+        res["poisson"] = poisson_arm(device)
     return cfg, res
+
+
+def _poisson_solve_ms(L, h, reps):
+    """Wall time of emoo_poisson_init (synchronous; the four solves, phiToE,
+    AToB and the E/B fill) on the fields the handle holds, best of reps."""
+    from apc_524_project_gb300 import abi
+
+    it = (C.c_int * 4)()
+    best, rc = None, None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        rc = L.emoo_poisson_init(h, it)
+        t = time.perf_counter() - t0
+        if rc not in (abi.OK, abi.ERR_NOT_CONVERGED):
+            abi.check(rc, "emoo_poisson_init")
+        best = t if best is None else min(best, t)
+    return best * 1e3, list(it), rc == abi.OK
+
+
+def poisson_arm(device):
+    """The field start (four Poisson solves, phiToE, AToB): the reference's
+    Jacobi iteration against the multigrid solve of the same discrete
+    equations, both on the GPU in FP64. (1) The Langmuir workload's start,
+    32^3 periodic, rho and J deposited from its 524,288 particles: the Jacobi
+    runs into its 10000-sweep cap (the odd-even mode of an even periodic grid
+    never decays); E then differs from the exact solution by that mode.
+    (2) A periodic box of the laser-plasma size, 512 x 128 x 128 cells,
+    seeded rho and J (mean-free noise)."""
+    import numpy as np
+    import torch
+    from apc_524_project_gb300 import abi, configs
+
+    L = abi.lib()
+    out = {}
+    n = (512, 128, 128)
+    big = configs.tiny("poisson512", n=n, init="poisson", ppc=1)
+    info = configs.input_info(big)
+    shape = tuple(v + 3 for v in n)
+    rng = np.random.default_rng(5)
+    src = {abi.RHO: rng.normal(0.0, 1e-3, shape)}
+    for q in range(3):
+        src[abi.JX + q] = rng.normal(0.0, 5e-4, shape)
+    box = {"workload": "periodic 512x128x128 cells, seeded rho and J"}
+    for solver, name in ((abi.POISSON_MULTIGRID, "multigrid"), (abi.POISSON_JACOBI, "jacobi")):
+        o = abi.Opts()
+        L.emoo_default_opts(C.byref(o))
+        o.device = device
+        o.capacity = 1
+        o.track_ids = 0
+        o.poisson_solver = solver
+        h = C.c_void_p()
+        abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
+        for fid, a in src.items():
+            abi.check(L.emoo_set_field(h, fid, a.ctypes.data_as(C.POINTER(C.c_double))), "emoo_set_field")
+        ms, it, ok = _poisson_solve_ms(L, h, 1 if solver == abi.POISSON_JACOBI else 3)
+        box[name] = {"ms": ms, "iterations" if solver == abi.POISSON_JACOBI else "v_cycles": it, "converged": ok}
+        abi.check(L.emoo_destroy(h))
+        torch.cuda.synchronize()
+    box["speedup"] = box["jacobi"]["ms"] / box["multigrid"]["ms"]
+    out["box512x128x128"] = box
+    cfg = configs.langmuir32()
+    N = cfg.total_particles()
+    ex = {}
+    lang = {"workload": "Langmuir 32^3 periodic field start, rho/J from 524,288 particles"}
+    for solver, name in ((abi.POISSON_JACOBI, "jacobi"), (abi.POISSON_MULTIGRID, "multigrid")):
+        h = _make_handle(cfg, abi.FP64, N, device, poisson_solver=solver)
+        ms, it, ok = _poisson_solve_ms(L, h, 1 if solver == abi.POISSON_JACOBI else 3)
+        lang[name] = {"ms": ms, "iterations" if solver == abi.POISSON_JACOBI else "v_cycles": it, "converged": ok}
+        a = np.zeros(tuple(v + 3 for v in cfg.n))
+        abi.check(L.emoo_get_field(h, abi.EX, a.ctypes.data_as(C.POINTER(C.c_double))), "emoo_get_field")
+        ex[name] = a
+        abi.check(L.emoo_destroy(h))
+    lang["speedup"] = lang["jacobi"]["ms"] / lang["multigrid"]["ms"]
+    lang["ex_rel_l2_jacobi_vs_multigrid"] = float(np.linalg.norm(ex["jacobi"] - ex["multigrid"]) /
+                                                  np.linalg.norm(ex["multigrid"]))
+    out["langmuir32"] = lang
+    return out
 
 
 def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
@@ -517,6 +600,13 @@ def main():
     if args.impl == "reference":
         reference_arm(args)
         return
+    if args.only == "poisson":
+        res = poisson_arm(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"metric": "field start (four Poisson solves + phiToE + AToB), multigrid",
+                          "value": res["box512x128x128"]["multigrid"]["ms"], "unit": "ms",
+                          "higher_is_better": False, "dtype": "f64 (FP32 V-cycles)", "data": "synthetic",
+                          "config": {"workload": res["box512x128x128"]["workload"]}, "poisson": res}), flush=True)
+        return
     from apc_524_project_gb300 import replicas
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -571,6 +661,8 @@ def main():
         line["adjoint"] = res["adjoint"]
     if "laser512" in res:
         line["laser512"] = res["laser512"]
+    if "poisson" in res:
+        line["poisson"] = res["poisson"]
     if "e2e" in res:
         e = res["e2e"]
         line["e2e"] = {"value": N * e["steps"] * world / e["t"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

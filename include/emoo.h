@@ -32,7 +32,7 @@ extern "C" {
 #define EMOO_OK 0
 #define EMOO_ERR_ARG (-1)            /* bad argument (null pointer, out-of-range id, size) */
 #define EMOO_ERR_OOM (-2)            /* device or host allocation failed, or capacity exceeded */
-#define EMOO_ERR_NOT_CONVERGED (-3)  /* Jacobi Poisson solve reached its iteration cap */
+#define EMOO_ERR_NOT_CONVERGED (-3)  /* Poisson solve reached its iteration (Jacobi) or cycle (multigrid) cap */
 #define EMOO_ERR_FIXED_OVERFLOW (-4) /* fixed-point current/charge accumulator saturated */
 #define EMOO_ERR_BOUNDS (-5)         /* a device-side bounds check recorded a bad index */
 #define EMOO_ERR_CUDA (-6)           /* a CUDA runtime call failed */
@@ -141,7 +141,27 @@ typedef struct emoo_opts {
     double rho_background_xmin; /* the background covers the physical points with x >= this
                                    (emoo_default_opts: -HUGE_VAL, every point) */
     int policy;            /* EMOO_POLICY_REFERENCE (default) or EMOO_POLICY_CORRECTED */
+    int poisson_solver;    /* EMOO_POISSON_JACOBI (default) or EMOO_POISSON_MULTIGRID */
+    double poisson_rtol;   /* multigrid stop: max |residual| <= rtol max |right side| (default 1e-10) */
 } emoo_opts;
+
+/* Field-start solvers for "poisson" initialisation. JACOBI is
+ * Poisson_Solver::run_poisson_solver_ (src/poisson/poisson.cpp:172-287) with
+ * its stop test and 10000-iteration cap, bit-compatible with the reference.
+ * MULTIGRID (no reference counterpart) solves the same discrete equations -
+ * the Jacobi iteration's fixed point: the 7-point Laplacian of phi (A) equals
+ * -4 pi rho (J) at every unknown point, periodic dimensions wrapping and
+ * external ones holding the PoissonBC planes 1 and n + 1 - by FP64 V-cycles
+ * until max |residual| <= poisson_rtol max |right side|, in tens of cycles
+ * where the Jacobi needs thousands of sweeps or never meets its test (on a
+ * periodic grid with an even side the Jacobi iteration's odd-even mode does
+ * not decay). With every dimension periodic the right side's mean is removed
+ * and the potential's mean is set to zero, invisible to phiToE / AToB. The
+ * iteration counts emoo_init_fields reports are then V-cycles. Both
+ * dimensions' sides must be periodic, or both external, for MULTIGRID
+ * (EMOO_ERR_UNSUPPORTED at emoo_create otherwise). */
+#define EMOO_POISSON_JACOBI 0
+#define EMOO_POISSON_MULTIGRID 1
 
 /* Physics policies. REFERENCE reproduces the reference's arithmetic with its
  * quirks (ghost-offset gather / deposit vertex, the Jx index of Grid::addJ,

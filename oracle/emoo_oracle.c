@@ -96,6 +96,10 @@ typedef struct {
     /* 1: the corrected-physics policy (no reference counterpart; see
      * orc_set_policy), 0: the reference's arithmetic */
     int policy;
+    /* field start solver: 0 the reference's Jacobi, 1 the exact discrete
+     * solution (see orc_set_poisson_solver) */
+    int poisson_solver;
+    double poisson_rtol;
 } orc_t;
 
 /* ------------------------------------------------------------------ */
@@ -1042,6 +1046,136 @@ static int jacobi(orc_t *c, int id1, int id2, const double *R, double tol, doubl
     return iternum;
 }
 
+/* The discrete problem the Jacobi iteration of run_poisson_solver_
+ * (src/poisson/poisson.cpp:216-241) has as its fixed point, solved outright:
+ * at every unknown point the 7-point Laplacian of u equals mult R, where a
+ * dimension with periodic field boundaries wraps (unknowns 1..n) and one with
+ * external boundaries holds the PoissonBC values on planes 1 and n + 1
+ * (unknowns 2..n). Conjugate gradients on -Laplacian (symmetric positive
+ * semi-definite), to |r| <= rtol |b| in the 2-norm; with every dimension
+ * periodic the right side's mean is removed first (the system is singular
+ * and consistent only then) and the solution's mean set to zero, which the
+ * field differences of phiToE / AToB do not see. The result goes to id1,
+ * ghost planes by the same boundary fill as the Jacobi, and a copy to id2.
+ * Returns the iteration count, or -1 when a side's field boundary is neither
+ * periodic nor external or the two sides of a dimension differ. *conv = 1
+ * when the tolerance was met within the iteration cap. */
+static int exact_poisson(orc_t *c, int id1, int id2, const double *R, double mult, double rtol, int *conv) {
+    int per[3], lo[3], hi[3], m[3];
+    *conv = 0;
+    for (int d = 0; d < 3; d++) {
+        int a = c->fbc[2 * d], b = c->fbc[2 * d + 1];
+        if (a != b || (a != BC_PERIODIC && a != BC_EXTERNAL)) return -1;
+        per[d] = a == BC_PERIODIC;
+        lo[d] = per[d] ? 1 : 2;
+        hi[d] = c->n[d];
+        m[d] = hi[d] - lo[d] + 1;
+        if (m[d] < 1) return -1;
+    }
+    double *u = c->slot[id1];
+    for (long o = 0; o < c->npts; o++) u[o] = 0.0;
+    orc_execute_bc(c, id1); /* the Dirichlet planes */
+    long nu = (long)m[0] * m[1] * m[2];
+    double *x = calloc(nu, sizeof(double)), *r = malloc(nu * sizeof(double));
+    double *p = malloc(nu * sizeof(double)), *q = malloc(nu * sizeof(double));
+    double cd[3];
+    for (int d = 0; d < 3; d++) cd[d] = 1.0 / (c->d[d] * c->d[d]);
+#define UIDX(a, b, e) (((long)(a) * m[1] + (b)) * m[2] + (e))
+    /* b = -mult R + (boundary neighbours' values) / h^2 */
+    for (int a = 0; a < m[0]; a++)
+        for (int b = 0; b < m[1]; b++)
+            for (int e = 0; e < m[2]; e++) {
+                int ii[3] = {a + lo[0], b + lo[1], e + lo[2]};
+                double v = -mult * R[IDX(c, ii[0], ii[1], ii[2])];
+                for (int d = 0; d < 3; d++) {
+                    if (per[d]) continue;
+                    int jj[3] = {ii[0], ii[1], ii[2]};
+                    if (ii[d] == lo[d]) {
+                        jj[d] = 1;
+                        v += cd[d] * u[IDX(c, jj[0], jj[1], jj[2])];
+                    }
+                    if (ii[d] == hi[d]) {
+                        jj[d] = c->n[d] + 1;
+                        v += cd[d] * u[IDX(c, jj[0], jj[1], jj[2])];
+                    }
+                }
+                r[UIDX(a, b, e)] = v;
+            }
+    int allper = per[0] && per[1] && per[2];
+    if (allper) {
+        double mean = 0.0;
+        for (long t = 0; t < nu; t++) mean += r[t];
+        mean /= (double)nu;
+        for (long t = 0; t < nu; t++) r[t] -= mean;
+    }
+    double bn = 0.0;
+    for (long t = 0; t < nu; t++) bn += r[t] * r[t];
+    bn = sqrt(bn);
+    double rr = bn * bn;
+    for (long t = 0; t < nu; t++) p[t] = r[t];
+    int it = 0;
+    const int cap = 100000;
+    while (sqrt(rr) > rtol * bn && it < cap) {
+        /* q = -Laplacian(p), homogeneous boundaries */
+        double pq = 0.0;
+        for (int a = 0; a < m[0]; a++)
+            for (int b = 0; b < m[1]; b++)
+                for (int e = 0; e < m[2]; e++) {
+                    int ii[3] = {a, b, e};
+                    double v = 2.0 * (cd[0] + cd[1] + cd[2]) * p[UIDX(a, b, e)];
+                    for (int d = 0; d < 3; d++)
+                        for (int sgn = -1; sgn <= 1; sgn += 2) {
+                            int jj[3] = {ii[0], ii[1], ii[2]};
+                            jj[d] += sgn;
+                            if (jj[d] < 0 || jj[d] >= m[d]) {
+                                if (!per[d]) continue;
+                                jj[d] = (jj[d] + m[d]) % m[d];
+                            }
+                            v -= cd[d] * p[UIDX(jj[0], jj[1], jj[2])];
+                        }
+                    q[UIDX(a, b, e)] = v;
+                    pq += v * p[UIDX(a, b, e)];
+                }
+        double alpha = rr / pq;
+        double rr1 = 0.0;
+        for (long t = 0; t < nu; t++) {
+            x[t] += alpha * p[t];
+            r[t] -= alpha * q[t];
+            rr1 += r[t] * r[t];
+        }
+        double beta = rr1 / rr;
+        rr = rr1;
+        for (long t = 0; t < nu; t++) p[t] = r[t] + beta * p[t];
+        it++;
+    }
+    *conv = sqrt(rr) <= rtol * bn;
+    if (allper) {
+        double mean = 0.0;
+        for (long t = 0; t < nu; t++) mean += x[t];
+        mean /= (double)nu;
+        for (long t = 0; t < nu; t++) x[t] -= mean;
+    }
+    for (int a = 0; a < m[0]; a++)
+        for (int b = 0; b < m[1]; b++)
+            for (int e = 0; e < m[2]; e++) u[IDX(c, a + lo[0], b + lo[1], e + lo[2])] = x[UIDX(a, b, e)];
+#undef UIDX
+    orc_execute_bc(c, id1);
+    memcpy(c->slot[id2], u, sizeof(double) * c->npts);
+    free(x);
+    free(r);
+    free(p);
+    free(q);
+    return it;
+}
+
+int orc_set_poisson_solver(void *h, int solver, double rtol) {
+    orc_t *c = (orc_t *)h;
+    if (solver != 0 && solver != 1) return -1;
+    c->poisson_solver = solver;
+    c->poisson_rtol = rtol > 0 ? rtol : 1e-13;
+    return 0;
+}
+
 /* phiToE, src/poisson/convertFields.cpp:10-68 (reads phi1, (g)) */
 static void phi_to_e(orc_t *c) {
     const double *phi = c->slot[EMOO_PHI1];
@@ -1086,6 +1220,20 @@ static void a_to_b(orc_t *c) {
  * Returns 1 when every solve converged. */
 static int poisson_init(orc_t *c, int *iters) {
     double mult = -4 * PI_D;
+    if (c->poisson_solver == 1) {
+        int ok = 1, cv;
+        for (int q = 0; q < 4; q++) {
+            int it = exact_poisson(c, q == 0 ? EMOO_PHI1 : EMOO_AX1 + (q - 1), q == 0 ? EMOO_PHI2 : EMOO_AX2 + (q - 1),
+                                   c->slot[q == 0 ? EMOO_RHO : EMOO_JX + (q - 1)], mult, c->poisson_rtol, &cv);
+            if (it < 0) return -1;
+            ok &= cv;
+            if (iters) iters[q] = it;
+            if (q == 0) phi_to_e(c);
+        }
+        a_to_b(c);
+        orc_execute_bc(c, EMOO_SEND_EB);
+        return ok;
+    }
     double a = c->conv_phi * CONV_RATIO;
     double tol = a < CONV_CRIT ? CONV_CRIT : a;
     int ok = 1, cv;
@@ -1132,7 +1280,7 @@ int orc_initialize_fields_only(void *h, int *iters) {
     else const_init(c);
     c->t = c->t0;
     c->dtp = c->dt;
-    return ok ? 0 : -3;
+    return ok < 0 ? -1 : ok ? 0 : -3;
 }
 
 /* src/main.cpp:159-179 */
@@ -1151,7 +1299,7 @@ int orc_init_fields(void *h, int *iters) {
     orc_interpolate(c);
     c->t = c->t0;
     c->dtp = c->dt;
-    return ok ? 0 : -3;
+    return ok < 0 ? -1 : ok ? 0 : -3;
 }
 
 void orc_set_time(void *h, double t, double dtp) {

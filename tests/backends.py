@@ -74,6 +74,7 @@ def _load_cpu_lib(path, prefix):
         f("set_wave_shape", C.c_int, [P, C.c_int, C.POINTER(abi.WaveShape)])
         f("set_rho_background_xmin", None, [P, C.c_double])
         f("set_policy", C.c_int, [P, C.c_int])
+        f("set_poisson_solver", C.c_int, [P, C.c_int, C.c_double])
     return L
 
 
@@ -250,12 +251,17 @@ class OracleBackend(CpuBackend):
         if self._f("set_policy")(self.h, policy) != 0:
             raise ValueError("orc_set_policy refused the policy")
 
+    def set_poisson_solver(self, solver, rtol=1e-13):
+        if self._f("set_poisson_solver")(self.h, solver, rtol) != 0:
+            raise ValueError("orc_set_poisson_solver refused the solver")
+
 
 class GpuBackend:
     """The product, through include/emoo.h."""
 
     def __init__(self, info, dt, t0=0.0, precision=abi.FP64, capacity=0, track_ids=1, device=0, rho_background=0.0,
-                 rho_background_xmin=None, policy=abi.POLICY_REFERENCE):
+                 rho_background_xmin=None, policy=abi.POLICY_REFERENCE, poisson_solver=abi.POISSON_JACOBI,
+                 poisson_rtol=None):
         self.L = abi.lib()
         self.info = info
         self.n = [info.nCell[d] for d in range(3)]
@@ -271,6 +277,9 @@ class GpuBackend:
         if rho_background_xmin is not None:
             o.rho_background_xmin = rho_background_xmin
         o.policy = policy
+        o.poisson_solver = poisson_solver
+        if poisson_rtol is not None:
+            o.poisson_rtol = poisson_rtol
         h = C.c_void_p()
         abi.check(self.L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
         self.h = h

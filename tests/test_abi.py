@@ -45,10 +45,11 @@ def test_input_info_layout_is_the_references():
 def test_strerror_and_default_opts():
     L = abi.lib()
     assert L.emoo_strerror(0) == b"ok"
-    assert L.emoo_strerror(abi.ERR_NOT_CONVERGED).startswith(b"Jacobi")
+    assert L.emoo_strerror(abi.ERR_NOT_CONVERGED).startswith(b"Poisson solve did not converge")
     o = abi.Opts()
     assert L.emoo_default_opts(C.byref(o)) == 0
     assert o.precision == abi.FP64 and o.deposit_rho == 1 and o.history_every == 10
+    assert o.poisson_solver == abi.POISSON_JACOBI and o.poisson_rtol == 1e-10
     assert L.emoo_default_opts(None) == abi.ERR_ARG
 
 

@@ -19,8 +19,12 @@
 // there). A dimension coarsens while its P is even and at least 4; the others
 // keep their spacing (semi-coarsening). One V-cycle: two red-black
 // Gauss-Seidel sweeps, residual, full-weighting restriction, the coarser
-// cycle, trilinear prolongation, two sweeps; the coarsest level is swept by
-// one thread block until its few unknowns settle. Each level is a dense
+// cycle, trilinear prolongation, two sweeps; the coarsest level is swept
+// until its few unknowns settle. The levels of at most 4096 unknowns run
+// their whole part of the cycle inside one thread block, in its shared memory
+// (one launch, block barriers between the stages): launched one kernel per
+// stage, they would cost a launch latency each for a few microseconds of
+// work, and from global memory each stage would wait on L2. Each level is a dense
 // (P+2)^3 block; periodic neighbours are found by index wrap, so no ghost
 // planes are kept. Red and black do not colour a periodic dimension of odd P
 // (points 1 and P are neighbours of one colour), so a level with one smooths
@@ -67,6 +71,7 @@ struct MgState {
     int per[3];
     double d[3];
     std::vector<Lv> lv;
+    size_t tail_from = 0;  // first level of the shared-memory tail (lv.size(): none)
     Fine fine = {};
     double *part = nullptr;   // per-block sums
     double *hpart = nullptr;  // pinned host copy
@@ -80,7 +85,9 @@ struct MgState {
 constexpr int RB = 256;      // reduction blocks
 constexpr int NU = 2;        // smoothing sweeps before and after the coarse correction
 constexpr float OMEGA = 6.0f / 7.0f;  // Jacobi damping, the 7-point stencil's smoothing optimum
-constexpr int COARSE_BLOCK_MAX = 4096;  // unknowns the one-block coarsest solve takes
+constexpr int TAIL_MAX = 4096;    // levels of at most this many unknowns run in the one-block tail
+constexpr int TAIL_LEVELS = 16;
+constexpr int TAIL_THREADS = 1024;
 
 __device__ __forceinline__ int64_t lidx(const Lv &L, int i, int j, int k) {
     return (int64_t)i * L.sx + (int64_t)j * L.sy + k;
@@ -127,60 +134,44 @@ __global__ void k_mg_jacobi(Lv L, const float *src, float *dst) {
     jacobi_point(L, src, dst, i, j, k);
 }
 
-// The coarsest level, swept `sweeps` times by one block (fixed trip counts;
-// every thread reaches every barrier).
-__global__ void k_mg_coarse(Lv L, int sweeps) {
-    const int m0 = L.hi[0] - L.lo[0] + 1, m1 = L.hi[1] - L.lo[1] + 1, m2 = L.hi[2] - L.lo[2] + 1;
-    const int n = m0 * m1 * m2;
-    for (int s = 0; s < sweeps; s++) {
-        for (int half = 0; half < 2; half++) {
-            for (int t = threadIdx.x; t < n; t += blockDim.x) {
-                const int k = L.lo[2] + t % m2, j = L.lo[1] + (t / m2) % m1, i = L.lo[0] + t / (m1 * m2);
-                if (L.rb) {
-                    if (((i + j + k) & 1) == half) gs_point(L, i, j, k);
-                } else if (half == 0) {
-                    jacobi_point(L, L.u, L.t, i, j, k);
-                } else {
-                    jacobi_point(L, L.t, L.u, i, j, k);
-                }
-            }
-            __syncthreads();
-        }
-    }
+// r = f - Laplacian(u) at the unknowns (FP32 levels)
+__device__ __forceinline__ void residual_point(const Lv &L, int i, int j, int k) {
+    const int64_t o = lidx(L, i, j, k);
+    L.r[o] = L.f[o] - (nb_sum(L, L.c, L.u, i, j, k) - L.diag * L.u[o]);
 }
 
-// r = f - Laplacian(u) at the unknowns (FP32 levels)
 __global__ void k_mg_residual(Lv L) {
     const int k = L.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = L.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
     const int i = L.lo[0] + blockIdx.z;
     if (k > L.hi[2] || j > L.hi[1] || i > L.hi[0]) return;
-    const int64_t o = lidx(L, i, j, k);
-    L.r[o] = L.f[o] - (nb_sum(L, L.c, L.u, i, j, k) - L.diag * L.u[o]);
+    residual_point(L, i, j, k);
 }
 
 // The FP64 residual of the fine problem: level 0's right side takes it (as
-// FP32), level 0's correction restarts at zero, and *dmax the maximum |r|.
+// FP32), level 0's correction restarts at zero, and *dmax the maximum |r|,
+// taken over the FP32 values (the stop test needs no more): this kernel runs
+// on the FP64 pipe, so everything after the residual itself stays off it.
 __global__ void k_mg_residual64(Lv L, Fine F, double *dmax) {
-    __shared__ double sh[8];
+    __shared__ float sh[8];
     const int k = L.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = L.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
     const int i = L.lo[0] + blockIdx.z;
-    double a = 0.0;
+    float a = 0.0f;
     if (k <= L.hi[2] && j <= L.hi[1] && i <= L.hi[0]) {
         const int64_t o = lidx(L, i, j, k);
-        const double r = F.f[o] - (nb_sum(L, F.c, F.u, i, j, k) - F.diag * F.u[o]);
-        L.f[o] = (float)r;
+        const float r = (float)(F.f[o] - (nb_sum(L, F.c, F.u, i, j, k) - F.diag * F.u[o]));
+        L.f[o] = r;
         L.u[o] = 0.0f;
-        a = fabs(r);
+        a = fabsf(r);
     }
-    for (int off = 16; off > 0; off >>= 1) a = fmax(a, __shfl_down_sync(0xffffffffu, a, off));
+    for (int off = 16; off > 0; off >>= 1) a = fmaxf(a, __shfl_down_sync(0xffffffffu, a, off));
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     if ((tid & 31) == 0) sh[tid >> 5] = a;
     __syncthreads();
     if (tid == 0) {
-        for (int w = 1; w < (int)((blockDim.x * blockDim.y) >> 5); w++) a = fmax(a, sh[w]);
-        atomic_max_nonneg(dmax, a);
+        for (int w = 1; w < (int)((blockDim.x * blockDim.y) >> 5); w++) a = fmaxf(a, sh[w]);
+        atomic_max_nonneg(dmax, (double)a);
     }
 }
 
@@ -207,11 +198,7 @@ __device__ __forceinline__ int tap(const Lv &F, int d, int C, int t, float &w) {
 }
 
 // coarse f = full-weighting restriction of the fine residual; coarse u = 0
-__global__ void k_mg_restrict(Lv F, Lv Cl) {
-    const int K = Cl.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
-    const int J = Cl.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
-    const int I = Cl.lo[0] + blockIdx.z;
-    if (K > Cl.hi[2] || J > Cl.hi[1] || I > Cl.hi[0]) return;
+__device__ __forceinline__ void restrict_point(const Lv &F, const Lv &Cl, int I, int J, int K) {
     float s = 0.0f;
     for (int a = 0; a < 3; a++) {
         float wa;
@@ -236,6 +223,14 @@ __global__ void k_mg_restrict(Lv F, Lv Cl) {
     Cl.u[o] = 0.0f;
 }
 
+__global__ void k_mg_restrict(Lv F, Lv Cl) {
+    const int K = Cl.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = Cl.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+    const int I = Cl.lo[0] + blockIdx.z;
+    if (K > Cl.hi[2] || J > Cl.hi[1] || I > Cl.hi[0]) return;
+    restrict_point(F, Cl, I, J, K);
+}
+
 // coarse index pair and weight of the second feeding fine index f along d
 __device__ __forceinline__ void interp(const Lv &F, const Lv &Cl, int d, int f, int &c0, int &c1, float &w1) {
     if (!F.crs[d]) {
@@ -255,29 +250,129 @@ __device__ __forceinline__ void interp(const Lv &F, const Lv &Cl, int d, int f, 
 }
 
 // fine u += trilinear interpolation of the coarse correction
-__global__ void k_mg_prolong(Lv Cl, Lv F) {
-    const int k = F.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = F.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
-    const int i = F.lo[0] + blockIdx.z;
-    if (k > F.hi[2] || j > F.hi[1] || i > F.hi[0]) return;
+__device__ __forceinline__ void prolong_point(const Lv &Cl, const Lv &F, int i, int j, int k) {
     int ci[2], cj[2], ck[2];
     float wi, wj, wk;
     interp(F, Cl, 0, i, ci[0], ci[1], wi);
     interp(F, Cl, 1, j, cj[0], cj[1], wj);
     interp(F, Cl, 2, k, ck[0], ck[1], wk);
+    // all eight taps, zero-weighted ones on a repeated (cached) address: the
+    // weights change with the parity of k, so skipping taps would split warps
     const float Wi[2] = {1.0f - wi, wi}, Wj[2] = {1.0f - wj, wj}, Wk[2] = {1.0f - wk, wk};
     float s = 0.0f;
-    for (int a = 0; a < 2; a++) {
-        if (Wi[a] == 0.0f) continue;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
         for (int b = 0; b < 2; b++) {
-            if (Wj[b] == 0.0f) continue;
-            for (int e = 0; e < 2; e++) {
-                if (Wk[e] == 0.0f) continue;
-                s += Wi[a] * Wj[b] * Wk[e] * Cl.u[lidx(Cl, ci[a], cj[b], ck[e])];
+            const int64_t row = (int64_t)ci[a] * Cl.sx + (int64_t)cj[b] * Cl.sy;
+            s += Wi[a] * Wj[b] * (Wk[0] * Cl.u[row + ck[0]] + Wk[1] * Cl.u[row + ck[1]]);
+        }
+    F.u[lidx(F, i, j, k)] += s;
+}
+
+__global__ void k_mg_prolong(Lv Cl, Lv F) {
+    const int k = F.lo[2] + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = F.lo[1] + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = F.lo[0] + blockIdx.z;
+    if (k > F.hi[2] || j > F.hi[1] || i > F.hi[0]) return;
+    prolong_point(Cl, F, i, j, k);
+}
+
+// ---- the one-block tail: levels lv[0..nl-1] of at most TAIL_MAX unknowns,
+// lv[0]'s right side already restricted and its u zero
+
+struct Tail {
+    int nl;
+    int sweeps;  // on the coarsest
+    int smem;    // floats of shared memory the levels take
+    Lv lv[TAIL_LEVELS];  // the global levels (lv[0]'s f in, u out)
+    int ou[TAIL_LEVELS], of[TAIL_LEVELS], orr[TAIL_LEVELS], ot[TAIL_LEVELS];  // their shared copies; ot < 0: none
+};
+
+// level l of the tail with its arrays in shared memory
+__device__ __forceinline__ Lv tail_level(const Tail &T, int l, float *sm) {
+    Lv L = T.lv[l];
+    L.u = sm + T.ou[l];
+    L.f = sm + T.of[l];
+    L.r = sm + T.orr[l];
+    L.t = T.ot[l] >= 0 ? sm + T.ot[l] : nullptr;
+    return L;
+}
+
+__device__ __forceinline__ void pt_of(const Lv &L, int t, int &i, int &j, int &k) {
+    const int m1 = L.hi[1] - L.lo[1] + 1, m2 = L.hi[2] - L.lo[2] + 1;
+    k = L.lo[2] + t % m2;
+    j = L.lo[1] + (t / m2) % m1;
+    i = L.lo[0] + t / (m1 * m2);
+}
+
+__device__ __forceinline__ int npts_of(const Lv &L) {
+    return (L.hi[0] - L.lo[0] + 1) * (L.hi[1] - L.lo[1] + 1) * (L.hi[2] - L.lo[2] + 1);
+}
+
+// Every loop below has a trip count fixed by the level; every thread of the
+// block reaches every barrier.
+__device__ void blk_smooth(const Lv &L, int sweeps) {
+    const int n = npts_of(L);
+    int i, j, k;
+    for (int s = 0; s < sweeps; s++)
+        for (int half = 0; half < 2; half++) {
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                pt_of(L, t, i, j, k);
+                if (L.rb) {
+                    if (((i + j + k) & 1) == half) gs_point(L, i, j, k);
+                } else if (half == 0) {
+                    jacobi_point(L, L.u, L.t, i, j, k);
+                } else {
+                    jacobi_point(L, L.t, L.u, i, j, k);
+                }
             }
+            __syncthreads();
+        }
+}
+
+__global__ void __launch_bounds__(TAIL_THREADS) k_mg_tail(Tail T) {
+    extern __shared__ float sm[];
+    int i, j, k;
+    for (int t = threadIdx.x; t < T.smem; t += blockDim.x) sm[t] = 0.0f;
+    __syncthreads();
+    {
+        const Lv G = T.lv[0], L = tail_level(T, 0, sm);
+        for (int t = threadIdx.x; t < npts_of(L); t += blockDim.x) {
+            pt_of(L, t, i, j, k);
+            L.f[lidx(L, i, j, k)] = G.f[lidx(G, i, j, k)];
         }
     }
-    F.u[lidx(F, i, j, k)] += s;
+    __syncthreads();
+    for (int l = 0; l + 1 < T.nl; l++) {
+        const Lv L = tail_level(T, l, sm), C = tail_level(T, l + 1, sm);
+        blk_smooth(L, NU);
+        for (int t = threadIdx.x; t < npts_of(L); t += blockDim.x) {
+            pt_of(L, t, i, j, k);
+            residual_point(L, i, j, k);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < npts_of(C); t += blockDim.x) {
+            pt_of(C, t, i, j, k);
+            restrict_point(L, C, i, j, k);
+        }
+        __syncthreads();
+    }
+    blk_smooth(tail_level(T, T.nl - 1, sm), T.sweeps);
+    for (int l = T.nl - 2; l >= 0; l--) {
+        const Lv L = tail_level(T, l, sm), C = tail_level(T, l + 1, sm);
+        for (int t = threadIdx.x; t < npts_of(L); t += blockDim.x) {
+            pt_of(L, t, i, j, k);
+            prolong_point(C, L, i, j, k);
+        }
+        __syncthreads();
+        blk_smooth(L, NU);
+    }
+    const Lv G = T.lv[0], L = tail_level(T, 0, sm);
+    for (int t = threadIdx.x; t < npts_of(L); t += blockDim.x) {
+        pt_of(L, t, i, j, k);
+        G.u[lidx(G, i, j, k)] = L.u[lidx(L, i, j, k)];
+    }
 }
 
 // the FP64 problem from the grid slots: u takes the slot's values on the
@@ -390,19 +485,48 @@ void smooth(emoo_handle *h, const Lv &L, int sweeps, int &launches) {
         }
 }
 
+int coarse_sweeps(const Lv &L) {
+    int m = 1;
+    for (int d = 0; d < 3; d++) m = std::max(m, L.hi[d] - L.lo[d] + 1);
+    return std::min(500, 2 * m * m + 8);
+}
+
+constexpr int TAIL_SMEM_MAX = 200 * 1024;
+
+// the tail from level l: its shared-memory layout, or nl = 0 when it does not fit
+Tail make_tail(const MgState *s, size_t l) {
+    Tail T = {};
+    if (s->lv.size() - l > (size_t)TAIL_LEVELS) return T;
+    int off = 0;
+    for (size_t q = l; q < s->lv.size(); q++) {
+        const Lv &L = s->lv[q];
+        const int n = (L.P[0] + 2) * (int)L.sx;
+        const int i = (int)(q - l);
+        T.lv[i] = L;
+        T.ou[i] = off;
+        T.of[i] = off + n;
+        T.orr[i] = off + 2 * n;
+        T.ot[i] = L.t ? off + 3 * n : -1;
+        off += (L.t ? 4 : 3) * n;
+    }
+    if ((size_t)off * sizeof(float) > (size_t)TAIL_SMEM_MAX) return T;
+    T.nl = (int)(s->lv.size() - l);
+    T.smem = off;
+    T.sweeps = coarse_sweeps(s->lv.back());
+    return T;
+}
+
 void vcycle(emoo_handle *h, MgState *s, size_t l, int &launches) {
     const Lv &L = s->lv[l];
     dim3 blk(32, 8);
-    if (l + 1 == s->lv.size()) {
-        int m = 1;
-        for (int d = 0; d < 3; d++) m = std::max(m, L.hi[d] - L.lo[d] + 1);
-        const int sweeps = std::min(500, 2 * m * m + 8);
-        if (unknowns(L) <= COARSE_BLOCK_MAX) {
-            launches++;
-            k_mg_coarse<<<1, 256, 0, h->stream>>>(L, sweeps);
-        } else {
-            smooth(h, L, sweeps, launches);
-        }
+    if (l == s->tail_from) {
+        const Tail T = make_tail(s, l);
+        launches++;
+        k_mg_tail<<<1, TAIL_THREADS, T.smem * sizeof(float), h->stream>>>(T);
+        return;
+    }
+    if (l + 1 == s->lv.size()) {  // a coarsest level too large for the tail
+        smooth(h, L, coarse_sweeps(L), launches);
         return;
     }
     const Lv &C = s->lv[l + 1];
@@ -489,6 +613,21 @@ int mg_setup(emoo_handle *h, MgState *s) {
                 hh[d] *= 2.0;
             }
     }
+    // the shared-memory tail: the first level of at most TAIL_MAX unknowns
+    // from which the rest fits
+    s->tail_from = s->lv.size();
+    for (size_t q = 0; q < s->lv.size(); q++)
+        if (unknowns(s->lv[q]) <= TAIL_MAX && make_tail(s, q).nl > 0) {
+            s->tail_from = q;
+            const Tail T = make_tail(s, q);
+            cudaError_t e = cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)(T.smem * sizeof(float)));
+            if (e != cudaSuccess) {
+                mg_release(s);
+                return cuda_status(e);
+            }
+            break;
+        }
     const Lv &L0 = s->lv[0];
     const size_t b64 = (size_t)(L0.P[0] + 2) * L0.sx * sizeof(double);
     for (int d = 0; d < 3; d++) s->fine.c[d] = 1.0 / (g.d[d] * g.d[d]);

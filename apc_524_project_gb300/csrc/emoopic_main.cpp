@@ -2,7 +2,11 @@
 // (one input file), same initialisation order and time loop as the reference
 // driver (src/main.cpp:45-336), through the class API of emoopic.hpp.
 //
-//   emoopic_gpu <input.txt> [--mixed] [--dt DT]
+//   emoopic_gpu <input.txt> [--mixed] [--dt DT] [--multigrid] [--corrected]
+//
+// --multigrid solves the "poisson" field start by multigrid instead of the
+// reference's Jacobi (EMOO_POISSON_MULTIGRID); --corrected selects the
+// corrected-physics policy (EMOO_POLICY_CORRECTED).
 //
 // Writes history.dat next to the input file like the reference, and the field
 // time series at the reference's cadence (t = 0, every nstep_fields steps, the
@@ -23,13 +27,19 @@
 
 int main(int argc, char **argv) {
     if (argc < 2) {
-        fprintf(stderr, "usage: %s <input.txt> [--mixed] [--dt DT]\n", argv[0]);
+        fprintf(stderr, "usage: %s <input.txt> [--mixed] [--dt DT] [--multigrid] [--corrected]\n", argv[0]);
         return 1;
     }
     emoo_opts &opt = emoopic::Options::get().o;
     for (int a = 2; a < argc; a++) {
         if (!strcmp(argv[a], "--mixed")) opt.precision = EMOO_MIXED;
         else if (!strcmp(argv[a], "--dt") && a + 1 < argc) opt.dt = atof(argv[++a]);
+        else if (!strcmp(argv[a], "--multigrid")) opt.poisson_solver = EMOO_POISSON_MULTIGRID;
+        else if (!strcmp(argv[a], "--corrected")) opt.policy = EMOO_POLICY_CORRECTED;
+        else {
+            fprintf(stderr, "unknown option %s\n", argv[a]);
+            return 1;
+        }
     }
     clock_t begin = clock();
     try {

@@ -58,12 +58,17 @@ def reference_load(info, seed=12345):
     return parts
 
 
-def test_driver_history_matches_oracle(tmp_path):
+@pytest.mark.parametrize("multigrid", [False, True])
+def test_driver_history_matches_oracle(tmp_path, multigrid):
+    """With --multigrid the driver starts from the multigrid solve (to its
+    default 1e-10 residual) and the oracle from its exact solve; the fields
+    then agree to about 1e-9, so the history to 1e-7."""
     build_native.build()
     src = os.path.join(DATA, "driver_small.txt")
     inp = tmp_path / "input.txt"
     shutil.copy(src, inp)
-    r = subprocess.run([build_native.DRIVER, str(inp)], capture_output=True, text=True, timeout=300)
+    cmd = [build_native.DRIVER, str(inp)] + (["--multigrid"] if multigrid else [])
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     rows = np.loadtxt(tmp_path / "history.dat", skiprows=1, ndmin=2)
     info = abi.InputInfo()
@@ -73,6 +78,8 @@ def test_driver_history_matches_oracle(tmp_path):
     dt = dx / 100.0
     parts = reference_load(info)
     o = OracleBackend(info, dt)
+    if multigrid:
+        o.set_poisson_solver(1)
     nid = 0
     for s, p in enumerate(parts):
         o.add_species(s, p, ids=np.arange(nid, nid + len(p["x"])))
@@ -85,4 +92,4 @@ def test_driver_history_matches_oracle(tmp_path):
             hist.append(h)
     mass = sum(info.mass_ratio[s] * len(p["x"]) for s, p in enumerate(parts))
     assert rows.shape == (len(hist), 8)
-    history_close(rows, np.array(hist), 1e-9, mass)
+    history_close(rows, np.array(hist), 1e-7 if multigrid else 1e-9, mass)

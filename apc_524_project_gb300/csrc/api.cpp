@@ -807,8 +807,7 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
         int prc = EMOO_OK;
         if (o.policy != EMOO_POLICY_REFERENCE && o.policy != EMOO_POLICY_CORRECTED) prc = EMOO_ERR_ARG;
         if (o.policy == EMOO_POLICY_CORRECTED) {
-            // the FP64 form with periodic particles and fields on every side
-            if (h->precision != EMOO_FP64) prc = EMOO_ERR_UNSUPPORTED;
+            // periodic particles and fields on every side (both forms)
             for (int s = 0; s < 6; s++)
                 if (h->bc.pbc[s] != PBC_PERIODIC || h->bc.fbc[s] != FBC_PERIODIC) prc = EMOO_ERR_UNSUPPORTED;
             h->policy = o.policy;

@@ -76,6 +76,7 @@ struct MGeom {
     int64_t npts;
     float dtid[3];  // dt / d
     float idf[3];   // 1 / d
+    float ddt[3];   // d / dt (0 when dt = 0)
     float fourpi_dt;
 };
 
@@ -252,6 +253,14 @@ __device__ __forceinline__ float4 edge_coef(float f00, float f10, float f11, flo
     return c;
 }
 
+// The corrected policy's weights over the cell's own lower corner,
+// a = 1 - o and b = o: the edge polynomial's coefficients, and for a face
+// component 0.5 ((1 - s) S0 + s S1) = d0 + d1 s.
+__device__ __forceinline__ float4 edge_coef_true(float f00, float f10, float f11, float f01) {
+    return make_float4(f00, f10 - f00, f01 - f00, (f00 - f10) + (f11 - f01));
+}
+
+template <bool CORR>
 __global__ void k_pack_m(MGeom g, MGather P, float4 *__restrict__ pack) {
     int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -261,23 +270,28 @@ __global__ void k_pack_m(MGeom g, MGather P, float4 *__restrict__ pack) {
     const int64_t o = (int64_t)i * sx + (int64_t)j * sy + k;
     const float *Ex = P.E[0], *Ey = P.E[1], *Ez = P.E[2];
     float4 *dst = pack + o * PACK_F4;
-    dst[0] = edge_coef(Ex[o], Ex[o + sy], Ex[o + sy + 1], Ex[o + 1]);
-    dst[1] = edge_coef(Ey[o], Ey[o + 1], Ey[o + sx + 1], Ey[o + sx]);
-    dst[2] = edge_coef(Ez[o], Ez[o + sx], Ez[o + sx + sy], Ez[o + sy]);
+    auto coef = [](float f00, float f10, float f11, float f01) {
+        return CORR ? edge_coef_true(f00, f10, f11, f01) : edge_coef(f00, f10, f11, f01);
+    };
+    // face term: d0 = S0 - S1/2 over the ghost-offset vertex, S0/2 over the true one
+    auto d0 = [](float s0, float s1) { return CORR ? 0.5f * s0 : s0 - 0.5f * s1; };
+    dst[0] = coef(Ex[o], Ex[o + sy], Ex[o + sy + 1], Ex[o + 1]);
+    dst[1] = coef(Ey[o], Ey[o + 1], Ey[o + sx + 1], Ey[o + sx]);
+    dst[2] = coef(Ez[o], Ez[o + sx], Ez[o + sx + sy], Ez[o + sy]);
     float s0, s1;
     float4 b;
     s0 = P.T[0][o] + P.B[0][o];
     s1 = P.T[0][o + sx] + P.B[0][o + sx];
-    b.x = s0 - 0.5f * s1;
+    b.x = d0(s0, s1);
     b.y = 0.5f * (s1 - s0);
     s0 = P.T[1][o] + P.B[1][o];
     s1 = P.T[1][o + sy] + P.B[1][o + sy];
-    b.z = s0 - 0.5f * s1;
+    b.z = d0(s0, s1);
     b.w = 0.5f * (s1 - s0);
     dst[3] = b;
     s0 = P.T[2][o] + P.B[2][o];
     s1 = P.T[2][o + 1] + P.B[2][o + 1];
-    dst[4] = make_float4(s0 - 0.5f * s1, 0.5f * (s1 - s0), 0.0f, 0.0f);
+    dst[4] = make_float4(d0(s0, s1), 0.5f * (s1 - s0), 0.0f, 0.0f);
 }
 
 // E and B at offsets (ox, oy, oz) of the cell whose pack starts at pk.
@@ -411,6 +425,81 @@ constexpr int FUSED_BLOCK = 256;
 constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
 constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: conflict-free both ways)
 
+__device__ __forceinline__ void order2(float &a, float &b) {
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Villasenor and Buneman's charge-conserving current of one particle's
+// straight move (the corrected policy), the FP64 vb_deposit of
+// particles_f64.cu in FP32 and in the old cell's units: s = the old in-cell
+// offsets, e = s + the displacement in cells (|e - s| < 1 per axis). The path
+// is split where it crosses a face (at most once per axis); the piece inside
+// cell c (old cell + (-1, 0, 1) per axis, wrapped periodically) with extent D
+// and mid-offsets m adds, for each axis a with transverse axes j, k, to its
+// cell's slots 4a .. 4a+3
+//   qd (D_a d_a / dt) ((1-m_j)(1-m_k) + D_j D_k/12, m_j (1-m_k) - .., m_j m_k + .., (1-m_j) m_k - ..).
+// Pieces in the particle's new cell `onew` are summed into w (the run
+// reduction commits them); the others are added to their cells' records here.
+// Crossing times come from comparisons and one fast divide; the cell of a
+// piece from comparisons (no conversion instruction).
+__device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, int ix, int iy, int iz, const float s[3],
+                                            const float e[3], float qd, int onew, float w[DEP_JSLOTS]) {
+    float t[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const bool lo = e[a] < 0.0f, hi = e[a] >= 1.0f;
+        t[a] = (lo || hi) ? __fdividef((hi ? 1.0f : 0.0f) - s[a], e[a] - s[a]) : 2.0f;
+    }
+    order2(t[0], t[1]);
+    order2(t[1], t[2]);
+    order2(t[0], t[1]);
+    const int io[3] = {ix, iy, iz};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float ta = k == 0 ? 0.0f : fminf(t[k - 1], 1.0f);
+        const float tb = k == 3 ? 1.0f : fminf(t[k], 1.0f);
+        if (!(tb > ta)) continue;
+        float m[3], Dd[3];
+        int ct = 0;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float de = e[a] - s[a];
+            const float ua = fmaf(ta, de, s[a]), ub = fmaf(tb, de, s[a]);
+            const float mid = 0.5f * (ua + ub);
+            const int c = mid < 0.0f ? -1 : (mid >= 1.0f ? 1 : 0);
+            m[a] = mid - (float)c;
+            Dd[a] = ub - ua;
+            int ii = io[a] + c;
+            ii = ii < 1 ? ii + g.n[a] : (ii > g.n[a] ? ii - g.n[a] : ii);
+            ct += ii * (a == 0 ? (int)g.sx : a == 1 ? (int)g.sy : 1);
+        }
+        float W[DEP_JSLOTS];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+            const float wa = qd * Dd[a] * g.ddt[a];
+            const float cr = Dd[jb] * Dd[kb] * (1.0f / 12.0f);
+            W[4 * a + 0] = wa * ((1.0f - m[jb]) * (1.0f - m[kb]) + cr);
+            W[4 * a + 1] = wa * (m[jb] * (1.0f - m[kb]) - cr);
+            W[4 * a + 2] = wa * (m[jb] * m[kb] + cr);
+            W[4 * a + 3] = wa * ((1.0f - m[jb]) * m[kb] - cr);
+        }
+        if (ct == onew) {
+#pragma unroll
+            for (int q = 0; q < DEP_JSLOTS; q++) w[q] += W[q];
+        } else {
+            unsigned long long *rec = D.wj + (size_t)ct * DEP_JSLOTS;
+#pragma unroll
+            for (int q = 0; q < DEP_JSLOTS; q++) {
+                const long long fx = f2ll_rn(W[q]);
+                if (fx != 0) atomicAdd(rec + dep_pos(q), (unsigned long long)fx);
+            }
+        }
+    }
+}
+
 // Fused gather + push + boundaries + deposit, one thread per particle.
 //
 // Deposit: each lane writes its particle's 20 contributions as a column of a
@@ -424,7 +513,11 @@ constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: 
 // Division and square roots use the hardware approximations (rsqrtf,
 // __fdividef, relative error a few 2^-24): the form's accuracy is FP32. No
 // conversion instruction runs per particle (see f2ll_rn, cell_step).
-template <bool REL, bool FIRST, bool PUSH>
+//
+// CORR: the corrected policy - the pack holds true-vertex coefficients, the
+// deposit at the current state uses the weights 1 - o and o, and the time
+// loop's current is the charge-conserving one of vb_pieces_m.
+template <bool REL, bool FIRST, bool PUSH, bool CORR = false>
 __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
               MDeposit D, int with_rho, const float *g0, DevCounters *ctr) {
@@ -446,6 +539,9 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
             float vx, vy, vz;
             int ix, iy, iz;
             split_cell(g, dv, c, ix, iy, iz);
+            const int ix0 = ix, iy0 = iy, iz0 = iz;
+            const float so[3] = {ox, oy, oz};
+            float mv[3] = {0.0f, 0.0f, 0.0f};
             if (!PUSH) {
                 // deposit at the current state (Particle_Handler::depositRhoJ)
                 float iga = 1.0f;
@@ -459,6 +555,9 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 push_m<REL, FIRST>(f, st.qp[s], g0, p, ux, uy, uz, vx, vy, vz);
                 // position update in cell units, then the boundaries per axis
                 float nx = ox + vx * g.dtid[0], ny = oy + vy * g.dtid[1], nz = oz + vz * g.dtid[2];
+                mv[0] = nx;
+                mv[1] = ny;
+                mv[2] = nz;
                 cell_step(nx, ix, ox);
                 cell_step(ny, iy, oy);
                 cell_step(nz, iz, oz);
@@ -484,12 +583,38 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                     S.uy[p] = uy;
                     S.uz[p] = uz;
                 }
-                if (st.deposit[s]) {
+                if (CORR && PUSH && st.deposit[s]) {
+                    active = true;
+                    float wv[DEP_JSLOTS];
+#pragma unroll
+                    for (int q = 0; q < DEP_JSLOTS; q++) wv[q] = 0.0f;
+                    vb_pieces_m(g, D, ix0, iy0, iz0, so, mv, st.qdep[s], onew, wv);
+                    float *w = col + lane;
+#pragma unroll
+                    for (int q = 0; q < DEP_JSLOTS; q++) w[q * DEP_STRIDE] = wv[q];
+                    if (with_rho) {  // rho at the new position, true-vertex weights
+                        const float qd = st.qdep[s];
+                        const float a[3] = {1.0f - ox, 1.0f - oy, 1.0f - oz}, b[3] = {ox, oy, oz};
+                        w[12 * DEP_STRIDE] = qd * a[0] * a[1] * a[2];
+                        w[13 * DEP_STRIDE] = qd * b[0] * a[1] * a[2];
+                        w[14 * DEP_STRIDE] = qd * b[0] * b[1] * a[2];
+                        w[15 * DEP_STRIDE] = qd * a[0] * b[1] * a[2];
+                        w[16 * DEP_STRIDE] = qd * a[0] * b[1] * b[2];
+                        w[17 * DEP_STRIDE] = qd * b[0] * b[1] * b[2];
+                        w[18 * DEP_STRIDE] = qd * b[0] * a[1] * b[2];
+                        w[19 * DEP_STRIDE] = qd * a[0] * a[1] * b[2];
+                    }
+                } else if (st.deposit[s]) {
                     active = true;
                     // deposit weights (src/particles/deposit.cpp:12-62) in
-                    // fixed-point units: (UNIT_RHOJ q / V) v_i (2 - o_j)(2 - o_k) etc.
+                    // fixed-point units: (UNIT_RHOJ q / V) v_i (2 - o_j)(2 - o_k) etc.;
+                    // over the true vertex (CORR) 1 - o and o
                     float a[3] = {2.0f - ox, 2.0f - oy, 2.0f - oz};
                     float b[3] = {ox - 1.0f, oy - 1.0f, oz - 1.0f};
+                    if (CORR) {
+                        a[0] = 1.0f - ox, a[1] = 1.0f - oy, a[2] = 1.0f - oz;
+                        b[0] = ox, b[1] = oy, b[2] = oz;
+                    }
                     const float qd = st.qdep[s];
                     float jx = qd * vx, jy = qd * vy, jz = qd * vz;
                     float *w = col + lane;
@@ -611,9 +736,13 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
 // records: point p gathers slot q of cell p - off(q), the inverse of the
 // deposit table. Integer sums, so the result equals committing every run
 // total to its point directly.
+//
+// corr: the corrected policy's Jx index - slot 4 (q 3) feeds point cell + 1,
+// not cell + sy (src/grid/oGrid.cpp:101 as the reference has it).
 __global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned long long *__restrict__ wj,
                                   const unsigned long long *__restrict__ wr, unsigned long long *Jx,
-                                  unsigned long long *Jy, unsigned long long *Jz, unsigned long long *rho, int what) {
+                                  unsigned long long *Jy, unsigned long long *Jz, unsigned long long *rho, int what,
+                                  int corr) {
     const int64_t first = (int64_t)sx + sy + 1;  // points below have no neighbour cell with particles
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
         if (what & 1) {
@@ -630,7 +759,8 @@ __global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned l
                 const unsigned long long g5 = __ldg(rec(p - sx - 1) + 8);
                 const unsigned long long g6 = __ldg(rec(p - sx - sy) + 9);
                 const ulonglong2 g4 = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p - sx) + 10));  // 10,11
-                jx = g0a.x + g2a + g2b.x + g3;   // q 0, 1, 3, 2
+                const unsigned long long q3 = corr ? __ldg(rec(p - 1) + 4) : g2b.x;
+                jx = g0a.x + g2a + q3 + g3;      // q 0, 1, 3, 2
                 jy = g0a.y + g1 + g5 + g4.x;     // q 4, 5, 6, 7
                 jz = g0b + g2b.y + g6 + g4.y;    // q 8, 11, 10, 9
             }
@@ -844,6 +974,53 @@ __global__ void k_fold_m(MGeom g, int d, long long *f0, long long *f1, long long
     int64_t t = (int64_t)it[0] * g.sx + (int64_t)it[1] * g.sy + it[2];
     long long *F = blockIdx.z == 0 ? f0 : (blockIdx.z == 1 ? f1 : f2);
     F[t] += F[s];
+}
+
+// The corrected policy's periodic fold and ghost fill along dim d over the
+// whole (n+3)^2 plane (dimension by dimension, so edge and corner lines
+// follow), as k_periodic_full of the FP64 form: fold f[n] += f[0],
+// f[1] += f[n+1], f[2] += f[n+2] (exact integer adds) on the fixed-point
+// arrays; ghost f[0] = f[n], f[n+1] = f[1], f[n+2] = f[2] on the FP32 ones.
+// One array per blockIdx.z.
+struct MFix4 {
+    long long *p[4];
+};
+struct MF9 {
+    float *p[9];
+};
+
+template <class T>
+__device__ __forceinline__ void periodic_full_line(const MGeom &g, T *F, int d, int r, int q, bool fold) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int n = g.n[d];
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    auto at = [&](int i) -> T & {
+        c[d] = i;
+        return F[(int64_t)c[0] * g.sx + (int64_t)c[1] * g.sy + c[2]];
+    };
+    if (fold) {
+        at(n) += at(0);
+        at(1) += at(n + 1);
+        at(2) += at(n + 2);
+    } else {
+        at(0) = at(n);
+        at(n + 1) = at(1);
+        at(n + 2) = at(2);
+    }
+}
+
+__global__ void k_fold_full_m(MGeom g, MFix4 fl, int d, int t1, int t2) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= t2 || r >= t1) return;
+    periodic_full_line(g, fl.p[blockIdx.z], d, r, q, true);
+}
+
+__global__ void k_ghost_full_m(MGeom g, MF9 fl, int d, int t1, int t2) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= t2 || r >= t1) return;
+    periodic_full_line(g, fl.p[blockIdx.z], d, r, q, false);
 }
 
 struct MPlane {
@@ -1259,6 +1436,7 @@ MGeom mgeom(emoo_handle *h, double dt) {
         m.n[d] = h->g.n[d];
         m.dtid[d] = (float)(dt / h->g.d[d]);
         m.idf[d] = (float)(1.0 / h->g.d[d]);
+        m.ddt[d] = dt > 0.0 ? (float)(h->g.d[d] / dt) : 0.0f;
     }
     m.sx = h->g.sx;
     m.sy = h->g.sy;
@@ -1442,7 +1620,10 @@ int mixed_to_f64(emoo_handle *h, int64_t at, int64_t n, double *x, double *y, do
     return EMOO_OK;
 }
 
+static int mixed_ghost_full(emoo_handle *h, bool e_only);
+
 int mixed_ghost_fill(emoo_handle *h) {
+    if (h->policy == EMOO_POLICY_CORRECTED) return mixed_ghost_full(h, false);
     // E/B ghost fill through the fixed storage slots, with LightBC planes for
     // external sides, in the reference's dimension order
     MGeom mg = mgeom(h, h->dtp);
@@ -1504,8 +1685,43 @@ int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n) {
     return EMOO_OK;
 }
 
+// The corrected policy's full-range fold (fixed point) or ghost fill (FP32)
+// of n arrays, dimension by dimension.
+static int mixed_periodic_full(emoo_handle *h, const MFix4 *fix, const MF9 *flt, int n) {
+    MGeom mg = mgeom(h, h->dtp);
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    for (int d = 0; d < 3; d++) {
+        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, n);
+        h->launches++;
+        if (fix) k_fold_full_m<<<grd, blk, 0, h->stream>>>(mg, *fix, d, g.tot[o1], g.tot[o2]);
+        else k_ghost_full_m<<<grd, blk, 0, h->stream>>>(mg, *flt, d, g.tot[o1], g.tot[o2]);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+static int mixed_fold_full(emoo_handle *h, int what) {
+    MFix4 fl = {};
+    int n = 0;
+    if (what & FOLD_J)
+        for (int c = 0; c < 3; c++) fl.p[n++] = h->mf->J[c];
+    if (what & FOLD_RHO) fl.p[n++] = h->mf->J[3];
+    return n ? mixed_periodic_full(h, &fl, nullptr, n) : EMOO_OK;
+}
+
+// E (3) or E, B and B_tm1 (9) ghost planes, corrected policy
+static int mixed_ghost_full(emoo_handle *h, bool e_only) {
+    MF9 fl = {};
+    for (int c = 0; c < 3; c++) fl.p[c] = h->mf->E[c];
+    for (int c = 0; c < 6; c++) fl.p[3 + c] = h->mf->Bslot[c];
+    return mixed_periodic_full(h, nullptr, &fl, e_only ? 3 : 9);
+}
+
 // what: FOLD_J (the two transverse J components), FOLD_RHO, or both
 static int mixed_fold(emoo_handle *h, int what) {
+    if (h->policy == EMOO_POLICY_CORRECTED) return mixed_fold_full(h, what);
     MGeom mg = mgeom(h, h->dtp);
     const Geom &g = h->g;
     for (int d = 0; d < 3; d++) {
@@ -1543,7 +1759,8 @@ static int mixed_cells_to_points(emoo_handle *h, int mode) {
     h->launches++;
     k_cells_to_points<<<nblk(h->g.npts, 152 * 8), 256, 0, h->stream>>>(
         h->g.npts, (int)h->g.sx, (int)h->g.sy, m->wj, m->wr, (unsigned long long *)m->J[0],
-        (unsigned long long *)m->J[1], (unsigned long long *)m->J[2], (unsigned long long *)m->J[3], what);
+        (unsigned long long *)m->J[1], (unsigned long long *)m->J[2], (unsigned long long *)m->J[3], what,
+        h->policy == EMOO_POLICY_CORRECTED ? 1 : 0);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
@@ -1598,17 +1815,22 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
     MState S = mstate(h);
     const float4 *pk = h->mf->pack;
     dim3 grd((unsigned)nb);
+    const bool corr = h->policy == EMOO_POLICY_CORRECTED;
     if (!push) {
         h->launches++;
-        if (rel && first)
-            k_fused_m<true, true, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
-                                                                             with_rho, g0, h->ctr);
-        else if (rel)
-            k_fused_m<true, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
-                                                                              with_rho, g0, h->ctr);
-        else
-            k_fused_m<false, false, false><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
-                                                                               with_rho, g0, h->ctr);
+#define EMOO_DEPOSIT_M(R, F, C)                                                                                  \
+    k_fused_m<R, F, false, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
+                                                                  h->ctr)
+        if (corr) {
+            if (rel && first) EMOO_DEPOSIT_M(true, true, true);
+            else if (rel) EMOO_DEPOSIT_M(true, false, true);
+            else EMOO_DEPOSIT_M(false, false, true);
+        } else {
+            if (rel && first) EMOO_DEPOSIT_M(true, true, false);
+            else if (rel) EMOO_DEPOSIT_M(true, false, false);
+            else EMOO_DEPOSIT_M(false, false, false);
+        }
+#undef EMOO_DEPOSIT_M
         EMOO_CUDA(cudaGetLastError());
         return mixed_finish_deposit(h, mode);
     }
@@ -1617,20 +1839,25 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
         dim3 blk(32, 8);
         dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
         h->launches++;
-        k_pack_m<<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        if (corr) k_pack_m<true><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        else k_pack_m<false><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
         EMOO_CUDA(cudaGetLastError());
     }
     h->launches++;
     if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
-    if (rel && first)
-        k_fused_m<true, true, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho,
-                                                                        g0, h->ctr);
-    else if (rel)
-        k_fused_m<true, false, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
-                                                                         with_rho, g0, h->ctr);
-    else
-        k_fused_m<false, false, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D,
-                                                                          with_rho, g0, h->ctr);
+#define EMOO_FUSED_M(R, F, C)                                                                                   \
+    k_fused_m<R, F, true, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
+                                                                 h->ctr)
+    if (corr) {
+        if (rel && first) EMOO_FUSED_M(true, true, true);
+        else if (rel) EMOO_FUSED_M(true, false, true);
+        else EMOO_FUSED_M(false, false, true);
+    } else {
+        if (rel && first) EMOO_FUSED_M(true, true, false);
+        else if (rel) EMOO_FUSED_M(true, false, false);
+        else EMOO_FUSED_M(false, false, false);
+    }
+#undef EMOO_FUSED_M
     EMOO_CUDA(cudaGetLastError());
     if (h->prof_on) {
         EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
@@ -1656,6 +1883,9 @@ static int mixed_yee(emoo_handle *h, double dtp, int es) {
         MCF3 T = {{mt_role(h, 0), mt_role(h, 1), mt_role(h, 2)}};
         h->launches++;
         k_yee_e_m<<<grd, blk, 0, h->stream>>>(mg, E, T, J, (float)dtp, (float)h->mf->q0);
+        // the B half reads E at plane n+1: refreshed first under the corrected
+        // policy (time-centred at the periodic wrap, as yee_f64)
+        if (h->policy == EMOO_POLICY_CORRECTED) EMOO_TRY(mixed_ghost_full(h, true));
         MF3 B = {{mb_role(h, 0), mb_role(h, 1), mb_role(h, 2)}};
         MCF3 Ec = {{E.p[0], E.p[1], E.p[2]}};
         h->launches++;
@@ -1880,7 +2110,7 @@ int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_a
         dim3 blk(32, 8);
         dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
         h->launches++;
-        k_pack_m<<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        k_pack_m<false><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);  // the adjoint runs the reference policy
         EMOO_CUDA(cudaGetLastError());
     }
     MSnapC SC{S.cell, {S.o[0], S.o[1], S.o[2]}, {S.u[0], S.u[1], S.u[2]}};

@@ -106,10 +106,11 @@ def test_reference_policy_does_not_conserve_charge():
 
 # ---- GPU -------------------------------------------------------------------
 
-def _gpu(cfg, precision=abi.FP64, policy=abi.POLICY_CORRECTED):
+def _gpu(cfg, precision=abi.FP64, policy=abi.POLICY_CORRECTED, poisson_solver=abi.POISSON_JACOBI):
     from backends import GpuBackend
 
-    g = GpuBackend(configs.input_info(cfg), cfg.dt, precision=precision, policy=policy)
+    g = GpuBackend(configs.input_info(cfg), cfg.dt, precision=precision, policy=policy, poisson_solver=poisson_solver,
+                   poisson_rtol=1e-12)
     _load(g, loading.sample_all(cfg))
     return g
 
@@ -154,8 +155,7 @@ def test_gpu_corrected_policy_keeps_gauss_law():
 
 @pytest.mark.gpu
 def test_gpu_corrected_policy_refuses_what_it_does_not_cover():
-    with pytest.raises(Exception):
-        _gpu(_cfg(1), precision=abi.MIXED)
+    _gpu(_cfg(1), precision=abi.MIXED).close()  # both forms take it
     walls = configs.tiny("walls", part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
                          field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
                          init="constant")
@@ -164,19 +164,19 @@ def test_gpu_corrected_policy_refuses_what_it_does_not_cover():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dt", [0.125, 0.5])
-def test_gpu_corrected_policy_is_stable_where_the_reference_is_not(dt):
+@pytest.mark.parametrize("dt,precision", [(0.125, abi.FP64), (0.5, abi.FP64), (0.5, abi.MIXED)])
+def test_gpu_corrected_policy_is_stable_where_the_reference_is_not(dt, precision):
     """Thermal plasma 16^3, 2 x 16 ppc, v_th 0.1c, 600 steps: the reference's
     arithmetic heats the plasma (total energy grows several-fold at dt 0.125,
     without bound at dt 0.5); the corrected policy keeps it within a few per
-    cent at both."""
+    cent at both, in both forms."""
     from backends import GpuBackend
 
     cfg = configs.thermal256(16)
     cfg.dt = dt
 
     def history(policy):
-        g = GpuBackend(configs.input_info(cfg), cfg.dt, policy=policy, track_ids=0)
+        g = GpuBackend(configs.input_info(cfg), cfg.dt, policy=policy, track_ids=0, precision=precision)
         for si, p in enumerate(loading.sample_all(cfg)):
             g.add_species(si, p)
         g.init_fields()
@@ -186,7 +186,7 @@ def test_gpu_corrected_policy_is_stable_where_the_reference_is_not(dt):
         return rows[:, 7] / rows[0, 7]
 
     ref, cor = history(abi.POLICY_REFERENCE), history(abi.POLICY_CORRECTED)
-    assert ref[-1] > 2.0, ref[-1]
+    assert not ref[-1] <= 2.0, ref[-1]  # in FP32 the blow-up can overflow to NaN
     assert np.abs(cor - 1.0).max() < 0.1, np.abs(cor - 1.0).max()
 
 
@@ -253,3 +253,68 @@ def test_gpu_vacuum_yee_is_time_centred_under_the_corrected_policy():
     assert ref > 1e6, ref
     assert cor < 2.0, cor
     assert abs(cor - _vacuum(_oracle_vacuum, 1)) <= 1e-9 * cor
+
+
+# ---- the mixed form under the corrected policy ---------------------------------
+
+MIXED_CORR_RTOL = 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("relativity", [0, 1])
+def test_gpu_mixed_corrected_policy_matches_fp64(relativity):
+    """The mixed form (FP32 positions, momenta and fields, fixed-point J)
+    against the FP64 form under the corrected policy: with the continuous
+    true-vertex gather there is no face discontinuity to amplify FP32
+    rounding, so after 6 steps (a sort every 3) the fields and particles agree
+    to FP32 precision and the crossing counts exactly. Both start from the
+    multigrid solve: the FP32 deposit leaves rho's mean at FP32 rounding
+    rather than zero, and on a periodic grid the reference's Jacobi then
+    drifts by that much per sweep and misses its absolute stop test (E is
+    unaffected); the multigrid removes the mean."""
+    cfg = _cfg(relativity, nstep_sort=3)
+    mg = abi.POISSON_MULTIGRID
+    g, m = _gpu(cfg, poisson_solver=mg), _gpu(cfg, precision=abi.MIXED, poisson_solver=mg)
+    assert g.init_fields()[0] == m.init_fields()[0] == 0
+    for ti in range(cfg.steps):
+        assert g.step(1) == m.step(1), ti
+    n = cfg.n
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ):
+        assert rel_l2(m.get_field(i), g.get_field(i)) <= MIXED_CORR_RTOL, (abi.FIELD_NAMES[i],
+                                                                            rel_l2(m.get_field(i), g.get_field(i)))
+    # J and rho at the physical points: after the fold the ghost planes hold
+    # leftovers nothing reads, and the two forms leave different ones (FP64
+    # deposits into unwrapped cells -1..n, the mixed form wraps first)
+    for i in (abi.JX, abi.JY, abi.JZ, abi.RHO):
+        a, b = m.get_field(i)[P], g.get_field(i)[P]
+        assert rel_l2(a, b) <= MIXED_CORR_RTOL, (abi.FIELD_NAMES[i], rel_l2(a, b))
+    pg, pm = by_id(g.particles()), by_id(m.particles())
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert rel_l2(pm[k], pg[k]) <= MIXED_CORR_RTOL, k
+    g.close()
+    m.close()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_corrected_policy_conserves_charge():
+    """The mixed form's FP32 Villasenor-Buneman current: rho(t + dt) - rho(t)
+    + dt div J = 0 to FP32 rounding of the path (the fixed-point quantum is
+    2^-32 of the largest charge), step after step, crossings included."""
+    cfg = _cfg(1, n=(8, 6, 5), steps=8)
+    n = cfg.n
+    m = _gpu(cfg, precision=abi.MIXED, poisson_solver=abi.POISSON_MULTIGRID)
+    assert m.init_fields()[0] == 0
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    rho0 = m.get_field(abi.RHO)[P].copy()
+    scale = np.abs(rho0).max()
+    crossed = 0
+    for ti in range(cfg.steps):
+        crossed += sum(m.step(1))
+        rho1 = m.get_field(abi.RHO)[P]
+        divj = _div([m.get_field(i) for i in (abi.JX, abi.JY, abi.JZ)], cfg.dx, n)
+        cont = (rho1 - rho0) + cfg.dt * divj
+        assert np.abs(cont).max() <= 1e-5 * scale, (ti, np.abs(cont).max(), scale)
+        rho0 = rho1.copy()
+    assert crossed > 0
+    m.close()

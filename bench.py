@@ -51,6 +51,7 @@ def _args():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-laser512", action="store_true")
     ap.add_argument("--no-poisson", action="store_true")
+    ap.add_argument("--no-corrected", action="store_true")
     ap.add_argument("--only", choices=["poisson"], default=None,
                     help="run one side measurement alone and print its JSON line")
     ap.add_argument("--cpu-procs", type=int, default=0)
@@ -284,9 +285,49 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
         res["adjoint"] = adjoint_arm()
     if not args.no_laser512:
         res["laser512"] = laser512_arm(device)
+    if not args.no_corrected:
+        res["corrected"] = corrected_arm(cfg, args, device)
     if not args.no_poisson:
         res["poisson"] = poisson_arm(device)
     return cfg, res
+
+
+def corrected_arm(cfg, args, device):
+    """The same workload and form under the corrected-physics policy (true
+    vertex, charge-conserving Villasenor-Buneman current, time-centred Yee at
+    the periodic wrap): loop throughput and the fused kernel's mean time."""
+    from apc_524_project_gb300 import abi, configs
+
+    L = abi.lib()
+    N = cfg.total_particles()
+    info = configs.input_info(cfg)
+    o = abi.Opts()
+    L.emoo_default_opts(C.byref(o))
+    o.precision = abi.MIXED
+    o.dt = cfg.dt
+    o.capacity = N
+    o.track_ids = 0
+    o.device = device
+    o.policy = abi.POLICY_CORRECTED
+    h = C.c_void_p()
+    abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
+    for si in range(len(cfg.species)):
+        g = configs.gen_params(cfg, si)
+        abi.check(L.emoo_load_generated(h, C.byref(g), cfg.count(cfg.species[si])), "emoo_load_generated")
+    it = (C.c_int * 4)()
+    rc = L.emoo_init_fields(h, it)
+    if rc not in (abi.OK, abi.ERR_NOT_CONVERGED):
+        abi.check(rc, "emoo_init_fields")
+    cnt = (C.c_int64 * 6)()
+    for _ in range(args.warmup):
+        abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
+    abi.check(L.emoo_set_profiling(h, 1))
+    t = _timed_steps(h, args.steps, lambda: None)
+    st = abi.Stats()
+    abi.check(L.emoo_get_stats(h, C.byref(st)))
+    abi.check(L.emoo_destroy(h))
+    return {"policy": "corrected", "form": "mixed", "value": N * args.steps / t, "unit": UNIT,
+            "ms_per_step": t / args.steps * 1e3, "fused_kernel_ms": st.timed_ms / max(1, st.timed_launches)}
 
 
 def _poisson_solve_ms(L, h, reps):
@@ -663,6 +704,8 @@ def main():
         line["laser512"] = res["laser512"]
     if "poisson" in res:
         line["poisson"] = res["poisson"]
+    if "corrected" in res:
+        line["corrected"] = res["corrected"]
     if "e2e" in res:
         e = res["e2e"]
         line["e2e"] = {"value": N * e["steps"] * world / e["t"], "unit": UNIT, "h2d_bytes_per_step": e["h2d"],

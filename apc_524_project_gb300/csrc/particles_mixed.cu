@@ -468,8 +468,9 @@ __device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, i
             const float de = e[a] - s[a];
             const float ua = fmaf(ta, de, s[a]), ub = fmaf(tb, de, s[a]);
             const float mid = 0.5f * (ua + ub);
-            const int c = mid < 0.0f ? -1 : (mid >= 1.0f ? 1 : 0);
-            m[a] = mid - (float)c;
+            const bool below = mid < 0.0f, above = mid >= 1.0f;
+            const int c = below ? -1 : (above ? 1 : 0);
+            m[a] = mid - (below ? -1.0f : (above ? 1.0f : 0.0f));  // no int-to-float conversion (FP64 pipe)
             Dd[a] = ub - ua;
             int ii = io[a] + c;
             ii = ii < 1 ? ii + g.n[a] : (ii > g.n[a] ? ii - g.n[a] : ii);

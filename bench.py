@@ -683,7 +683,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload_desc(cfg), "form": "mixed (int32 cell + FP32 offset, FP32 u and fields, "
                                                           "int64 fixed-point J/rho)",
-                   "particles": N, "l2": "inputs larger than L2 (15 GB particle state per GPU), no flush",
+                   "particles": N,
+                   "l2": f"inputs larger than L2 ({N * 28 / 1e9:.1f} GB particle state per GPU, 129 MB L2), no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "kernel": "k_fused_m (gather+push+BC+deposit)",

@@ -584,7 +584,7 @@ int mg_setup(emoo_handle *h, MgState *s) {
             L.crs[d] = (P[d] % 2 == 0) && P[d] >= 4;
         }
         if (L.hi[0] < L.lo[0] || L.hi[1] < L.lo[1] || L.hi[2] < L.lo[2] || L.hi[0] - L.lo[0] + 1 > 65535) {
-            mg_release(s);
+            mg_release(s);  // no unknowns (checked by the caller first), or too many planes for one grid launch
             return EMOO_ERR_UNSUPPORTED;
         }
         const double diag = 2.0 * (1.0 / (hh[0] * hh[0]) + 1.0 / (hh[1] * hh[1]) + 1.0 / (hh[2] * hh[2]));
@@ -680,6 +680,17 @@ void multigrid_free(emoo_handle *h) {
 // the outer steps (V-cycles) run, *converged whether max |r| <= rtol max |r0|
 // was met within the cap.
 int multigrid_f64(emoo_handle *h, int id1, int id2, int rid, double mult, int *cycles, int *converged) {
+    bool none = false;  // an external dimension of one cell has no unknowns: the boundary planes are the solution
+    for (int d = 0; d < 3; d++) none = none || (h->bc.fbc[2 * d] != FBC_PERIODIC && h->g.n[d] < 2);
+    if (none) {
+        EMOO_CUDA(cudaMemsetAsync(h->slot[id1], 0, (size_t)h->g.npts * sizeof(double), h->stream));
+        EMOO_TRY(poisson_field_bc(h, id1));
+        EMOO_CUDA(cudaMemcpyAsync(h->slot[id2], h->slot[id1], (size_t)h->g.npts * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, h->stream));
+        if (cycles) *cycles = 0;
+        if (converged) *converged = 1;
+        return EMOO_OK;
+    }
     if (!h->mg) h->mg = new MgState();
     MgState *s = (MgState *)h->mg;
     EMOO_TRY(mg_setup(h, s));

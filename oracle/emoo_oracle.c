@@ -1070,11 +1070,15 @@ static int exact_poisson(orc_t *c, int id1, int id2, const double *R, double mul
         lo[d] = per[d] ? 1 : 2;
         hi[d] = c->n[d];
         m[d] = hi[d] - lo[d] + 1;
-        if (m[d] < 1) return -1;
     }
     double *u = c->slot[id1];
     for (long o = 0; o < c->npts; o++) u[o] = 0.0;
     orc_execute_bc(c, id1); /* the Dirichlet planes */
+    if (m[0] < 1 || m[1] < 1 || m[2] < 1) { /* no unknowns: the boundary planes are the solution */
+        memcpy(c->slot[id2], u, sizeof(double) * c->npts);
+        *conv = 1;
+        return 0;
+    }
     long nu = (long)m[0] * m[1] * m[2];
     double *x = calloc(nu, sizeof(double)), *r = malloc(nu * sizeof(double));
     double *p = malloc(nu * sizeof(double)), *q = malloc(nu * sizeof(double));

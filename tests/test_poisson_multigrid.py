@@ -125,6 +125,23 @@ def test_oracle_exact_solve_meets_the_discrete_equations(bc):
     o.close()
 
 
+def test_oracle_exact_solve_without_unknowns():
+    """An external dimension of one cell leaves no unknown point: the
+    potentials are the PoissonBC planes (E itself is then rewritten by the
+    external-field fill, plane 1 being a boundary plane too)."""
+    fb = ("external", "external") + ("periodic",) * 4
+    cfg = _box((1, 6, 4), fb, bound_phi=(0.1, -0.2, 0.0, 0.0, 0.0, 0.0))
+    o = _oracle(cfg, 1)
+    rho, J = _sources(o.get_field(abi.RHO).shape)
+    _set_sources(o, rho, J)
+    rc, it = o.initialize_fields_only()
+    assert rc == 0 and it == [0, 0, 0, 0]
+    phi = o.get_field(abi.PHI1)
+    assert np.all(phi[1] == 0.1) and np.all(phi[2] == -0.2)
+    np.testing.assert_array_equal(o.get_field(abi.PHI2), phi)
+    o.close()
+
+
 def test_oracle_exact_solve_matches_fft_on_a_periodic_box():
     cfg = _box((8, 6, 10), dx=(1.0, 0.5, 2.0))
     o = _oracle(cfg, 1)
@@ -198,6 +215,10 @@ CASES = {
     "external_x": ((16, 12, 8), ("external", "external") + ("periodic",) * 4, (1.0, 1.0, 1.0)),
     "external_all": ((12, 10, 9), ("external",) * 6, (0.7, 1.0, 1.3)),
     "periodic_x_external_yz": ((32, 8, 8), ("periodic", "periodic") + ("external",) * 4, (1.0, 1.0, 1.0)),
+    # degenerate: no unknowns at all (the boundary planes are the solution),
+    # and the smallest periodic grid (one level, every neighbour a wrap)
+    "external_x_one_cell": ((1, 6, 4), ("external", "external") + ("periodic",) * 4, (1.0, 1.0, 1.0)),
+    "periodic_2": ((2, 2, 2), ("periodic",) * 6, (1.0, 1.0, 1.0)),
 }
 
 

@@ -210,6 +210,8 @@ PROTOTYPES = {
     "emoo_input_message": (C.c_char_p, []),
     "emoo_process_info": (C.c_int, [C.POINTER(InputInfo)]),
     "emoo_set_particles": (C.c_int, [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D, _D, _D]),
+    "emoo_attach_particles": (C.c_int, [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D, _D, _D]),
+    "emoo_detach_particles": (C.c_int, [_P]),
     "emoo_get_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "emoo_set_profiling": (C.c_int, [_P, C.c_int]),
     "emoo_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),

@@ -716,6 +716,7 @@ using namespace emoo;
 extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
                            emoo_ad_result *out, double *grad_theta, double *grad_v) {
     if (!h || !spec || !out) return EMOO_ERR_ARG;
+    if (h->host_mode) return EMOO_ERR_STATE;  // it steps the particle store
     if (h->info.electrostatic == 1 || h->policy != EMOO_POLICY_REFERENCE) return EMOO_ERR_UNSUPPORTED;
     if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)

@@ -717,13 +717,56 @@ int read_counters(emoo_handle *h, int64_t *counts6, bool accumulate) {
     return EMOO_OK;
 }
 
+// Every entry point: the handle's device current, and the device particle
+// store refreshed from host-resident arrays if a streamed step left it stale.
 #define HANDLE_CHECK(h)                      \
     do {                                     \
         if (!(h)) return EMOO_ERR_ARG;       \
         EMOO_TRY(set_device(h));             \
+        EMOO_TRY(host_store_sync(h));        \
+    } while (0)
+
+// Entry points that change the particle store: not while the particles are
+// host-resident (emoo_detach_particles first).
+#define STORE_WRITE_CHECK(h)                               \
+    do {                                                   \
+        if ((h)->host_mode) return EMOO_ERR_STATE;         \
     } while (0)
 
 }  // namespace
+
+namespace emoo {
+
+// The attached arrays into the device store (the loader's conversion).
+static int host_upload(emoo_handle *h) {
+    for (int s = 0; s < h->nspec; s++) {
+        const emoo_handle::Attached &a = h->attached[s];
+        if (h->count[s] > 0)
+            EMOO_TRY(mixed_from_f64(h, h->off[s], h->count[s], a.p[0], a.p[1], a.p[2], a.p[3], a.p[4], a.p[5],
+                                    a.p[6]));
+    }
+    h->store_stale = 0;
+    if (h->opts.deposit_rho) h->rho_stale = 1;  // rho follows the store
+    return EMOO_OK;
+}
+
+// The device store into the attached arrays (the readback's conversion).
+static int host_download(emoo_handle *h) {
+    for (int s = 0; s < h->nspec; s++) {
+        const emoo_handle::Attached &a = h->attached[s];
+        if (h->count[s] > 0)
+            EMOO_TRY(mixed_to_f64(h, h->off[s], h->count[s], a.p[0], a.p[1], a.p[2], a.p[3], a.p[4], a.p[5],
+                                  a.p[6]));
+    }
+    return EMOO_OK;
+}
+
+int host_store_sync(emoo_handle *h) {
+    if (!h->host_mode || !h->store_stale) return EMOO_OK;
+    return host_upload(h);
+}
+
+}  // namespace emoo
 
 extern "C" {
 
@@ -891,6 +934,7 @@ int emoo_destroy(emoo_handle *h) {
     dfree(h->wproff);
     if (h->jacobi_state) cudaFree(h->jacobi_state);
     multigrid_free(h);
+    if (h->mhost) cudaFree(h->mhost);
     for (int i = 0; i < 2; i++)
         if (h->prof_ev[i]) cudaEventDestroy(h->prof_ev[i]);
     for (cudaEvent_t e : h->prof_pending) cudaEventDestroy(e);
@@ -927,6 +971,7 @@ int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x,
                         const double *vx, const double *vy, const double *vz, const double *gamma,
                         const int64_t *ids) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     EMOO_TRY(compact(h));
     if (species < 0 || species >= h->nspec || n < 0) return EMOO_ERR_ARG;
@@ -966,6 +1011,7 @@ int emoo_load_particles(emoo_handle *h, int species, int64_t n, const double *x,
 
 int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     EMOO_TRY(compact(h));
     if (!g || g->species < 0 || g->species >= h->nspec || n < 0) return EMOO_ERR_ARG;
@@ -1009,6 +1055,18 @@ int emoo_num_particles(emoo_handle *h, int species, int64_t *n) {
 
 int emoo_get_particles(emoo_handle *h, int species, int64_t cap, double *x, double *y, double *z, double *vx,
                        double *vy, double *vz, double *gamma, int64_t *ids, int64_t *n) {
+    if (h && h->host_mode && !ids) {  // the attached arrays are the state: copied as they are
+        if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
+        const int64_t cnt = h->count[species];
+        *n = cnt;
+        if (cap < cnt || !x || !y || !z || !vx || !vy || !vz) return EMOO_ERR_ARG;
+        const emoo_handle::Attached &a = h->attached[species];
+        double *out[7] = {x, y, z, vx, vy, vz, gamma};
+        for (int q = 0; q < 7; q++)
+            if (out[q] && a.p[q] && out[q] != a.p[q]) memcpy(out[q], a.p[q], sizeof(double) * (size_t)cnt);
+        if (gamma && !a.p[6]) memset(gamma, 0, sizeof(double) * (size_t)cnt);
+        return EMOO_OK;
+    }
     HANDLE_CHECK(h);
     if (species < 0 || species >= h->nspec || !n) return EMOO_ERR_ARG;
     EMOO_TRY(compact(h));
@@ -1131,6 +1189,7 @@ int emoo_poisson_init(emoo_handle *h, int iters[4]) {
 
 int emoo_sort(emoo_handle *h) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     EMOO_TRY(do_sort(h));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
@@ -1148,6 +1207,7 @@ int emoo_interpolate(emoo_handle *h) {
 
 int emoo_push(emoo_handle *h) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(push_cached_f64(h, h->dtp));
@@ -1157,6 +1217,7 @@ int emoo_push(emoo_handle *h) {
 
 int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(reset_counters(h));
@@ -1321,7 +1382,8 @@ int emoo_ad_nparams(const emoo_handle *h) {
 }
 
 int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
-    HANDLE_CHECK(h);
+    if (!h) return EMOO_ERR_ARG;
+    EMOO_TRY(set_device(h));  // host-resident particles: the store is refreshed below only where needed
     if (nsteps < 0) return EMOO_ERR_ARG;
     EMOO_TRY(reset_counters(h));
     // with deposit_rho the step deposits J only and leaves rho pending
@@ -1331,6 +1393,24 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
     const int fold_what = lazy_rho ? FOLD_J : FOLD_ALL;
     for (int it = 0; it < nsteps; it++) {
         int64_t ti = h->step_index;
+        if (h->host_mode) {
+            // host-resident particles: stream them through the fused kernel, in
+            // both directions at once over the host link; a step that sorts,
+            // writes a history row or makes the first push (or has particle
+            // removal) runs on the device store between an upload and a readback
+            const bool sort_now = h->info.nstep_sort > 0 && ti % h->info.nstep_sort == 0;
+            const bool streamed = h->precision == EMOO_MIXED && !sort_now && ti < h->next_hist &&
+                                  !(h->info.relativity != 0 && h->first_push) && !has_absorbing(h);
+            if (streamed) {
+                EMOO_TRY(mixed_step_host(h, h->dtp, fold_what));
+                h->store_stale = 1;
+                h->t += h->dtp;
+                h->step_index++;
+                if (lazy_rho) h->rho_stale = 1;
+                continue;
+            }
+            EMOO_TRY(host_store_sync(h));
+        }
         if (h->info.nstep_sort > 0 && ti % h->info.nstep_sort == 0) EMOO_TRY(do_sort(h));
         if (ti >= h->next_hist) {
             double row[8];
@@ -1353,6 +1433,7 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
         h->t += h->dtp;
         h->step_index++;
         if (lazy_rho) h->rho_stale = 1;
+        if (h->host_mode) EMOO_TRY(host_download(h));
     }
     int64_t c6[6];
     const int rc = read_counters(h, c6, false);
@@ -1400,9 +1481,56 @@ int emoo_check(emoo_handle *h) {
     return read_err(h);
 }
 
+int emoo_attach_particles(emoo_handle *h, int species, int64_t n, double *x, double *y, double *z, double *vx,
+                          double *vy, double *vz, double *gamma) {
+    HANDLE_CHECK(h);
+    // the mixed form, and no particle removal (the arrays keep their length)
+    if (h->precision != EMOO_MIXED || has_absorbing(h)) return EMOO_ERR_UNSUPPORTED;
+    if (species < 0 || species >= h->nspec) return EMOO_ERR_ARG;
+    EMOO_TRY(materialize_rho(h));
+    EMOO_TRY(compact(h));
+    if (n != h->count[species]) return EMOO_ERR_ARG;
+    double *p[7] = {x, y, z, vx, vy, vz, gamma};
+    const bool rel = h->info.relativity != 0;
+    for (int q = 0; q < 7; q++) {
+        if (!p[q] && (q < 6 || rel)) return EMOO_ERR_ARG;
+        if (p[q] && n > 0 && !mixed_device_accessible(h, p[q])) return EMOO_ERR_UNSUPPORTED;
+    }
+    emoo_handle::Attached &a = h->attached[species];
+    a.n = n;
+    for (int q = 0; q < 7; q++) a.p[q] = p[q];
+    bool all = true;
+    for (int s = 0; s < h->nspec; s++) all = all && h->attached[s].n == h->count[s];
+    if (all) {
+        MHost m = {};
+        m.g = h->g;
+        m.rel = rel ? 1 : 0;
+        for (int s = 0; s < h->nspec; s++) {
+            const emoo_handle::Attached &b = h->attached[s];
+            m.x[s] = b.p[0], m.y[s] = b.p[1], m.z[s] = b.p[2];
+            m.vx[s] = b.p[3], m.vy[s] = b.p[4], m.vz[s] = b.p[5], m.gam[s] = b.p[6];
+        }
+        if (!h->mhost) EMOO_CUDA(cudaMalloc(&h->mhost, sizeof(MHost)));
+        EMOO_CUDA(cudaMemcpyAsync(h->mhost, &m, sizeof(MHost), cudaMemcpyHostToDevice, h->stream));
+        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+        h->host_mode = 1;
+        h->store_stale = 1;  // the arrays are the particle state from now on
+    }
+    return EMOO_OK;
+}
+
+int emoo_detach_particles(emoo_handle *h) {
+    HANDLE_CHECK(h);  // refreshes the store from the arrays
+    for (int s = 0; s < EMOO_NSPEC; s++) h->attached[s] = emoo_handle::Attached();
+    h->host_mode = 0;
+    h->store_stale = 0;
+    return EMOO_OK;
+}
+
 int emoo_set_particles(emoo_handle *h, int species, int64_t n, const double *x, const double *y, const double *z,
                        const double *vx, const double *vy, const double *vz, const double *gamma) {
     HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
     EMOO_TRY(compact(h));
     if (species < 0 || species >= h->nspec || n != h->count[species]) return EMOO_ERR_ARG;

@@ -46,6 +46,16 @@ struct Geom {
     int vshift = 0;
 };
 
+// Host-resident particles (emoo_attach_particles): the caller's FP64 arrays
+// per species, and the geometry the fused kernel converts with. Lives in
+// device memory; the kernel reads it through one pointer.
+struct MHost {
+    Geom g;
+    int rel;
+    double *x[EMOO_NSPEC], *y[EMOO_NSPEC], *z[EMOO_NSPEC];
+    double *vx[EMOO_NSPEC], *vy[EMOO_NSPEC], *vz[EMOO_NSPEC], *gam[EMOO_NSPEC];
+};
+
 // Per-species constants, precomputed on the host in the reference's order of
 // operations so the device arithmetic stays bit-identical to the reference.
 struct SpeciesTab {
@@ -156,6 +166,15 @@ struct emoo_handle {
     int poisson_solver = 0;      // EMOO_POISSON_JACOBI / EMOO_POISSON_MULTIGRID
     double poisson_rtol = 1e-10; // multigrid stop, relative to the start residual
     void *mg = nullptr;          // multigrid levels (multigrid.cu), kept between solves
+    // host-resident particles: the attached arrays are the state; the device
+    // store is refreshed from them (store_stale) before anything reads it
+    struct Attached {
+        int64_t n = -1;  // -1: not attached
+        double *p[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    } attached[EMOO_NSPEC];
+    int host_mode = 0;
+    int store_stale = 0;
+    emoo::MHost *mhost = nullptr;  // device copy of the attached pointers
 
     double dt = 0.0;    // configured step
     double t = 0.0;     // time_phys
@@ -218,6 +237,12 @@ int ghost_full_f64(emoo_handle *h);
 int ghost_e_full_f64(emoo_handle *h);
 int poisson_field_bc(emoo_handle *h, int id);
 int multigrid_f64(emoo_handle *h, int id1, int id2, int rid, double mult, int *cycles, int *converged);
+int mixed_step_host(emoo_handle *h, double dtp, int fold_what);
+bool mixed_device_accessible(const emoo_handle *h, const void *p);
+// host-resident particles: refresh the device store from the attached arrays
+// when a streamed step left it stale (every entry point that reads the store
+// calls it); EMOO_ERR_STATE from entry points that would change the store
+int host_store_sync(emoo_handle *h);
 void multigrid_free(emoo_handle *h);
 int plane_set_f64(emoo_handle *h, const PlaneSet *ps, int n);
 int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mult, int *iters, int *converged);

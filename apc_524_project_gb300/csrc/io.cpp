@@ -134,6 +134,8 @@ extern "C" {
 
 int emoo_write_fields(emoo_handle *h, const char *dir, int which) {
     if (!h || !dir || which < EMOO_FIELDS_RHO || which > EMOO_FIELDS_ALL) return EMOO_ERR_ARG;
+    EMOO_CUDA(cudaSetDevice(h->dev));
+    EMOO_TRY(host_store_sync(h));  // rho is deposited from the store
     const std::string d = std::string(dir) + "/";
     EMOO_TRY(make_dir(d));
     const bool start = !exists(d + "time.f64");
@@ -170,6 +172,7 @@ int emoo_write_fields(emoo_handle *h, const char *dir, int which) {
 int emoo_write_restart(emoo_handle *h, const char *path) {
     if (!h || !path) return EMOO_ERR_ARG;
     EMOO_CUDA(cudaSetDevice(h->dev));
+    EMOO_TRY(host_store_sync(h));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     RestartHeader hd;
     memset(&hd, 0, sizeof(hd));
@@ -213,6 +216,7 @@ int emoo_write_restart(emoo_handle *h, const char *path) {
 
 int emoo_read_restart(emoo_handle *h, const char *path) {
     if (!h || !path) return EMOO_ERR_ARG;
+    if (h->host_mode) return EMOO_ERR_STATE;  // it replaces the particle store
     EMOO_CUDA(cudaSetDevice(h->dev));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     File F;

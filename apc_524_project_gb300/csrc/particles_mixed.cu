@@ -425,6 +425,65 @@ constexpr int FUSED_BLOCK = 256;
 constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
 constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: conflict-free both ways)
 
+// One particle from FP64 position, velocity and gamma to the mixed state
+// (cell, in-cell offsets, u); false when the position is outside the box or
+// not a number. vmode (relativistic, before the first push): u holds v and
+// g0 the loaded gamma. Shared by the loader and the host-resident step, so
+// both convert bit-identically.
+__device__ __forceinline__ bool f64_to_m(const Geom &g, const double pos[3], const double v[3], double ga, int rel,
+                                         int vmode, int32_t &cell, float o[3], float u[3], float &g0) {
+    int ci[3];
+    bool ok = true;
+    for (int d = 0; d < 3; d++) {
+        double t = (pos[d] - g.x0[d]) * g.id[d];  // cells from x0
+        double fl = floor(t);
+        ci[d] = (int)fl + 1;
+        float of = (float)(t - fl);
+        if (of >= 1.0f) {
+            of = 0.0f;
+            ci[d] += 1;
+        }
+        o[d] = of;
+        if (!(t == t) || ci[d] < 1 || ci[d] > g.n[d]) ok = false;
+    }
+    if (!ok) return false;
+    cell = (int32_t)((int64_t)ci[0] * g.sx + (int64_t)ci[1] * g.sy + ci[2]);
+    if (rel && vmode) {
+        for (int d = 0; d < 3; d++) u[d] = (float)v[d];
+        g0 = (float)ga;
+    } else {
+        const double f = rel ? ga : 1.0;
+        for (int d = 0; d < 3; d++) u[d] = (float)(f * v[d]);
+    }
+    return true;
+}
+
+// The mixed state of one live particle back to FP64: out = x, y, z, vx, vy,
+// vz, gamma (gamma 0 for the non-relativistic pusher, as new_particle()).
+__device__ __forceinline__ void m_to_f64(const Geom &g, int32_t c, const float o[3], const float uf[3], int rel,
+                                         double out[7]) {
+    int ix = (int)(c / g.sx);
+    int64_t r = c - ix * g.sx;
+    int iy = (int)(r / g.sy);
+    int iz = (int)(r - iy * g.sy);
+    out[0] = g.x0[0] + g.d[0] * ((double)(ix - 1) + (double)o[0]);
+    out[1] = g.x0[1] + g.d[1] * ((double)(iy - 1) + (double)o[1]);
+    out[2] = g.x0[2] + g.d[2] * ((double)(iz - 1) + (double)o[2]);
+    double ux = uf[0], uy = uf[1], uz = uf[2];
+    double ga = rel ? sqrt(1.0 + ux * ux + uy * uy + uz * uz) : 1.0;
+    out[3] = ux / ga;
+    out[4] = uy / ga;
+    out[5] = uz / ga;
+    out[6] = rel ? ga : 0.0;
+}
+
+// A dropped particle in the caller's arrays, as the readback writes it.
+__device__ __forceinline__ void host_dead(const MHost &H, int s, int64_t i) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    H.x[s][i] = H.y[s][i] = H.z[s][i] = H.vx[s][i] = H.vy[s][i] = H.vz[s][i] = nan;
+    if (H.gam[s]) H.gam[s][i] = 0.0;
+}
+
 __device__ __forceinline__ void order2(float &a, float &b) {
     const float lo = fminf(a, b), hi = fmaxf(a, b);
     a = lo;
@@ -518,10 +577,15 @@ __device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, i
 // CORR: the corrected policy - the pack holds true-vertex coefficients, the
 // deposit at the current state uses the weights 1 - o and o, and the time
 // loop's current is the charge-conserving one of vb_pieces_m.
-template <bool REL, bool FIRST, bool PUSH, bool CORR = false>
+//
+// HOST (with PUSH, after the first push): the particle state is read from and
+// written back to the caller's FP64 arrays (Hp) instead of the device store,
+// converted as the loader and readback convert (f64_to_m, m_to_f64), so one
+// launch moves every particle over the host link in both directions at once.
+template <bool REL, bool FIRST, bool PUSH, bool CORR = false, bool HOST = false>
 __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
-              MDeposit D, int with_rho, const float *g0, DevCounters *ctr) {
+              MDeposit D, int with_rho, const float *g0, DevCounters *ctr, const MHost *__restrict__ Hp) {
     __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
     __shared__ int s_key[FUSED_WARPS][32];
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -532,11 +596,34 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     int mask = 0;
     int onew = 0;
     if (p < np) {
-        int32_t c = S.cell[p];
+        int32_t c;
+        float ox, oy, oz, ux, uy, uz;
+        int hs = 0;
+        int64_t hi = 0;
+        if (HOST) {
+            hs = species_of_m(st, p);
+            hi = p - st.off[hs];
+            const double pos[3] = {Hp->x[hs][hi], Hp->y[hs][hi], Hp->z[hs][hi]};
+            const double v[3] = {Hp->vx[hs][hi], Hp->vy[hs][hi], Hp->vz[hs][hi]};
+            const double ga = Hp->gam[hs] ? Hp->gam[hs][hi] : 0.0;
+            float o3[3], u3[3], gz;
+            if (f64_to_m(Hp->g, pos, v, ga, Hp->rel, 0, c, o3, u3, gz)) {
+                ox = o3[0], oy = o3[1], oz = o3[2];
+                ux = u3[0], uy = u3[1], uz = u3[2];
+            } else {  // outside the box (the loader's bounds check): dropped as the readback drops it
+                if (pos[0] == pos[0]) atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
+                host_dead(*Hp, hs, hi);
+                c = -1;
+            }
+        } else {
+            c = S.cell[p];
+        }
         if (c >= 0) {
             const int s = species_of_m(st, p);
-            float ox = S.ox[p], oy = S.oy[p], oz = S.oz[p];
-            float ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+            if (!HOST) {
+                ox = S.ox[p], oy = S.oy[p], oz = S.oz[p];
+                ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+            }
             float vx, vy, vz;
             int ix, iy, iz;
             split_cell(g, dv, c, ix, iy, iz);
@@ -567,15 +654,28 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
             }
             if (mask & 64) {
-                S.cell[p] = -1;
+                if (HOST) host_dead(*Hp, hs, hi);
+                else S.cell[p] = -1;
             } else if (ix < 1 || ix > g.n[0] || iy < 1 || iy > g.n[1] || iz < 1 || iz > g.n[2]) {
                 // moved more than a box length in one step: record, drop
                 atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
-                S.cell[p] = -1;
+                if (HOST) host_dead(*Hp, hs, hi);
+                else S.cell[p] = -1;
                 mask |= 64;
             } else {
                 onew = ix * (int)g.sx + iy * (int)g.sy + iz;  // < npts < 2^31 (checked in mixed_alloc)
-                if (PUSH) {
+                if (PUSH && HOST) {
+                    const float o3[3] = {ox, oy, oz}, u3[3] = {ux, uy, uz};
+                    double out[7];
+                    m_to_f64(Hp->g, onew, o3, u3, Hp->rel, out);
+                    Hp->x[hs][hi] = out[0];
+                    Hp->y[hs][hi] = out[1];
+                    Hp->z[hs][hi] = out[2];
+                    Hp->vx[hs][hi] = out[3];
+                    Hp->vy[hs][hi] = out[4];
+                    Hp->vz[hs][hi] = out[5];
+                    if (Hp->gam[hs]) Hp->gam[hs][hi] = out[6];
+                } else if (PUSH) {
                     S.cell[p] = onew;
                     S.ox[p] = ox;
                     S.oy[p] = oy;
@@ -790,44 +890,24 @@ __global__ void k_from_f64(Geom g, MState S, int64_t at, int64_t n, const double
                            const double *z, const double *vx, const double *vy, const double *vz, const double *gam,
                            int rel, int vmode, float *g0, DevCounters *ctr) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double pos[3] = {x[i], y[i], z[i]};
-        int ci[3];
-        float of[3];
-        bool ok = true;
-        for (int d = 0; d < 3; d++) {
-            double t = (pos[d] - g.x0[d]) * g.id[d];  // cells from x0
-            double fl = floor(t);
-            ci[d] = (int)fl + 1;
-            float o = (float)(t - fl);
-            if (o >= 1.0f) {
-                o = 0.0f;
-                ci[d] += 1;
-            }
-            of[d] = o;
-            if (ci[d] < 1 || ci[d] > g.n[d]) ok = false;
-        }
-        int64_t p = at + i;
-        if (!ok) {
+        const double pos[3] = {x[i], y[i], z[i]}, v[3] = {vx[i], vy[i], vz[i]};
+        const double ga = gam ? gam[i] : 0.0;  // new_particle() leaves gamma at 0
+        int32_t cell;
+        float o[3], u[3], gz = 0.0f;
+        const int64_t p = at + i;
+        if (!f64_to_m(g, pos, v, ga, rel, vmode, cell, o, u, gz)) {
             atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
             S.cell[p] = -1;
             continue;
         }
-        S.cell[p] = (int32_t)((int64_t)ci[0] * g.sx + (int64_t)ci[1] * g.sy + ci[2]);
-        S.ox[p] = of[0];
-        S.oy[p] = of[1];
-        S.oz[p] = of[2];
-        double ga = gam ? gam[i] : 0.0;  // new_particle() leaves gamma at 0
-        if (rel && vmode) {
-            S.ux[p] = (float)vx[i];
-            S.uy[p] = (float)vy[i];
-            S.uz[p] = (float)vz[i];
-            g0[p] = (float)ga;
-        } else {
-            double f = rel ? ga : 1.0;
-            S.ux[p] = (float)(f * vx[i]);
-            S.uy[p] = (float)(f * vy[i]);
-            S.uz[p] = (float)(f * vz[i]);
-        }
+        S.cell[p] = cell;
+        S.ox[p] = o[0];
+        S.oy[p] = o[1];
+        S.oz[p] = o[2];
+        S.ux[p] = u[0];
+        S.uy[p] = u[1];
+        S.uz[p] = u[2];
+        if (rel && vmode) g0[p] = gz;
     }
 }
 
@@ -841,26 +921,23 @@ __global__ void k_to_f64(Geom g, MState S, int64_t at, int64_t n, double *x, dou
             if (gam) gam[i] = 0.0;
             continue;
         }
-        int ix = (int)(c / g.sx);
-        int64_t r = c - ix * g.sx;
-        int iy = (int)(r / g.sy);
-        int iz = (int)(r - iy * g.sy);
-        x[i] = g.x0[0] + g.d[0] * ((double)(ix - 1) + (double)S.ox[p]);
-        y[i] = g.x0[1] + g.d[1] * ((double)(iy - 1) + (double)S.oy[p]);
-        z[i] = g.x0[2] + g.d[2] * ((double)(iz - 1) + (double)S.oz[p]);
-        double ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+        const float o[3] = {S.ox[p], S.oy[p], S.oz[p]}, u[3] = {S.ux[p], S.uy[p], S.uz[p]};
+        double out[7];
+        m_to_f64(g, c, o, u, rel, out);
+        x[i] = out[0];
+        y[i] = out[1];
+        z[i] = out[2];
         if (rel && g0) {  // before the first push: loaded v and gamma
-            vx[i] = ux;
-            vy[i] = uy;
-            vz[i] = uz;
+            vx[i] = u[0];
+            vy[i] = u[1];
+            vz[i] = u[2];
             if (gam) gam[i] = (double)g0[p];
             continue;
         }
-        double ga = rel ? sqrt(1.0 + ux * ux + uy * uy + uz * uz) : 1.0;
-        vx[i] = ux / ga;
-        vy[i] = uy / ga;
-        vz[i] = uz / ga;
-        if (gam) gam[i] = rel ? ga : 0.0;
+        vx[i] = out[3];
+        vy[i] = out[4];
+        vz[i] = out[5];
+        if (gam) gam[i] = out[6];
     }
 }
 
@@ -1526,6 +1603,9 @@ void mixed_free(emoo_handle *h) {
 // or managed memory, or any host memory on a device that uses the host's
 // page tables (a coherent CPU-GPU link). Then the conversion kernels move
 // the caller's arrays themselves, at the link's bandwidth, without staging.
+static bool device_accessible(const emoo_handle *h, const void *p);
+bool mixed_device_accessible(const emoo_handle *h, const void *p) { return device_accessible(h, p); }
+
 static bool device_accessible(const emoo_handle *h, const void *p) {
     if (!p) return true;
     cudaPointerAttributes a;
@@ -1794,7 +1874,7 @@ static int mixed_finish_deposit(emoo_handle *h, int mode) {
 // Gather + push + boundaries + deposit (push = false: deposit at the current
 // state), then J and rho at the points from the per-cell sums. The per-cell
 // sums must have been zeroed (mixed_deposit_zero).
-static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
+static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, bool host = false) {
     const int with_rho = mode != DEP_J ? 1 : 0;
     if (h->np == 0) return mixed_finish_deposit(h, mode);
     MGeom mg = mgeom(h, dtp);
@@ -1821,7 +1901,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
         h->launches++;
 #define EMOO_DEPOSIT_M(R, F, C)                                                                                  \
     k_fused_m<R, F, false, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
-                                                                  h->ctr)
+                                                                  h->ctr, nullptr)
         if (corr) {
             if (rel && first) EMOO_DEPOSIT_M(true, true, true);
             else if (rel) EMOO_DEPOSIT_M(true, false, true);
@@ -1848,8 +1928,19 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
     if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
 #define EMOO_FUSED_M(R, F, C)                                                                                   \
     k_fused_m<R, F, true, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
-                                                                 h->ctr)
-    if (corr) {
+                                                                 h->ctr, nullptr)
+#define EMOO_FUSED_HOST(R, C)                                                                                    \
+    k_fused_m<R, false, true, C, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, 0, \
+                                                                           g0, h->ctr, h->mhost)
+    if (host) {  // the host-resident step: after the first push, J only
+        if (corr) {
+            if (rel) EMOO_FUSED_HOST(true, true);
+            else EMOO_FUSED_HOST(false, true);
+        } else {
+            if (rel) EMOO_FUSED_HOST(true, false);
+            else EMOO_FUSED_HOST(false, false);
+        }
+    } else if (corr) {
         if (rel && first) EMOO_FUSED_M(true, true, true);
         else if (rel) EMOO_FUSED_M(true, false, true);
         else EMOO_FUSED_M(false, false, true);
@@ -1859,6 +1950,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true) {
         else EMOO_FUSED_M(false, false, false);
     }
 #undef EMOO_FUSED_M
+#undef EMOO_FUSED_HOST
     EMOO_CUDA(cudaGetLastError());
     if (h->prof_on) {
         EMOO_CUDA(cudaEventRecord(h->prof_ev[1], h->stream));
@@ -1893,6 +1985,18 @@ static int mixed_yee(emoo_handle *h, double dtp, int es) {
         k_yee_b_m<<<grd, blk, 0, h->stream>>>(mg, B, T, Ec, (float)dtp);
     }
     EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// One step of the loop on the host-resident particles (emoo_attach_particles):
+// J only, after the first push, without a sort or a history row this step.
+int mixed_step_host(emoo_handle *h, double dtp, int fold_what) {
+    if (!h->mhost || (h->info.relativity != 0 && h->first_push)) return EMOO_ERR_STATE;
+    EMOO_TRY(mixed_deposit_zero(h, DEP_J));
+    EMOO_TRY(mixed_fused(h, dtp, DEP_J, true, true));
+    EMOO_TRY(mixed_fold(h, fold_what));
+    EMOO_TRY(mixed_yee(h, dtp, h->info.electrostatic == 1));
+    EMOO_TRY(mixed_ghost_fill(h));
     return EMOO_OK;
 }
 

@@ -335,6 +335,27 @@ int emoo_time(emoo_handle *h, double *t, double *dt);
  * last call; cleared by reading. */
 int emoo_check(emoo_handle *h);
 
+/* Host-resident particles (mixed form; no reference counterpart). Makes the
+ * caller's FP64 arrays of one species (n = its current count, in the order
+ * emoo_get_particles returns; gamma required for the relativistic pusher)
+ * the particle state: once every species is attached, emoo_step streams
+ * them through the GPU, reading and writing the arrays in place within one
+ * kernel, so the host link carries both directions at once. The result
+ * equals, bit for bit, emoo_set_particles + emoo_step(1) +
+ * emoo_get_particles per step on the same arrays; a step that sorts, writes
+ * a history row or makes the first push runs that way. The arrays must stay
+ * valid and addressable by the GPU (pinned, or any host memory where the
+ * device reads pageable memory); EMOO_ERR_UNSUPPORTED otherwise, for the FP64
+ * form, or with absorbing particle boundaries (the arrays keep their
+ * length). While attached, entry points that change the particle store
+ * (load, set, sort, push, particle BCs, restart read, emoo_ad_run) return
+ * EMOO_ERR_STATE; those that read it see the arrays' state; and
+ * emoo_get_particles copies the arrays. emoo_detach_particles ends it, with
+ * the device store holding the arrays' state. */
+int emoo_attach_particles(emoo_handle *h, int species, int64_t n, double *x, double *y, double *z, double *vx,
+                          double *vy, double *vz, double *gamma);
+int emoo_detach_particles(emoo_handle *h);
+
 /* Overwrites the state of the n particles of a species (n must equal its
  * current count) from caller-owned host SoA arrays, in device order (the
  * order emoo_get_particles returns). For callers that keep the particle

@@ -1045,6 +1045,10 @@ int emoo_load_generated(emoo_handle *h, const emoo_gen_params *g, int64_t n) {
 }
 
 int emoo_num_particles(emoo_handle *h, int species, int64_t *n) {
+    if (h && h->host_mode && n && species < h->nspec) {  // counts do not change while attached
+        *n = species < 0 ? h->np : h->count[species];
+        return EMOO_OK;
+    }
     HANDLE_CHECK(h);
     if (!n) return EMOO_ERR_ARG;
     if (species >= h->nspec) return EMOO_ERR_ARG;

@@ -238,7 +238,10 @@ def test_gpu_multigrid_matches_oracle(case):
     ro, _ = o.initialize_fields_only()
     assert rg == 0 and ro == 0, (rg, ro)
     assert max(itg) <= CYCLE_CAP.get(case, 40), itg
+    unknowns = all(n[d] >= (1 if fb[2 * d] == "periodic" else 2) for d in range(3))
     for s, r in zip(SLOTS, SOURCES):
+        if not unknowns:
+            break
         res, scale = _residual(g.get_field(s), g.get_field(r), cfg)
         assert res <= 1e-11 * scale, (abi.FIELD_NAMES[s], res, scale)
     for i in list(range(13)) + [abi.PHI1, abi.PHI2, abi.AX1, abi.AY1, abi.AZ1]:

@@ -36,6 +36,11 @@ METRIC = "particle-steps/s/GPU"
 UNIT = "particle-steps/s"
 
 
+# Host link, both directions at once (a kernel reading and writing pinned host
+# memory concurrently), measured on these GB300 nodes: 167 GB/s each way.
+HOST_LINK_DUPLEX_GBS = 334.0
+
+
 def _args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -729,6 +734,11 @@ def main():
                        "ms_per_step": e["t"] / e["steps"] * 1e3,
                        "path": "FP64 host arrays attached (emoo_attach_particles), emoo_step streams them through "
                                "the GPU every step; sort and history steps as upload + step + readback",
+                       # the bound: both link directions at once, 167 GB/s each way measured on these nodes
+                       # by a kernel reading and writing pinned host memory (profiles/fused_mixed_host64.md)
+                       "host_link": {"achieved_gbs": (e["h2d"] + e["d2h"]) * e["steps"] / e["t"] / 1e9,
+                                     "peak_gbs": HOST_LINK_DUPLEX_GBS,
+                                     "frac": (e["h2d"] + e["d2h"]) * e["steps"] / e["t"] / 1e9 / HOST_LINK_DUPLEX_GBS},
                        "roundtrip": {"value": N * e["roundtrip_steps"] * world / e["t_roundtrip"], "unit": UNIT,
                                      "ms_per_step": e["t_roundtrip"] / e["roundtrip_steps"] * 1e3,
                                      "path": "emoo_set_particles + emoo_step(1) + emoo_get_particles per step"}}

@@ -735,7 +735,7 @@ def main():
                        "path": "FP64 host arrays attached (emoo_attach_particles), emoo_step streams them through "
                                "the GPU every step; sort and history steps as upload + step + readback",
                        # the bound: both link directions at once, 167 GB/s each way measured on these nodes
-                       # by a kernel reading and writing pinned host memory (profiles/fused_mixed_host64.md)
+                       # by a kernel reading and writing pinned host memory
                        "host_link": {"achieved_gbs": (e["h2d"] + e["d2h"]) * e["steps"] / e["t"] / 1e9,
                                      "peak_gbs": HOST_LINK_DUPLEX_GBS,
                                      "frac": (e["h2d"] + e["d2h"]) * e["steps"] / e["t"] / 1e9 / HOST_LINK_DUPLEX_GBS},

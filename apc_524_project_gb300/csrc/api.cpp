@@ -1496,9 +1496,9 @@ int emoo_attach_particles(emoo_handle *h, int species, int64_t n, double *x, dou
     if (n != h->count[species]) return EMOO_ERR_ARG;
     double *p[7] = {x, y, z, vx, vy, vz, gamma};
     const bool rel = h->info.relativity != 0;
-    for (int q = 0; q < 7; q++) {
+    for (int q = 0; q < 7 && n > 0; q++) {  // an empty species needs no arrays
         if (!p[q] && (q < 6 || rel)) return EMOO_ERR_ARG;
-        if (p[q] && n > 0 && !mixed_device_accessible(h, p[q])) return EMOO_ERR_UNSUPPORTED;
+        if (p[q] && !mixed_device_accessible(h, p[q])) return EMOO_ERR_UNSUPPORTED;
     }
     emoo_handle::Attached &a = h->attached[species];
     a.n = n;

@@ -716,9 +716,18 @@ def main():
     if "fp64" in res:
         f = res["fp64"]
         v64 = N * args.fp64_steps * world / f["t"]
+        # the FP64 form's push, counted as the survey of the path counts it: about 70
+        # FP64 operations per particle for the relativistic (Vay) pusher, 30 for Boris,
+        # with the square roots and divisions apart (2 and 4 for Vay, 0 and 1 for Boris)
+        rel = cfg.relativity != 0
+        ops, sq, dv = (70, 2, 4) if rel else (30, 0, 1)
         line["fp64"] = {"value": v64, "unit": UNIT, "steps": args.fp64_steps,
                         "ms_per_step": f["t"] / args.fp64_steps * 1e3, "fused_kernel_ms": f["fused_ms"],
-                        "mixed_over_fp64": value / v64}
+                        "mixed_over_fp64": value / v64,
+                        "push_flops": {"fp64_ops_per_particle": ops, "sqrt_per_particle": sq, "div_per_particle": dv,
+                                       "achieved_gflops": N * ops / (f["fused_ms"] / 1e3) / 1e9,
+                                       "bound": "FP64 pipe (the form keeps the reference's operation order, "
+                                                "no FMA, IEEE divisions and square roots)"}}
     if "adjoint" in res:
         line["adjoint"] = res["adjoint"]
     if "laser512" in res:

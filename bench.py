@@ -716,9 +716,9 @@ def main():
     if "fp64" in res:
         f = res["fp64"]
         v64 = N * args.fp64_steps * world / f["t"]
-        # the FP64 form's push, counted as the survey of the path counts it: about 70
-        # FP64 operations per particle for the relativistic (Vay) pusher, 30 for Boris,
-        # with the square roots and divisions apart (2 and 4 for Vay, 0 and 1 for Boris)
+        # the FP64 form's push by operation count: about 70 FP64 operations per particle
+        # for the relativistic (Vay) pusher, 30 for Boris, with the square roots and
+        # divisions counted apart (2 and 4 for Vay, 0 and 1 for Boris)
         rel = cfg.relativity != 0
         ops, sq, dv = (70, 2, 4) if rel else (30, 0, 1)
         line["fp64"] = {"value": v64, "unit": UNIT, "steps": args.fp64_steps,

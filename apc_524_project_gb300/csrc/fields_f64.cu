@@ -626,23 +626,55 @@ int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mul
     dim3 blk(32, 8);
     dim3 grd = phys_grid(g, blk);
     int rb = reduce_blocks(g);
+    // Sweeps are queued in batches of 32 (an even count, so every batch starts
+    // on the same ping-pong parity), captured once as a CUDA graph and
+    // replayed: at small grids each sweep's three kernels would otherwise cost
+    // a launch latency each. Once the stop test has fired they are no-ops.
     const int batch = 32;
-    JacobiState hs;
-    int launched = 0;
-    for (;;) {
-        for (int b = 0; b < batch && launched <= ITER_MAX; b++, launched++) {
-            bool even = (launched % 2) == 0;
-            h->launches++;
+    int batch_launches = 0;
+    auto queue_batch = [&]() -> int {
+        for (int b = 0; b < batch; b++) {
+            const bool even = (b % 2) == 0;
+            batch_launches++;
             k_jacobi<<<grd, blk, 0, h->stream>>>(g, even ? u1 : u2, even ? u2 : u1, R, ax, ay, az, af, mult, st);
+            const int64_t before = h->launches;
             EMOO_TRY(single_field_bc(h, even ? id2 : id1, &st->done));
-            h->launches++;
+            batch_launches += (int)(h->launches - before);
+            h->launches = before;
+            batch_launches++;
             k_jacobi_check<<<rb, 256, 0, h->stream>>>(g, u1, u2, tol, st);
         }
-        EMOO_CUDA(cudaGetLastError());
-        EMOO_CUDA(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream));
-        EMOO_CUDA(cudaStreamSynchronize(h->stream));
+        return EMOO_OK;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    EMOO_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int qrc = queue_batch();
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+    if (qrc != EMOO_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return qrc != EMOO_OK ? qrc : cuda_status(ce);
+    }
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return cuda_status(ie);
+    JacobiState hs;
+    int launched = 0;
+    int rc = EMOO_OK;
+    for (;;) {
+        cudaError_t e = cudaGraphLaunch(exec, h->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_status(e);
+            break;
+        }
+        h->launches += batch_launches;
+        launched += batch;
         if (hs.done || launched > ITER_MAX) break;
     }
+    cudaGraphExecDestroy(exec);
+    if (rc != EMOO_OK) return rc;
     if (iters) *iters = hs.iter - 1;
     if (converged) *converged = hs.converged;
     return EMOO_OK;

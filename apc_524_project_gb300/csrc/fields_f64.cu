@@ -171,7 +171,7 @@ struct JacobiState {
     int done;
     int iter;       // iterations completed
     int converged;
-    int pad;
+    int skip;       // boundary fills no-ops (one sweep after done, with the test in the sweep)
     double maxdiff; // current iteration's max |u2 - u1|
     unsigned int blocks_done;
     unsigned int pad2;
@@ -232,6 +232,71 @@ __global__ void k_jacobi_check(Geom g, const double *u1, const double *u2, doubl
         __threadfence();
         double md = *((volatile double *)&st->maxdiff);
         int it = st->iter;  // iternum of this iteration
+        if (md < tol) {
+            st->done = 1;
+            st->converged = 1;
+        } else if (it >= ITER_MAX) {
+            st->done = 1;
+            st->converged = 0;
+        }
+        st->iter = it + 1;
+        st->maxdiff = 0.0;
+        st->blocks_done = 0u;
+    }
+}
+
+// One Jacobi sweep with the stop test of k_jacobi_check folded in, for grids
+// periodic on every side: there the boundary fill writes only ghost planes,
+// so max |u2 - u1| over the physical points is max |dst - src| of this sweep,
+// the same value in any order. The sweep's arithmetic is k_jacobi's. Once the
+// test has fired, the next sweep sets `skip`, so the fill after the last
+// sweep still runs and the later ones do not.
+__global__ void k_jacobi_fused(Geom g, const double *src, double *dst, const double *R, double ax, double ay,
+                               double az, double af, double mult, double tol, JacobiState *st) {
+    if (st->done) {
+        if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) st->skip = 1;
+        return;
+    }
+    __shared__ double smax[32];
+    __shared__ bool last;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int i = blockIdx.z + 1;
+    double m = 0.0;
+    if (k <= g.n[2] && j <= g.n[1]) {
+        const int64_t o = gidx(g, i, j, k);
+        const double v = ax * (src[o - g.sx] + src[o + g.sx]) + ay * (src[o - g.sy] + src[o + g.sy]) +
+                         az * (src[o - 1] + src[o + 1]) - af * R[o] * mult;
+        dst[o] = v;
+        m = fabs(v - src[o]);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const double q = __shfl_down_sync(0xffffffffu, m, off);
+        m = q > m ? q : m;
+    }
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nw = (int)((blockDim.x * blockDim.y) >> 5);
+    if (lane == 0) smax[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        m = lane < nw ? smax[lane] : 0.0;
+        for (int off = 16; off > 0; off >>= 1) {
+            const double q = __shfl_down_sync(0xffffffffu, m, off);
+            m = q > m ? q : m;
+        }
+        if (lane == 0) {
+            atomic_max_nonneg(&st->maxdiff, m);
+            __threadfence();
+            const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+            const unsigned int prev = atomicAdd(&st->blocks_done, 1u);
+            last = (prev == nb - 1);
+        }
+    }
+    __syncthreads();
+    if (last && tid == 0) {
+        __threadfence();
+        const double md = *((volatile double *)&st->maxdiff);
+        const int it = st->iter;
         if (md < tol) {
             st->done = 1;
             st->converged = 1;
@@ -632,17 +697,29 @@ int jacobi_f64(emoo_handle *h, int id1, int id2, int rid, double tol, double mul
     // a launch latency each. Once the stop test has fired they are no-ops.
     const int batch = 32;
     int batch_launches = 0;
+    // With every side periodic the stop test can run inside the sweep: one
+    // kernel fewer per sweep, which pays where launches dominate. On large
+    // grids the sweep's per-block FP64 max trees (FP64 pipe) cost more than
+    // the separate check's grid-stride reduction, so it stays separate there.
+    bool all_periodic = (int64_t)g.n[0] * g.n[1] * g.n[2] <= (int64_t)1 << 21;
+    for (int sd = 0; sd < 6; sd++) all_periodic = all_periodic && h->bc.fbc[sd] == FBC_PERIODIC;
     auto queue_batch = [&]() -> int {
         for (int b = 0; b < batch; b++) {
             const bool even = (b % 2) == 0;
             batch_launches++;
-            k_jacobi<<<grd, blk, 0, h->stream>>>(g, even ? u1 : u2, even ? u2 : u1, R, ax, ay, az, af, mult, st);
+            if (all_periodic)  // (and small)
+                k_jacobi_fused<<<grd, blk, 0, h->stream>>>(g, even ? u1 : u2, even ? u2 : u1, R, ax, ay, az, af, mult,
+                                                           tol, st);
+            else
+                k_jacobi<<<grd, blk, 0, h->stream>>>(g, even ? u1 : u2, even ? u2 : u1, R, ax, ay, az, af, mult, st);
             const int64_t before = h->launches;
-            EMOO_TRY(single_field_bc(h, even ? id2 : id1, &st->done));
+            EMOO_TRY(single_field_bc(h, even ? id2 : id1, all_periodic ? &st->skip : &st->done));
             batch_launches += (int)(h->launches - before);
             h->launches = before;
-            batch_launches++;
-            k_jacobi_check<<<rb, 256, 0, h->stream>>>(g, u1, u2, tol, st);
+            if (!all_periodic) {
+                batch_launches++;
+                k_jacobi_check<<<rb, 256, 0, h->stream>>>(g, u1, u2, tol, st);
+            }
         }
         return EMOO_OK;
     };

@@ -58,16 +58,18 @@ def reference_load(info, seed=12345):
     return parts
 
 
-@pytest.mark.parametrize("multigrid", [False, True])
-def test_driver_history_matches_oracle(tmp_path, multigrid):
+@pytest.mark.parametrize("flags", [[], ["--multigrid"], ["--corrected"]])
+def test_driver_history_matches_oracle(tmp_path, flags):
     """With --multigrid the driver starts from the multigrid solve (to its
     default 1e-10 residual) and the oracle from its exact solve; the fields
-    then agree to about 1e-9, so the history to 1e-7."""
+    then agree to about 1e-9, so the history to 1e-7. With --corrected both
+    run the corrected-physics policy."""
+    multigrid = "--multigrid" in flags
     build_native.build()
     src = os.path.join(DATA, "driver_small.txt")
     inp = tmp_path / "input.txt"
     shutil.copy(src, inp)
-    cmd = [build_native.DRIVER, str(inp)] + (["--multigrid"] if multigrid else [])
+    cmd = [build_native.DRIVER, str(inp)] + flags
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     rows = np.loadtxt(tmp_path / "history.dat", skiprows=1, ndmin=2)
@@ -80,6 +82,8 @@ def test_driver_history_matches_oracle(tmp_path, multigrid):
     o = OracleBackend(info, dt)
     if multigrid:
         o.set_poisson_solver(1)
+    if "--corrected" in flags:
+        o.set_policy(1)
     nid = 0
     for s, p in enumerate(parts):
         o.add_species(s, p, ids=np.arange(nid, nid + len(p["x"])))

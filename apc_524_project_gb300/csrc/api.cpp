@@ -679,15 +679,8 @@ int execute_bc_slots(emoo_handle *h, int send_id) {
     return EMOO_OK;
 }
 
-int history_row(emoo_handle *h, double out8[8]) {
-    double m4[4], e6[6];
-    if (h->precision == EMOO_FP64) {
-        EMOO_TRY(particle_moments_f64(h, m4));
-        EMOO_TRY(field_energy_f64(h, e6));
-    } else {
-        EMOO_TRY(mixed_moments(h, m4));
-        EMOO_TRY(mixed_field_energy(h, e6));
-    }
+// The history row from the particle moments and field energies.
+void history_from(const emoo_handle *h, const double m4[4], const double e6[6], double out8[8]) {
     double B_en = e6[3] + e6[4] + e6[5];
     double E_en = e6[0] + e6[1] + e6[2];
     out8[0] = h->t;
@@ -698,6 +691,18 @@ int history_row(emoo_handle *h, double out8[8]) {
     out8[5] = B_en;
     out8[6] = E_en;
     out8[7] = B_en + E_en + m4[0];
+}
+
+int history_row(emoo_handle *h, double out8[8]) {
+    double m4[4], e6[6];
+    if (h->precision == EMOO_FP64) {
+        EMOO_TRY(particle_moments_f64(h, m4));
+        EMOO_TRY(field_energy_f64(h, e6));
+    } else {
+        EMOO_TRY(mixed_moments(h, m4));
+        EMOO_TRY(mixed_field_energy(h, e6));
+    }
+    history_from(h, m4, e6, out8);
     return EMOO_OK;
 }
 
@@ -1403,10 +1408,22 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]) {
             // writes a history row or makes the first push (or has particle
             // removal) runs on the device store between an upload and a readback
             const bool sort_now = h->info.nstep_sort > 0 && ti % h->info.nstep_sort == 0;
-            const bool streamed = h->precision == EMOO_MIXED && !sort_now && ti < h->next_hist &&
+            const bool hist_now = ti >= h->next_hist;
+            const bool streamed = h->precision == EMOO_MIXED && !sort_now &&
                                   !(h->info.relativity != 0 && h->first_push) && !has_absorbing(h);
             if (streamed) {
-                EMOO_TRY(mixed_step_host(h, h->dtp, fold_what));
+                // a history row: field energies before the step, particle moments
+                // from the pre-push state the kernel also leaves in the device store
+                double e6[6];
+                if (hist_now) EMOO_TRY(mixed_field_energy(h, e6));
+                EMOO_TRY(mixed_step_host(h, h->dtp, fold_what, hist_now ? 1 : 0));
+                if (hist_now) {
+                    double m4[4], row[8];
+                    EMOO_TRY(mixed_moments(h, m4));
+                    history_from(h, m4, e6, row);
+                    h->hist_rows.insert(h->hist_rows.end(), row, row + 8);
+                    h->next_hist += h->opts.history_every;
+                }
                 h->store_stale = 1;
                 h->t += h->dtp;
                 h->step_index++;

@@ -585,7 +585,8 @@ __device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, i
 template <bool REL, bool FIRST, bool PUSH, bool CORR = false, bool HOST = false>
 __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
-              MDeposit D, int with_rho, const float *g0, DevCounters *ctr, const MHost *__restrict__ Hp) {
+              MDeposit D, int with_rho, const float *g0, DevCounters *ctr, const MHost *__restrict__ Hp,
+              int store_pre) {
     __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
     __shared__ int s_key[FUSED_WARPS][32];
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -614,6 +615,13 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 if (pos[0] == pos[0]) atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
                 host_dead(*Hp, hs, hi);
                 c = -1;
+            }
+            if (store_pre) {  // the state before the push into the device store, as an upload leaves it
+                S.cell[p] = c;
+                if (c >= 0) {
+                    S.ox[p] = ox, S.oy[p] = oy, S.oz[p] = oz;
+                    S.ux[p] = ux, S.uy[p] = uy, S.uz[p] = uz;
+                }
             }
         } else {
             c = S.cell[p];
@@ -1874,7 +1882,8 @@ static int mixed_finish_deposit(emoo_handle *h, int mode) {
 // Gather + push + boundaries + deposit (push = false: deposit at the current
 // state), then J and rho at the points from the per-cell sums. The per-cell
 // sums must have been zeroed (mixed_deposit_zero).
-static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, bool host = false) {
+static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, bool host = false,
+                       int store_pre = 0) {
     const int with_rho = mode != DEP_J ? 1 : 0;
     if (h->np == 0) return mixed_finish_deposit(h, mode);
     MGeom mg = mgeom(h, dtp);
@@ -1901,7 +1910,7 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, b
         h->launches++;
 #define EMOO_DEPOSIT_M(R, F, C)                                                                                  \
     k_fused_m<R, F, false, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
-                                                                  h->ctr, nullptr)
+                                                                  h->ctr, nullptr, 0)
         if (corr) {
             if (rel && first) EMOO_DEPOSIT_M(true, true, true);
             else if (rel) EMOO_DEPOSIT_M(true, false, true);
@@ -1928,10 +1937,10 @@ static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, b
     if (h->prof_on) EMOO_CUDA(cudaEventRecord(h->prof_ev[0], h->stream));
 #define EMOO_FUSED_M(R, F, C)                                                                                   \
     k_fused_m<R, F, true, C><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, with_rho, g0, \
-                                                                 h->ctr, nullptr)
+                                                                 h->ctr, nullptr, 0)
 #define EMOO_FUSED_HOST(R, C)                                                                                    \
     k_fused_m<R, false, true, C, true><<<grd, FUSED_BLOCK, 0, h->stream>>>(mg, dv, st, h->bc, pk, S, h->np, D, 0, \
-                                                                           g0, h->ctr, h->mhost)
+                                                                           g0, h->ctr, h->mhost, store_pre)
     if (host) {  // the host-resident step: after the first push, J only
         if (corr) {
             if (rel) EMOO_FUSED_HOST(true, true);
@@ -1990,10 +1999,13 @@ static int mixed_yee(emoo_handle *h, double dtp, int es) {
 
 // One step of the loop on the host-resident particles (emoo_attach_particles):
 // J only, after the first push, without a sort or a history row this step.
-int mixed_step_host(emoo_handle *h, double dtp, int fold_what) {
+// store_pre: the kernel also writes the state it read (before the push) into
+// the device store, which then holds what an upload would have left (for the
+// history row of this step).
+int mixed_step_host(emoo_handle *h, double dtp, int fold_what, int store_pre) {
     if (!h->mhost || (h->info.relativity != 0 && h->first_push)) return EMOO_ERR_STATE;
     EMOO_TRY(mixed_deposit_zero(h, DEP_J));
-    EMOO_TRY(mixed_fused(h, dtp, DEP_J, true, true));
+    EMOO_TRY(mixed_fused(h, dtp, DEP_J, true, true, store_pre));
     EMOO_TRY(mixed_fold(h, fold_what));
     EMOO_TRY(mixed_yee(h, dtp, h->info.electrostatic == 1));
     EMOO_TRY(mixed_ghost_fill(h));

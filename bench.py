@@ -516,9 +516,10 @@ def _e2e(h, cfg, steps, dist_barrier, dist_max, roundtrip_steps=2):
     """The particle state in FP64 host arrays (pinned), every step crossing
     the host link both ways. Headline: the arrays attached
     (emoo_attach_particles) and `steps` loop steps in one emoo_step call,
-    which streams them through the fused kernel in place; the steps that sort
-    (every 20) or write a history row (every 10) run as an upload, a device
-    step and a readback - 20 steps hold one sort and two history rows. Beside it: the per-step round trip emoo_set_particles +
+    which streams them through the fused kernel in place (a history step also
+    leaves the pre-push state in the device store for the moments); the step
+    that sorts (every 20) runs as an upload, a device step and a readback -
+    20 steps hold one sort and two history rows. Beside it: the per-step round trip emoo_set_particles +
     emoo_step(1) + emoo_get_particles, which gives bit-identical results."""
     import numpy as np
     import torch
@@ -742,7 +743,7 @@ def main():
                        "d2h_bytes_per_step": e["d2h"], "steps": e["steps"], "pinned": e["pinned"],
                        "ms_per_step": e["t"] / e["steps"] * 1e3,
                        "path": "FP64 host arrays attached (emoo_attach_particles), emoo_step streams them through "
-                               "the GPU every step; sort and history steps as upload + step + readback",
+                               "the GPU every step; the sort step as upload + step + readback",
                        # the bound: both link directions at once, 167 GB/s each way measured on these nodes
                        # by a kernel reading and writing pinned host memory
                        "host_link": {"achieved_gbs": (e["h2d"] + e["d2h"]) * e["steps"] / e["t"] / 1e9,

@@ -342,8 +342,9 @@ int emoo_check(emoo_handle *h);
  * them through the GPU, reading and writing the arrays in place within one
  * kernel, so the host link carries both directions at once. The result
  * equals, bit for bit, emoo_set_particles + emoo_step(1) +
- * emoo_get_particles per step on the same arrays; a step that sorts, writes
- * a history row or makes the first push runs that way. The arrays must stay
+ * emoo_get_particles per step on the same arrays; a step that sorts or makes
+ * the first push runs that way (a history row is taken from the state the
+ * streamed kernel also leaves in the device store). The arrays must stay
  * valid and addressable by the GPU (pinned, or any host memory where the
  * device reads pageable memory); EMOO_ERR_UNSUPPORTED otherwise, for the FP64
  * form, or with absorbing particle boundaries (the arrays keep their

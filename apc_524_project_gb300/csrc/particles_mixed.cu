@@ -589,7 +589,9 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
               int store_pre) {
     __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
     __shared__ int s_key[FUSED_WARPS][32];
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // a 32-bit product (mixed_fused refuses 2^32 particles or more): the state
+    // arrays are then addressed with one wide multiply-add each
+    const int64_t p = (int64_t)(blockIdx.x * blockDim.x + threadIdx.x);
     const int lane = threadIdx.x & 31;
     float *col = s_w[threadIdx.x >> 5];
     int *keys = s_key[threadIdx.x >> 5];
@@ -1885,6 +1887,7 @@ static int mixed_finish_deposit(emoo_handle *h, int mode) {
 static int mixed_fused(emoo_handle *h, double dtp, int mode, bool push = true, bool host = false,
                        int store_pre = 0) {
     const int with_rho = mode != DEP_J ? 1 : 0;
+    if (h->np > (int64_t)UINT32_MAX - FUSED_BLOCK) return EMOO_ERR_UNSUPPORTED;  // k_fused_m's 32-bit index
     if (h->np == 0) return mixed_finish_deposit(h, mode);
     MGeom mg = mgeom(h, dtp);
     MSpecies st = mspecies(h, dtp);

@@ -313,7 +313,8 @@ int emoo_evolve_fields(emoo_handle *h, int electrostatic);
 /* The fused time loop: nsteps passes of src/main.cpp:221-287 (sort every
  * nstep_sort, history every history_every, gather+push+BC+deposit in one
  * kernel, fold, Yee update, ghost fill). Crossing counts accumulate into
- * counts6 (may be null). */
+ * counts6 (may be null). With host-resident particles (emoo_attach_particles)
+ * each step reads and writes the attached arrays. */
 int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]);
 
 /* The history row of src/IO/output.cpp:52-123 for the current state:

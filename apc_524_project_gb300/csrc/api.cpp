@@ -1207,9 +1207,9 @@ int emoo_sort(emoo_handle *h) {
 
 int emoo_interpolate(emoo_handle *h) {
     HANDLE_CHECK(h);
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(compact(h));
-    EMOO_TRY(interpolate_f64(h));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_interpolate(h));
+    else EMOO_TRY(interpolate_f64(h));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return read_err(h);
 }

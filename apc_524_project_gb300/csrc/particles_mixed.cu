@@ -2159,6 +2159,44 @@ int mixed_field_energy(emoo_handle *h, double out6[6]) {
 
 namespace emoo {
 
+// Particle_Handler::InterpolateEB (src/particles/particle_handler.cpp:138-173)
+// for the mixed form: each live particle's E and B from the interpolation
+// pack into the FP64 per-particle cache (q * cap + p), as the fused kernel
+// gathers them; a removed particle's entries are NaN.
+__global__ void k_interpolate_m(const float4 *__restrict__ pack, MState S, int64_t np, int64_t cap, double *fc) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t c = S.cell[p];
+        float f[6];
+        if (c >= 0) {
+            gather_pack(pack + (int64_t)c * PACK_F4, S.ox[p], S.oy[p], S.oz[p], f);
+            for (int q = 0; q < 6; q++) fc[(size_t)q * cap + p] = (double)f[q];
+        } else {
+            for (int q = 0; q < 6; q++) fc[(size_t)q * cap + p] = __longlong_as_double(0x7ff8000000000000LL);
+        }
+    }
+}
+
+int mixed_interpolate(emoo_handle *h) {
+    if (!h->fcache) EMOO_CUDA(cudaMalloc(&h->fcache, sizeof(double) * 6 * (size_t)h->cap));
+    MGeom mg = mgeom(h, h->dtp);
+    MGather P;
+    for (int c = 0; c < 3; c++) {
+        P.E[c] = h->mf->E[c];
+        P.B[c] = mb_role(h, c);
+        P.T[c] = mt_role(h, c);
+    }
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
+    h->launches += 2;
+    if (h->policy == EMOO_POLICY_CORRECTED) k_pack_m<true><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+    else k_pack_m<false><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+    if (h->np > 0)
+        k_interpolate_m<<<nblk(h->np), 256, 0, h->stream>>>(h->mf->pack, mstate(h), h->np, h->cap, h->fcache);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 // Particle_Handler::depositRhoJ for the mixed form: zero, then deposit every
 // live non-test particle at its current position (no push).
 int mixed_deposit(emoo_handle *h, int with_rho) {

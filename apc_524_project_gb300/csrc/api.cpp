@@ -1218,8 +1218,8 @@ int emoo_push(emoo_handle *h) {
     HANDLE_CHECK(h);
     STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
-    EMOO_TRY(push_cached_f64(h, h->dtp));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_push_cached(h));
+    else EMOO_TRY(push_cached_f64(h, h->dtp));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return EMOO_OK;
 }
@@ -1228,9 +1228,9 @@ int emoo_apply_particle_bc(emoo_handle *h, int64_t counts6[6]) {
     HANDLE_CHECK(h);
     STORE_WRITE_CHECK(h);
     EMOO_TRY(materialize_rho(h));
-    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
     EMOO_TRY(reset_counters(h));
-    EMOO_TRY(particle_bc_f64(h));
+    if (h->precision != EMOO_FP64) EMOO_TRY(mixed_particle_bc(h));
+    else EMOO_TRY(particle_bc_f64(h));
     int rc = read_counters(h, counts6, false);
     const bool absorbing = has_absorbing(h);
     // clearGhosts: removed particles leave the store (compaction by the sort)

@@ -240,6 +240,8 @@ int multigrid_f64(emoo_handle *h, int id1, int id2, int rid, double mult, int *c
 int mixed_step_host(emoo_handle *h, double dtp, int fold_what, int store_pre);
 int mixed_moments(emoo_handle *h, double out4[4]);
 int mixed_interpolate(emoo_handle *h);
+int mixed_push_cached(emoo_handle *h);
+int mixed_particle_bc(emoo_handle *h);
 int mixed_field_energy(emoo_handle *h, double out6[6]);
 bool mixed_device_accessible(const emoo_handle *h, const void *p);
 // host-resident particles: refresh the device store from the attached arrays

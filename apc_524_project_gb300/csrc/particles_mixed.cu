@@ -2176,6 +2176,93 @@ __global__ void k_interpolate_m(const float4 *__restrict__ pack, MState S, int64
     }
 }
 
+// Particle_Handler::Push with the cached fields (src/particles/particle_handler.cpp:124-128)
+// in the mixed form: the fused kernel's push and cell update (push_m,
+// cell_step) without the boundaries, which emoo_apply_particle_bc applies. A
+// particle may then sit in a ghost cell (0 or n + 1); one that moved further
+// is recorded as a bounds error and dropped, as the fused kernel drops it.
+template <bool REL, bool FIRST>
+__global__ void k_push_cached_m(MGeom g, Div3 dv, MSpecies st, MState S, int64_t np, int64_t cap,
+                                const double *__restrict__ fc, const float *g0, DevCounters *ctr) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const int32_t c = S.cell[p];
+    if (c < 0) return;
+    const int s = species_of_m(st, p);
+    float f[6];
+    for (int q = 0; q < 6; q++) f[q] = (float)fc[(size_t)q * cap + p];
+    float ux = S.ux[p], uy = S.uy[p], uz = S.uz[p], vx, vy, vz;
+    push_m<REL, FIRST>(f, st.qp[s], g0, p, ux, uy, uz, vx, vy, vz);
+    int ix, iy, iz;
+    split_cell(g, dv, c, ix, iy, iz);
+    float ox = S.ox[p], oy = S.oy[p], oz = S.oz[p];
+    cell_step(ox + vx * g.dtid[0], ix, ox);
+    cell_step(oy + vy * g.dtid[1], iy, oy);
+    cell_step(oz + vz * g.dtid[2], iz, oz);
+    if (ix < 0 || ix > g.n[0] + 1 || iy < 0 || iy > g.n[1] + 1 || iz < 0 || iz > g.n[2] + 1) {
+        atomicOr(&ctr->err, (unsigned long long)ERR_BOUNDS);
+        S.cell[p] = -1;
+        return;
+    }
+    S.cell[p] = ix * (int)g.sx + iy * (int)g.sy + iz;
+    S.ox[p] = ox, S.oy[p] = oy, S.oz[p] = oz;
+    S.ux[p] = ux, S.uy[p] = uy, S.uz[p] = uz;
+}
+
+// executeParticleBoundaryConditions (src/particles/particle_handler.cpp:287-295)
+// in the mixed form: the six sides in the fused kernel's order (axis_bc),
+// crossings counted per side, removed particles marked.
+__global__ void k_particle_bc_m(MGeom g, Div3 dv, BCTab bc, MState S, int64_t np, DevCounters *ctr) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int mask = 0;
+    if (p < np && S.cell[p] >= 0) {
+        int ix, iy, iz;
+        split_cell(g, dv, S.cell[p], ix, iy, iz);
+        float o[3] = {S.ox[p], S.oy[p], S.oz[p]}, u[3] = {S.ux[p], S.uy[p], S.uz[p]}, v = 0.0f;
+        mask |= axis_bc(bc, 0, g.n[0], ix, o[0], u[0], v);
+        if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, o[1], u[1], v);
+        if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, o[2], u[2], v);
+        if (mask & 64) {
+            S.cell[p] = -1;
+        } else {
+            S.cell[p] = ix * (int)g.sx + iy * (int)g.sy + iz;
+            S.ox[p] = o[0], S.oy[p] = o[1], S.oz[p] = o[2];
+            S.ux[p] = u[0], S.uy[p] = u[1], S.uz[p] = u[2];
+        }
+    }
+    if (__any_sync(0xffffffffu, mask & 63)) count_cross(ctr, mask & 63);
+}
+
+int mixed_push_cached(emoo_handle *h) {
+    if (h->np == 0) return EMOO_OK;
+    if (!h->fcache) return EMOO_ERR_STATE;
+    const bool rel = h->info.relativity != 0, first = rel && h->first_push && h->g0;
+    MGeom mg = mgeom(h, h->dtp);
+    const unsigned nb = (unsigned)((h->np + 255) / 256);
+    h->launches++;
+    if (rel && first)
+        k_push_cached_m<true, true><<<nb, 256, 0, h->stream>>>(mg, div3(h), mspecies(h, h->dtp), mstate(h), h->np,
+                                                               h->cap, h->fcache, h->g0, h->ctr);
+    else if (rel)
+        k_push_cached_m<true, false><<<nb, 256, 0, h->stream>>>(mg, div3(h), mspecies(h, h->dtp), mstate(h), h->np,
+                                                                h->cap, h->fcache, h->g0, h->ctr);
+    else
+        k_push_cached_m<false, false><<<nb, 256, 0, h->stream>>>(mg, div3(h), mspecies(h, h->dtp), mstate(h), h->np,
+                                                                 h->cap, h->fcache, h->g0, h->ctr);
+    EMOO_CUDA(cudaGetLastError());
+    if (first) h->first_push = 0;
+    return EMOO_OK;
+}
+
+int mixed_particle_bc(emoo_handle *h) {
+    if (h->np == 0) return EMOO_OK;
+    h->launches++;
+    k_particle_bc_m<<<(unsigned)((h->np + 255) / 256), 256, 0, h->stream>>>(mgeom(h, h->dtp), div3(h), h->bc,
+                                                                            mstate(h), h->np, h->ctr);
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 int mixed_interpolate(emoo_handle *h) {
     if (!h->fcache) EMOO_CUDA(cudaMalloc(&h->fcache, sizeof(double) * 6 * (size_t)h->cap));
     MGeom mg = mgeom(h, h->dtp);

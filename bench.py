@@ -156,7 +156,7 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ GPU arms
 
-def _make_handle(cfg, precision, capacity, device, poisson_solver=0):
+def _make_handle(cfg, precision, capacity, device, poisson_solver=0, policy=0):
     from apc_524_project_gb300 import abi, configs
 
     L = abi.lib()
@@ -165,6 +165,7 @@ def _make_handle(cfg, precision, capacity, device, poisson_solver=0):
     L.emoo_default_opts(C.byref(o))
     o.precision = precision
     o.poisson_solver = poisson_solver
+    o.policy = policy
     o.dt = cfg.dt
     o.capacity = capacity
     o.track_ids = 0
@@ -301,28 +302,11 @@ def corrected_arm(cfg, args, device):
     """The same workload and form under the corrected-physics policy (true
     vertex, charge-conserving Villasenor-Buneman current, time-centred Yee at
     the periodic wrap): loop throughput and the fused kernel's mean time."""
-    from apc_524_project_gb300 import abi, configs
+    from apc_524_project_gb300 import abi
 
     L = abi.lib()
     N = cfg.total_particles()
-    info = configs.input_info(cfg)
-    o = abi.Opts()
-    L.emoo_default_opts(C.byref(o))
-    o.precision = abi.MIXED
-    o.dt = cfg.dt
-    o.capacity = N
-    o.track_ids = 0
-    o.device = device
-    o.policy = abi.POLICY_CORRECTED
-    h = C.c_void_p()
-    abi.check(L.emoo_create(C.byref(info), C.byref(o), C.byref(h)), "emoo_create")
-    for si in range(len(cfg.species)):
-        g = configs.gen_params(cfg, si)
-        abi.check(L.emoo_load_generated(h, C.byref(g), cfg.count(cfg.species[si])), "emoo_load_generated")
-    it = (C.c_int * 4)()
-    rc = L.emoo_init_fields(h, it)
-    if rc not in (abi.OK, abi.ERR_NOT_CONVERGED):
-        abi.check(rc, "emoo_init_fields")
+    h = _make_handle(cfg, abi.MIXED, N, device, policy=abi.POLICY_CORRECTED)
     cnt = (C.c_int64 * 6)()
     for _ in range(args.warmup):
         abi.check(L.emoo_step(h, 1, cnt), "emoo_step")

@@ -309,3 +309,48 @@ def test_gpu_multigrid_refusals():
     mixed_sides = _box((8, 8, 8), ("external", "periodic") + ("periodic",) * 4)
     with pytest.raises(abi.EmooError):
         GpuBackend(configs.input_info(mixed_sides), 0.4, poisson_solver=abi.POISSON_MULTIGRID)
+
+
+def test_oracle_exact_solve_matches_a_sparse_direct_solve():
+    """Every side external, anisotropic cells: the oracle's conjugate-gradient
+    solve against scipy's sparse direct solve of the same equations (unknowns
+    2..n per dimension, the PoissonBC planes 1 and n + 1 moved to the right
+    side)."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    cfg = _box((7, 6, 5), ("external",) * 6, dx=(0.7, 1.1, 1.6), bound_phi=(0.3, -0.1, 0.2, 0.05, -0.2, 0.15))
+    o = _oracle(cfg, 1)
+    rho, J = _sources(o.get_field(abi.RHO).shape)
+    _set_sources(o, rho - 2e-4, J)
+    assert o.initialize_fields_only()[0] == 0
+    u = o.get_field(abi.PHI1)
+    n = cfg.n
+    m = [n[d] - 1 for d in range(3)]          # unknowns 2..n
+    N = m[0] * m[1] * m[2]
+    idx = lambda a, b, c: (a * m[1] + b) * m[2] + c  # noqa: E731
+    rows, cols, vals = [], [], []
+    rhs = np.zeros(N)
+    R = o.get_field(abi.RHO)
+    for a in range(m[0]):
+        for b in range(m[1]):
+            for c in range(m[2]):
+                i, j, k = a + 2, b + 2, c + 2
+                r = idx(a, b, c)
+                rhs[r] = -FOUR_PI * R[i, j, k]
+                diag = 0.0
+                for d, (di, dj, dk) in enumerate(((1, 0, 0), (0, 1, 0), (0, 0, 1))):
+                    w = 1.0 / cfg.dx[d] ** 2
+                    diag -= 2 * w
+                    for sgn in (-1, 1):
+                        ii, jj, kk = i + sgn * di, j + sgn * dj, k + sgn * dk
+                        aa, bb, cc = ii - 2, jj - 2, kk - 2
+                        if 0 <= aa < m[0] and 0 <= bb < m[1] and 0 <= cc < m[2]:
+                            rows.append(r), cols.append(idx(aa, bb, cc)), vals.append(w)
+                        else:  # a boundary plane value, as the fill left it
+                            rhs[r] -= w * u[ii, jj, kk]
+                rows.append(r), cols.append(r), vals.append(diag)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(N, N))
+    x = spl.spsolve(A, rhs)
+    got = u[2:n[0] + 1, 2:n[1] + 1, 2:n[2] + 1].reshape(-1)
+    assert np.abs(got - x).max() <= 1e-11 * np.abs(x).max()
+    o.close()

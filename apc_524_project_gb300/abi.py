@@ -160,6 +160,20 @@ class WaveShape(C.Structure):
     ]
 
 
+class RestartDesc(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int),
+        ("n", C.c_int * 3),
+        ("nspec", C.c_int),
+        ("has_ids", C.c_int),
+        ("np", C.c_int64),
+        ("count", C.c_int64 * NSPEC),
+        ("t", C.c_double),
+        ("step_index", C.c_int64),
+        ("nhist_rows", C.c_int64),
+    ]
+
+
 class AdResult(C.Structure):
     _fields_ = [
         ("objective", C.c_double),
@@ -222,6 +236,7 @@ PROTOTYPES = {
     "emoo_write_fields": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "emoo_write_restart": (C.c_int, [_P, C.c_char_p]),
     "emoo_read_restart": (C.c_int, [_P, C.c_char_p]),
+    "emoo_restart_info": (C.c_int, [C.c_char_p, C.POINTER(RestartDesc)]),
     "emoo_ad_run": (C.c_int, [_P, C.POINTER(AdSpec), C.c_int, _D, _D, C.POINTER(AdResult), _D, _D]),
 }
 

@@ -140,14 +140,26 @@ struct Parser {
             return fail("unknown word");
         }
         const char *s = p;
-        if (*p == '+' || *p == '-') p++;
         if (p + 1 < end && p[0] == '0' && (p[1] == 'x' || p[1] == 'X')) {
+            // libconfig's hex token takes no sign; without the L suffix it is a
+            // 32-bit int (strtoul truncated), with it a 64-bit one
             p += 2;
             while (p < end && isxdigit((unsigned char)*p)) p++;
             std::string t(s, p);
-            v.type = Value::Int;
-            v.i = strtoll(t.c_str(), nullptr, 16);
-        } else {
+            const unsigned long long u = strtoull(t.c_str(), nullptr, 16);
+            if (p < end && *p == 'L') {
+                p++;
+                if (p < end && *p == 'L') p++;
+                v.type = Value::Int64;
+                v.i = (long long)u;
+            } else {
+                v.type = Value::Int;
+                v.i = (int32_t)(uint32_t)(unsigned long)strtoul(t.c_str(), nullptr, 16);
+            }
+            return true;
+        }
+        if (*p == '+' || *p == '-') p++;
+        {
             bool flt = false;
             while (p < end && (isdigit((unsigned char)*p) || *p == '.' || *p == 'e' || *p == 'E' ||
                                ((*p == '+' || *p == '-') && (p[-1] == 'e' || p[-1] == 'E')))) {
@@ -159,15 +171,18 @@ struct Parser {
             if (flt) {
                 v.type = Value::Float;
                 v.f = strtod(t.c_str(), nullptr);
-            } else {
+            } else if (p < end && *p == 'L') {
+                // 64-bit integer token (libconfig: atoll)
+                p++;
+                if (p < end && *p == 'L') p++;
+                v.type = Value::Int64;
                 v.i = strtoll(t.c_str(), nullptr, 10);
-                v.type = (v.i > 2147483647LL || v.i < -2147483648LL) ? Value::Int64 : Value::Int;
+            } else {
+                // plain integer token: libconfig reads it with atoi, a 32-bit
+                // int (larger values wrap; they are not promoted to 64 bits)
+                v.type = Value::Int;
+                v.i = (int32_t)(uint32_t)(unsigned long)strtol(t.c_str(), nullptr, 10);
             }
-        }
-        if (p < end && (*p == 'L' || *p == 'l')) {
-            p++;
-            if (p < end && (*p == 'L' || *p == 'l')) p++;
-            v.type = Value::Int64;
         }
         return true;
     }
@@ -193,6 +208,10 @@ struct Parser {
             for (;;) {
                 Value e;
                 if (!(c == '[' ? scalar(e) : value(e))) return false;
+                // an array's elements all take the type of its first element
+                // (libconfig's parser refuses anything else); lists mix types
+                if (c == '[' && !v.elems.empty() && e.type != v.elems[0].type)
+                    return fail("mismatched element type in array");
                 v.elems.push_back(e);
                 skip();
                 if (p < end && *p == ',') {
@@ -608,7 +627,8 @@ int emoo_process_info(emoo_input_info *in) {
     if (in->nwaves >= EMOO_NWAVE) return EMOO_ERR_INPUT;
     for (int i = 0; i < in->nwaves; i++)
         if (in->inPolE[i] < 0 || in->inPolE[i] > 3) return EMOO_ERR_INPUT;
-    in->nparticles_domain = in->nparticles_tot;  // Domain, one rank (src/domain/domain.cpp:102-106)
+    // nparticles_domain is left alone: the reference's Domain sets it
+    // (src/domain/domain.cpp:100), not ProcessInfo
     return err ? EMOO_ERR_INPUT : EMOO_OK;
 }
 

@@ -96,20 +96,22 @@ int get(FILE *f, void *dev, size_t bytes, std::vector<char> &buf, cudaStream_t s
     return EMOO_OK;
 }
 
-// The arrays of the restart file in order: fields, then particles.
+// The arrays of the restart file in order: fields, then particles. The
+// optional particle arrays (FP64 gamma, the mixed form's loaded gamma before
+// the first push, ids) are present as the header's flags say.
 struct Arrays {
     std::vector<std::pair<void *, size_t>> fields;     // pointer, bytes
     std::vector<std::pair<void *, size_t>> particles;  // pointer, bytes per particle
 };
 
-Arrays state_arrays(emoo_handle *h) {
+Arrays state_arrays(emoo_handle *h, bool with_gam, bool with_g0, bool with_ids) {
     Arrays a;
     const size_t npts = (size_t)h->g.npts;
     if (h->precision == EMOO_FP64) {
         for (int id = 0; id <= EMOO_BZ_TM1; id++) a.fields.push_back({h->slot[id], sizeof(double) * npts});
-        void *P[7] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->gam};
-        for (int k = 0; k < 7; k++)
-            if (P[k]) a.particles.push_back({P[k], sizeof(double)});
+        void *P[6] = {h->x, h->y, h->z, h->vx, h->vy, h->vz};
+        for (void *p : P) a.particles.push_back({p, sizeof(double)});
+        if (with_gam) a.particles.push_back({h->gam, sizeof(double)});
     } else {
         float *E[3], *Bs[6];
         long long *J[4];
@@ -122,10 +124,64 @@ Arrays state_arrays(emoo_handle *h) {
         a.particles.push_back({h->cell, sizeof(int32_t)});
         void *P[6] = {h->ox, h->oy, h->oz, h->ux, h->uy, h->uz};
         for (void *p : P) a.particles.push_back({p, sizeof(float)});
-        if (h->first_push && h->g0) a.particles.push_back({h->g0, sizeof(float)});
+        if (with_g0) a.particles.push_back({h->g0, sizeof(float)});
     }
-    if (h->ids) a.particles.push_back({h->ids, sizeof(int64_t)});
+    if (with_ids) a.particles.push_back({h->ids, sizeof(int64_t)});
     return a;
+}
+
+// Size in bytes of a restart file with this header: the header, the history
+// rows, the fields and np particles, in the layout state_arrays gives.
+int64_t restart_bytes(const RestartHeader &hd) {
+    const int64_t npts = (int64_t)(hd.n[0] + 3) * (hd.n[1] + 3) * (hd.n[2] + 3);
+    int64_t field = 0, part = 0;
+    if (hd.precision == EMOO_FP64) {
+        field = 13 * 8 * npts;
+        part = 6 * 8 + (hd.has_gam ? 8 : 0);
+    } else {
+        field = 9 * 4 * npts + 4 * 8 * npts;
+        part = 4 + 6 * 4 + (hd.has_g0 ? 4 : 0);
+    }
+    if (hd.has_ids) part += 8;
+    return (int64_t)sizeof(RestartHeader) + hd.nhist_rows * 8 * (int64_t)sizeof(double) + field + hd.np * part;
+}
+
+bool flag(int32_t v) { return v == 0 || v == 1; }
+
+// Reads the header of `path` and checks that it describes a well-formed file:
+// known version and precision, grid sizes and species count in range, 0/1
+// flags, gamma arrays present as the writer stores them, non-negative
+// per-species counts (zero past nspec) that sum to np, and a file of exactly
+// the size the header implies (so no array can be read short). Nothing but
+// the header is read. EMOO_ERR_INPUT for anything else.
+int read_header(const char *path, RestartHeader &hd) {
+    File F;
+    if (!(F.f = fopen(path, "rb"))) return EMOO_ERR_INPUT;
+    if (fread(&hd, sizeof(hd), 1, F.f) != 1 || memcmp(hd.magic, MAGIC, 8) != 0 || hd.version != 1)
+        return EMOO_ERR_INPUT;
+    if ((hd.precision != EMOO_FP64 && hd.precision != EMOO_MIXED) || hd.nspec < 0 || hd.nspec > EMOO_NSPEC)
+        return EMOO_ERR_INPUT;
+    for (int d = 0; d < 3; d++)
+        if (hd.n[d] < 1 || hd.n[d] > (1 << 16)) return EMOO_ERR_INPUT;
+    if (!flag(hd.bswap) || !flag(hd.rho_stale) || !flag(hd.first_push) || !flag(hd.has_ids) ||
+        !flag(hd.has_gam) || !flag(hd.has_g0) || !flag(hd.dead_pending))
+        return EMOO_ERR_INPUT;
+    if (hd.np < 0 || hd.np >= (int64_t)UINT32_MAX || hd.nhist_rows < 0 || hd.nhist_rows > ((int64_t)1 << 40))
+        return EMOO_ERR_INPUT;
+    int64_t sum = 0;
+    for (int s = 0; s < EMOO_NSPEC; s++) {
+        if (hd.count[s] < 0 || (s >= hd.nspec && hd.count[s] != 0)) return EMOO_ERR_INPUT;
+        sum += hd.count[s];
+    }
+    if (sum != hd.np) return EMOO_ERR_INPUT;
+    // the FP64 store always carries gamma once it holds particles; the mixed
+    // form's loaded gamma exists only before its first push
+    if (hd.precision == EMOO_FP64 && (hd.has_g0 || (hd.np > 0 && !hd.has_gam))) return EMOO_ERR_INPUT;
+    if (hd.precision == EMOO_MIXED && (hd.has_gam || (hd.has_g0 && !hd.first_push))) return EMOO_ERR_INPUT;
+    if (fseeko(F.f, 0, SEEK_END) != 0) return EMOO_ERR_INPUT;
+    const off_t size = ftello(F.f);
+    if (size < 0 || (int64_t)size != restart_bytes(hd)) return EMOO_ERR_INPUT;
+    return EMOO_OK;
 }
 
 }  // namespace
@@ -184,7 +240,7 @@ int emoo_write_restart(emoo_handle *h, const char *path) {
     hd.bswap = h->bswap;
     hd.rho_stale = h->rho_stale;
     hd.first_push = h->first_push;
-    hd.has_ids = h->ids != nullptr;
+    hd.has_ids = h->opts.track_ids != 0;
     hd.has_gam = h->precision == EMOO_FP64 && h->gam != nullptr;
     hd.has_g0 = h->precision != EMOO_FP64 && h->first_push && h->g0;
     hd.dead_pending = h->dead_pending;
@@ -202,7 +258,7 @@ int emoo_write_restart(emoo_handle *h, const char *path) {
     if (hd.nhist_rows &&
         fwrite(h->hist_rows.data(), sizeof(double), h->hist_rows.size(), F.f) != h->hist_rows.size())
         return EMOO_ERR_INPUT;
-    const Arrays A = state_arrays(h);
+    const Arrays A = state_arrays(h, hd.has_gam, hd.has_g0, hd.has_ids);
     std::vector<char> buf;
     for (const auto &f : A.fields) EMOO_TRY(put(F.f, f.first, f.second, buf, h->stream));
     for (const auto &p : A.particles) EMOO_TRY(put(F.f, p.first, p.second * (size_t)h->np, buf, h->stream));
@@ -214,38 +270,67 @@ int emoo_write_restart(emoo_handle *h, const char *path) {
     return EMOO_OK;
 }
 
+int emoo_restart_info(const char *path, emoo_restart_desc *out) {
+    if (!path || !out) return EMOO_ERR_ARG;
+    RestartHeader hd;
+    EMOO_TRY(read_header(path, hd));
+    memset(out, 0, sizeof(*out));
+    out->precision = hd.precision;
+    for (int d = 0; d < 3; d++) out->n[d] = hd.n[d];
+    out->nspec = hd.nspec;
+    out->has_ids = hd.has_ids;
+    out->np = hd.np;
+    for (int s = 0; s < EMOO_NSPEC; s++) out->count[s] = hd.count[s];
+    out->t = hd.t;
+    out->step_index = hd.step_index;
+    out->nhist_rows = hd.nhist_rows;
+    return EMOO_OK;
+}
+
 int emoo_read_restart(emoo_handle *h, const char *path) {
     if (!h || !path) return EMOO_ERR_ARG;
     if (h->host_mode) return EMOO_ERR_STATE;  // it replaces the particle store
+    // every check before the handle changes: a malformed file or one of
+    // another configuration leaves the handle as it was
+    RestartHeader hd;
+    EMOO_TRY(read_header(path, hd));
+    if (hd.precision != h->precision || hd.nspec != h->nspec || hd.n[0] != h->g.n[0] || hd.n[1] != h->g.n[1] ||
+        hd.n[2] != h->g.n[2] || hd.has_ids != (h->opts.track_ids != 0))
+        return EMOO_ERR_STATE;
+    if (hd.has_g0 && h->info.relativity == 0) return EMOO_ERR_STATE;
     EMOO_CUDA(cudaSetDevice(h->dev));
     EMOO_CUDA(cudaStreamSynchronize(h->stream));
     File F;
-    if (!(F.f = fopen(path, "rb"))) return EMOO_ERR_INPUT;
-    RestartHeader hd;
-    if (fread(&hd, sizeof(hd), 1, F.f) != 1 || memcmp(hd.magic, MAGIC, 8) != 0 || hd.version != 1)
-        return EMOO_ERR_INPUT;
-    if (hd.precision != h->precision || hd.nspec != h->nspec || hd.n[0] != h->g.n[0] || hd.n[1] != h->g.n[1] ||
-        hd.n[2] != h->g.n[2] || hd.has_ids != (h->ids != nullptr) || hd.np < 0)
-        return EMOO_ERR_STATE;
+    if (!(F.f = fopen(path, "rb")) || fseeko(F.f, (off_t)sizeof(hd), SEEK_SET) != 0) return EMOO_ERR_INPUT;
     std::vector<double> rows((size_t)hd.nhist_rows * 8);
     if (!rows.empty() && fread(rows.data(), sizeof(double), rows.size(), F.f) != rows.size()) return EMOO_ERR_INPUT;
     EMOO_TRY(reserve_store(h, std::max<int64_t>(hd.np, 1)));
     if (hd.has_g0 && !h->g0) EMOO_CUDA(cudaMalloc(&h->g0, sizeof(float) * (size_t)h->cap));
+    // from here on the store is overwritten; an I/O error part-way leaves it
+    // empty (no particles, fields to be set again), never inconsistent
     h->first_push = hd.first_push;
     int64_t off = 0;
     for (int s = 0; s < EMOO_NSPEC; s++) {
         h->off[s] = off;
-        h->count[s] = s < h->nspec ? hd.count[s] : 0;
+        h->count[s] = hd.count[s];
         off += h->count[s];
     }
     h->off[EMOO_NSPEC] = off;
-    if (off != hd.np) return EMOO_ERR_INPUT;
     h->np = hd.np;
-    const Arrays A = state_arrays(h);
-    if (h->precision == EMOO_FP64 && (bool)hd.has_gam != (h->gam != nullptr)) return EMOO_ERR_STATE;
+    const Arrays A = state_arrays(h, hd.has_gam, hd.has_g0, hd.has_ids);
     std::vector<char> buf;
-    for (const auto &f : A.fields) EMOO_TRY(get(F.f, f.first, f.second, buf, h->stream));
-    for (const auto &p : A.particles) EMOO_TRY(get(F.f, p.first, p.second * (size_t)h->np, buf, h->stream));
+    int rc = EMOO_OK;
+    for (const auto &f : A.fields)
+        if (rc == EMOO_OK) rc = get(F.f, f.first, f.second, buf, h->stream);
+    for (const auto &p : A.particles)
+        if (rc == EMOO_OK) rc = get(F.f, p.first, p.second * (size_t)h->np, buf, h->stream);
+    if (rc != EMOO_OK) {
+        for (int s = 0; s <= EMOO_NSPEC; s++) h->off[s] = 0;
+        for (int s = 0; s < EMOO_NSPEC; s++) h->count[s] = 0;
+        h->np = 0;
+        h->fields_initialised = 0;
+        return rc;
+    }
     h->bswap = hd.bswap;
     h->rho_stale = hd.rho_stale;
     h->t = hd.t;

@@ -528,7 +528,34 @@ int emoo_write_fields(emoo_handle *h, const char *dir, int which);
  * shapes and other emoo_set_* settings are configuration and are set again by
  * the caller. Continuing from a restart reproduces the uninterrupted run. */
 int emoo_write_restart(emoo_handle *h, const char *path);
+
+/* emoo_read_restart checks the whole file before it changes the handle: the
+ * header must be well formed (emoo_restart_info) and must match the handle's
+ * grid, species, precision, id tracking and pusher (EMOO_ERR_STATE
+ * otherwise); the handle is then untouched. Only an I/O error while the
+ * arrays are read leaves it changed, with an empty particle store and its
+ * fields to be set again (EMOO_ERR_INPUT). */
 int emoo_read_restart(emoo_handle *h, const char *path);
+
+/* What a restart file holds, from its header. */
+typedef struct emoo_restart_desc {
+    int precision; /* EMOO_FP64 or EMOO_MIXED */
+    int n[3];      /* physical cells per dimension */
+    int nspec;
+    int has_ids;
+    int64_t np;
+    int64_t count[EMOO_NSPEC];
+    double t;
+    int64_t step_index;
+    int64_t nhist_rows;
+} emoo_restart_desc;
+
+/* Reads and checks the header of a restart file without a handle (host only):
+ * magic and version, precision, grid sizes, 0/1 flags, non-negative species
+ * counts (zero past nspec) summing to np, the optional arrays as the writer
+ * stores them, and a file length equal to what the header implies.
+ * EMOO_ERR_INPUT when any of these fails. */
+int emoo_restart_info(const char *path, emoo_restart_desc *out);
 
 /* Runs spec->nsteps steps from the handle's current state and leaves it at
  * the final state. dtheta (emoo_ad_nparams) and dv (3 np host doubles: vx of

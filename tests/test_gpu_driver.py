@@ -21,7 +21,7 @@ UNIT_VTH = 0.002232
 
 def reference_load(info, seed=12345):
     """Particles as Particle_Handler::Load in emoopic.hpp makes them."""
-    npart = info.nparticles_domain
+    npart = info.nparticles_tot  # the one domain holds them all (Domain, src/domain/domain.cpp:100)
     counts = [0] * info.nspecies
     ispec, cden = 0, info.dens_frac[0]
     for ip in range(npart):

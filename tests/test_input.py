@@ -97,7 +97,7 @@ def test_process_info_scales_super_particles():
     assert info.mass_ratio[1] == pytest.approx(100.0 * ratio)
     assert info.charge_ratio[0] == pytest.approx(-ratio)
     assert info.temp[0] == pytest.approx(2.5 * ratio)
-    assert info.nparticles_domain == 3000000000
+    assert info.nparticles_domain == 0  # set by the Domain (src/domain/domain.cpp:100), not ProcessInfo
 
 
 def test_process_info_rejects_inconsistent_boundaries():

@@ -405,7 +405,11 @@ int emoo_get_stats(emoo_handle *h, emoo_stats *s);
  * that loads the library until the process exits; n above
  * EMOO_NOALLOC_SORT_MAX is rejected with EMOO_ERR_ARG. The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress) with the
- * device current; make that first call before any stream capture. All calls
+ * device current; make that first call before any stream capture. The
+ * address is kept for the life of the process: it belongs to the device's
+ * primary context, so a cudaDeviceReset (or anything else that destroys that
+ * context) makes it stale, and this entry point must not be called on that
+ * device afterwards. All calls
  * share the array and it keeps the last call's contents, so calls whose GPU
  * work overlaps race: order them (one stream, or events). */
 int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, int key_bits, uint32_t *perm, void *stream);

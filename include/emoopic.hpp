@@ -19,6 +19,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -119,47 +120,187 @@ class Relativistic_Boris : public Pusher {
 };
 
 // ---------------------------------------------------------------- boundaries
-// The string registries of the reference (Part_BC_Factory,
+// The reference's string registries (Part_BC_Factory,
 // src/boundaries/particle_bc_factory.hpp:20-110; Field_BC_Factory,
-// src/boundaries/field_bc_factory.hpp:20-87). The GPU applies the boundaries
-// inside its kernels; the objects validate the names the input selects.
+// src/boundaries/field_bc_factory.hpp:20-87): a boundary type is declared
+// under a name with a factory function (declare, or a static
+// RegisterParticleBoundary / RegisterFieldBoundary object), and the names in
+// input.txt are looked up there, "Unable to find particle boundary <name>"
+// (or field) when absent. The built-in names are registered by the
+// factories themselves: "periodic", "reflecting", "absorbing" (particles)
+// and "periodic", "external" (fields).
+//
+// The GPU applies the boundaries inside its kernels, so a boundary object
+// only says which device boundary it is (kind()); a type declared under a new
+// name - a subclass of BC_P_Reflecting, say - runs as the kind it returns.
+// Before the device handle is created, the input's side names are replaced
+// by the kinds their objects return.
+class Domain;
+class Grid;
+
 class BC_Particle {
    public:
-    explicit BC_Particle(const std::string &t) : type(t) {}
+    BC_Particle(Domain *, int dim_Index, short isRight, const std::string &t)
+        : type(t), dim_Index_(dim_Index), isRight_(isRight) {}
+    virtual ~BC_Particle() {}
+    virtual const char *kind() const = 0;  // "periodic", "reflecting" or "absorbing"
     std::string type;
+
+   protected:
+    int dim_Index_;
+    short isRight_;
 };
+class BC_P_Periodic : public BC_Particle {
+   public:
+    using BC_Particle::BC_Particle;
+    const char *kind() const override { return "periodic"; }
+};
+class BC_P_Reflecting : public BC_Particle {
+   public:
+    using BC_Particle::BC_Particle;
+    const char *kind() const override { return "reflecting"; }
+};
+class BC_P_Absorbing : public BC_Particle {  // no reference counterpart: particles leaving are removed
+   public:
+    using BC_Particle::BC_Particle;
+    const char *kind() const override { return "absorbing"; }
+};
+
 class BC_Field {
    public:
-    explicit BC_Field(const std::string &t) : type(t) {}
-    std::string type;
+    BC_Field(int side, Domain *, Grid *, Input_Info_t *) : side_(side) {}
+    virtual ~BC_Field() {}
+    virtual const char *kind() const = 0;  // "periodic" or "external"
+
+   protected:
+    int side_;  // -1 / +1 along dimension dim, as the reference numbers sides (1-based |side|)
 };
+class BC_F_Periodic : public BC_Field {
+   public:
+    using BC_Field::BC_Field;
+    const char *kind() const override { return "periodic"; }
+};
+class BC_F_External : public BC_Field {
+   public:
+    using BC_Field::BC_Field;
+    const char *kind() const override { return "external"; }
+};
+
+template <typename T>
+BC_Particle *makeBCParticle(Domain *domain, int dim_Index, short isRight, std::string type) {
+    return new T(domain, dim_Index, isRight, type);
+}
+template <typename T>
+BC_Field *makeBCField(int side, Domain *domain, Grid *grids, Input_Info_t *info) {
+    return new T(side, domain, grids, info);
+}
+
+namespace emoopic {
+// writes a device kind over an input side name
+inline void set_name(char *dst, const char *kind) {
+    strncpy(dst, kind, EMOO_NCHAR - 1);
+    dst[EMOO_NCHAR - 1] = 0;
+}
+}  // namespace emoopic
 
 class Part_BC_Factory {
    public:
+    typedef BC_Particle *(*Factory)(Domain *domain, int dim_Index, short isRight, std::string type);
     static Part_BC_Factory &getInstance() {
         static Part_BC_Factory f;
         return f;
     }
-    BC_Particle **constructConditions(Domain *, Input_Info_t *info) {
-        BC_Particle **ret = new BC_Particle *[6];
-        for (int i = 0; i < 6; i++) {
-            std::string t(info->parts_bound[i]);
-            if (t != "periodic" && t != "reflecting" && t != "absorbing")
-                throw std::runtime_error("Unable to find particle boundary " + t);
-            ret[i] = new BC_Particle(t);
+    // the first declaration of a name stands, as the reference's map insert
+    void declare(const std::string &type, Factory factory) { registry_.insert(std::make_pair(type, factory)); }
+    Factory lookup(const std::string &type) const {
+        auto i = registry_.find(type);
+        if (i == registry_.end()) throw std::runtime_error("Unable to find particle boundary " + type);
+        return i->second;
+    }
+    std::vector<const std::string *> types() const {
+        std::vector<const std::string *> t;
+        for (const auto &kv : registry_) t.push_back(&kv.first);
+        return t;
+    }
+    // one object per side (x-, x+, y-, y+, z-, z+); the input's names become
+    // the objects' device kinds. The caller deletes the objects and the array.
+    BC_Particle **constructConditions(Domain *domain, Input_Info_t *info) {
+        BC_Particle **ret = new BC_Particle *[6]();
+        try {
+            for (int i = 0; i < 6; i++) {
+                ret[i] = lookup(info->parts_bound[i])(domain, i / 2, (short)(i % 2), info->parts_bound[i]);
+                emoopic::set_name(info->parts_bound[i], ret[i]->kind());
+            }
+        } catch (...) {
+            for (int i = 0; i < 6; i++) delete ret[i];
+            delete[] ret;
+            throw;
         }
         return ret;
     }
+
+   private:
+    Part_BC_Factory() {
+        declare("periodic", makeBCParticle<BC_P_Periodic>);
+        declare("reflecting", makeBCParticle<BC_P_Reflecting>);
+        declare("absorbing", makeBCParticle<BC_P_Absorbing>);
+    }
+    std::map<std::string, Factory> registry_;
 };
 
-class Grid;
+struct RegisterParticleBoundary {
+    RegisterParticleBoundary(const std::string &type, Part_BC_Factory::Factory factory) {
+        Part_BC_Factory::getInstance().declare(type, factory);
+    }
+};
+
 class Field_BC_Factory {
    public:
+    typedef BC_Field *(*Factory)(int side, Domain *domain, Grid *grids, Input_Info_t *info);
     static Field_BC_Factory &getInstance() {
         static Field_BC_Factory f;
         return f;
     }
-    void Construct(Domain *, Grid *grids, Input_Info_t *info);
+    void declare(const std::string &type, Factory factory) { registry_.insert(std::make_pair(type, factory)); }
+    Factory lookup(const std::string &type) const {
+        auto i = registry_.find(type);
+        if (i == registry_.end()) throw std::runtime_error("Unable to find field boundary " + type);
+        return i->second;
+    }
+    std::vector<const std::string *> types() const {
+        std::vector<const std::string *> t;
+        for (const auto &kv : registry_) t.push_back(&kv.first);
+        return t;
+    }
+    // The input's field side names become their objects' device kinds (the
+    // Grid does this before it creates the device handle).
+    void resolve(Domain *domain, Input_Info_t *info) {
+        for (int i = 0; i < 6; i++) {
+            const int side = (i % 2 ? 1 : -1) * (i / 2 + 1);
+            BC_Field *b = lookup(info->fields_bound[i])(side, domain, nullptr, info);
+            emoopic::set_name(info->fields_bound[i], b->kind());
+            delete b;
+        }
+    }
+    // The reference wires one object per side to the grid here; on the GPU
+    // the handle holds the sides, so this checks that every name resolves.
+    void Construct(Domain *domain, Grid *, Input_Info_t *info) {
+        Input_Info_t tmp = *info;
+        resolve(domain, &tmp);
+    }
+
+   private:
+    Field_BC_Factory() {
+        declare("periodic", makeBCField<BC_F_Periodic>);
+        declare("external", makeBCField<BC_F_External>);
+    }
+    std::map<std::string, Factory> registry_;
+};
+
+struct RegisterFieldBoundary {
+    RegisterFieldBoundary(const std::string &type, Field_BC_Factory::Factory factory) {
+        Field_BC_Factory::getInstance().declare(type, factory);
+    }
 };
 
 // ---------------------------------------------------------------- Grid
@@ -168,6 +309,7 @@ class Field_BC_Factory {
 class Grid {
    public:
     Grid(Domain *domain, Input_Info_t *info) : info_(*info) {
+        Field_BC_Factory::getInstance().resolve(domain, &info_);
         emoo_opts o = emoopic::Options::get().o;
         if (o.dt <= 0) o.dt = domain->getmindx() / 100.0;  // src/main.cpp:213-214
         if (o.capacity <= 0) o.capacity = info->nparticles_tot;
@@ -179,8 +321,21 @@ class Grid {
     Grid(const Grid &) = delete;
     Grid &operator=(const Grid &) = delete;
 
-    int evolveFields(double) { return emoo_evolve_fields(h_, 0); }
-    int evolveFieldsES(double) { return emoo_evolve_fields(h_, 1); }
+    // The device handle advances by its own step (emoo_opts.dt); a dt other
+    // than that step is refused rather than silently replaced.
+    int evolveFields(double dt) {
+        check_dt(dt, "evolveFields");
+        return emoo_evolve_fields(h_, 0);
+    }
+    int evolveFieldsES(double dt) {
+        check_dt(dt, "evolveFieldsES");
+        return emoo_evolve_fields(h_, 1);
+    }
+    void check_dt(double dt, const char *what) {
+        double hdt = 0.0;
+        emoo_time(h_, nullptr, &hdt);
+        if (dt != hdt) throw emoopic::Error(EMOO_ERR_ARG, std::string(what) + ": dt differs from the handle's step");
+    }
     void executeBC(int sendID) { emoopic::check(emoo_execute_bc(h_, sendID), "executeBC"); }
     virtual void InitializeFields(Input_Info_t *) {
         int it[4];
@@ -228,13 +383,6 @@ class Poisson_Solver : public Grid {
             emoopic::check(rc, "Poisson_Solver::InitializeFields");
     }
 };
-
-inline void Field_BC_Factory::Construct(Domain *, Grid *, Input_Info_t *info) {
-    for (int i = 0; i < 6; i++) {
-        std::string t(info->fields_bound[i]);
-        if (t != "periodic" && t != "external") throw std::runtime_error("Unable to find field boundary " + t);
-    }
-}
 
 class Particle_Compare {
    public:
@@ -302,7 +450,10 @@ class Particle_Handler {
                            "Load");
         }
     }
-    void Push(double) { emoopic::check(emoo_push(grid_->handle()), "Push"); }
+    void Push(double dt) {
+        grid_->check_dt(dt, "Push");
+        emoopic::check(emoo_push(grid_->handle()), "Push");
+    }
     long nParticles() {
         int64_t n = 0;
         emoo_num_particles(grid_->handle(), -1, &n);

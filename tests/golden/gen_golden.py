@@ -92,6 +92,25 @@ def gen_edges():
     np.savez_compressed(os.path.join(HERE, "edges.npz"), cell_id=cid, particle_fields=pf, **fields)
 
 
+def gen_sort_order():
+    """The reference's particle order after one SortParticles on the
+    sorted_test particles (after the field start): ids, species and cell keys
+    (Grid::getCellID) in storage order."""
+    cfg, dt, steps, exact = cases.make("sorted_test")
+    info = configs.input_info(cfg)
+    parts = loading.sample_all(cfg)
+    b = RefBackend(info, dt)
+    load(b, parts)
+    b.init_fields()
+    b.sort()
+    p = b.particles()
+    keys = np.array([b.cell_id(x, y, z) for x, y, z in zip(p["x"], p["y"], p["z"])], dtype=np.int64)
+    b.close()
+    np.savez_compressed(os.path.join(HERE, "sort_order.npz"), sample_sha256=np.array(particles_hash(parts)),
+                        id=np.asarray(p["id"], dtype=np.int64), type=np.asarray(p["type"], dtype=np.int32),
+                        key=keys)
+
+
 def gen_pusher():
     st, fl = cases.pusher_inputs()
     out = {}
@@ -143,13 +162,16 @@ def main():
     sys.path.insert(0, ROOT)
     import __graft_entry__  # noqa: F401  (build() compiles libemoo.so)
     __graft_entry__.build()
-    which = sys.argv[1:] or (list(cases.CASES) + ["edges", "pusher"] + [f"summary:{k}" for k in cases.SUMMARY_CASES])
+    which = sys.argv[1:] or (list(cases.CASES) + ["edges", "pusher", "sort_order"] +
+                             [f"summary:{k}" for k in cases.SUMMARY_CASES])
     for w in which:
         print("generating", w, flush=True)
         if w == "edges":
             gen_edges()
         elif w == "pusher":
             gen_pusher()
+        elif w == "sort_order":
+            gen_sort_order()
         elif w.startswith("summary:"):
             gen_summary(w.split(":", 1)[1])
         else:

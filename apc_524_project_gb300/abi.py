@@ -21,6 +21,7 @@ ERR_CUDA = -6
 ERR_INPUT = -7
 ERR_STATE = -8
 ERR_UNSUPPORTED = -9
+ERR_TIMEOUT = -10
 
 FP64 = 0
 MIXED = 1
@@ -219,6 +220,7 @@ PROTOTYPES = {
     "emoo_gauss_residual": (C.c_int, [_P, _D]),
     "emoo_time": (C.c_int, [_P, _D, _D]),
     "emoo_check": (C.c_int, [_P]),
+    "emoo_perturb": (C.c_int, [_P, C.c_uint64, C.c_double]),
     "emoo_read_input": (C.c_int, [C.c_char_p, C.POINTER(InputInfo)]),
     "emoo_parse_input": (C.c_int, [C.c_char_p, C.POINTER(InputInfo)]),
     "emoo_input_message": (C.c_char_p, []),

@@ -79,6 +79,7 @@ int read_err(emoo_handle *h) {
     EMOO_CUDA(cudaMemcpyAsync(&h->ctr->err, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
     if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
     if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
+    if (c.err & ERR_WAIT) return EMOO_ERR_TIMEOUT;
     return EMOO_OK;
 }
 
@@ -257,6 +258,7 @@ void pulse_derivs(const emoo_handle *h, int w, double t, double dt, double scale
 }  // namespace
 
 int emoo::light_planes_public(emoo_handle *h, int s, PlaneSet *ps) { return light_planes(h, s, ps, false); }
+int emoo::light_planes_slots(emoo_handle *h, int s, PlaneSet *ps) { return light_planes(h, s, ps, true); }
 
 namespace {
 int do_sort(emoo_handle *h);  // below
@@ -719,6 +721,7 @@ int read_counters(emoo_handle *h, int64_t *counts6, bool accumulate) {
         for (int s = 0; s < 6; s++) counts6[s] = (accumulate ? counts6[s] : 0) + (int64_t)c.cross[s];
     if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
     if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
+    if (c.err & ERR_WAIT) return EMOO_ERR_TIMEOUT;
     return EMOO_OK;
 }
 
@@ -804,6 +807,7 @@ const char *emoo_strerror(int s) {
         case EMOO_ERR_INPUT: return "input error";
         case EMOO_ERR_STATE: return "invalid call for the handle state";
         case EMOO_ERR_UNSUPPORTED: return "unsupported option combination";
+        case EMOO_ERR_TIMEOUT: return "a bounded device-side wait gave up";
         default: return "unknown status";
     }
 }
@@ -855,9 +859,17 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
         int prc = EMOO_OK;
         if (o.policy != EMOO_POLICY_REFERENCE && o.policy != EMOO_POLICY_CORRECTED) prc = EMOO_ERR_ARG;
         if (o.policy == EMOO_POLICY_CORRECTED) {
-            // periodic particles and fields on every side (both forms)
-            for (int s = 0; s < 6; s++)
-                if (h->bc.pbc[s] != PBC_PERIODIC || h->bc.fbc[s] != FBC_PERIODIC) prc = EMOO_ERR_UNSUPPORTED;
+            // every dimension periodic (particle and field sides) or walled
+            // (particle sides reflecting or absorbing, field sides external)
+            for (int d = 0; d < 3; d++) {
+                const int pl = h->bc.pbc[2 * d], pr = h->bc.pbc[2 * d + 1];
+                const int fl = h->bc.fbc[2 * d], fr = h->bc.fbc[2 * d + 1];
+                const bool periodic = pl == PBC_PERIODIC && pr == PBC_PERIODIC && fl == FBC_PERIODIC &&
+                                      fr == FBC_PERIODIC;
+                const bool walled = pl != PBC_PERIODIC && pr != PBC_PERIODIC && fl == FBC_EXTERNAL &&
+                                    fr == FBC_EXTERNAL;
+                if (!periodic && !walled) prc = EMOO_ERR_UNSUPPORTED;
+            }
             h->policy = o.policy;
             h->g.vshift = 1;
         }
@@ -1494,6 +1506,16 @@ int emoo_time(emoo_handle *h, double *t, double *dt) {
     if (!h) return EMOO_ERR_ARG;
     if (t) *t = h->t;
     if (dt) *dt = h->dt;
+    return EMOO_OK;
+}
+
+int emoo_perturb(emoo_handle *h, uint64_t seed, double rel) {
+    HANDLE_CHECK(h);
+    STORE_WRITE_CHECK(h);
+    if (h->precision != EMOO_FP64) return EMOO_ERR_UNSUPPORTED;
+    if (!(rel >= 0.0 && rel < 1.0)) return EMOO_ERR_ARG;
+    EMOO_TRY(perturb_f64(h, seed, rel));
+    EMOO_CUDA(cudaStreamSynchronize(h->stream));
     return EMOO_OK;
 }
 

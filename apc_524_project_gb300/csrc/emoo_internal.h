@@ -23,7 +23,7 @@ enum { PBC_PERIODIC = 0, PBC_REFLECTING = 1, PBC_ABSORBING = 2 };
 enum { FBC_PERIODIC = 0, FBC_EXTERNAL = 1 };
 
 // Device error word bits.
-enum { ERR_BOUNDS = 1, ERR_FIXED_OVERFLOW = 2, ERR_NAN = 4 };
+enum { ERR_BOUNDS = 1, ERR_FIXED_OVERFLOW = 2, ERR_NAN = 4, ERR_WAIT = 8 };
 
 // Grid geometry in the reference layout: (n+3)^3 points per field, C order,
 // physical points 1..n, ghost planes 0 and n+1, extra plane n+2
@@ -263,6 +263,7 @@ void species_tab(emoo_handle *h, double dtp, SpeciesTab &st);
 int interpolate_f64(emoo_handle *h);
 int push_cached_f64(emoo_handle *h, double dtp);
 int particle_bc_f64(emoo_handle *h);
+int perturb_f64(emoo_handle *h, uint64_t seed, double rel);
 int deposit_f64(emoo_handle *h, int with_rho);
 int fused_step_f64(emoo_handle *h, double dtp, int with_rho);
 int deposit_rho_f64(emoo_handle *h);  // rho alone at the current positions, plus the background
@@ -333,6 +334,7 @@ int prof_accumulate(emoo_handle *h);
 int ad_execute_bc(emoo_handle *h, int send_id);
 int ad_bc_ops(emoo_handle *h, std::vector<AdBcOp> &ops);
 int light_planes_public(emoo_handle *h, int s, PlaneSet *ps);
+int light_planes_slots(emoo_handle *h, int s, PlaneSet *ps);  // the FP64 slots' planes
 int sort_with_permutation(emoo_handle *h, uint32_t *perm_out);
 int reserve_store(emoo_handle *h, int64_t cap);  // particle capacity, contents kept
 

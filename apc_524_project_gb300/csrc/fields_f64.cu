@@ -544,13 +544,61 @@ __global__ void k_periodic_full(Geom g, Slots9 fl, int d, int fold) {
     }
 }
 
+// Mirror fold at a reflecting wall (corrected policy, no reference
+// counterpart): a particle reflected at the wall moved along the mirror image
+// of the part of its straight path beyond it, so the current that part
+// deposited in the ghost layer goes to the mirrored points inside - the
+// component normal to the wall negated, the transverse ones as they are - and
+// the ghost values are cleared. Left wall (vertex plane 1): normal edge 0 ->
+// 1, transverse plane 0 -> 2; right wall (plane n+1): normal edge n+1 -> n,
+// transverse plane n+2 -> n. Whole transverse range; blockIdx.z = component.
+__global__ void k_mirror_fold(Geom g, Slots9 fl, int d, int right) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= g.tot[o2] || r >= g.tot[o1]) return;
+    const int a = blockIdx.z;
+    double *F = fl.p[a];
+    const int n = g.n[d];
+    const bool normal = a == d;
+    const int src = normal ? (right ? n + 1 : 0) : (right ? n + 2 : 0);
+    const int dst = normal ? (right ? n : 1) : (right ? n : 2);
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    c[d] = src;
+    const int64_t ks = gidx(g, c[0], c[1], c[2]);
+    c[d] = dst;
+    const int64_t kd = gidx(g, c[0], c[1], c[2]);
+    if (normal) F[kd] -= F[ks];
+    else F[kd] += F[ks];
+    F[ks] = 0.0;
+}
+
+// The corrected policy's folds (fold = 1, the arrays J and / or rho) or ghost
+// copies (fold = 0), dimension by dimension so edge and corner lines follow:
+// periodic dimensions as images over the whole range; walled dimensions
+// (corrected policy with reflecting or absorbing particle sides) fold J by
+// mirror at reflecting sides only (at absorbing ones the current of the path
+// beyond the wall stays in the ghost layer) and copy nothing (their field
+// sides are LightBC planes).
 static int periodic_full(emoo_handle *h, const int *ids, int nids, int fold) {
     const Geom &g = h->g;
     Slots9 fl;
     for (int k = 0; k < nids; k++) fl.p[k] = h->slot[ids[k]];
     dim3 blk(32, 8);
-    for (int d = 0; d < 3; d++) {  // dimension by dimension: edge and corner lines follow
+    for (int d = 0; d < 3; d++) {
         const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) {
+            const bool j3 = fold && nids >= 3 && ids[0] == EMOO_JX && ids[1] == EMOO_JY && ids[2] == EMOO_JZ;
+            for (int r = 0; r < 2 && j3; r++) {
+                if (h->bc.pbc[2 * d + r] != PBC_REFLECTING) continue;
+                dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, 3);
+                h->launches++;
+                k_mirror_fold<<<grd, blk, 0, h->stream>>>(g, fl, d, r);
+            }
+            continue;
+        }
         dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, nids);
         h->launches++;
         k_periodic_full<<<grd, blk, 0, h->stream>>>(g, fl, d, fold);
@@ -568,15 +616,30 @@ int fold_full_f64(emoo_handle *h, int what) {
     return periodic_full(h, ids, n, 1);
 }
 
+// LightBC planes of every external side (E and B roles through the slots).
+static int light_all_f64(emoo_handle *h) {
+    for (int s = 0; s < 6; s++) {
+        if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
+        PlaneSet ps[6];
+        const int n = light_planes_slots(h, s, ps);
+        EMOO_TRY(plane_set_f64(h, ps, n));
+    }
+    return EMOO_OK;
+}
+
+// E's boundary values between the Yee halves (corrected policy): periodic
+// images and LightBC planes, so the B half reads E at the new time everywhere.
 int ghost_e_full_f64(emoo_handle *h) {
     static const int ids[3] = {EMOO_EX, EMOO_EY, EMOO_EZ};
-    return periodic_full(h, ids, 3, 0);
+    EMOO_TRY(periodic_full(h, ids, 3, 0));
+    return light_all_f64(h);
 }
 
 int ghost_full_f64(emoo_handle *h) {
     static const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1,
                                EMOO_BZ_TM1};
-    return periodic_full(h, ids, 9, 0);
+    EMOO_TRY(periodic_full(h, ids, 9, 0));
+    return light_all_f64(h);
 }
 
 static int plane_launch(emoo_handle *h, const PlaneSet *ps, int n, const int *skip) {

@@ -424,6 +424,24 @@ __device__ void vb_deposit(const Geom &g, const DepositPtrs &D, const double p0[
 // The corrected policy's time-loop kernel: gather at the current position
 // (the cell's own vertex), push, the charge-conserving current of the move,
 // then the (periodic) boundaries.
+// A move that ends beyond an absorbing wall removes the particle; its whole
+// charge must cross the wall's vertex plane for continuity to hold there, so
+// the path is continued along the wall's normal to the next vertex plane
+// beyond the wall (x0 - d or x0 + L + d), a piece inside the ghost cell
+// (corrected policy, as the oracle's absorbed_exit).
+__device__ void absorbed_exit(const Geom &g, const BCTab &bc, const DepositPtrs &D, const double p1[3],
+                              double coef) {
+    double a[3] = {p1[0], p1[1], p1[2]};
+    for (int d = 0; d < 3; d++) {
+        double b[3] = {a[0], a[1], a[2]};
+        if (bc.pbc[2 * d] == PBC_ABSORBING && a[d] < bc.xmin[d]) b[d] = bc.xmin[d] - g.d[d];
+        else if (bc.pbc[2 * d + 1] == PBC_ABSORBING && a[d] > bc.xmax[d]) b[d] = bc.xmax[d] + g.d[d];
+        else continue;
+        vb_deposit(g, D, a, b, coef);
+        a[d] = b[d];
+    }
+}
+
 template <bool REL>
 __global__ void __launch_bounds__(256) k_fused_vb(Geom g, SpeciesTab st, BCTab bc, GatherPtrs P, PState S, int64_t np,
                                                   DepositPtrs D, double dt, DevCounters *ctr) {
@@ -450,7 +468,10 @@ __global__ void __launch_bounds__(256) k_fused_vb(Geom g, SpeciesTab st, BCTab b
                     boris_push(st.qp[s], f, dt, x, y, z, vx, vy, vz);
                 }
                 double pos[3] = {x, y, z}, v[3] = {vx, vy, vz};
-                if (st.deposit[s] && dt > 0.0) vb_deposit(g, D, p0, pos, st.uq[s] / g.vol / dt);
+                if (st.deposit[s] && dt > 0.0) {
+                    vb_deposit(g, D, p0, pos, st.uq[s] / g.vol / dt);
+                    absorbed_exit(g, bc, D, pos, st.uq[s] / g.vol / dt);
+                }
                 mask = apply_bc(bc, pos, v);
                 if (mask & 64) pos[0] = __longlong_as_double(0x7ff8000000000000LL);
                 S.x[p] = pos[0]; S.y[p] = pos[1]; S.z[p] = pos[2];
@@ -584,6 +605,36 @@ DepositPtrs deposit_ptrs(emoo_handle *h) {
 PState pstate(emoo_handle *h) { return PState{h->x, h->y, h->z, h->vx, h->vy, h->vz, h->gam}; }
 
 int blocks_for(int64_t n, int t = 256) { return (int)std::max<int64_t>(1, (n + t - 1) / t); }
+
+// ---- sensitivity probe (no reference counterpart) -------------------------
+
+// Uniform in [-1, 1) from (seed, particle or point, component): splitmix64.
+__device__ __forceinline__ double unit_noise(uint64_t seed, uint64_t i, uint64_t comp) {
+    uint64_t z = seed + (i * 8u + comp + 1u) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 4503599627370496.0) - 1.0;  // 2^-52 steps over [-1, 1)
+}
+
+// Every live particle: v *= 1 + rel u, x += rel d u per component (u the
+// noise above), a moved position kept only while it stays inside the box.
+__global__ void k_perturb_particles(Geom g, PState S, int64_t np, uint64_t seed, double rel) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= np || S.x[p] != S.x[p]) return;
+    double *pos[3] = {S.x, S.y, S.z}, *vel[3] = {S.vx, S.vy, S.vz};
+    for (int c = 0; c < 3; c++) {
+        vel[c][p] *= 1.0 + rel * unit_noise(seed, (uint64_t)p, c);
+        const double x = pos[c][p] + rel * g.d[c] * unit_noise(seed, (uint64_t)p, 3 + c);
+        if (x >= g.x0[c] && x < g.x0[c] + g.n[c] * g.d[c]) pos[c][p] = x;
+    }
+}
+
+// f *= 1 + rel u at every point of one field (comp tells fields apart).
+__global__ void k_perturb_field(double *f, int64_t n, uint64_t seed, uint64_t comp, double rel) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) f[i] *= 1.0 + rel * unit_noise(seed, (uint64_t)i, comp);
+}
 
 }  // namespace
 
@@ -734,6 +785,21 @@ int compact_keys_f64(emoo_handle *h) {
     h->launches++;
     k_compact_keys<<<blocks_for(h->np), 256, 0, h->stream>>>(st, h->x, h->np, h->key[0]);
     EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+int perturb_f64(emoo_handle *h, uint64_t seed, double rel) {
+    if (h->np) {
+        h->launches++;
+        k_perturb_particles<<<blocks_for(h->np), 256, 0, h->stream>>>(h->g, pstate(h), h->np, seed, rel);
+        EMOO_CUDA(cudaGetLastError());
+    }
+    const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
+    for (int k = 0; k < 9; k++) {
+        h->launches++;
+        k_perturb_field<<<blocks_for(h->g.npts), 256, 0, h->stream>>>(h->slot[ids[k]], h->g.npts, seed, 8 + k, rel);
+        EMOO_CUDA(cudaGetLastError());
+    }
     return EMOO_OK;
 }
 

@@ -72,6 +72,7 @@ __device__ __forceinline__ int species_of_m(const MSpecies &st, int64_t p) {
 
 struct MGeom {
     int n[3];
+    int wrap[3];  // 1: the dimension is periodic (pieces of a path wrap); 0: walled
     int64_t sx, sy;
     int64_t npts;
     float dtid[3];  // dt / d
@@ -490,6 +491,49 @@ __device__ __forceinline__ void order2(float &a, float &b) {
     b = hi;
 }
 
+// A warp's list of J totals for cells other than the run reduction's (the
+// corrected policy's pieces in a particle's old or intermediate cells), in
+// shared memory, committed twelve lanes per entry, two entries per pass.
+// Each total is rounded to the fixed-point quantum once and added with an
+// integer atomic, so the order of the list does not change J.
+constexpr int DEP_LIST = 32;
+
+struct DepList {
+    float (*val)[DEP_LIST + 1];  // [DEP_JSLOTS][DEP_LIST + 1]
+    int *key;                    // [DEP_LIST]
+    int n;                       // entries held (the same in every lane)
+};
+
+template <bool GUARD>
+__device__ __forceinline__ void list_flush(DepList &L, const MDeposit &D, int lane) {
+    __syncwarp();
+    const int q = lane & 15, half = lane >> 4;
+    if (q < DEP_JSLOTS) {
+        const int pos = dep_pos(q);
+        for (int e = half; e < L.n; e += 2)
+            atomicAdd(D.wj + (size_t)L.key[e] * DEP_JSLOTS + pos, (unsigned long long)f2ll_rn<GUARD>(L.val[q][e]));
+    }
+    __syncwarp();
+    L.n = 0;
+}
+
+// Appends (cell, v) of every lane with `has` set; called by all lanes.
+template <bool GUARD>
+__device__ __forceinline__ void list_append(DepList &L, const MDeposit &D, int lane, bool has, int cell,
+                                            const float v[DEP_JSLOTS]) {
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    if (m == 0u) return;
+    const int cnt = __popc(m);
+    if (L.n + cnt > DEP_LIST) list_flush<GUARD>(L, D, lane);
+    if (has) {
+        const int e = L.n + __popc(m & lanemask_lt());
+        L.key[e] = cell;
+#pragma unroll
+        for (int q = 0; q < DEP_JSLOTS; q++) L.val[q][e] = v[q];
+    }
+    L.n += cnt;
+}
+
 // Villasenor and Buneman's charge-conserving current of one particle's
 // straight move (the corrected policy), the FP64 vb_deposit of
 // particles_f64.cu in FP32 and in the old cell's units: s = the old in-cell
@@ -500,11 +544,47 @@ __device__ __forceinline__ void order2(float &a, float &b) {
 // cell's slots 4a .. 4a+3
 //   qd (D_a d_a / dt) ((1-m_j)(1-m_k) + D_j D_k/12, m_j (1-m_k) - .., m_j m_k + .., (1-m_j) m_k - ..).
 // Pieces in the particle's new cell `onew` are summed into w (the run
-// reduction commits them); the others are added to their cells' records here.
+// reduction commits them); the others are appended to the warp's list. All
+// lanes of the warp call it (dep false: no pieces).
 // Crossing times come from comparisons and one fast divide; the cell of a
 // piece from comparisons (no conversion instruction).
-__device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, int ix, int iy, int iz, const float s[3],
-                                            const float e[3], float qd, int onew, float w[DEP_JSLOTS]) {
+// One straight piece of a path inside one cell, endpoints ua -> ub in the
+// old cell's units (ix, iy, iz that cell): its cell's linear index (wrapped
+// into [1, n] along periodic axes; a ghost cell along walled ones) and its
+// twelve terms.
+__device__ __forceinline__ void vb_piece(const MGeom &g, const int io[3], const float ua[3], const float ub[3],
+                                         float qd, int &ct, float W[DEP_JSLOTS]) {
+    float m[3], Dd[3];
+    ct = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float mid = 0.5f * (ua[a] + ub[a]);
+        const bool below = mid < 0.0f, above = mid >= 1.0f;
+        const int c = below ? -1 : (above ? 1 : 0);
+        m[a] = mid - (below ? -1.0f : (above ? 1.0f : 0.0f));  // no int-to-float conversion (FP64 pipe)
+        Dd[a] = ub[a] - ua[a];
+        int ii = io[a] + c;
+        // periodic: wrapped into [1, n]; walled: the ghost cell 0 or n + 1
+        // (mirrored back by the fold at a reflecting wall)
+        if (g.wrap[a]) ii = ii < 1 ? ii + g.n[a] : (ii > g.n[a] ? ii - g.n[a] : ii);
+        ct += ii * (a == 0 ? (int)g.sx : a == 1 ? (int)g.sy : 1);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+        const float wa = qd * Dd[a] * g.ddt[a];
+        const float cr = Dd[jb] * Dd[kb] * (1.0f / 12.0f);
+        W[4 * a + 0] = wa * ((1.0f - m[jb]) * (1.0f - m[kb]) + cr);
+        W[4 * a + 1] = wa * (m[jb] * (1.0f - m[kb]) - cr);
+        W[4 * a + 2] = wa * (m[jb] * m[kb] + cr);
+        W[4 * a + 3] = wa * ((1.0f - m[jb]) * m[kb] - cr);
+    }
+}
+
+template <bool GUARD>
+__device__ __forceinline__ void vb_pieces_list(const MGeom &g, const BCTab &bc, DepList &L, const MDeposit &D,
+                                               int lane, bool dep, int ix, int iy, int iz, const float s[3],
+                                               const float e[3], float qd, int onew, float w[DEP_JSLOTS]) {
     float t[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -519,44 +599,45 @@ __device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, i
     for (int k = 0; k < 4; k++) {
         const float ta = k == 0 ? 0.0f : fminf(t[k - 1], 1.0f);
         const float tb = k == 3 ? 1.0f : fminf(t[k], 1.0f);
-        if (!(tb > ta)) continue;
-        float m[3], Dd[3];
-        int ct = 0;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const float de = e[a] - s[a];
-            const float ua = fmaf(ta, de, s[a]), ub = fmaf(tb, de, s[a]);
-            const float mid = 0.5f * (ua + ub);
-            const bool below = mid < 0.0f, above = mid >= 1.0f;
-            const int c = below ? -1 : (above ? 1 : 0);
-            m[a] = mid - (below ? -1.0f : (above ? 1.0f : 0.0f));  // no int-to-float conversion (FP64 pipe)
-            Dd[a] = ub - ua;
-            int ii = io[a] + c;
-            ii = ii < 1 ? ii + g.n[a] : (ii > g.n[a] ? ii - g.n[a] : ii);
-            ct += ii * (a == 0 ? (int)g.sx : a == 1 ? (int)g.sy : 1);
-        }
+        const bool valid = dep && tb > ta;
         float W[DEP_JSLOTS];
+        int ct = 0;
+        if (valid) {
+            float ua[3], ub[3];
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const int jb = (a + 1) % 3, kb = (a + 2) % 3;
-            const float wa = qd * Dd[a] * g.ddt[a];
-            const float cr = Dd[jb] * Dd[kb] * (1.0f / 12.0f);
-            W[4 * a + 0] = wa * ((1.0f - m[jb]) * (1.0f - m[kb]) + cr);
-            W[4 * a + 1] = wa * (m[jb] * (1.0f - m[kb]) - cr);
-            W[4 * a + 2] = wa * (m[jb] * m[kb] + cr);
-            W[4 * a + 3] = wa * ((1.0f - m[jb]) * m[kb] - cr);
-        }
-        if (ct == onew) {
+            for (int a = 0; a < 3; a++) {
+                const float de = e[a] - s[a];
+                ua[a] = fmaf(ta, de, s[a]);
+                ub[a] = fmaf(tb, de, s[a]);
+            }
+            vb_piece(g, io, ua, ub, qd, ct, W);
+            if (ct == onew) {
 #pragma unroll
-            for (int q = 0; q < DEP_JSLOTS; q++) w[q] += W[q];
-        } else {
-            unsigned long long *rec = D.wj + (size_t)ct * DEP_JSLOTS;
-#pragma unroll
-            for (int q = 0; q < DEP_JSLOTS; q++) {
-                const long long fx = f2ll_rn(W[q]);
-                if (fx != 0) atomicAdd(rec + dep_pos(q), (unsigned long long)fx);
+                for (int q = 0; q < DEP_JSLOTS; q++) w[q] += W[q];
             }
         }
+        list_append<GUARD>(L, D, lane, valid && ct != onew, ct, W);
+    }
+    // a move that ends beyond an absorbing wall removes the particle: its path
+    // continues along the wall's normal to the next vertex plane beyond the
+    // wall (offset -1 or 2 in the old cell's units), so that its whole charge
+    // crosses the wall's plane (the FP64 form's absorbed_exit)
+    float a0[3] = {e[0], e[1], e[2]};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int io_a = a == 0 ? ix : a == 1 ? iy : iz;
+        const bool left = bc.pbc[2 * a] == PBC_ABSORBING && io_a == 1 && a0[a] < 0.0f;
+        const bool right = bc.pbc[2 * a + 1] == PBC_ABSORBING && io_a == g.n[a] && a0[a] >= 1.0f;
+        const bool has = dep && (left || right);
+        float W[DEP_JSLOTS];
+        int ct = 0;
+        if (has) {
+            float b0[3] = {a0[0], a0[1], a0[2]};
+            b0[a] = left ? -1.0f : 2.0f;
+            vb_piece(g, io, a0, b0, qd, ct, W);
+            a0[a] = b0[a];
+        }
+        list_append<GUARD>(L, D, lane, has, ct, W);
     }
 }
 
@@ -576,7 +657,7 @@ __device__ __forceinline__ void vb_pieces_m(const MGeom &g, const MDeposit &D, i
 //
 // CORR: the corrected policy - the pack holds true-vertex coefficients, the
 // deposit at the current state uses the weights 1 - o and o, and the time
-// loop's current is the charge-conserving one of vb_pieces_m.
+// loop's current is the charge-conserving one of vb_pieces_list.
 //
 // HOST (with PUSH, after the first push): the particle state is read from and
 // written back to the caller's FP64 arrays (Hp) instead of the device store,
@@ -589,6 +670,9 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
               int store_pre) {
     __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
     __shared__ int s_key[FUSED_WARPS][32];
+    constexpr bool VBL = CORR && PUSH;  // the corrected policy's pieces go through a list
+    __shared__ float s_pl[VBL ? FUSED_WARPS : 1][DEP_JSLOTS][DEP_LIST + 1];
+    __shared__ int s_plk[VBL ? FUSED_WARPS : 1][DEP_LIST];
     // a 32-bit product (mixed_fused refuses 2^32 particles or more): the state
     // arrays are then addressed with one wide multiply-add each
     const int64_t p = (int64_t)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -598,6 +682,10 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
     bool active = false;
     int mask = 0;
     int onew = 0;
+    // the corrected policy's move, for its pieces after the divergent part
+    bool vb_dep = false;
+    int vb_i[3] = {0, 0, 0};
+    float vb_s[3] = {0.0f, 0.0f, 0.0f}, vb_e[3] = {0.0f, 0.0f, 0.0f}, vb_qd = 0.0f;
     if (p < np) {
         int32_t c;
         float ox, oy, oz, ux, uy, uz;
@@ -662,6 +750,17 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
                 if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
                 if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
+                const bool wild = !(mask & 64) && (ix < 1 || ix > g.n[0] || iy < 1 || iy > g.n[1] || iz < 1 ||
+                                                   iz > g.n[2]);  // dropped below, no current
+                if (VBL && st.deposit[s] && !wild) {
+                    // the charge-conserving current of the whole move, also of
+                    // a particle the boundaries remove (pieces after the branch)
+                    vb_dep = true;
+                    vb_i[0] = ix0, vb_i[1] = iy0, vb_i[2] = iz0;
+#pragma unroll
+                    for (int a = 0; a < 3; a++) vb_s[a] = so[a], vb_e[a] = mv[a];
+                    vb_qd = st.qdep[s];
+                }
             }
             if (mask & 64) {
                 if (HOST) host_dead(*Hp, hs, hi);
@@ -696,13 +795,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 }
                 if (CORR && PUSH && st.deposit[s]) {
                     active = true;
-                    float wv[DEP_JSLOTS];
-#pragma unroll
-                    for (int q = 0; q < DEP_JSLOTS; q++) wv[q] = 0.0f;
-                    vb_pieces_m(g, D, ix0, iy0, iz0, so, mv, st.qdep[s], onew, wv);
                     float *w = col + lane;
-#pragma unroll
-                    for (int q = 0; q < DEP_JSLOTS; q++) w[q * DEP_STRIDE] = wv[q];
                     if (with_rho) {  // rho at the new position, true-vertex weights
                         const float qd = st.qdep[s];
                         const float a[3] = {1.0f - ox, 1.0f - oy, 1.0f - oz}, b[3] = {ox, oy, oz};
@@ -753,6 +846,22 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                     }
                 }
             }
+        }
+    }
+    if (VBL) {
+        // Villasenor-Buneman pieces with the whole warp present: the new
+        // cell's into the column, the others through the warp's list
+        DepList PL{s_pl[threadIdx.x >> 5], s_plk[threadIdx.x >> 5], 0};
+        float wv[DEP_JSLOTS];
+#pragma unroll
+        for (int q = 0; q < DEP_JSLOTS; q++) wv[q] = 0.0f;
+        // a particle the boundaries removed has no new cell: all its pieces go to the list
+        vb_pieces_list<true>(g, bc, PL, D, lane, vb_dep, vb_i[0], vb_i[1], vb_i[2], vb_s, vb_e, vb_qd,
+                             active ? onew : -1, wv);
+        if (PL.n) list_flush<true>(PL, D, lane);
+        if (vb_dep && active) {
+#pragma unroll
+            for (int q = 0; q < DEP_JSLOTS; q++) col[q * DEP_STRIDE + lane] = wv[q];
         }
     }
     if (__any_sync(0xffffffffu, mask & 63)) count_cross(ctr, mask & 63);
@@ -854,11 +963,34 @@ __global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned l
                                   const unsigned long long *__restrict__ wr, unsigned long long *Jx,
                                   unsigned long long *Jy, unsigned long long *Jz, unsigned long long *rho, int what,
                                   int corr) {
-    const int64_t first = (int64_t)sx + sy + 1;  // points below have no neighbour cell with particles
+    // points from sx + sy + 1 on have every neighbour record; below that (the
+    // low ghost planes, which only walled dimensions' pieces reach) each
+    // record is read where it exists
+    const int64_t first = (int64_t)sx + sy + 1;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npts; p += (int64_t)gridDim.x * blockDim.x) {
+        if (p < first) {
+            auto slot = [&](const unsigned long long *w, int ns, int64_t c, int k) -> unsigned long long {
+                return c >= 0 ? w[c * ns + k] : 0ull;
+            };
+            if (what & 1) {
+                const unsigned long long q3 = corr ? slot(wj, DEP_JSLOTS, p - 1, 4) : slot(wj, DEP_JSLOTS, p - sy, 4);
+                Jx[p] = slot(wj, DEP_JSLOTS, p, 0) + slot(wj, DEP_JSLOTS, p - sy, 3) + q3 +
+                        slot(wj, DEP_JSLOTS, p - sy - 1, 7);
+                Jy[p] = slot(wj, DEP_JSLOTS, p, 1) + slot(wj, DEP_JSLOTS, p - 1, 6) +
+                        slot(wj, DEP_JSLOTS, p - sx - 1, 8) + slot(wj, DEP_JSLOTS, p - sx, 10);
+                Jz[p] = slot(wj, DEP_JSLOTS, p, 2) + slot(wj, DEP_JSLOTS, p - sy, 5) +
+                        slot(wj, DEP_JSLOTS, p - sx - sy, 9) + slot(wj, DEP_JSLOTS, p - sx, 11);
+            }
+            if (what & 2)
+                rho[p] = slot(wr, DEP_RSLOTS, p, 0) + slot(wr, DEP_RSLOTS, p - sy, 1) + slot(wr, DEP_RSLOTS, p - 1, 2) +
+                         slot(wr, DEP_RSLOTS, p - sy - 1, 3) + slot(wr, DEP_RSLOTS, p - sx - 1, 4) +
+                         slot(wr, DEP_RSLOTS, p - sx - sy, 5) + slot(wr, DEP_RSLOTS, p - sx, 6) +
+                         slot(wr, DEP_RSLOTS, p - sx - sy - 1, 7);
+            continue;
+        }
         if (what & 1) {
             unsigned long long jx = 0, jy = 0, jz = 0;
-            if (p >= first) {
+            {
                 // J record of cell c: wj + 12 c (96 bytes, 32-byte aligned)
                 auto rec = [&](int64_t c) { return wj + c * DEP_JSLOTS; };
                 const ulonglong2 g0a = __ldg(reinterpret_cast<const ulonglong2 *>(rec(p)));        // slots 0,1
@@ -881,7 +1013,7 @@ __global__ void k_cells_to_points(int64_t npts, int sx, int sy, const unsigned l
         }
         if (what & 2) {
             unsigned long long r = 0;
-            if (p >= first) {
+            {
                 auto rec = [&](int64_t c) { return wr + c * DEP_RSLOTS; };
                 r = __ldg(rec(p)) + __ldg(rec(p - sy) + 1) + __ldg(rec(p - 1) + 2) + __ldg(rec(p - sy - 1) + 3) +
                     __ldg(rec(p - sx - 1) + 4) + __ldg(rec(p - sx - sy) + 5) + __ldg(rec(p - sx) + 6) +
@@ -1530,6 +1662,7 @@ MGeom mgeom(emoo_handle *h, double dt) {
     m.sy = h->g.sy;
     m.npts = h->g.npts;
     m.fourpi_dt = (float)(4.0 * PI_D * dt);
+    for (int d = 0; d < 3; d++) m.wrap[d] = h->bc.pbc[2 * d] == PBC_PERIODIC ? 1 : 0;
     return m;
 }
 
@@ -1744,7 +1877,6 @@ int mixed_ghost_fill(emoo_handle *h) {
             continue;
         }
         EMOO_TRY(flush());
-        extern int light_planes_public(emoo_handle * h, int s, PlaneSet *ps);
         for (int r = 0; r < 2; r++) {
             int s = 2 * d + r;
             if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
@@ -1776,14 +1908,51 @@ int mixed_plane_sets(emoo_handle *h, const PlaneSet *ps, int n) {
     return EMOO_OK;
 }
 
+// The FP64 form's k_mirror_fold on the fixed-point J (integer adds, exact):
+// the current a reflected particle deposited beyond its wall goes to the
+// mirrored points inside, normal component negated; ghost values cleared.
+__global__ void k_mirror_fold_m(MGeom g, MFix4 fl, int d, int right, int t1, int t2) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= t2 || r >= t1) return;
+    const int a = blockIdx.z;
+    long long *F = fl.p[a];
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int n = g.n[d];
+    const bool normal = a == d;
+    const int src = normal ? (right ? n + 1 : 0) : (right ? n + 2 : 0);
+    const int dst = normal ? (right ? n : 1) : (right ? n : 2);
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    c[d] = src;
+    const int64_t ks = (int64_t)c[0] * g.sx + (int64_t)c[1] * g.sy + c[2];
+    c[d] = dst;
+    const int64_t kd = (int64_t)c[0] * g.sx + (int64_t)c[1] * g.sy + c[2];
+    if (normal) F[kd] -= F[ks];
+    else F[kd] += F[ks];
+    F[ks] = 0;
+}
+
 // The corrected policy's full-range fold (fixed point) or ghost fill (FP32)
-// of n arrays, dimension by dimension.
+// of n arrays, dimension by dimension: periodic dimensions as images over the
+// whole range; walled ones fold J (fix with Jx, Jy, Jz first) by mirror at
+// reflecting sides and copy nothing (their field sides are LightBC planes).
 static int mixed_periodic_full(emoo_handle *h, const MFix4 *fix, const MF9 *flt, int n) {
     MGeom mg = mgeom(h, h->dtp);
     const Geom &g = h->g;
     dim3 blk(32, 8);
     for (int d = 0; d < 3; d++) {
         const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) {
+            const bool j3 = fix && n >= 3 && fix->p[0] == h->mf->J[0];
+            for (int r = 0; r < 2 && j3; r++) {
+                if (h->bc.pbc[2 * d + r] != PBC_REFLECTING) continue;
+                dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, 3);
+                h->launches++;
+                k_mirror_fold_m<<<grd, blk, 0, h->stream>>>(mg, *fix, d, r, g.tot[o1], g.tot[o2]);
+            }
+            continue;
+        }
         dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, n);
         h->launches++;
         if (fix) k_fold_full_m<<<grd, blk, 0, h->stream>>>(mg, *fix, d, g.tot[o1], g.tot[o2]);
@@ -1802,12 +1971,21 @@ static int mixed_fold_full(emoo_handle *h, int what) {
     return n ? mixed_periodic_full(h, &fl, nullptr, n) : EMOO_OK;
 }
 
-// E (3) or E, B and B_tm1 (9) ghost planes, corrected policy
+// E (3) or E, B and B_tm1 (9) ghost planes, corrected policy, then the
+// LightBC planes of external sides (between the Yee halves too, so that the
+// B half reads E at the new time at the boundary planes as at the wrap)
 static int mixed_ghost_full(emoo_handle *h, bool e_only) {
     MF9 fl = {};
     for (int c = 0; c < 3; c++) fl.p[c] = h->mf->E[c];
     for (int c = 0; c < 6; c++) fl.p[3 + c] = h->mf->Bslot[c];
-    return mixed_periodic_full(h, nullptr, &fl, e_only ? 3 : 9);
+    EMOO_TRY(mixed_periodic_full(h, nullptr, &fl, e_only ? 3 : 9));
+    for (int s = 0; s < 6; s++) {
+        if (h->bc.fbc[s] != FBC_EXTERNAL) continue;
+        PlaneSet ps[6];
+        const int n = light_planes_public(h, s, ps);
+        EMOO_TRY(mixed_plane_sets(h, ps, n));
+    }
+    return EMOO_OK;
 }
 
 // what: FOLD_J (the two transverse J components), FOLD_RHO, or both

@@ -39,6 +39,7 @@ extern "C" {
 #define EMOO_ERR_INPUT (-7)          /* input file missing, unparsable or inconsistent */
 #define EMOO_ERR_STATE (-8)          /* call not valid in the handle's current state */
 #define EMOO_ERR_UNSUPPORTED (-9)    /* option combination not implemented */
+#define EMOO_ERR_TIMEOUT (-10)       /* a bounded device-side wait gave up (the kernel skipped what it waited for) */
 
 /* Precision forms. */
 #define EMOO_FP64 0  /* FP64 positions, velocities, fields and current (reference parity form) */
@@ -331,6 +332,15 @@ int emoo_gauss_residual(emoo_handle *h, double out2[2]);
 
 /* Current simulation time and step size. */
 int emoo_time(emoo_handle *h, double *t, double *dt);
+
+/* Sensitivity probe (no reference counterpart; FP64 form only): multiplies
+ * every live particle's velocity components and every point of E, B and
+ * B_tm1 by (1 + rel u), and moves each position component by rel d u (kept
+ * only inside the box), u uniform in [-1, 1) and independent per particle or
+ * point and component, drawn from seed. With rel = 2^-24 applied after every
+ * step, an ensemble of FP64 runs measures how far FP32 rounding alone moves
+ * the loop's result: the bar the mixed form's error is stated against. */
+int emoo_perturb(emoo_handle *h, uint64_t seed, double rel);
 
 /* Device-side error word (bounds checks, fixed-point saturation) since the
  * last call; cleared by reading. */

@@ -47,6 +47,11 @@
 #include <string.h>
 
 #include "../include/emoo.h"
+/* The input generator of the CPU legs: the seeded per-particle sampler the
+ * library compiles into its host and device loaders (the same inline code,
+ * separately rounded basic operations only), so the CPU baseline and the
+ * reference arm generate their particles without loading the product. */
+#include "../apc_524_project_gb300/csrc/loader_common.h"
 
 #define UNIT_ACC 0.58668774          /* src/globals.hpp:12 */
 #define UNIT_RHOJ 4.80320427e-13     /* src/globals.hpp:16 */
@@ -525,6 +530,7 @@ static void poisson_bc(orc_t *c, int s, int id) {
 static void full_plane(orc_t *c, double *f, int dim, int src, int dst, int sum);
 static void corrected_fold(orc_t *c);
 static void corrected_ghosts(orc_t *c);
+static void corrected_e_bounds(orc_t *c);
 
 int orc_execute_bc(void *h, int send_id) {
     orc_t *c = (orc_t *)h;
@@ -965,16 +971,10 @@ static void evolve(orc_t *c, double dt) {
                 Ez[o] = Ez[o] - dt * ((Tx[o] - Tx[IDX(c, i, j - 1, k)]) / dy - (Ty[o] - Ty[IDX(c, i - 1, j, k)]) / dx +
                                       4 * PI_D * Jz[o]);
             }
-    /* corrected policy: the B half below reads E at plane n+1, so refresh
-     * E's periodic ghosts first (time-centred leapfrog at the wrap) */
-    if (c->policy)
-        for (int dim = 0; dim < 3; dim++)
-            for (int a = 0; a < 3; a++) {
-                double *f = c->slot[EMOO_EX + a];
-                full_plane(c, f, dim, c->n[dim], 0, 0);
-                full_plane(c, f, dim, 1, c->n[dim] + 1, 0);
-                full_plane(c, f, dim, 2, c->n[dim] + 2, 0);
-            }
+    /* corrected policy: the B half below reads E at plane n+1 and at the
+     * boundary planes, so E's periodic images and LightBC planes are set
+     * first (time-centred leapfrog at the wrap and at external sides) */
+    if (c->policy) corrected_e_bounds(c);
     for (int i = 1; i <= nx; i++)
         for (int j = 1; j <= ny; j++)
             for (int k = 1; k <= nz; k++) {
@@ -1383,17 +1383,25 @@ int orc_gauss_residual(void *h, double *out2) {
 /* the corrected-physics policy (no reference counterpart)              */
 
 /* Selects the corrected-physics policy (1) or the reference's arithmetic
- * (0). The corrected policy needs periodic particle and field boundaries on
- * every side (-1 otherwise): gather and deposit use the cell's own lower
- * corner as vertex, the current comes from Villasenor and Buneman's
- * charge-conserving deposit along each particle's straight path, and ghost
- * copies and folds cover the whole transverse range of every component. */
+ * (0). Under the corrected policy every dimension is either periodic
+ * (particle and field sides) or walled (particle sides reflecting or
+ * absorbing, field sides external; -1 otherwise): gather and deposit use the
+ * cell's own lower corner as vertex, the current comes from Villasenor and
+ * Buneman's charge-conserving deposit along each particle's straight path,
+ * periodic ghost copies and folds cover the whole transverse range of every
+ * component, the current a reflected particle deposited beyond its wall is
+ * mirrored back (mirror_fold), and E's boundary values - periodic images or
+ * LightBC planes - are set between the two halves of the Yee update. */
 int orc_set_policy(void *h, int policy) {
     orc_t *c = (orc_t *)h;
     if (policy != 0 && policy != 1) return -1;
     if (policy)
-        for (int s = 0; s < 6; s++)
-            if (c->pbc[s] != BC_PERIODIC || c->fbc[s] != BC_PERIODIC) return -1;
+        for (int d = 0; d < 3; d++) {
+            const int pl = c->pbc[2 * d], pr = c->pbc[2 * d + 1], fl = c->fbc[2 * d], fr = c->fbc[2 * d + 1];
+            const int periodic = pl == BC_PERIODIC && pr == BC_PERIODIC && fl == BC_PERIODIC && fr == BC_PERIODIC;
+            const int walled = pl != BC_PERIODIC && pr != BC_PERIODIC && fl == BC_EXTERNAL && fr == BC_EXTERNAL;
+            if (!periodic && !walled) return -1;
+        }
     c->policy = policy;
     return 0;
 }
@@ -1455,6 +1463,26 @@ static void vb_deposit(orc_t *c, const double p0[3], const double p1[3], double 
     }
 }
 
+/* A particle whose move ends beyond an absorbing wall leaves the domain in
+ * this step (the particle boundaries remove it). Its whole charge must cross
+ * the wall's vertex plane for the continuity equation to hold there, so the
+ * path is continued along the wall's normal to the next vertex plane beyond
+ * the wall (x0 - d, or x0 + L + d): that piece, inside the ghost cell, adds
+ * the flux of the charge the move's end point still left on the wall plane.
+ * (Corrected policy, no reference counterpart.) */
+static void absorbed_exit(orc_t *c, const double p1[3], double coef) {
+    double a[3] = {p1[0], p1[1], p1[2]};
+    for (int d = 0; d < 3; d++) {
+        const double xmin = c->x0[d], xmax = xmin + c->L[d];  /* the particle boundaries' limits */
+        double b[3] = {a[0], a[1], a[2]};
+        if (c->pbc[2 * d] == BC_ABSORBING && a[d] < xmin) b[d] = xmin - c->d[d];
+        else if (c->pbc[2 * d + 1] == BC_ABSORBING && a[d] > xmax) b[d] = xmax + c->d[d];
+        else continue;
+        vb_deposit(c, a, b, coef);
+        a[d] = b[d];
+    }
+}
+
 /* Push with the cached fields and the charge-conserving current of the
  * move (before the boundaries wrap the particle). */
 static void push_vb(orc_t *c, double dt) {
@@ -1472,7 +1500,9 @@ static void push_vb(orc_t *c, double dt) {
         c->vx[p] = st[3]; c->vy[p] = st[4]; c->vz[p] = st[5]; c->g[p] = st[6];
         if (c->info.isTestParticle[s] || !(dt > 0)) continue;
         double p1[3] = {st[0], st[1], st[2]};
-        vb_deposit(c, p0, p1, UNIT_RHOJ * c->info.charge_ratio[s] / vol / dt);
+        const double coef = UNIT_RHOJ * c->info.charge_ratio[s] / vol / dt;
+        vb_deposit(c, p0, p1, coef);
+        absorbed_exit(c, p1, coef);
     }
 }
 
@@ -1506,10 +1536,55 @@ static void full_plane(orc_t *c, double *f, int dim, int src, int dst, int sum) 
         }
 }
 
+/* Mirror fold at a reflecting wall (corrected policy; no reference
+ * counterpart). A particle that crossed the wall during the push is
+ * reflected (x -> 2 x_wall - x, v_n -> -v_n, src/boundaries/b_particles/
+ * bc_p_reflecting.cpp:43-52), so it moved along the mirror image of the part
+ * of its straight path that lies beyond the wall. The Villasenor-Buneman
+ * current that part deposited in the ghost layer therefore belongs to the
+ * mirrored points inside: the component normal to the wall with its sign
+ * reversed, the transverse ones unchanged, and charge stays conserved at
+ * every point. Left wall (vertex plane 1): normal edge 0 -> edge 1,
+ * transverse plane 0 -> plane 2; right wall (plane n+1): normal edge n+1 ->
+ * edge n, transverse plane n+2 -> plane n. The ghost values are cleared.
+ * Whole transverse range, so corners follow the other dimensions' folds. */
+static void mirror_fold(orc_t *c, int dim, int right) {
+    const int n = c->n[dim];
+    const int o1 = (dim == 0) ? 1 : 0, o2 = (dim == 2) ? 1 : 2;
+    for (int a = 0; a < 3; a++) {
+        double *f = c->slot[EMOO_JX + a];
+        const int normal = a == dim;
+        const int src = normal ? (right ? n + 1 : 0) : (right ? n + 2 : 0);
+        const int dst = normal ? (right ? n : 1) : (right ? n : 2);
+        for (int p = 0; p < c->tot[o1]; p++)
+            for (int q = 0; q < c->tot[o2]; q++) {
+                int is[3], id_[3];
+                is[dim] = src; id_[dim] = dst;
+                is[o1] = id_[o1] = p;
+                is[o2] = id_[o2] = q;
+                long ks = IDX(c, is[0], is[1], is[2]), kd = IDX(c, id_[0], id_[1], id_[2]);
+                if (normal) f[kd] -= f[ks];
+                else f[kd] += f[ks];
+                f[ks] = 0.0;
+            }
+    }
+}
+
+static int dim_periodic(const orc_t *c, int dim) { return c->fbc[2 * dim] == BC_PERIODIC; }
+
+/* Folds of the corrected policy: periodic dimensions as images over the
+ * whole range; a reflecting wall mirrors its ghost current back; at an
+ * absorbing wall the current of the path beyond it stays in the ghost layer
+ * (it carried the charge out: continuity holds there too). */
 static void corrected_fold(orc_t *c) {
     const int ids[4] = {EMOO_JX, EMOO_JY, EMOO_JZ, EMOO_RHO};
     for (int dim = 0; dim < 3; dim++) {
         int n = c->n[dim];
+        if (!dim_periodic(c, dim)) {
+            for (int r = 0; r < 2; r++)
+                if (c->pbc[2 * dim + r] == BC_REFLECTING) mirror_fold(c, dim, r);
+            continue;
+        }
         for (int k = 0; k < 4; k++) {
             double *f = c->slot[ids[k]];
             full_plane(c, f, dim, 0, n, 1);
@@ -1519,10 +1594,28 @@ static void corrected_fold(orc_t *c) {
     }
 }
 
+/* E's boundary values of the corrected policy: periodic images over the
+ * whole range, LightBC planes on external sides (the latter at the step's
+ * time, as the loop's executeBC(-1) sets them). */
+static void corrected_e_bounds(orc_t *c) {
+    for (int dim = 0; dim < 3; dim++) {
+        if (!dim_periodic(c, dim)) continue;
+        for (int a = 0; a < 3; a++) {
+            double *f = c->slot[EMOO_EX + a];
+            full_plane(c, f, dim, c->n[dim], 0, 0);
+            full_plane(c, f, dim, 1, c->n[dim] + 1, 0);
+            full_plane(c, f, dim, 2, c->n[dim] + 2, 0);
+        }
+    }
+    for (int s = 0; s < 6; s++)
+        if (c->fbc[s] == BC_EXTERNAL) light_bc(c, s, c->t, c->dtp);
+}
+
 static void corrected_ghosts(orc_t *c) {
     const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
     for (int dim = 0; dim < 3; dim++) {
         int n = c->n[dim];
+        if (!dim_periodic(c, dim)) continue;
         for (int k = 0; k < 9; k++) {
             double *f = c->slot[ids[k]];
             full_plane(c, f, dim, n, 0, 0);
@@ -1530,6 +1623,8 @@ static void corrected_ghosts(orc_t *c) {
             full_plane(c, f, dim, 2, n + 2, 0);
         }
     }
+    for (int s = 0; s < 6; s++)
+        if (c->fbc[s] == BC_EXTERNAL) light_bc(c, s, c->t, c->dtp);
 }
 
 /* One pass of the driver loop, src/main.cpp:221-287 (history cadence of
@@ -1574,4 +1669,23 @@ int orc_step(void *h, int ti, long *counts6, double *hist8, int *hist_written) {
     orc_interpolate(c);
     c->t += c->dtp;
     return 0;
+}
+
+/* Particles [first, first + n) of the sampler stream g into caller arrays
+ * (gamma may be null): bit-identical to the library's emoo_generate_host. */
+int orc_generate(const emoo_gen_params *g, int64_t first, int64_t n, double *x, double *y, double *z, double *vx,
+                 double *vy, double *vz, double *gamma) {
+    if (!g || n < 0 || (n > 0 && (!x || !y || !z || !vx || !vy || !vz))) return EMOO_ERR_ARG;
+    for (int64_t i = 0; i < n; i++) {
+        double o[7];
+        emoo_sample_particle(g, first + i, o);
+        x[i] = o[0];
+        y[i] = o[1];
+        z[i] = o[2];
+        vx[i] = o[3];
+        vy[i] = o[4];
+        vz[i] = o[5];
+        if (gamma) gamma[i] = o[6];
+    }
+    return EMOO_OK;
 }

@@ -229,6 +229,15 @@ class RefBackend(CpuBackend):
 
 
 class OracleBackend(CpuBackend):
+    @classmethod
+    def generator(cls):
+        """The oracle's copy of the seeded sampler (orc_generate), for
+        loading.sample_species(generate=...) without the product library."""
+        fn = cls.lib().orc_generate
+        fn.restype = C.c_int
+        fn.argtypes = [C.POINTER(abi.GenParams), C.c_int64, C.c_int64, _D, _D, _D, _D, _D, _D, _D]
+        return fn
+
     prefix = "orc_"
     path = ORACLE_LIB
 

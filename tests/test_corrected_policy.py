@@ -1,11 +1,11 @@
 """The corrected-physics policy (no reference counterpart): the cell's own
 lower corner as gather / deposit vertex, the Villasenor-Buneman
 charge-conserving current, ghost copies and folds over the whole range of
-every component; periodic boundaries only.
+every component; periodic boundaries here (walls: tests/test_corrected_walls.py).
 
 CPU (oracle): the discrete continuity equation rho(t + dt) - rho(t) + dt div J
 = 0 holds at every point to rounding, so the Gauss-law residual div E - 4 pi
-rho keeps its initial value step after step; the policy refuses walls.
+rho keeps its initial value step after step.
 GPU: the FP64 form against the oracle, and the residual's conservation."""
 import numpy as np
 import pytest
@@ -75,16 +75,6 @@ def test_oracle_continuity_and_gauss_law(relativity):
         rho0 = rho1.copy()
     res = _div([o.get_field(i) for i in (abi.EX, abi.EY, abi.EZ)], cfg.dx, n) - 4 * np.pi * rho0
     assert np.abs(res - res0).max() <= 1e-10 * 4 * np.pi * scale
-    o.close()
-
-
-def test_oracle_refuses_walls():
-    cfg = configs.tiny("walls", part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
-                       field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
-                       init="constant")
-    o = OracleBackend(configs.input_info(cfg), cfg.dt)
-    with pytest.raises(ValueError):
-        o.set_policy(1)
     o.close()
 
 

@@ -1,0 +1,212 @@
+"""Walls under the corrected-physics policy (no reference counterpart).
+
+A walled dimension has reflecting or absorbing particle sides and external
+(LightBC) field sides. The corrected policy deposits the Villasenor-Buneman
+current of each particle's whole straight path, also the part beyond a wall:
+a reflecting wall mirrors that part back inside (the reflected particle moved
+along its mirror image), an absorbing wall leaves it in the ghost layer (the
+charge went out through the wall). LightBC's planes are also set between the
+two halves of the Yee update, as the periodic images are.
+
+CPU (oracle): walls are crossed; the continuity equation
+rho(t + dt) - rho(t) + dt div J = 0 holds at every vertex, the wall planes
+included, to rounding; the Gauss-law residual div E - 4 pi rho keeps its
+initial value at the vertices whose E edges LightBC does not write.
+GPU: the FP64 form against the oracle (1e-9), the mixed form against the FP64
+form (1e-5), crossing counts exact; the 64^3 laser workload (reflecting walls
+and external field sides in x) runs under the policy with bounded energy.
+"""
+import numpy as np
+import pytest
+
+from apc_524_project_gb300 import abi, configs, loading
+from backends import OracleBackend, by_id, rel_l2
+
+FP64_RTOL = 1e-9
+MIXED_RTOL = 1e-5
+W = configs.Wave
+
+WALLS = {
+    "reflecting": ("reflecting", "reflecting"),
+    "absorbing": ("absorbing", "absorbing"),
+    "mixed": ("reflecting", "absorbing"),
+}
+
+
+def _cfg(walls, relativity=1, n=(8, 5, 4), dx=(0.9, 1.1, 0.8), vth=0.2, steps=10):
+    return configs.tiny(
+        "corr_walls", n=n, dx=dx, relativity=relativity, init="constant", vth=vth, steps=steps, dt=0.3,
+        part_bc=WALLS[walls] + ("periodic",) * 4, field_bc=("external", "external") + ("periodic",) * 4,
+        waves=[W(-1, 2, 0.05, 0.8, 30.0, 0.3, 1.0), W(1, 3, 0.02, 1.1, 45.0, 0.5, 0.5)])
+
+
+def _load(b, parts):
+    nid = 0
+    for si, p in enumerate(parts):
+        b.add_species(si, p, ids=np.arange(nid, nid + len(p["x"])))
+        nid += len(p["x"])
+
+
+def _oracle(cfg):
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    o.set_policy(1)
+    _load(o, loading.sample_all(cfg))
+    return o
+
+
+def _vertex_range(n, walled):
+    """Vertex planes per dimension: 1..n (periodic), 1..n+1 (walled)."""
+    return tuple(slice(1, n[d] + (2 if walled[d] else 1)) for d in range(3))
+
+
+def _images(f, n, walled):
+    """Periodic dimensions' ghost planes 0 and n+1 set to their images n and
+    1; walled dimensions' ghost values kept (the current beyond the wall)."""
+    g = f.copy()
+    for d in range(3):
+        if walled[d]:
+            continue
+        src, dst = [slice(None)] * 3, [slice(None)] * 3
+        src[d], dst[d] = n[d], 0
+        g[tuple(dst)] = g[tuple(src)]
+        src[d], dst[d] = 1, n[d] + 1
+        g[tuple(dst)] = g[tuple(src)]
+    return g
+
+
+def _div(f, dx, n, walled):
+    """Backward-difference divergence of an edge field at the vertices."""
+    V = _vertex_range(n, walled)
+    out = 0.0
+    for d in range(3):
+        a = _images(f[d], n, walled)
+        lo = list(V)
+        lo[d] = slice(V[d].start - 1, V[d].stop - 1)
+        out = out + (a[V] - a[tuple(lo)]) / dx[d]
+    return out
+
+
+@pytest.mark.parametrize("walls", sorted(WALLS))
+def test_oracle_walls_conserve_charge(walls):
+    cfg = _cfg(walls)
+    n, walled = cfg.n, (True, False, False)
+    o = _oracle(cfg)
+    o.init_fields()
+    V = _vertex_range(n, walled)
+    crossed = np.zeros(6, dtype=np.int64)
+    c, _ = o.step(0)  # the constant field start deposits no rho: begin after one step
+    crossed += np.array(c)
+    rho0 = o.get_field(abi.RHO)[V].copy()
+    E = lambda: [o.get_field(i) for i in (abi.EX, abi.EY, abi.EZ)]  # noqa: E731
+    res0 = _div(E(), cfg.dx, n, walled) - 4 * np.pi * rho0
+    scale = np.abs(rho0).max()
+    for ti in range(1, cfg.steps):
+        c, _ = o.step(ti)
+        crossed += np.array(c)
+        rho1 = o.get_field(abi.RHO)[V]
+        divj = _div([o.get_field(i) for i in (abi.JX, abi.JY, abi.JZ)], cfg.dx, n, walled)
+        cont = (rho1 - rho0) + cfg.dt * divj
+        assert np.abs(cont).max() <= 1e-12 * scale, (ti, np.abs(cont).max(), scale)
+        rho0 = rho1.copy()
+    assert crossed[0] > 0 and crossed[1] > 0, crossed
+    # LightBC writes E on the edge planes 1 and n along x and the transverse E on
+    # vertex planes 1 and n+1: the residual is conserved at vertex planes 3..n-1
+    res = _div(E(), cfg.dx, n, walled) - 4 * np.pi * rho0
+    inner = (slice(2, n[0] - 1), slice(None), slice(None))
+    assert np.abs((res - res0)[inner]).max() <= 1e-10 * 4 * np.pi * scale
+    o.close()
+
+
+def test_oracle_refuses_half_walled_dimensions():
+    """A dimension with periodic particles but external fields (or the other
+    way round) is neither periodic nor walled: the policy refuses it."""
+    cfg = configs.tiny("half", part_bc=("periodic",) * 6,
+                       field_bc=("external", "external") + ("periodic",) * 4, init="constant")
+    o = OracleBackend(configs.input_info(cfg), cfg.dt)
+    with pytest.raises(ValueError):
+        o.set_policy(1)
+    o.close()
+
+
+# ---- GPU -------------------------------------------------------------------
+
+def _gpu(cfg, precision=abi.FP64):
+    from backends import GpuBackend
+
+    g = GpuBackend(configs.input_info(cfg), cfg.dt, precision=precision, policy=abi.POLICY_CORRECTED)
+    _load(g, loading.sample_all(cfg))
+    return g
+
+
+def _fields(b):
+    return {i: b.get_field(i) for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.JX, abi.JY, abi.JZ,
+                                        abi.RHO)}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("walls", sorted(WALLS))
+def test_gpu_walls_match_oracle(walls):
+    cfg = _cfg(walls)
+    o = _oracle(cfg)
+    g = _gpu(cfg)
+    o.init_fields()
+    g.init_fields()
+    co = np.zeros(6, dtype=np.int64)
+    for ti in range(cfg.steps):
+        c, _ = o.step(ti)
+        co += np.array(c)
+    cg = np.array(g.step(cfg.steps))
+    np.testing.assert_array_equal(cg, co)
+    po, pg = by_id(o.particles()), by_id(g.particles())
+    np.testing.assert_array_equal(po["id"], pg["id"])
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        assert rel_l2(pg[k], po[k]) <= FP64_RTOL, k
+    fo, fg = _fields(o), _fields(g)
+    for i in fo:
+        assert rel_l2(fg[i], fo[i]) <= FP64_RTOL, (abi.FIELD_NAMES[i], rel_l2(fg[i], fo[i]))
+    assert g.check() == abi.OK
+    o.close()
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("walls", sorted(WALLS))
+def test_gpu_mixed_walls_match_fp64(walls):
+    cfg = _cfg(walls, steps=6)
+    f = _gpu(cfg)
+    m = _gpu(cfg, abi.MIXED)
+    f.init_fields()
+    m.init_fields()
+    cf, cm = np.array(f.step(cfg.steps)), np.array(m.step(cfg.steps))
+    np.testing.assert_array_equal(cm, cf)
+    phys = tuple(slice(1, v + 2) for v in cfg.n)
+    ff, fm = _fields(f), _fields(m)
+    for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.JX, abi.JY, abi.JZ):
+        err = rel_l2(fm[i][phys], ff[i][phys])
+        assert err <= MIXED_RTOL, (abi.FIELD_NAMES[i], err)
+    assert f.check() == abi.OK and m.check() == abi.OK
+    f.close()
+    m.close()
+
+
+@pytest.mark.gpu
+def test_laser64_under_the_corrected_policy_stays_bounded():
+    """The differentiation workload (64^3, y-polarised wave from x-left,
+    reflecting particle walls and external field sides in x, 128 steps) under
+    the corrected policy: the total energy at every history row stays within
+    a small factor of the energy the wave has brought in by then (the
+    reference scheme's grows without bound on it)."""
+    from apc_524_project_gb300 import differentiate
+
+    cfg = configs.laser64()
+    g = _gpu(cfg, abi.MIXED)
+    g.init_fields()
+    g.step(128)
+    rows = g.history_rows()
+    assert np.all(np.isfinite(rows))
+    tot = rows[:, 7]
+    assert tot[-1] <= 3.0 * tot.max(), tot
+    assert tot[-1] < 10.0 * tot[len(tot) // 2] + 1e-300, tot
+    assert g.check() == abi.OK
+    g.close()
+    _ = differentiate

@@ -5,10 +5,14 @@ its error is stated against the FP64 GPU form:
   * initial state: positions to FP32 offset precision, fields <= 1e-7;
   * a stable run (the external-wave, reflecting case): relative L2 of E, B,
     J, rho <= MIXED_RTOL after 12 steps, crossing counts identical;
-  * runs where the reference scheme itself amplifies perturbations (see the
-    stability note in the FP64 tests): the mixed error after N steps stays
-    within SENS_FACTOR times the FP64 form's own response to a 1e-7 relative
-    velocity perturbation;
+  * runs where the scheme itself amplifies perturbations: the mixed error
+    after N steps stays within ENSEMBLE_FACTOR times the spread of an FP64
+    ensemble perturbed after every step by the mixed form's own one-step
+    rounding (emoo_perturb; the amplitude measured, a few FP32 ulps): what
+    FP32 rounding alone does to this loop, measured instead of assumed
+    (apc_524_project_gb300/precision.py);
+    the thermal plasma of the 256^3 benchmark, scaled to 24^3, is checked
+    that way over 100 steps in tests/test_mixed_error.py;
   * the fixed-point current makes runs bit-reproducible.
 """
 import numpy as np
@@ -21,13 +25,11 @@ from golden import cases
 pytestmark = pytest.mark.gpu
 
 MIXED_RTOL = 2e-6
-# The FP64 probe perturbs the velocities once, by 1e-7, at t = 0. The mixed
-# form rounds positions, velocities and fields to FP32 (2^-24 ~ 6e-8 relative)
-# on every one of the N steps, and each of those roundings is then amplified by
-# the same growing modes for the rest of the run. With N = 8-12 steps and the
-# growth these cases show, the accumulated response measures 15-30 times the
-# single-kick one; 100 leaves room for that and still fails on an O(1) error.
-SENS_FACTOR = 100.0
+# The mixed error may be at most this many times the largest distance of the
+# FP64 ensemble's members from the unperturbed FP64 run.
+ENSEMBLE_FACTOR = 2.0
+ENSEMBLE_MEMBERS = 6
+FP32_ROUNDING = 2.0 ** -24
 
 
 def _load(b, parts):
@@ -38,23 +40,35 @@ def _load(b, parts):
         nid += n
 
 
-def _run(cfg, dt, steps, precision, perturb=0.0):
+INIT_FIELDS = (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.BX_TM1, abi.BY_TM1, abi.BZ_TM1)
+
+
+def _run(cfg, dt, steps, precision, perturb_seed=None, start_fields=None, rel=FP32_ROUNDING):
+    """Runs cfg for `steps` steps; perturb_seed: after every step perturb the
+    FP64 state by relative amplitude rel (emoo_perturb) with that seed;
+    start_fields: E, B, B_tm1 to start from instead of the handle's own field
+    start (returned as out["start"])."""
     info = configs.input_info(cfg)
     parts = loading.sample_all(cfg)
-    if perturb:
-        for p in parts:
-            for k in ("vx", "vy", "vz"):
-                p[k] = p[k] * (1.0 + perturb)
     b = GpuBackend(info, dt, precision=precision)
     _load(b, parts)
     b.init_fields()
+    if start_fields is not None:
+        for i, a in start_fields.items():
+            b.set_field(i, a)
+    start = {i: b.get_field(i) for i in INIT_FIELDS}
     counts = np.zeros(6, dtype=np.int64)
-    for _ in range(steps):
+    if perturb_seed is not None:  # the mixed form rounds the state it loads, too
+        abi.check(b.L.emoo_perturb(b.h, perturb_seed * 1000003 + steps + 7, rel))
+    for t in range(steps):
         counts += np.array(b.step(1))
+        if perturb_seed is not None:
+            abi.check(b.L.emoo_perturb(b.h, perturb_seed * 1000003 + t, rel))
     out = {i: b.get_field(i) for i in (abi.EX, abi.EY, abi.EZ, abi.BX, abi.BY, abi.BZ, abi.JX, abi.RHO)}
     out["p"] = by_id(b.particles())
     out["counts"] = counts
     out["hist"] = b.history_rows()
+    out["start"] = start
     assert b.check() == abi.OK
     b.close()
     return out
@@ -82,16 +96,43 @@ def test_mixed_stable_case_within_fp32_tolerance():
     np.testing.assert_allclose(m["hist"][:, 4:], f["hist"][:, 4:], rtol=1e-6)
 
 
+def _one_step_rounding(cfg, dt, start_fields):
+    """The mixed form's rounding in one step: RMS relative velocity difference
+    against the FP64 form from the same particles and fields, times sqrt(3)
+    (the amplitude of uniform noise with that RMS), at least 2^-24."""
+    f = _run(cfg, dt, 1, abi.FP64)
+    m = _run(cfg, dt, 1, abi.MIXED, start_fields=start_fields)
+    vf = np.stack([f["p"][k] for k in ("vx", "vy", "vz")], axis=1)
+    vm = np.stack([m["p"][k] for k in ("vx", "vy", "vz")], axis=1)
+    nf = np.linalg.norm(vf, axis=1)
+    r = np.linalg.norm(vm - vf, axis=1)[nf > 0] / nf[nf > 0]
+    return max(FP32_ROUNDING, float(np.sqrt(3.0 * np.mean(r * r))))
+
+
 @pytest.mark.parametrize("name", ["periodic_poisson", "aniso_const", "sorted_test"])
-def test_mixed_error_within_fp64_sensitivity(name):
+def test_mixed_error_within_its_rounding_spread(name):
+    """On the golden cases (reference policy, 8-12 steps), started from the
+    FP64 form's field start, the mixed form's distance from the FP64 form is
+    at most ENSEMBLE_FACTOR times the largest distance of FP64 runs perturbed
+    after every step by the mixed form's own one-step rounding (measured, a
+    few FP32 ulps): on these small cases a few particles that end a step
+    within rounding of a cell face, where the reference's gather jumps,
+    decide the distance, so the largest member is the yardstick. (Each
+    form's own Jacobi start on a periodic grid drifts in
+    the potential's mean, by an amount set by its deposit's rounding, which
+    AToB turns into a uniform B: a difference of the field start, stated
+    apart, not of the loop.)"""
     cfg, dt, steps, _ = cases.make(name)
-    m = _run(cfg, dt, steps, abi.MIXED)
     f = _run(cfg, dt, steps, abi.FP64)
-    fp = _run(cfg, dt, steps, abi.FP64, perturb=1e-7)
+    m = _run(cfg, dt, steps, abi.MIXED, start_fields=f["start"])
+    rel = _one_step_rounding(cfg, dt, f["start"])
+    assert rel < 1e-5, rel
+    ens = [_run(cfg, dt, steps, abi.FP64, perturb_seed=k + 1, rel=rel) for k in range(ENSEMBLE_MEMBERS)]
+    phys = tuple(slice(1, v + 1) for v in cfg.n)
     for i in (abi.EX, abi.BY, abi.JX):
-        err = rel_l2(m[i], f[i])
-        sens = rel_l2(fp[i], f[i])
-        assert err <= SENS_FACTOR * max(sens, 1e-7), (abi.FIELD_NAMES[i], err, sens)
+        err = rel_l2(m[i][phys], f[i][phys])
+        spread = [rel_l2(e[i][phys], f[i][phys]) for e in ens]
+        assert err <= ENSEMBLE_FACTOR * max(spread), (abi.FIELD_NAMES[i], err, spread, rel)
 
 
 def test_mixed_divergence_starts_at_a_cell_face():

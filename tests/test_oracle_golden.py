@@ -102,3 +102,14 @@ def test_oracle_langmuir32_summary():
         assert float(np.sqrt(np.sum(f * f))) == float(g[f"final_norm_{i}"])
     history_close(np.array(hist), g["history"], 1e-15, total_mass(info, parts))
     b.close()
+
+
+def test_oracle_sampler_equals_the_library_sampler():
+    """The CPU legs generate particles with the oracle's copy of the sampler
+    (orc_generate); it produces the library's arrays bit for bit."""
+    cfg = configs.thermal256(8)
+    for si in range(len(cfg.species)):
+        a = loading.sample_species(cfg, si)
+        b = loading.sample_species(cfg, si, generate=OracleBackend.generator())
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=k)

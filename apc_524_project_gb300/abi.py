@@ -21,7 +21,6 @@ ERR_CUDA = -6
 ERR_INPUT = -7
 ERR_STATE = -8
 ERR_UNSUPPORTED = -9
-ERR_TIMEOUT = -10
 
 FP64 = 0
 MIXED = 1

@@ -375,5 +375,81 @@ AD_HD void jterms_rev(const CellGeo &c, double uq, const double r[3], const doub
     }
 }
 
+
+// ---- charge-conserving current (corrected policy) --------------------------
+//
+// Villasenor and Buneman's current of a straight move p0 -> p1 (vb_deposit in
+// particles_f64.cu, same operations in the same order): the path, in cell
+// units u = (p - x0) / d, is split where it crosses a face (at most once per
+// axis); piece k with ends ua, ub in cell c = floor((ua + ub) / 2), offsets
+// aa = ua - c, bb = ub - c, extent D = bb - aa and mid m = (aa + bb) / 2 adds
+// to axis a's four edges coef d_a D_a ((1-m_j)(1-m_k) + D_j D_k / 12,
+// m_j (1-m_k) - .., (1-m_j) m_k - .., m_j m_k + ..) (edges at j, j+1 / k,
+// k+1). Which faces are crossed and which cell a piece is in are decided on
+// the primal values; the piece ends and weights carry the derivative.
+struct VbGeo {
+    double x0[3], id[3], d[3];
+};
+
+template <class T>
+struct VbPiece {
+    int cell[3];
+    T W[12];  // 4 a + e: axis a, edge e (bit 0: +1 along j, bit 1: +1 along k)
+};
+
+AD_HD double cst(double v, const double *) { return v; }
+AD_HD Dual cst(double v, const Dual *) { return mk(v); }
+
+template <class T>
+AD_HD int vb_eval(const VbGeo &g, const T p0[3], const T p1[3], double coef, VbPiece<T> out[4]) {
+    const T *tag = nullptr;
+    T u0[3], u1[3], ts[5];
+    int nt = 0;
+    ts[nt++] = cst(0.0, tag);
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        u0[a] = (p0[a] - g.x0[a]) * g.id[a];
+        u1[a] = (p1[a] - g.x0[a]) * g.id[a];
+        const double f0 = floor(val(u0[a])), f1 = floor(val(u1[a]));
+        if (f0 != f1) {
+            const double b = f0 > f1 ? f0 : f1;
+            ts[nt++] = (b - u0[a]) / (u1[a] - u0[a]);
+        }
+    }
+    ts[nt++] = cst(1.0, tag);
+    for (int i = 2; i < nt - 1; i++)
+        for (int j = i; j > 1 && val(ts[j]) < val(ts[j - 1]); j--) {
+            const T t = ts[j];
+            ts[j] = ts[j - 1];
+            ts[j - 1] = t;
+        }
+    int n = 0;
+    for (int sgi = 0; sgi + 1 < nt; sgi++) {
+        const T ta = ts[sgi], tb = ts[sgi + 1];
+        if (!(val(tb) > val(ta))) continue;
+        T m[3], D[3];
+        VbPiece<T> &pc = out[n++];
+        AD_UNROLL
+        for (int a = 0; a < 3; a++) {
+            const T ua = u0[a] + ta * (u1[a] - u0[a]), ub = u0[a] + tb * (u1[a] - u0[a]);
+            pc.cell[a] = (int)floor(0.5 * (val(ua) + val(ub)));
+            const T aa = ua - (double)pc.cell[a], bb = ub - (double)pc.cell[a];
+            D[a] = bb - aa;
+            m[a] = 0.5 * (aa + bb);
+        }
+        AD_UNROLL
+        for (int a = 0; a < 3; a++) {
+            const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+            const T w = coef * g.d[a] * D[a];
+            const T cr = D[jb] * D[kb] / 12.0;
+            pc.W[4 * a + 0] = w * ((1.0 - m[jb]) * (1.0 - m[kb]) + cr);
+            pc.W[4 * a + 1] = w * (m[jb] * (1.0 - m[kb]) - cr);
+            pc.W[4 * a + 2] = w * ((1.0 - m[jb]) * m[kb] - cr);
+            pc.W[4 * a + 3] = w * (m[jb] * m[kb] + cr);
+        }
+    }
+    return n;
+}
+
 }  // namespace ad
 }  // namespace emoo

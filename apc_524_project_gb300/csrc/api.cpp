@@ -79,7 +79,6 @@ int read_err(emoo_handle *h) {
     EMOO_CUDA(cudaMemcpyAsync(&h->ctr->err, &zero, sizeof(zero), cudaMemcpyHostToDevice, h->stream));
     if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
     if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
-    if (c.err & ERR_WAIT) return EMOO_ERR_TIMEOUT;
     return EMOO_OK;
 }
 
@@ -721,7 +720,6 @@ int read_counters(emoo_handle *h, int64_t *counts6, bool accumulate) {
         for (int s = 0; s < 6; s++) counts6[s] = (accumulate ? counts6[s] : 0) + (int64_t)c.cross[s];
     if (c.err & ERR_FIXED_OVERFLOW) return EMOO_ERR_FIXED_OVERFLOW;
     if (c.err & ERR_BOUNDS) return EMOO_ERR_BOUNDS;
-    if (c.err & ERR_WAIT) return EMOO_ERR_TIMEOUT;
     return EMOO_OK;
 }
 
@@ -807,7 +805,6 @@ const char *emoo_strerror(int s) {
         case EMOO_ERR_INPUT: return "input error";
         case EMOO_ERR_STATE: return "invalid call for the handle state";
         case EMOO_ERR_UNSUPPORTED: return "unsupported option combination";
-        case EMOO_ERR_TIMEOUT: return "a bounded device-side wait gave up";
         default: return "unknown status";
     }
 }

@@ -23,7 +23,7 @@ enum { PBC_PERIODIC = 0, PBC_REFLECTING = 1, PBC_ABSORBING = 2 };
 enum { FBC_PERIODIC = 0, FBC_EXTERNAL = 1 };
 
 // Device error word bits.
-enum { ERR_BOUNDS = 1, ERR_FIXED_OVERFLOW = 2, ERR_NAN = 4, ERR_WAIT = 8 };
+enum { ERR_BOUNDS = 1, ERR_FIXED_OVERFLOW = 2, ERR_NAN = 4 };
 
 // Grid geometry in the reference layout: (n+3)^3 points per field, C order,
 // physical points 1..n, ghost planes 0 and n+1, extra plane n+2

@@ -622,6 +622,9 @@ __device__ __forceinline__ void vb_pieces_list(const MGeom &g, const BCTab &bc, 
     // continues along the wall's normal to the next vertex plane beyond the
     // wall (offset -1 or 2 in the old cell's units), so that its whole charge
     // crosses the wall's plane (the FP64 form's absorbed_exit)
+    const bool absorbs = bc.pbc[0] == PBC_ABSORBING || bc.pbc[1] == PBC_ABSORBING || bc.pbc[2] == PBC_ABSORBING ||
+                         bc.pbc[3] == PBC_ABSORBING || bc.pbc[4] == PBC_ABSORBING || bc.pbc[5] == PBC_ABSORBING;
+    if (!absorbs) return;  // the same for every lane
     float a0[3] = {e[0], e[1], e[2]};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -750,17 +753,15 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 mask |= axis_bc(bc, 0, g.n[0], ix, ox, ux, vx);
                 if (!(mask & 64)) mask |= axis_bc(bc, 1, g.n[1], iy, oy, uy, vy);
                 if (!(mask & 64)) mask |= axis_bc(bc, 2, g.n[2], iz, oz, uz, vz);
-                const bool wild = !(mask & 64) && (ix < 1 || ix > g.n[0] || iy < 1 || iy > g.n[1] || iz < 1 ||
-                                                   iz > g.n[2]);  // dropped below, no current
-                if (VBL && st.deposit[s] && !wild) {
-                    // the charge-conserving current of the whole move, also of
-                    // a particle the boundaries remove (pieces after the branch)
-                    vb_dep = true;
-                    vb_i[0] = ix0, vb_i[1] = iy0, vb_i[2] = iz0;
+            }
+            if (VBL && (mask & 64) && st.deposit[s]) {
+                // an absorbing wall removed the particle: the current of its
+                // whole move still goes in (pieces after the branch)
+                vb_dep = true;
+                vb_i[0] = ix0, vb_i[1] = iy0, vb_i[2] = iz0;
 #pragma unroll
-                    for (int a = 0; a < 3; a++) vb_s[a] = so[a], vb_e[a] = mv[a];
-                    vb_qd = st.qdep[s];
-                }
+                for (int a = 0; a < 3; a++) vb_s[a] = so[a], vb_e[a] = mv[a];
+                vb_qd = st.qdep[s];
             }
             if (mask & 64) {
                 if (HOST) host_dead(*Hp, hs, hi);
@@ -795,6 +796,11 @@ __global__ void __launch_bounds__(FUSED_BLOCK, 5)
                 }
                 if (CORR && PUSH && st.deposit[s]) {
                     active = true;
+                    vb_dep = true;
+                    vb_i[0] = ix0, vb_i[1] = iy0, vb_i[2] = iz0;
+#pragma unroll
+                    for (int a = 0; a < 3; a++) vb_s[a] = so[a], vb_e[a] = mv[a];
+                    vb_qd = st.qdep[s];
                     float *w = col + lane;
                     if (with_rho) {  // rho at the new position, true-vertex weights
                         const float qd = st.qdep[s];

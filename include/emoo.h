@@ -39,7 +39,6 @@ extern "C" {
 #define EMOO_ERR_INPUT (-7)          /* input file missing, unparsable or inconsistent */
 #define EMOO_ERR_STATE (-8)          /* call not valid in the handle's current state */
 #define EMOO_ERR_UNSUPPORTED (-9)    /* option combination not implemented */
-#define EMOO_ERR_TIMEOUT (-10)       /* a bounded device-side wait gave up (the kernel skipped what it waited for) */
 
 /* Precision forms. */
 #define EMOO_FP64 0  /* FP64 positions, velocities, fields and current (reference parity form) */

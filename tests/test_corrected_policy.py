@@ -145,12 +145,15 @@ def test_gpu_corrected_policy_keeps_gauss_law():
 
 @pytest.mark.gpu
 def test_gpu_corrected_policy_refuses_what_it_does_not_cover():
+    """Both forms take the policy; a dimension that is neither periodic
+    (particle and field sides) nor walled (reflecting or absorbing particle
+    sides, external field sides) is refused, and so is the adjoint run."""
     _gpu(_cfg(1), precision=abi.MIXED).close()  # both forms take it
-    walls = configs.tiny("walls", part_bc=("reflecting", "reflecting", "periodic", "periodic", "periodic", "periodic"),
-                         field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
-                         init="constant")
+    half = configs.tiny("half", part_bc=("periodic",) * 6,
+                        field_bc=("external", "external", "periodic", "periodic", "periodic", "periodic"),
+                        init="constant")
     with pytest.raises(Exception):
-        _gpu(walls)
+        _gpu(half)
 
 
 @pytest.mark.gpu

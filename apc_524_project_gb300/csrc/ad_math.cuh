@@ -77,7 +77,40 @@ struct CellGeo {
     double d[3];
     double area[3];  // d[j] * d[k]
     double vol;
+    // reciprocals for the reverse functions (their products need only be
+    // accurate), and the forward divisions' exact shortcut: where d[i] or
+    // area[i] is a power of two, x * (1 / d) is x / d to the bit
+    double id[3], iarea[3], ivol;
+    int p2[3], p2area[3], p2vol;
 };
+
+// x / d as the FP64 kernels compute it (multiplication by the exact
+// reciprocal when d is a power of two)
+template <class T>
+AD_HD T divp(const T &x, double d, double id, int p2) {
+    return p2 ? x * id : x / d;
+}
+
+// The geometry of cells with spacings d0, d1, d2 (host and device).
+AD_HD CellGeo make_cell_geo(double d0, double d1, double d2) {
+    CellGeo c;
+    c.d[0] = d0;
+    c.d[1] = d1;
+    c.d[2] = d2;
+    for (int i = 0; i < 3; i++) c.area[i] = c.d[(i + 1) % 3] * c.d[(i + 2) % 3];
+    c.vol = c.d[0] * c.d[1] * c.d[2];
+    for (int i = 0; i < 3; i++) {
+        c.id[i] = 1.0 / c.d[i];
+        c.iarea[i] = 1.0 / c.area[i];
+        int e;
+        c.p2[i] = frexp(c.d[i], &e) == 0.5;
+        c.p2area[i] = frexp(c.area[i], &e) == 0.5;
+    }
+    c.ivol = 1.0 / c.vol;
+    int e;
+    c.p2vol = frexp(c.vol, &e) == 0.5;
+    return c;
+}
 
 // ---- gather ---------------------------------------------------------------
 //
@@ -94,10 +127,10 @@ AD_HD void gather_eval(const CellGeo &c, const T v[18], const T ds[3], T out[6])
         e = e + ds[j] * (lk - ds[k]) * v[4 * i + 1];
         e = e + ds[j] * ds[k] * v[4 * i + 2];
         e = e + (lj - ds[j]) * ds[k] * v[4 * i + 3];
-        e = e / c.area[i];
+        e = divp(e, c.area[i], c.iarea[i], c.p2area[i]);
         T b = (li - ds[i]) * v[12 + 2 * i];
         b = b + ds[i] * v[12 + 2 * i + 1];
-        b = b / li;
+        b = divp(b, li, c.id[i], c.p2[i]);
         out[i] = e;
         out[3 + i] = b;
     }
@@ -113,10 +146,10 @@ AD_HD void gather_eval(const CellGeo &c, const double v[18], const double ds[3],
         e += ds[j] * (lk - ds[k]) * v[4 * i + 1];
         e += ds[j] * ds[k] * v[4 * i + 2];
         e += (lj - ds[j]) * ds[k] * v[4 * i + 3];
-        e = e / c.area[i];
+        e = divp(e, c.area[i], c.iarea[i], c.p2area[i]);
         double b = (li - ds[i]) * v[12 + 2 * i];
         b += ds[i] * v[12 + 2 * i + 1];
-        b = b / li;
+        b = divp(b, li, c.id[i], c.p2[i]);
         out[i] = e;
         out[3 + i] = b;
     }
@@ -128,7 +161,7 @@ AD_HD void gather_rev(const CellGeo &c, const double v[18], const double ds[3], 
     for (int i = 0; i < 3; i++) {
         const int j = (i + 1) % 3, k = (i + 2) % 3;
         const double lj = c.d[j], lk = c.d[k], li = c.d[i];
-        const double ls = lout[i] / c.area[i];
+        const double ls = lout[i] * c.iarea[i];
         const double A = lj - ds[j], Bk = lk - ds[k];
         lv[4 * i] += ls * A * Bk;
         lv[4 * i + 1] += ls * ds[j] * Bk;
@@ -136,7 +169,7 @@ AD_HD void gather_rev(const CellGeo &c, const double v[18], const double ds[3], 
         lv[4 * i + 3] += ls * A * ds[k];
         lds[j] += ls * (-Bk * v[4 * i] + Bk * v[4 * i + 1] + ds[k] * v[4 * i + 2] - ds[k] * v[4 * i + 3]);
         lds[k] += ls * (-A * v[4 * i] - ds[j] * v[4 * i + 1] + ds[j] * v[4 * i + 2] + A * v[4 * i + 3]);
-        const double lb = lout[3 + i] / li;
+        const double lb = lout[3 + i] * c.id[i];
         lv[12 + 2 * i] += lb * (li - ds[i]);
         lv[12 + 2 * i + 1] += lb * ds[i];
         lds[i] += lb * (v[12 + 2 * i + 1] - v[12 + 2 * i]);
@@ -251,66 +284,99 @@ AD_HD void vay_eval(double qp, const T f[6], double dt, T x[3], T v[3], T &gamma
     gamma = gi;
 }
 
-// Adjoint of vay_eval at inputs (f, v, gamma): lx, lv, lg hold the output
-// adjoints on entry and the input adjoints on exit; lf receives the field
-// adjoint.
-AD_HD void vay_rev(double qp, const double f[6], double dt, const double v_in[3], double g_in, double lx[3],
-                   double lv[3], double &lg, double lf[6]) {
+// The intermediates of one Vay step, for its reverse.
+struct VayTape {
+    double up[3], tau[3], tsq, sigma, ustar, gi1, gi, tt[3], s, udott, w[3], vout[3];
+};
+
+// vay_eval<double> keeping its intermediates: the same operations in the
+// same order (bit-identical x, v, gamma).
+AD_HD void vay_fwd(double qp, const double f[6], double dt, double x[3], double v[3], double &gamma, VayTape &T) {
     const double e[3] = {f[0], f[1], f[2]}, b[3] = {f[3], f[4], f[5]};
-    double vXb[3], up[3], tau[3];
-    cross3(v_in, b, vXb);
-    for (int a = 0; a < 3; a++) up[a] = g_in * v_in[a] + qp * (e[a] + vXb[a]) + qp * e[a];
-    const double gps = 1.0 + up[0] * up[0] + up[1] * up[1] + up[2] * up[2];
-    for (int a = 0; a < 3; a++) tau[a] = qp * b[a];
-    const double tsq = tau[0] * tau[0] + tau[1] * tau[1] + tau[2] * tau[2];
-    const double sigma = gps - tsq;
-    const double ustar = up[0] * tau[0] + up[1] * tau[1] + up[2] * tau[2];
-    const double gi1 = ::sqrt(sigma * sigma + 4.0 * (tsq + ustar * ustar));
-    const double gi = ::sqrt(0.5 * (sigma + gi1));
-    double tt[3];
-    for (int a = 0; a < 3; a++) tt[a] = tau[a] / gi;
-    const double s = 1.0 / (1.0 + tt[0] * tt[0] + tt[1] * tt[1] + tt[2] * tt[2]);
-    const double udott = ustar / gi;
-    double cr[3], w[3], vout[3];
-    cross3(up, tt, cr);
-    for (int a = 0; a < 3; a++) w[a] = up[a] + udott * tt[a] + cr[a];
-    for (int a = 0; a < 3; a++) vout[a] = s * w[a] / gi;
-    // reverse
+    double vXb[3];
+    cross3(v, b, vXb);
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) T.up[a] = gamma * v[a] + qp * (e[a] + vXb[a]) + qp * e[a];
+    const double gps = 1.0 + T.up[0] * T.up[0] + T.up[1] * T.up[1] + T.up[2] * T.up[2];
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) T.tau[a] = qp * b[a];
+    T.tsq = T.tau[0] * T.tau[0] + T.tau[1] * T.tau[1] + T.tau[2] * T.tau[2];
+    T.sigma = gps - T.tsq;
+    T.ustar = T.up[0] * T.tau[0] + T.up[1] * T.tau[1] + T.up[2] * T.tau[2];
+    T.gi1 = ::sqrt(T.sigma * T.sigma + 4.0 * (T.tsq + T.ustar * T.ustar));
+    T.gi = ::sqrt(0.5 * (T.sigma + T.gi1));
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) T.tt[a] = T.tau[a] / T.gi;
+    T.s = 1.0 / (1.0 + T.tt[0] * T.tt[0] + T.tt[1] * T.tt[1] + T.tt[2] * T.tt[2]);
+    T.udott = T.ustar / T.gi;
+    double cr[3];
+    cross3(T.up, T.tt, cr);
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) T.w[a] = T.up[a] + T.udott * T.tt[a] + cr[a];
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        T.vout[a] = T.s * T.w[a] / T.gi;
+        v[a] = T.vout[a];
+        x[a] = x[a] + dt * v[a];
+    }
+    gamma = T.gi;
+}
+
+// Adjoint of vay_eval from its tape (inputs v_in, g_in, fields f): lx, lv,
+// lg hold the output adjoints on entry and the input adjoints on exit; lf
+// receives the field adjoint. Divisions by gi and gi1 are products with
+// their reciprocals.
+AD_HD void vay_rev_tape(const VayTape &T, double qp, const double f[6], double dt, const double v_in[3], double g_in,
+                        double lx[3], double lv[3], double &lg, double lf[6]) {
+    const double b[3] = {f[3], f[4], f[5]};
+    const double igi = 1.0 / T.gi, igi1 = 1.0 / T.gi1;
+    const double *up = T.up, *tau = T.tau, *tt = T.tt, *w = T.w, *vout = T.vout;
+    const double gi = T.gi, gi1 = T.gi1, s = T.s, udott = T.udott, sigma = T.sigma, ustar = T.ustar;
     double lvo[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lvo[a] = lv[a] + dt * lx[a];
     double lgi = lg;
     double luint[3];
-    for (int a = 0; a < 3; a++) luint[a] = lvo[a] / gi;
-    lgi += -(vout[0] * lvo[0] + vout[1] * lvo[1] + vout[2] * lvo[2]) / gi;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) luint[a] = lvo[a] * igi;
+    lgi += -(vout[0] * lvo[0] + vout[1] * lvo[1] + vout[2] * lvo[2]) * igi;
     // uint = s w
     const double ls = w[0] * luint[0] + w[1] * luint[1] + w[2] * luint[2];
     double lw[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lw[a] = s * luint[a];
     double lup[3], ltt[3], tmp[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lup[a] = lw[a];
     const double ludott = tt[0] * lw[0] + tt[1] * lw[1] + tt[2] * lw[2];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) ltt[a] = udott * lw[a];
     cross3(tt, lw, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lup[a] += tmp[a];
     cross3(lw, up, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) ltt[a] += tmp[a];
     // udott = ustar / gi
-    double lustar = ludott / gi;
-    lgi += -udott * ludott / gi;
+    double lustar = ludott * igi;
+    lgi += -udott * ludott * igi;
     // s = 1 / (1 + tt.tt)
+    AD_UNROLL
     for (int a = 0; a < 3; a++) ltt[a] += -2.0 * s * s * ls * tt[a];
     // tt = tau / gi
     double ltau[3];
-    for (int a = 0; a < 3; a++) ltau[a] = ltt[a] / gi;
-    lgi += -(tt[0] * ltt[0] + tt[1] * ltt[1] + tt[2] * ltt[2]) / gi;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) ltau[a] = ltt[a] * igi;
+    lgi += -(tt[0] * ltt[0] + tt[1] * ltt[1] + tt[2] * ltt[2]) * igi;
     // gi = sqrt(0.5 (sigma + gi1))
-    double lsigma = 0.25 * lgi / gi;
-    const double lgi1 = 0.25 * lgi / gi;
+    double lsigma = 0.25 * lgi * igi;
+    const double lgi1 = 0.25 * lgi * igi;
     // gi1 = sqrt(sigma^2 + 4 tsq + 4 ustar^2)
-    lsigma += lgi1 * sigma / gi1;
-    double ltsq = 2.0 * lgi1 / gi1;
-    lustar += 4.0 * ustar * lgi1 / gi1;
+    lsigma += lgi1 * sigma * igi1;
+    double ltsq = 2.0 * lgi1 * igi1;
+    lustar += 4.0 * ustar * lgi1 * igi1;
     // ustar = up . tau
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         lup[a] += tau[a] * lustar;
         ltau[a] += up[a] * lustar;
@@ -318,26 +384,46 @@ AD_HD void vay_rev(double qp, const double f[6], double dt, const double v_in[3]
     // sigma = gps - tsq
     const double lgps = lsigma;
     ltsq -= lsigma;
+    AD_UNROLL
     for (int a = 0; a < 3; a++) ltau[a] += 2.0 * tau[a] * ltsq;
     // gps = 1 + up.up
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lup[a] += 2.0 * up[a] * lgps;
     // up = g v + qp (e + v x b) + qp e
     double lb[3], le[3], lvxb[3];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         lb[a] = qp * ltau[a];
         le[a] = 2.0 * qp * lup[a];
         lvxb[a] = qp * lup[a];
     }
     lg = v_in[0] * lup[0] + v_in[1] * lup[1] + v_in[2] * lup[2];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lv[a] = g_in * lup[a];
     cross3(b, lvxb, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lv[a] += tmp[a];
     cross3(lvxb, v_in, tmp);
+    AD_UNROLL
     for (int a = 0; a < 3; a++) lb[a] += tmp[a];
+    AD_UNROLL
     for (int a = 0; a < 3; a++) {
         lf[a] += le[a];
         lf[3 + a] += lb[a];
     }
+    (void)gi;
+    (void)gi1;
+}
+
+// Adjoint of vay_eval at inputs (f, v, gamma): lx, lv, lg hold the output
+// adjoints on entry and the input adjoints on exit; lf receives the field
+// adjoint.
+AD_HD void vay_rev(double qp, const double f[6], double dt, const double v_in[3], double g_in, double lx[3],
+                   double lv[3], double &lg, double lf[6]) {
+    VayTape T;
+    double x[3] = {0.0, 0.0, 0.0}, v[3] = {v_in[0], v_in[1], v_in[2]}, g = g_in;
+    vay_fwd(qp, f, dt, x, v, g, T);
+    vay_rev_tape(T, qp, f, dt, v_in, g_in, lx, lv, lg, lf);
 }
 
 // ---- current deposit ----------------------------------------------------
@@ -350,7 +436,7 @@ AD_HD void jterms_eval(const CellGeo &c, double uq, const T r[3], const T vv[3],
         const int j = (i + 1) % 3, k = (i + 2) % 3;
         const double lj = c.d[j], lk = c.d[k];
         const T cur = uq * vv[i];
-        const T ratio = (cur / c.vol) / c.area[i];
+        const T ratio = divp(divp(cur, c.vol, c.ivol, c.p2vol), c.area[i], c.iarea[i], c.p2area[i]);
         out[4 * i] = ratio * (lj - r[j]) * (lk - r[k]);
         out[4 * i + 1] = ratio * r[j] * (lk - r[k]);
         out[4 * i + 2] = ratio * r[j] * r[k];
@@ -365,11 +451,11 @@ AD_HD void jterms_rev(const CellGeo &c, double uq, const double r[3], const doub
     for (int i = 0; i < 3; i++) {
         const int j = (i + 1) % 3, k = (i + 2) % 3;
         const double lj = c.d[j], lk = c.d[k];
-        const double ratio = ((uq * vv[i]) / c.vol) / c.area[i];
+        const double ratio = uq * vv[i] * c.ivol * c.iarea[i];
         const double A = lj - r[j], Bk = lk - r[k];
         const double l0 = lout[4 * i], l1 = lout[4 * i + 1], l2 = lout[4 * i + 2], l3 = lout[4 * i + 3];
         const double lratio = l0 * A * Bk + l1 * r[j] * Bk + l2 * r[j] * r[k] + l3 * A * r[k];
-        lvv[i] += lratio * uq / c.vol / c.area[i];
+        lvv[i] += lratio * uq * c.ivol * c.iarea[i];
         lr[j] += ratio * (-l0 * Bk + l1 * Bk + l2 * r[k] - l3 * r[k]);
         lr[k] += ratio * (-l0 * A - l1 * r[j] + l2 * r[j] + l3 * A);
     }
@@ -449,6 +535,101 @@ AD_HD int vb_eval(const VbGeo &g, const T p0[3], const T p1[3], double coef, VbP
         }
     }
     return n;
+}
+
+// Adjoint of vb_eval, written out by hand (one pass instead of six dual
+// ones). lw(piece, cell, a, e) returns the adjoint of piece `piece`'s weight
+// W[4 a + e] (the adjoint of the grid point it lands on; 0 for a piece the
+// deposit skips); the derivatives of p0 and p1 are added to lp0 and lp1.
+// Per piece, with l_e the four adjoints of axis a (j, k the other two axes):
+//   W_e = w (P_e +- cr), w = coef d_a D_a, cr = D_j D_k / 12,
+//   P = ((1-m_j)(1-m_k), m_j (1-m_k), (1-m_j) m_k, m_j m_k);
+// then D = ub - ua, m = (ua + ub) / 2 - cell, ua = u0 + ta (u1 - u0) (ub with
+// tb), a crossing t = (b - u0) / (u1 - u0) of its axis, u = (p - x0) / d.
+template <class LW>
+AD_HD void vb_rev(const VbGeo &g, const double p0[3], const double p1[3], double coef, LW lw, double lp0[3],
+                  double lp1[3]) {
+    double u0[3], u1[3], ts[5];
+    int ax[5];
+    int nt = 0;
+    ts[nt] = 0.0;
+    ax[nt++] = -1;
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        u0[a] = (p0[a] - g.x0[a]) * g.id[a];
+        u1[a] = (p1[a] - g.x0[a]) * g.id[a];
+        const double f0 = floor(u0[a]), f1 = floor(u1[a]);
+        if (f0 != f1) {
+            const double b = f0 > f1 ? f0 : f1;
+            ts[nt] = (b - u0[a]) / (u1[a] - u0[a]);
+            ax[nt++] = a;
+        }
+    }
+    ts[nt] = 1.0;
+    ax[nt++] = -1;
+    for (int i = 2; i < nt - 1; i++)
+        for (int j = i; j > 1 && ts[j] < ts[j - 1]; j--) {
+            const double t = ts[j];
+            ts[j] = ts[j - 1];
+            ts[j - 1] = t;
+            const int q = ax[j];
+            ax[j] = ax[j - 1];
+            ax[j - 1] = q;
+        }
+    double lts[5] = {0, 0, 0, 0, 0}, lu0[3] = {0, 0, 0}, lu1[3] = {0, 0, 0};
+    int n = 0;
+    for (int sgi = 0; sgi + 1 < nt; sgi++) {
+        const double ta = ts[sgi], tb = ts[sgi + 1];
+        if (!(tb > ta)) continue;
+        double m[3], D[3], du[3];
+        int cell[3];
+        AD_UNROLL
+        for (int a = 0; a < 3; a++) {
+            du[a] = u1[a] - u0[a];
+            const double ua = u0[a] + ta * du[a], ub = u0[a] + tb * du[a];
+            cell[a] = (int)floor(0.5 * (ua + ub));
+            const double aa = ua - (double)cell[a], bb = ub - (double)cell[a];
+            D[a] = bb - aa;
+            m[a] = 0.5 * (aa + bb);
+        }
+        double lD[3] = {0, 0, 0}, lm[3] = {0, 0, 0};
+        AD_UNROLL
+        for (int a = 0; a < 3; a++) {
+            const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+            const double l0 = lw(n, cell, a, 0), l1 = lw(n, cell, a, 1), l2 = lw(n, cell, a, 2), l3 = lw(n, cell, a, 3);
+            const double w = coef * g.d[a] * D[a];
+            const double cr = D[jb] * D[kb] * (1.0 / 12.0);
+            const double mj = m[jb], mk = m[kb];
+            const double lwa = l0 * ((1.0 - mj) * (1.0 - mk) + cr) + l1 * (mj * (1.0 - mk) - cr) +
+                               l2 * ((1.0 - mj) * mk - cr) + l3 * (mj * mk + cr);
+            const double lcr = w * (l0 - l1 - l2 + l3);
+            lm[jb] += w * (-l0 * (1.0 - mk) + l1 * (1.0 - mk) - l2 * mk + l3 * mk);
+            lm[kb] += w * (-l0 * (1.0 - mj) - l1 * mj + l2 * (1.0 - mj) + l3 * mj);
+            lD[a] += coef * g.d[a] * lwa;
+            lD[jb] += lcr * D[kb] * (1.0 / 12.0);
+            lD[kb] += lcr * D[jb] * (1.0 / 12.0);
+        }
+        AD_UNROLL
+        for (int a = 0; a < 3; a++) {
+            const double lua = -lD[a] + 0.5 * lm[a], lub = lD[a] + 0.5 * lm[a];
+            lu0[a] += lua * (1.0 - ta) + lub * (1.0 - tb);
+            lu1[a] += lua * ta + lub * tb;
+            lts[sgi] += lua * du[a];
+            lts[sgi + 1] += lub * du[a];
+        }
+        n++;
+    }
+    for (int i = 1; i + 1 < nt; i++) {
+        const int a = ax[i];
+        const double idu = 1.0 / (u1[a] - u0[a]), t = ts[i];
+        lu0[a] += lts[i] * (t - 1.0) * idu;
+        lu1[a] += lts[i] * (-t * idu);
+    }
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        lp0[a] += lu0[a] * g.id[a];
+        lp1[a] += lu1[a] * g.id[a];
+    }
 }
 
 }  // namespace ad

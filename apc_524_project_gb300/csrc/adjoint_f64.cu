@@ -70,13 +70,21 @@ using adf::k_plane_adj;
 using adf::k_yee_b_adj;
 using adf::k_yee_e_adj;
 
+// the kernels' own geometry, reciprocals and power-of-two flags (so the
+// recomputed forward divides exactly as the primal step does)
 __device__ __forceinline__ CellGeo cell_geo(const Geom &g) {
     CellGeo c;
     for (int a = 0; a < 3; a++) {
         c.d[a] = g.d[a];
         c.area[a] = g.area[a];
+        c.id[a] = g.id[a];
+        c.iarea[a] = g.iarea[a];
+        c.p2[a] = g.p2[a];
+        c.p2area[a] = g.area_p2[a];
     }
     c.vol = g.vol;
+    c.ivol = g.ivol;
+    c.p2vol = g.vol_p2;
     return c;
 }
 
@@ -141,11 +149,106 @@ __device__ __forceinline__ int bc_t(const BCTab &bc, T p[3], T v[3]) {
     return flips;
 }
 
+// ---- charge-conserving current (corrected policy) ----------------------------
+
+__device__ __forceinline__ ad::VbGeo vb_geo(const Geom &g) {
+    ad::VbGeo v;
+    for (int a = 0; a < 3; a++) {
+        v.x0[a] = g.x0[a];
+        v.id[a] = g.id[a];
+        v.d[a] = g.d[a];
+    }
+    return v;
+}
+
+// Grid point of weight e of axis a of a current piece in cell c (the indexing
+// of vb_deposit in particles_f64.cu), or -1 where that deposit skips the
+// piece (a cell outside -1..n along some axis).
+__device__ __forceinline__ int64_t vb_point(const Geom &g, const int c[3], int a, int e) {
+    for (int b = 0; b < 3; b++)
+        if (c[b] < -1 || c[b] + 2 >= g.tot[b]) return -1;
+    int ii[3] = {c[0] + 1, c[1] + 1, c[2] + 1};
+    ii[(a + 1) % 3] += e & 1;
+    ii[(a + 2) % 3] += e >> 1;
+    return gidx(g, ii[0], ii[1], ii[2]);
+}
+
+// Tangent of vb_deposit: the derivative of every weight added to dJ.
+__device__ void vb_tlm(const Geom &g, const JPtrs &dJ, const Dual p0[3], const Dual p1[3], double coef) {
+    ad::VbPiece<Dual> pc[4];
+    const int n = ad::vb_eval(vb_geo(g), p0, p1, coef, pc);
+    for (int k = 0; k < n; k++)
+        for (int a = 0; a < 3; a++)
+            for (int e = 0; e < 4; e++) {
+                const int64_t pt = vb_point(g, pc[k].cell, a, e);
+                if (pt >= 0) atomicAdd(dJ.J[a] + pt, pc[k].W[4 * a + e].d);
+            }
+}
+
+// Adjoint of vb_deposit: adds the derivatives of sum(LJ W) to lp0, lp1.
+__device__ void vb_adj(const Geom &g, const JPtrs &LJ, const double p0[3], const double p1[3], double coef,
+                       double lp0[3], double lp1[3]) {
+    auto lw = [&](int, const int *c, int a, int e) -> double {
+        const int64_t pt = vb_point(g, c, a, e);
+        return pt >= 0 ? LJ.J[a][pt] : 0.0;
+    };
+    ad::vb_rev(vb_geo(g), p0, p1, coef, lw, lp0, lp1);
+}
+
+// The exit extension past absorbing walls (absorbed_exit in particles_f64.cu):
+// from the end of the move, along each axis whose absorbing side was crossed,
+// a straight piece to the fixed vertex plane beyond the wall.
+__device__ int exit_path(const Geom &g, const BCTab &bc, const double p1[3], double A[4][3], int dk[3]) {
+    int K = 0;
+    for (int c = 0; c < 3; c++) A[0][c] = p1[c];
+    for (int d = 0; d < 3; d++) {
+        double b[3] = {A[K][0], A[K][1], A[K][2]};
+        if (bc.pbc[2 * d] == PBC_ABSORBING && A[K][d] < bc.xmin[d]) b[d] = bc.xmin[d] - g.d[d];
+        else if (bc.pbc[2 * d + 1] == PBC_ABSORBING && A[K][d] > bc.xmax[d]) b[d] = bc.xmax[d] + g.d[d];
+        else continue;
+        dk[K] = d;
+        for (int c = 0; c < 3; c++) A[K + 1][c] = b[c];
+        K++;
+    }
+    return K;
+}
+
+__device__ void exit_tlm(const Geom &g, const BCTab &bc, const JPtrs &dJ, const Dual p1[3], double coef) {
+    Dual a[3] = {p1[0], p1[1], p1[2]};
+    for (int d = 0; d < 3; d++) {
+        Dual b[3] = {a[0], a[1], a[2]};
+        if (bc.pbc[2 * d] == PBC_ABSORBING && a[d].v < bc.xmin[d]) b[d] = mk(bc.xmin[d] - g.d[d]);
+        else if (bc.pbc[2 * d + 1] == PBC_ABSORBING && a[d].v > bc.xmax[d]) b[d] = mk(bc.xmax[d] + g.d[d]);
+        else continue;
+        vb_tlm(g, dJ, a, b, coef);
+        a[d] = b[d];
+    }
+}
+
+// Adjoint of the exit extension: the pieces in reverse; the coordinate a piece
+// sets to the wall's plane is a constant, its other ones pass through.
+__device__ void exit_adj(const Geom &g, const BCTab &bc, const JPtrs &LJ, const double p1[3], double coef,
+                         double lp1[3]) {
+    double A[4][3];
+    int dk[3];
+    const int K = exit_path(g, bc, p1, A, dk);
+    double lA[3] = {0.0, 0.0, 0.0};
+    for (int k = K - 1; k >= 0; k--) {
+        double la[3] = {0.0, 0.0, 0.0}, lb[3] = {lA[0], lA[1], lA[2]};
+        vb_adj(g, LJ, A[k], A[k + 1], coef, la, lb);
+        lb[dk[k]] = 0.0;
+        for (int c = 0; c < 3; c++) lA[c] = la[c] + lb[c];
+    }
+    for (int c = 0; c < 3; c++) lp1[c] += lA[c];
+}
+
 // ---- tangent particle kernel ---------------------------------------------
 //
 // Reads the primal state before the step (P, F) and the tangents (dP, dF),
 // writes the tangents after the step and adds the tangent current to dJ.
-template <bool REL>
+// CORR: the corrected policy (gather at the cell's own vertex, the
+// charge-conserving current of the move before the boundaries).
+template <bool REL, bool CORR>
 __global__ void k_tlm_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs F, FPtrs dF, PArr dP, int64_t np,
                                 double dt, JPtrs dJ) {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -174,17 +277,23 @@ __global__ void k_tlm_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
         pos[a] = mk(P.p[a][p], dP.p[a][p]);
         vel[a] = mk(P.p[3 + a][p], dP.p[3 + a][p]);
     }
+    const Dual p0[3] = {pos[0], pos[1], pos[2]};
     const int ic[3] = {ix, iy, iz};
-    for (int a = 0; a < 3; a++) ds[a] = pos[a] - (g.x0[a] + g.d[a] * ic[a]);
+    for (int a = 0; a < 3; a++) ds[a] = pos[a] - (g.x0[a] + g.d[a] * (ic[a] - g.vshift));
     ad::gather_eval(cg, v18, ds, f);
     Dual gam = mk(REL ? P.p[6][p] : 1.0, REL ? dP.p[6][p] : 0.0);
     if (REL) ad::vay_eval(st.qp[s], f, dt, pos, vel, gam);
     else ad::boris_eval(st.qp[s], f, dt, pos, vel);
+    if (CORR && st.deposit[s] && dt > 0.0) {
+        const double coef = st.uq[s] / g.vol / dt;
+        vb_tlm(g, dJ, p0, pos, coef);
+        exit_tlm(g, bc, dJ, pos, coef);
+    }
     if (bc_t(bc, pos, vel) < 0) {
         for (int a = 0; a < 7; a++) dP.p[a][p] = 0.0;
         return;
     }
-    if (st.deposit[s]) {
+    if (!CORR && st.deposit[s]) {
         cell_of(g, pos[0].v, pos[1].v, pos[2].v, ix, iy, iz);
         if (cell_ok(g, ix, iy, iz)) {
             const int64_t o2 = gidx(g, ix, iy, iz);
@@ -207,8 +316,8 @@ __global__ void k_tlm_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
 // P, F: the primal state before the step (from the tape). L: the particle
 // adjoints, after the step on entry, before it on exit. LJ: the adjoint of
 // the deposited current. LF: field adjoints that receive the gather's
-// adjoint (atomics).
-template <bool REL>
+// adjoint (atomics). CORR as in k_tlm_particles.
+template <bool REL, bool CORR>
 __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs F, PArr L, int64_t np, double dt,
                                 JPtrs LJ, FOut LF) {
     const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -230,18 +339,20 @@ __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
     }
     const CellGeo cg = cell_geo(g);
     const int ic[3] = {ix, iy, iz};
-    double pos[3], vel[3], ds[3], f[6];
+    double pos[3], vel[3], ds[3], f[6], p0[3];
     for (int a = 0; a < 3; a++) {
-        pos[a] = P.p[a][p];
+        pos[a] = p0[a] = P.p[a][p];
         vel[a] = P.p[3 + a][p];
-        ds[a] = pos[a] - (g.x0[a] + g.d[a] * ic[a]);
+        ds[a] = pos[a] - (g.x0[a] + g.d[a] * (ic[a] - g.vshift));
     }
     ad::gather_eval(cg, v18, ds, f);
     const double v_in[3] = {vel[0], vel[1], vel[2]};
     const double g_in = REL ? P.p[6][p] : 1.0;
     double gam = g_in;
-    if (REL) ad::vay_eval(st.qp[s], f, dt, pos, vel, gam);
+    ad::VayTape vt;
+    if (REL) ad::vay_fwd(st.qp[s], f, dt, pos, vel, gam, vt);
     else ad::boris_eval(st.qp[s], f, dt, pos, vel);
+    const double p1[3] = {pos[0], pos[1], pos[2]};  // the end of the move, before the boundaries
     const int flips = bc_t(bc, pos, vel);
     double lx[3], lv[3], lg = REL ? L.p[6][p] : 0.0;
     for (int a = 0; a < 3; a++) {
@@ -252,7 +363,7 @@ __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
         for (int a = 0; a < 3; a++) lx[a] = lv[a] = 0.0;
         lg = 0.0;
     } else {
-        if (st.deposit[s]) {
+        if (!CORR && st.deposit[s]) {
             int jx, jy, jz;
             cell_of(g, pos[0], pos[1], pos[2], jx, jy, jz);
             if (cell_ok(g, jx, jy, jz)) {
@@ -270,8 +381,16 @@ __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
                 lv[a] = -lv[a];
             }
     }
+    double lp0[3] = {0.0, 0.0, 0.0};
+    if (CORR && st.deposit[s] && dt > 0.0) {  // the current of the move, also for a removed particle
+        const double coef = st.uq[s] / g.vol / dt;
+        double lp1[3] = {0.0, 0.0, 0.0};
+        vb_adj(g, LJ, p0, p1, coef, lp0, lp1);
+        exit_adj(g, bc, LJ, p1, coef, lp1);
+        for (int a = 0; a < 3; a++) lx[a] += lp1[a];
+    }
     double lf[6] = {0, 0, 0, 0, 0, 0};
-    if (REL) ad::vay_rev(st.qp[s], f, dt, v_in, g_in, lx, lv, lg, lf);
+    if (REL) ad::vay_rev_tape(vt, st.qp[s], f, dt, v_in, g_in, lx, lv, lg, lf);
     else ad::boris_rev(st.qp[s], f, dt, v_in, lx, lv, lf);
     double l18[18] = {0}, lds[3] = {0, 0, 0};
     ad::gather_rev(cg, v18, ds, lf, l18, lds);
@@ -285,7 +404,7 @@ __global__ void k_adj_particles(Geom g, SpeciesTab st, BCTab bc, CPArr P, FPtrs 
         }
     }
     for (int a = 0; a < 3; a++) {
-        L.p[a][p] = lx[a] + lds[a];
+        L.p[a][p] = lx[a] + lds[a] + lp0[a];
         L.p[3 + a][p] = lv[a];
     }
     if (REL) L.p[6][p] = lg;
@@ -395,7 +514,10 @@ __global__ void k_objective_kin_seed(SpeciesTab st, CPArr P, PArr L, int64_t np,
     }
 }
 
+// grid of the grid-stride kernels (objectives, seeds)
 int pblocks(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 64)); }
+// grid of the one-thread-per-particle kernels: every particle gets a thread
+int pblocks_all(int64_t n) { return (int)std::max<int64_t>(1, (n + 255) / 256); }
 
 // ---- host side -----------------------------------------------------------
 
@@ -575,11 +697,40 @@ int objective(emoo_handle *h, const ObjSpec &os, double *const *dslots, double *
 
 }  // namespace
 
+// The tangent planes of a list of plane ops: each value's derivative along
+// dtheta, written into the tangent slots.
+static int tangent_planes(emoo_handle *h, const std::vector<AdBcOp> &ops, double *const *dslot,
+                          const double *dtheta) {
+    for (const AdBcOp &op : ops) {
+        if (op.kind != 1) continue;
+        double v = 0.0, vs = 0.0;
+        if (dtheta) {
+            for (size_t k = 0; k < op.ku.size(); k++) v += op.cu[k] * dtheta[op.ku[k]];
+            for (size_t k = 0; k < op.ks.size(); k++) vs += op.cs[k] * dtheta[op.ks[k]];
+        }
+        PlaneSet ps{dslot[op.slot], op.dim, op.idx, v, vs, op.t1, op.t2, nullptr, nullptr};
+        EMOO_TRY(plane_set_f64(h, &ps, 1));
+    }
+    return EMOO_OK;
+}
+
+static bool corrected(const emoo_handle *h) { return h->policy == EMOO_POLICY_CORRECTED; }
+
+template <bool REL>
+static void launch_tlm(emoo_handle *h, bool corr, const SpeciesTab &st, CPArr P, FPtrs F, FPtrs dF, PArr D,
+                       int64_t np, JPtrs dJ) {
+    const int nb = pblocks_all(np);
+    if (corr)
+        k_tlm_particles<REL, true><<<nb, 256, 0, h->stream>>>(h->g, st, h->bc, P, F, dF, D, np, h->dtp, dJ);
+    else
+        k_tlm_particles<REL, false><<<nb, 256, 0, h->stream>>>(h->g, st, h->bc, P, F, dF, D, np, h->dtp, dJ);
+}
+
 // tangent step: dP, dslot advance with the primal step
 static int tlm_step(emoo_handle *h, AdRun &R, double **dP, double *const *dslot, const double *dtheta) {
     SpeciesTab st;
     species_tab(h, h->dtp, st);
-    const Geom &g = h->g;
+    const bool corr = corrected(h);
     for (int c = 0; c < 3; c++)
         EMOO_CUDA(cudaMemsetAsync(dslot[EMOO_JX + c], 0, sizeof(double) * R.npts, h->stream));
     CPArr P{{h->x, h->y, h->z, h->vx, h->vy, h->vz, h->gam}};
@@ -587,37 +738,51 @@ static int tlm_step(emoo_handle *h, AdRun &R, double **dP, double *const *dslot,
     PArr D{{dP[0], dP[1], dP[2], dP[3], dP[4], dP[5], dP[6]}};
     JPtrs dJ{{dslot[EMOO_JX], dslot[EMOO_JY], dslot[EMOO_JZ]}};
     h->launches++;
-    if (R.rel)
-        k_tlm_particles<true><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, P, F, dF, D, R.np, h->dtp, dJ);
-    else
-        k_tlm_particles<false><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, P, F, dF, D, R.np, h->dtp, dJ);
+    if (R.rel) launch_tlm<true>(h, corr, st, P, F, dF, D, R.np, dJ);
+    else launch_tlm<false>(h, corr, st, P, F, dF, D, R.np, dJ);
     EMOO_CUDA(cudaGetLastError());
     // primal particle step, then the linear field part on both
     EMOO_TRY(fused_step_f64(h, h->dtp, 0));
     EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
-    {
-        SlotSwap sw(h, dslot);
-        EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+    if (corr) {
+        // the tangent fields through the same halves, periodic images and
+        // plane sets (the planes' derivative values) as the primal ones
+        {
+            SlotSwap sw(h, dslot);
+            EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+        }
         EMOO_TRY(yee_f64(h, h->dtp));
-    }
-    EMOO_TRY(yee_f64(h, h->dtp));
-    std::vector<AdBcOp> ops;
-    EMOO_TRY(ad_bc_ops(h, ops));
-    EMOO_TRY(ad_execute_bc(h, EMOO_SEND_EB));
-    {
+        std::vector<AdBcOp> ops;
+        EMOO_TRY(ad_bc_ops(h, ops));
+        EMOO_TRY(ad_execute_bc(h, EMOO_SEND_EB));
+        SlotSwap sw(h, dslot);
+        static const int ids_e[3] = {EMOO_EX, EMOO_EY, EMOO_EZ};
+        static const int ids9[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ,
+                                    EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
+        EMOO_TRY(yee_half_f64(h, h->dtp, 0));
+        EMOO_TRY(periodic_copies_f64(h, ids_e, 3));
+        EMOO_TRY(tangent_planes(h, ops, dslot, dtheta));
+        EMOO_TRY(yee_half_f64(h, h->dtp, 1));
+        EMOO_TRY(periodic_copies_f64(h, ids9, 9));
+        EMOO_TRY(tangent_planes(h, ops, dslot, dtheta));
+    } else {
+        {
+            SlotSwap sw(h, dslot);
+            EMOO_TRY(ad_execute_bc(h, EMOO_SEND_JRHO));
+            EMOO_TRY(yee_f64(h, h->dtp));
+        }
+        EMOO_TRY(yee_f64(h, h->dtp));
+        std::vector<AdBcOp> ops;
+        EMOO_TRY(ad_bc_ops(h, ops));
+        EMOO_TRY(ad_execute_bc(h, EMOO_SEND_EB));
         SlotSwap sw(h, dslot);
         static const int ids_eb[6] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ};
         for (const AdBcOp &op : ops) {
             if (op.kind == 0) {
                 EMOO_TRY(ghost_fill_f64(h, ids_eb, 6, op.mask));
             } else {
-                double v = 0.0, vs = 0.0;
-                if (dtheta) {
-                    for (size_t k = 0; k < op.ku.size(); k++) v += op.cu[k] * dtheta[op.ku[k]];
-                    for (size_t k = 0; k < op.ks.size(); k++) vs += op.cs[k] * dtheta[op.ks[k]];
-                }
-                PlaneSet ps{dslot[op.slot], op.dim, op.idx, v, vs, op.t1, op.t2, nullptr, nullptr};
-                EMOO_TRY(plane_set_f64(h, &ps, 1));
+                const std::vector<AdBcOp> one(1, op);
+                EMOO_TRY(tangent_planes(h, one, dslot, dtheta));
             }
         }
     }
@@ -636,10 +801,66 @@ struct PlaneLedger {
 };
 
 // adjoint of one step, given the state before it (snapshot S)
+// Adjoints of plane sets, last first, each recorded in the ledger.
+static int planes_adj(emoo_handle *h, const std::vector<AdBcOp> &ops, double *const *lslot, PlaneLedger &pl) {
+    for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
+        const AdBcOp &op = *it;
+        if (op.kind != 1) continue;
+        if (pl.ops.size() >= pl.cap) return EMOO_ERR_STATE;
+        double *sums = pl.sums + 2 * adf::PLANE_BLOCKS * pl.ops.size();
+        pl.ops.push_back(op);
+        h->launches++;
+        k_plane_adj<<<adf::PLANE_BLOCKS, 256, 0, h->stream>>>(h->g, lslot[op.slot], op.dim, op.idx, op.t1, op.t2,
+                                                              sums);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// Adjoint of the corrected policy's whole-range periodic copies (fold = 0) or
+// folds (fold = 1) of the slots `ids`, with the mirror folds of J at
+// reflecting walls (fold = 1 on the J slots): dimensions and sides reversed.
+static int periodic_full_adj(emoo_handle *h, double *const *lslot, const int *ids, int nids, int fold) {
+    const Geom &g = h->g;
+    adf::Slots9T<double> fl{};
+    for (int k = 0; k < nids; k++) fl.p[k] = lslot[ids[k]];
+    dim3 blk(32, 8);
+    for (int d = 2; d >= 0; d--) {
+        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) {
+            if (!fold) continue;
+            for (int r = 1; r >= 0; r--) {
+                if (h->bc.pbc[2 * d + r] != PBC_REFLECTING) continue;
+                dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, 3);
+                h->launches++;
+                adf::k_mirror_fold_adj<double><<<grd, blk, 0, h->stream>>>(g, fl, d, r);
+            }
+            continue;
+        }
+        dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, nids);
+        h->launches++;
+        adf::k_periodic_full_adj<double><<<grd, blk, 0, h->stream>>>(g, fl, d, fold);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+template <bool REL>
+static void launch_adj(emoo_handle *h, bool corr, const SpeciesTab &st, CPArr P, FPtrs F, PArr LP, int64_t np,
+                       JPtrs LJ, FOut LF) {
+    const int nb = pblocks_all(np);
+    if (corr)
+        k_adj_particles<REL, true><<<nb, 256, 0, h->stream>>>(h->g, st, h->bc, P, F, LP, np, h->dtp, LJ, LF);
+    else
+        k_adj_particles<REL, false><<<nb, 256, 0, h->stream>>>(h->g, st, h->bc, P, F, LP, np, h->dtp, LJ, LF);
+}
+
+// adjoint of one step, given the state before it (snapshot S)
 static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, double *const *lslot, PlaneLedger &pl) {
     const Geom &g = h->g;
+    const bool corr = corrected(h);
     const int b1 = S.bswap ^ 1;  // B roles after the step's Yee update
-    // 1. executeBC(-1) at the step's time, in reverse
+    // the boundary operations at the step's time and roles
     std::vector<AdBcOp> ops;
     {
         const double t_save = h->t;
@@ -651,60 +872,74 @@ static int adj_step(emoo_handle *h, AdRun &R, const Snapshot &S, double **L, dou
         h->bswap = b_save;
         EMOO_TRY(rc);
     }
-    for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
-        const AdBcOp &op = *it;
-        if (op.kind == 0) {
-            Slots6 fl{{lslot[EMOO_EX], lslot[EMOO_EY], lslot[EMOO_EZ], lslot[EMOO_BX], lslot[EMOO_BY], lslot[EMOO_BZ]}};
-            for (int d = 2; d >= 0; d--) {
-                if (!((op.mask >> d) & 1)) continue;
-                const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-                dim3 blk(32, 8);
-                dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 6);
-                for (int side = 1; side >= 0; side--) {
-                    h->launches++;
-                    k_ghost_adj<<<grd, blk, 0, h->stream>>>(g, fl, d, side);
-                }
-            }
-        } else {
-            if (pl.ops.size() >= pl.cap) return EMOO_ERR_STATE;
-            double *sums = pl.sums + 2 * adf::PLANE_BLOCKS * pl.ops.size();
-            pl.ops.push_back(op);
-            h->launches++;
-            k_plane_adj<<<adf::PLANE_BLOCKS, 256, 0, h->stream>>>(g, lslot[op.slot], op.dim, op.idx, op.t1, op.t2,
-                                                                  sums);
-        }
-    }
-    EMOO_CUDA(cudaGetLastError());
-    // 2. Yee update, in reverse (B then E), roles after the step
     FOut A = field_out(lslot, b1);
     JPtrs LJ{{lslot[EMOO_JX], lslot[EMOO_JY], lslot[EMOO_JZ]}};
     dim3 blk(32, 8);
-    h->launches += 2;
     const adf::YeeCoef<double> yc = adf::yee_coef<double>(g, h->dtp);
-    k_yee_b_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A);
-    k_yee_e_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A, LJ);
-    // 3. the J fold, in reverse
-    for (int d = 2; d >= 0; d--) {
-        if (h->bc.fbc[2 * d] != FBC_PERIODIC) continue;
-        const int f0 = (d == 0) ? EMOO_JY : EMOO_JX;
-        const int f1 = (d == 2) ? EMOO_JY : EMOO_JZ;
-        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
-        dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 2);
+    if (corr) {
+        // forward: E half, E images, planes, B half, E/B/B_tm1 images, planes
+        static const int ids_e[3] = {EMOO_EX, EMOO_EY, EMOO_EZ};
+        static const int ids9[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ,
+                                    EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
+        static const int ids_j[3] = {EMOO_JX, EMOO_JY, EMOO_JZ};
+        EMOO_TRY(planes_adj(h, ops, lslot, pl));
+        EMOO_TRY(periodic_full_adj(h, lslot, ids9, 9, 0));
+        h->launches += 2;
+        k_yee_b_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A);
+        // the B half overwrote the B role's physical points: the values the
+        // planes set there between the halves reach nothing
+        adf::Slots9T<double> lb{{A.B[0], A.B[1], A.B[2]}};
+        adf::k_clear_phys<double><<<dim3((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]), blk, 0, h->stream>>>(g, lb);
+        EMOO_TRY(planes_adj(h, ops, lslot, pl));
+        EMOO_TRY(periodic_full_adj(h, lslot, ids_e, 3, 0));
         h->launches++;
-        k_fold_adj<<<grd, blk, 0, h->stream>>>(g, d, lslot[f0], lslot[f1]);
+        k_yee_e_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A, LJ);
+        EMOO_TRY(periodic_full_adj(h, lslot, ids_j, 3, 1));
+    } else {
+        // 1. executeBC(-1), in reverse
+        for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
+            const AdBcOp &op = *it;
+            if (op.kind == 0) {
+                Slots6 fl{{lslot[EMOO_EX], lslot[EMOO_EY], lslot[EMOO_EZ], lslot[EMOO_BX], lslot[EMOO_BY],
+                           lslot[EMOO_BZ]}};
+                for (int d = 2; d >= 0; d--) {
+                    if (!((op.mask >> d) & 1)) continue;
+                    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+                    dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 6);
+                    for (int side = 1; side >= 0; side--) {
+                        h->launches++;
+                        k_ghost_adj<<<grd, blk, 0, h->stream>>>(g, fl, d, side);
+                    }
+                }
+            } else {
+                const std::vector<AdBcOp> one(1, op);
+                EMOO_TRY(planes_adj(h, one, lslot, pl));
+            }
+        }
+        EMOO_CUDA(cudaGetLastError());
+        // 2. Yee update, in reverse (B then E), roles after the step
+        h->launches += 2;
+        k_yee_b_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A);
+        k_yee_e_adj<<<grid_all(g, blk), blk, 0, h->stream>>>(g, yc, A, LJ);
+        // 3. the J fold, in reverse
+        for (int d = 2; d >= 0; d--) {
+            if (h->bc.fbc[2 * d] != FBC_PERIODIC) continue;
+            const int f0 = (d == 0) ? EMOO_JY : EMOO_JX;
+            const int f1 = (d == 2) ? EMOO_JY : EMOO_JZ;
+            const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+            dim3 grd((g.n[o2] + 31) / 32, (g.n[o1] + 7) / 8, 2);
+            h->launches++;
+            k_fold_adj<<<grd, blk, 0, h->stream>>>(g, d, lslot[f0], lslot[f1]);
+        }
     }
-    // 4. particles: deposit, boundaries, push, gather, in reverse
+    // particles: deposit, boundaries, push, gather, in reverse
     SpeciesTab st;
     species_tab(h, h->dtp, st);
     PArr LP{{L[0], L[1], L[2], L[3], L[4], L[5], L[6]}};
     FOut LF = field_out(lslot, S.bswap);
     h->launches++;
-    if (R.rel)
-        k_adj_particles<true><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, R.snap_particles(S), R.snap_fields(S),
-                                                                   LP, R.np, h->dtp, LJ, LF);
-    else
-        k_adj_particles<false><<<pblocks(R.np), 256, 0, h->stream>>>(g, st, h->bc, R.snap_particles(S),
-                                                                    R.snap_fields(S), LP, R.np, h->dtp, LJ, LF);
+    if (R.rel) launch_adj<true>(h, corr, st, R.snap_particles(S), R.snap_fields(S), LP, R.np, LJ, LF);
+    else launch_adj<false>(h, corr, st, R.snap_particles(S), R.snap_fields(S), LP, R.np, LJ, LF);
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }
@@ -717,7 +952,9 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
                            emoo_ad_result *out, double *grad_theta, double *grad_v) {
     if (!h || !spec || !out) return EMOO_ERR_ARG;
     if (h->host_mode) return EMOO_ERR_STATE;  // it steps the particle store
-    if (h->info.electrostatic == 1 || h->policy != EMOO_POLICY_REFERENCE) return EMOO_ERR_UNSUPPORTED;
+    if (h->info.electrostatic == 1) return EMOO_ERR_UNSUPPORTED;
+    // the mixed form's differentiated step is the reference policy's only
+    if (h->precision == EMOO_MIXED && h->policy != EMOO_POLICY_REFERENCE) return EMOO_ERR_UNSUPPORTED;
     if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
         return EMOO_ERR_ARG;
@@ -852,7 +1089,7 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
         EMOO_TRY(ad_bc_ops(h, ops));
         size_t per = 0;
         for (const AdBcOp &op : ops) per += op.kind == 1;
-        pl.cap = per * (size_t)N;
+        pl.cap = per * (size_t)N * (corrected(h) ? 2 : 1);  // the corrected step sets them twice
         if (pl.cap && !(pl.sums = R.alloc(2 * adf::PLANE_BLOCKS * pl.cap))) return EMOO_ERR_OOM;
         pl.ops.reserve(pl.cap);
     }

@@ -30,6 +30,10 @@ template <class R>
 struct Slots6T {
     R *p[6];
 };
+template <class R>
+struct Slots9T {
+    R *p[9];
+};
 
 __device__ __forceinline__ bool phys(const Geom &g, int i, int j, int k) {
     return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];
@@ -151,6 +155,79 @@ __global__ void k_ghost_adj(Geom g, Slots6T<R> fl, int d, int side) {
     const int64_t ps = gidx(g, is[0], is[1], is[2]), pd = gidx(g, it[0], it[1], it[2]);
     F[ps] += F[pd];
     F[pd] = (R)0;
+}
+
+// ---- corrected policy ------------------------------------------------------
+//
+// Adjoint of the whole-range periodic operations along d, per transverse
+// point of the (n+3)^2 plane, the forward steps reversed (so any n is exact):
+// fold = 1 reverses f[n] += f[0], f[1] += f[n+1], f[2] += f[n+2];
+// fold = 0 reverses f[0] = f[n], f[n+1] = f[1], f[n+2] = f[2].
+// One field per blockIdx.z.
+template <class R>
+__global__ void k_periodic_full_adj(Geom g, Slots9T<R> fl, int d, int fold) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= g.tot[o2] || r >= g.tot[o1]) return;
+    R *F = fl.p[blockIdx.z];
+    const int n = g.n[d];
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    auto at = [&](int i) -> R & {
+        c[d] = i;
+        return F[gidx(g, c[0], c[1], c[2])];
+    };
+    if (fold) {
+        at(n + 2) += at(2);
+        at(n + 1) += at(1);
+        at(0) += at(n);
+    } else {
+        at(2) += at(n + 2);
+        at(n + 2) = (R)0;
+        at(1) += at(n + 1);
+        at(n + 1) = (R)0;
+        at(n) += at(0);
+        at(0) = (R)0;
+    }
+}
+
+// Adjoint of the mirror fold at a reflecting wall (dst += s src, src = 0, s =
+// -1 for the component normal to the wall): L[src] = s L[dst]. Same launch
+// shape as the forward; blockIdx.z = component.
+template <class R>
+__global__ void k_mirror_fold_adj(Geom g, Slots9T<R> fl, int d, int right) {
+    const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y * blockDim.y + threadIdx.y;
+    if (q >= g.tot[o2] || r >= g.tot[o1]) return;
+    const int a = blockIdx.z;
+    R *F = fl.p[a];
+    const int n = g.n[d];
+    const bool normal = a == d;
+    const int src = normal ? (right ? n + 1 : 0) : (right ? n + 2 : 0);
+    const int dst = normal ? (right ? n : 1) : (right ? n : 2);
+    int c[3];
+    c[o1] = r;
+    c[o2] = q;
+    c[d] = src;
+    const int64_t ks = gidx(g, c[0], c[1], c[2]);
+    c[d] = dst;
+    const int64_t kd = gidx(g, c[0], c[1], c[2]);
+    F[ks] = normal ? -F[kd] : F[kd];
+}
+
+// Clears three arrays at the physical points (the adjoint of values a step
+// overwrites there).
+template <class R>
+__global__ void k_clear_phys(Geom g, Slots9T<R> fl) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int i = blockIdx.z + 1;
+    if (k > g.n[2] || j > g.n[1]) return;
+    const int64_t p = gidx(g, i, j, k);
+    for (int c = 0; c < 3; c++) fl.p[c][p] = (R)0;
 }
 
 // Adjoint of a plane set v + vs t1[p] t2[q]: the plane's values depend only

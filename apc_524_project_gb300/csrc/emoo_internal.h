@@ -235,6 +235,10 @@ int fold_f64(emoo_handle *h, int dim, int what = FOLD_ALL);
 int fold_full_f64(emoo_handle *h, int what);
 int ghost_full_f64(emoo_handle *h);
 int ghost_e_full_f64(emoo_handle *h);
+// one half of yee_f64 with the current B roles and no boundary work: E (half
+// 0) or B (half 1); and the corrected policy's periodic ghost copies alone
+int yee_half_f64(emoo_handle *h, double dt, int half);
+int periodic_copies_f64(emoo_handle *h, const int *ids, int nids);
 int poisson_field_bc(emoo_handle *h, int id);
 int multigrid_f64(emoo_handle *h, int id1, int id2, int rid, double mult, int *cycles, int *converged);
 int mixed_step_host(emoo_handle *h, double dtp, int fold_what, int store_pre);

@@ -458,6 +458,25 @@ int yee_f64(emoo_handle *h, double dt) {
     return EMOO_OK;
 }
 
+int yee_half_f64(emoo_handle *h, double dt, int half) {
+    const Geom &g = h->g;
+    dim3 blk(32, 8);
+    dim3 grd = phys_grid(g, blk);
+    CF3 T = {{role_t(h, 0), role_t(h, 1), role_t(h, 2)}};
+    h->launches++;
+    if (half == 0) {
+        F3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
+        CF3 J = {{h->slot[EMOO_JX], h->slot[EMOO_JY], h->slot[EMOO_JZ]}};
+        k_yee_e<<<grd, blk, 0, h->stream>>>(g, dt, E, T, J);
+    } else {
+        F3 B = {{role_b(h, 0), role_b(h, 1), role_b(h, 2)}};
+        CF3 E = {{h->slot[EMOO_EX], h->slot[EMOO_EY], h->slot[EMOO_EZ]}};
+        k_yee_b<<<grd, blk, 0, h->stream>>>(g, dt, B, T, E);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 int yee_es_f64(emoo_handle *h, double dt) {
     const Geom &g = h->g;
     dim3 blk(32, 8);
@@ -634,6 +653,8 @@ int ghost_e_full_f64(emoo_handle *h) {
     EMOO_TRY(periodic_full(h, ids, 3, 0));
     return light_all_f64(h);
 }
+
+int periodic_copies_f64(emoo_handle *h, const int *ids, int nids) { return periodic_full(h, ids, nids, 0); }
 
 int ghost_full_f64(emoo_handle *h) {
     static const int ids[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ, EMOO_BX_TM1, EMOO_BY_TM1,

@@ -2,10 +2,10 @@
 
 A Problem holds a workload and its initial particles. Every evaluation
 builds a fresh handle (FP64, or the mixed-precision form: objective and
-adjoint only), loads the particles with the velocity
-perturbation dv added (gamma kept), sets the wave amplitudes and phases and
-the wave shapes (with the envelope coefficients from theta), starts the
-fields and runs emoo_ad_run:
+adjoint only; the reference policy or, FP64 only, the corrected one), loads
+the particles with the velocity perturbation dv added (gamma kept), sets
+the wave amplitudes and phases and the wave shapes (with the envelope
+coefficients from theta), starts the fields and runs emoo_ad_run:
 
   * objective(theta, dv)            the objective alone (the primal loop)
   * tangent(theta, dv, dtheta, ddv) the objective's derivative along a direction
@@ -27,8 +27,9 @@ from . import abi, configs, loading
 
 class Problem:
     def __init__(self, cfg, nsteps=None, slab=(48, 56), checkpoint_every=16, parts=None, objective="field",
-                 species=-1, precision=abi.FP64):
+                 species=-1, precision=abi.FP64, policy=abi.POLICY_REFERENCE):
         self.cfg = cfg
+        self.policy = policy
         self.info0 = configs.input_info(cfg)
         self.nsteps = cfg.steps if nsteps is None else nsteps
         self.slab = slab
@@ -56,6 +57,7 @@ class Problem:
         o = abi.Opts()
         L.emoo_default_opts(C.byref(o))
         o.precision = self.precision
+        o.policy = self.policy
         o.dt = self.cfg.dt
         o.capacity = self.np
         o.rho_background = configs.rho_background(self.cfg)

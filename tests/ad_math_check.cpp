@@ -31,13 +31,8 @@ static void report(const char *what, double got, double want, double tol) {
 }
 
 static CellGeo geo() {
-    CellGeo c;
-    c.d[0] = U(0.5, 1.5);
-    c.d[1] = U(0.5, 1.5);
-    c.d[2] = U(0.5, 1.5);
-    for (int i = 0; i < 3; i++) c.area[i] = c.d[(i + 1) % 3] * c.d[(i + 2) % 3];
-    c.vol = c.d[0] * c.d[1] * c.d[2];
-    return c;
+    const double d0 = U(0.5, 1.5), d1 = U(0.5, 1.5), d2 = U(0.5, 1.5);
+    return make_cell_geo(d0, d1, d2);
 }
 
 // generic check of a map R^n -> R^m given as double and Dual evaluations
@@ -257,6 +252,48 @@ int main() {
                 jterms_m_rev(qd, x, x + 3, l, jt, jt + 3);
             };
             check("mixed jterms", 6, 12, x0, fd, fdual, frev, 1e-7);
+        }
+        // ---- Villasenor-Buneman current: inputs p0[3], p1[3] -> the weights of
+        // up to 4 pieces (zero-padded); the ends stay clear of the cell faces so
+        // the central difference sees the same pieces
+        for (int sub = 0; sub < 4; sub++) {
+            VbGeo vg;
+            for (int a = 0; a < 3; a++) {
+                vg.d[a] = c.d[a];
+                vg.id[a] = 1.0 / c.d[a];
+                vg.x0[a] = U(-2, 2);
+            }
+            const double coef = U(-2, 2);
+            double x0[6];
+            for (int a = 0; a < 3; a++) {
+                const double u0 = std::floor(U(0, 8)) + U(0.05, 0.95);
+                double u1 = u0 + U(-0.9, 0.9);
+                while (u1 - std::floor(u1) < 0.05 || u1 - std::floor(u1) > 0.95) u1 = u0 + U(-0.9, 0.9);
+                x0[a] = vg.x0[a] + u0 * vg.d[a];
+                x0[3 + a] = vg.x0[a] + u1 * vg.d[a];
+            }
+            auto fd = [&](const double *x, double *y) {
+                VbPiece<double> pc[4];
+                for (int i = 0; i < 48; i++) y[i] = 0.0;
+                const int n = vb_eval(vg, x, x + 3, coef, pc);
+                for (int k = 0; k < n; k++)
+                    for (int i = 0; i < 12; i++) y[12 * k + i] = pc[k].W[i];
+            };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual a[3], b[3];
+                VbPiece<Dual> pc[4];
+                for (int i = 0; i < 3; i++) { a[i] = mk(x[i], d[i]); b[i] = mk(x[3 + i], d[3 + i]); }
+                for (int i = 0; i < 48; i++) jd[i] = 0.0;
+                const int n = vb_eval(vg, a, b, coef, pc);
+                for (int k = 0; k < n; k++)
+                    for (int i = 0; i < 12; i++) jd[12 * k + i] = pc[k].W[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                for (int i = 0; i < 6; i++) jt[i] = 0.0;
+                auto lw = [&](int k, const int *, int a, int e) { return l[12 * k + 4 * a + e]; };
+                vb_rev(vg, x, x + 3, coef, lw, jt, jt + 3);
+            };
+            check("vb current", 6, 48, x0, fd, fdual, frev, 1e-7);
         }
     }
     std::printf("%s (%d failures)\n", failures ? "FAILED" : "PASSED", failures);

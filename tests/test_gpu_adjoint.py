@@ -115,3 +115,26 @@ def test_primal_run_is_the_time_loop():
     vol = P.cfg.dx[0] * P.cfg.dx[1] * P.cfg.dx[2]
     g.close()
     assert abs(0.5 * vol * e - obj) <= 1e-12 * obj
+
+
+@pytest.mark.parametrize("policy", ["reference", "corrected"])
+def test_every_particle_gets_its_gradient(policy):
+    """More particles than one thread per particle of a capped grid would
+    reach (2,654,208 > 152 x 64 x 256): with the kinetic energy of all
+    particles as the objective, every particle's velocity gradient is
+    nonzero, the last loaded ones included, and a velocity-direction tangent
+    equals the adjoint's inner product."""
+    from apc_524_project_gb300 import abi
+
+    cfg = configs.tiny("many", n=(48, 48, 48), ppc=12, relativity=1, init="constant", vth=0.05, steps=2, dt=0.3)
+    pol = abi.POLICY_CORRECTED if policy == "corrected" else abi.POLICY_REFERENCE
+    P = Problem(cfg, nsteps=2, slab=(0, 48), checkpoint_every=2, objective="kinetic", policy=pol)
+    assert P.np > 152 * 64 * 256
+    g = P.gradient()
+    gv = g["grad_v"]
+    assert np.all(np.abs(gv).sum(axis=0) > 0)
+    rng = np.random.default_rng(9)
+    ddv = 1e-3 * rng.uniform(-1, 1, (3, P.np))
+    t = P.tangent(np.zeros(P.theta0.shape), ddv)["tangent"]
+    adj = float(np.sum(gv * ddv))
+    assert abs(adj - t) <= DOT_RTOL * abs(t), (adj, t)

@@ -397,7 +397,7 @@ def full_run(cfg, device):
                       "drift_from_step_10": abs(tot[-1] - tot[1]) / abs(tot[1]) if len(tot) > 1 else None})
         else:
             grow = [i * 10 for i, v in enumerate(tot) if not (abs(v) <= 2.0 * abs(tot[1]))] if len(tot) > 1 else []
-            r["first_row_beyond_2x_step_10_energy"] = grow[0] if grow else None
+            r["first_step_beyond_2x_step_10_energy"] = grow[0] if grow else None
         res[name] = r
     return res
 

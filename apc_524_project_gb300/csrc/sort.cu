@@ -1,9 +1,10 @@
 // sort.cu - stable counting sort of particles by (species, cell).
 //
 // The key (species * ncell + cellID, < 2^32) is sorted by least-significant-
-// digit passes of a stable counting sort over 8-bit digits, carrying the
-// original particle index; the SoA payload is then gathered once through the
-// resulting permutation. Each pass: a per-tile digit histogram, an exclusive
+// digit passes of a stable counting sort over digits of up to 9 bits (a
+// 26-bit key takes three passes instead of four 8-bit ones), carrying the
+// original particle index; the SoA payload is then gathered through the
+// resulting permutation, up to four 4-byte arrays per launch. Each pass: a per-tile digit histogram, an exclusive
 // scan of the digit-major (digit, tile) table, and a scatter in which every
 // warp ranks its items in order with __match_any_sync, so equal keys keep
 // their input order (stability) and the permutation is deterministic.
@@ -26,12 +27,14 @@ namespace {
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 16;  // per thread
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
-constexpr int RS_BINS = 256;
+constexpr int RS_BINS = 256;   // 8-bit digits
+constexpr int RS_BINS9 = 512;  // 9-bit digits
 
+template <int BINS>
 __global__ void __launch_bounds__(RS_THREADS) k_hist(const uint32_t *keys, int64_t n, int shift, uint32_t mask,
                                                      uint32_t *hist, int nblocks) {
-    __shared__ uint32_t cnt[RS_BINS];
-    cnt[threadIdx.x] = 0;
+    __shared__ uint32_t cnt[BINS];
+    for (int d = threadIdx.x; d < BINS; d += RS_THREADS) cnt[d] = 0;
     __syncthreads();
     int64_t base = (int64_t)blockIdx.x * RS_TILE;
     for (int i = 0; i < RS_ITEMS; i++) {
@@ -39,24 +42,29 @@ __global__ void __launch_bounds__(RS_THREADS) k_hist(const uint32_t *keys, int64
         if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & mask], 1u);
     }
     __syncthreads();
-    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+    for (int d = threadIdx.x; d < BINS; d += RS_THREADS) hist[(int64_t)d * nblocks + blockIdx.x] = cnt[d];
 }
 
 // One stable counting-sort pass over a tile: rank every item within the tile
 // (warps in order, items of a warp in order), reorder the tile by digit in
 // shared memory, then write each digit's items as one contiguous stretch at
 // the digit's global offset for this tile, so the stores are coalesced.
+// BINS: 256 (8-bit digits) or 512 (9-bit). The per-warp digit counts (at most
+// 32 * RS_ITEMS) and their within-tile offsets (below RS_TILE) fit 16 bits.
+template <int BINS>
 __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, const uint32_t *vin, uint32_t *kout,
                                                         uint32_t *vout, int64_t n, int shift, uint32_t mask,
                                                         const uint32_t *hist, int nblocks) {
-    __shared__ uint32_t wc[RS_THREADS / 32][RS_BINS];
+    static_assert(BINS % RS_THREADS == 0 && RS_TILE <= 65535, "digits per thread; 16-bit counts");
+    constexpr int DPT = BINS / RS_THREADS;  // digits per thread
+    __shared__ uint16_t wc[RS_THREADS / 32][BINS];
     __shared__ uint32_t s_key[RS_TILE];
     __shared__ uint32_t s_val[RS_TILE];
-    __shared__ uint32_t s_start[RS_BINS];  // tile-local start of each digit
-    __shared__ uint32_t s_gbase[RS_BINS];  // global start of each digit's stretch from this tile
+    __shared__ uint32_t s_start[BINS];  // tile-local start of each digit
+    __shared__ uint32_t s_gbase[BINS];  // global start of each digit's stretch from this tile
     __shared__ uint32_t s_wsum[RS_THREADS / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < (RS_THREADS / 32) * RS_BINS; i += RS_THREADS) (&wc[0][0])[i] = 0;
+    for (int i = threadIdx.x; i < (RS_THREADS / 32) * BINS; i += RS_THREADS) (&wc[0][0])[i] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * (32 * RS_ITEMS);
     // keys and values are read again when the tile is placed, and the ranks
@@ -77,23 +85,30 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
             uint32_t dg = (key[c] >> shift) & mask;
             unsigned tag = valid ? dg : (0x10000u + lane);
             unsigned peers = __match_any_sync(0xffffffffu, tag);
-            uint32_t b = valid ? wc[w][dg] : 0u;
+            uint32_t b = valid ? (uint32_t)wc[w][dg] : 0u;
             const uint32_t r = b + __popc(peers & lt);
             rank2[c >> 1] = (c & 1) ? (rank2[c >> 1] | (r << 16)) : r;
             __syncwarp();
-            if (valid && lane == __ffs(peers) - 1) wc[w][dg] = b + __popc(peers);
+            if (valid && lane == __ffs(peers) - 1) wc[w][dg] = (uint16_t)(b + __popc(peers));
             __syncwarp();
         }
     }
     __syncthreads();
-    // per digit (one thread each): warp offsets within the tile's digit
-    // stretch, the tile's digit total, then an exclusive scan over digits
-    static_assert(RS_BINS == RS_THREADS, "one thread per digit");
-    const int d = threadIdx.x;
+    // per digit (DPT consecutive digits per thread): warp offsets within the
+    // tile's digit stretch, the tile's digit totals, then an exclusive scan
+    // over digits
+    uint32_t totd[DPT];
     uint32_t tot = 0;
-    for (int ww = 0; ww < RS_THREADS / 32; ww++) {
-        uint32_t t = wc[ww][d];
-        wc[ww][d] = tot;
+#pragma unroll
+    for (int k = 0; k < DPT; k++) {
+        const int d = threadIdx.x * DPT + k;
+        uint32_t t = 0;
+        for (int ww = 0; ww < RS_THREADS / 32; ww++) {
+            const uint32_t x = wc[ww][d];
+            wc[ww][d] = (uint16_t)t;
+            t += x;
+        }
+        totd[k] = t;
         tot += t;
     }
     uint32_t incl = tot;
@@ -104,10 +119,15 @@ __global__ void __launch_bounds__(RS_THREADS) k_scatter(const uint32_t *kin, con
     }
     if (lane == 31) s_wsum[w] = incl;
     __syncthreads();
-    uint32_t wpre = 0;
-    for (int ww = 0; ww < w; ww++) wpre += s_wsum[ww];
-    s_start[d] = wpre + incl - tot;
-    s_gbase[d] = hist[(int64_t)d * nblocks + blockIdx.x];
+    uint32_t run = incl - tot;
+    for (int ww = 0; ww < w; ww++) run += s_wsum[ww];
+#pragma unroll
+    for (int k = 0; k < DPT; k++) {
+        const int d = threadIdx.x * DPT + k;
+        s_start[d] = run;
+        run += totd[k];
+        s_gbase[d] = hist[(int64_t)d * nblocks + blockIdx.x];
+    }
     __syncthreads();
 #pragma unroll
     for (int c = 0; c < RS_ITEMS; c++) {
@@ -247,6 +267,65 @@ int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
     return EMOO_OK;
 }
 
+// Up to four 4-byte arrays through one permutation read: dst[a][i] =
+// src[a][perm[i]] for a < K, four consecutive items per thread as k_gather.
+struct Gather4 {
+    const uint32_t *src[4];
+    uint32_t *dst[4];
+};
+
+template <int K>
+__global__ void k_gather_k(Gather4 g, const uint32_t *__restrict__ perm, int64_t n) {
+    const int64_t n4 = n >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n4; j += stride) {
+        const uint4 pp = __ldg(reinterpret_cast<const uint4 *>(perm) + j);
+        uint4 v[K];
+#pragma unroll
+        for (int a = 0; a < K; a++) {
+            const uint32_t *__restrict__ s = g.src[a];
+            v[a] = make_uint4(s[pp.x], s[pp.y], s[pp.z], s[pp.w]);
+        }
+#pragma unroll
+        for (int a = 0; a < K; a++) reinterpret_cast<uint4 *>(g.dst[a])[j] = v[a];
+    }
+    for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t q = perm[i];
+#pragma unroll
+        for (int a = 0; a < K; a++) g.dst[a][i] = g.src[a][q];
+    }
+}
+
+// Permutes k (<= 4) 4-byte SoA arrays with one launch, each into a scratch
+// buffer of cap 4-byte elements (h->pay4 and h->pay4x, allocated on first
+// use), then swaps every array with its buffer.
+int gather_group4(emoo_handle *h, void **arrs[], int k, const uint32_t *perm, int64_t n) {
+    if (k < 1 || k > 4 || n > h->cap) return EMOO_ERR_STATE;
+    void **scr[4] = {&h->pay4, &h->pay4x[0], &h->pay4x[1], &h->pay4x[2]};
+    for (int a = 0; a < k; a++)
+        if (!*scr[a]) EMOO_CUDA(cudaMalloc(scr[a], sizeof(uint32_t) * (size_t)h->cap));
+    Gather4 g{};
+    for (int a = 0; a < k; a++) {
+        g.src[a] = (const uint32_t *)*arrs[a];
+        g.dst[a] = (uint32_t *)*scr[a];
+    }
+    const int nb = std::max(1, (int)std::min<int64_t>((n / 4 + 255) / 256, 152 * 16));
+    h->launches++;
+    switch (k) {
+        case 1: k_gather_k<1><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
+        case 2: k_gather_k<2><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
+        case 3: k_gather_k<3><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
+        default: k_gather_k<4><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
+    }
+    EMOO_CUDA(cudaGetLastError());
+    for (int a = 0; a < k; a++) {
+        void *t = *arrs[a];
+        *arrs[a] = *scr[a];
+        *scr[a] = t;
+    }
+    return EMOO_OK;
+}
+
 __global__ void k_species_bounds(const uint32_t *keys, int64_t n, int nspec, int64_t ncell, int64_t *bounds) {
     int s = threadIdx.x;
     if (s > nspec) return;
@@ -262,10 +341,16 @@ __global__ void k_species_bounds(const uint32_t *keys, int64_t n, int nspec, int
 
 }  // namespace
 
+// Digit widths: ceil(key_bits / 9) passes of equal width (at most 9 bits);
+// a pass wider than 8 bits uses the 512-bin kernels.
 int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
     if (n <= 0) return EMOO_OK;
+    const int kb = std::max(1, key_bits);
+    const int passes = (kb + 8) / 9;
+    const int width = (kb + passes - 1) / passes;
+    const int bins = width > 8 ? RS_BINS9 : RS_BINS;
     int nblocks = (int)tiles(n);
-    size_t need_hist = (size_t)RS_BINS * nblocks;
+    size_t need_hist = (size_t)bins * nblocks;
     if (h->hist_cap < need_hist) {
         if (h->hist) cudaFree(h->hist);
         h->hist = nullptr;
@@ -279,23 +364,31 @@ int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
         EMOO_CUDA(cudaMalloc(&h->scan_tmp, need_scan * sizeof(uint32_t)));
         h->scan_cap = need_scan;
     }
-    int passes = std::max(1, (key_bits + 7) / 8);
-    int cur = 0;
+    int cur = 0, shift = 0;
     for (int ps = 0; ps < passes; ps++) {
-        int shift = ps * 8;
-        int bits = std::min(8, key_bits - shift);
-        if (bits <= 0) bits = 1;
-        uint32_t mask = (1u << bits) - 1u;
+        const int bits = std::min(width, kb - shift);
+        const uint32_t mask = (1u << bits) - 1u;
+        const int64_t nh = (int64_t)(bits > 8 ? RS_BINS9 : RS_BINS) * nblocks;
+        const uint32_t *vin = ps == 0 ? nullptr : h->perm[cur];
         h->launches++;
-        k_hist<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], n, shift, mask, h->hist, nblocks);
+        if (bits > 8)
+            k_hist<RS_BINS9><<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], n, shift, mask, h->hist, nblocks);
+        else
+            k_hist<RS_BINS><<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], n, shift, mask, h->hist, nblocks);
         EMOO_CUDA(cudaGetLastError());
-        EMOO_TRY(scan_excl(h, h->hist, (int64_t)need_hist, h->scan_tmp));
+        EMOO_TRY(scan_excl(h, h->hist, nh, h->scan_tmp));
         h->launches++;
-        k_scatter<<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], ps == 0 ? nullptr : h->perm[cur],
-                                                         h->key[cur ^ 1], h->perm[cur ^ 1], n, shift, mask, h->hist,
-                                                         nblocks);
+        if (bits > 8)
+            k_scatter<RS_BINS9><<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], vin, h->key[cur ^ 1],
+                                                                       h->perm[cur ^ 1], n, shift, mask, h->hist,
+                                                                       nblocks);
+        else
+            k_scatter<RS_BINS><<<nblocks, RS_THREADS, 0, h->stream>>>(h->key[cur], vin, h->key[cur ^ 1],
+                                                                      h->perm[cur ^ 1], n, shift, mask, h->hist,
+                                                                      nblocks);
         EMOO_CUDA(cudaGetLastError());
         cur ^= 1;
+        shift += bits;
     }
     // leave the result in slot 0
     if (cur == 1) {
@@ -316,14 +409,11 @@ int gather_payload(emoo_handle *h, int64_t n) {
         EMOO_TRY(gather_one(h, h->vz, perm, n));
         EMOO_TRY(gather_one(h, h->gam, perm, n));
     } else {
-        EMOO_TRY(gather_one(h, h->cell, perm, n));
-        EMOO_TRY(gather_one(h, h->ox, perm, n));
-        EMOO_TRY(gather_one(h, h->oy, perm, n));
-        EMOO_TRY(gather_one(h, h->oz, perm, n));
-        EMOO_TRY(gather_one(h, h->ux, perm, n));
-        EMOO_TRY(gather_one(h, h->uy, perm, n));
-        EMOO_TRY(gather_one(h, h->uz, perm, n));
-        if (h->first_push) EMOO_TRY(gather_one(h, h->g0, perm, n));
+        // the seven (eight before the first push) 4-byte arrays in two launches
+        void **a1[4] = {(void **)&h->cell, (void **)&h->ox, (void **)&h->oy, (void **)&h->oz};
+        EMOO_TRY(gather_group4(h, a1, 4, perm, n));
+        void **a2[4] = {(void **)&h->ux, (void **)&h->uy, (void **)&h->uz, (void **)&h->g0};
+        EMOO_TRY(gather_group4(h, a2, (h->first_push && h->g0) ? 4 : 3, perm, n));
     }
     EMOO_TRY(gather_one(h, h->ids, perm, n));
     return EMOO_OK;
@@ -445,10 +535,10 @@ extern "C" int emoo_sort_permutation_noalloc(const uint32_t *keys, int64_t n, in
         uint32_t *kout = last ? nullptr : sc->key[ps & 1];
         // alternate so that the last pass lands in the caller's array
         uint32_t *vout = ((passes - 1 - ps) % 2 == 0) ? perm : scr_perm;
-        k_hist<<<nblocks, RS_THREADS, 0, s>>>(kin, n, shift, mask, sc->hist, nblocks);
+        k_hist<RS_BINS><<<nblocks, RS_THREADS, 0, s>>>(kin, n, shift, mask, sc->hist, nblocks);
         EMOO_CUDA(cudaGetLastError());
         EMOO_TRY(noalloc_scan(s, sc->hist, nhist, sc->scan));
-        k_scatter<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, mask, sc->hist, nblocks);
+        k_scatter<RS_BINS><<<nblocks, RS_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, mask, sc->hist, nblocks);
         EMOO_CUDA(cudaGetLastError());
         kin = kout;
         vin = vout;

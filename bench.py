@@ -59,8 +59,11 @@ def _args():
     ap.add_argument("--no-corrected", action="store_true")
     ap.add_argument("--no-mixed-error", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
-    ap.add_argument("--only", choices=["poisson", "twostream"], default=None,
+    ap.add_argument("--only", choices=["poisson", "twostream", "adjoint"], default=None,
                     help="run one side measurement alone and print its JSON line")
+    ap.add_argument("--ad-policy", choices=["reference", "corrected"], default="corrected",
+                    help="--only adjoint: the policy differentiated")
+    ap.add_argument("--ad-steps", type=int, default=128, help="--only adjoint: the horizon")
     ap.add_argument("--cpu-procs", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=6)
     return ap.parse_args()
@@ -878,6 +881,22 @@ def main():
                           "value": res["mixed"]["value"], "unit": UNIT, "higher_is_better": True,
                           "dtype": "f32 (mixed) / f64", "data": "synthetic", "config": {"workload": res["workload"]},
                           "twostream": res}), flush=True)
+        return
+    if args.only == "adjoint":
+        # one gradient of the 64^3 laser workload (FP64), timed by emoo_ad_run's events
+        from apc_524_project_gb300 import abi, configs
+        from apc_524_project_gb300.differentiate import Problem
+
+        pol = abi.POLICY_CORRECTED if args.ad_policy == "corrected" else abi.POLICY_REFERENCE
+        P = Problem(configs.laser64(), nsteps=args.ad_steps, slab=(48, 56), checkpoint_every=16, policy=pol)
+        g = P.gradient()
+        ratio = (g["recompute_ms"] + g["reverse_ms"]) / g["forward_ms"]
+        print(json.dumps({"metric": "adjoint / forward cost, laser 64^3 FP64", "value": ratio, "unit": "ratio",
+                          "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": f"laser 64^3, 4,194,304 particles, {args.ad_steps} steps, "
+                                                 f"{args.ad_policy} policy, checkpoints every 16"},
+                          "forward_ms": g["forward_ms"], "recompute_ms": g["recompute_ms"],
+                          "reverse_ms": g["reverse_ms"], "objective": g["objective"]}), flush=True)
         return
     from apc_524_project_gb300 import replicas
 

@@ -666,8 +666,19 @@ __device__ __forceinline__ void vb_pieces_list(const MGeom &g, const BCTab &bc, 
 // written back to the caller's FP64 arrays (Hp) instead of the device store,
 // converted as the loader and readback convert (f64_to_m, m_to_f64), so one
 // launch moves every particle over the host link in both directions at once.
+// Resident blocks per SM the register budget is cut for: 6 (40 registers,
+// no spills) for the reference policy on the device store, where more warps
+// hide the L2 latency that grows as particles drift between sorts (12.59 against
+// 13.06 ms a launch over a 20-step sort interval at 256^3); 5 (48 registers)
+// for the corrected policy's pieces and the host-resident conversions, which
+// spill at 40.
+template <bool CORR, bool HOST>
+constexpr int fused_min_blocks() {
+    return (CORR || HOST) ? 5 : 6;
+}
+
 template <bool REL, bool FIRST, bool PUSH, bool CORR = false, bool HOST = false>
-__global__ void __launch_bounds__(FUSED_BLOCK, 5)
+__global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
     k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
               MDeposit D, int with_rho, const float *g0, DevCounters *ctr, const MHost *__restrict__ Hp,
               int store_pre) {

@@ -666,15 +666,16 @@ __device__ __forceinline__ void vb_pieces_list(const MGeom &g, const BCTab &bc, 
 // written back to the caller's FP64 arrays (Hp) instead of the device store,
 // converted as the loader and readback convert (f64_to_m, m_to_f64), so one
 // launch moves every particle over the host link in both directions at once.
-// Resident blocks per SM the register budget is cut for: 6 (40 registers,
-// no spills) for the reference policy on the device store, where more warps
-// hide the L2 latency that grows as particles drift between sorts (12.59 against
-// 13.06 ms a launch over a 20-step sort interval at 256^3); 5 (48 registers)
-// for the corrected policy's pieces and the host-resident conversions, which
-// spill at 40.
+// Resident blocks per SM the register budget is cut for, measured over a
+// 20-step sort interval at 256^3: 6 (40 registers, no spills) for the
+// reference policy on the device store, where more warps hide the L2 latency
+// that grows as particles drift between sorts (12.59 against 13.06 ms a launch
+// at 5); 4 (64 registers, no spills) for the corrected policy's pieces (19.23
+// against 20.01 ms at 5 with 148 bytes of spills, 24.6 ms at 6); 5 (48
+// registers) for the host-resident conversions.
 template <bool CORR, bool HOST>
 constexpr int fused_min_blocks() {
-    return (CORR || HOST) ? 5 : 6;
+    return CORR ? 4 : (HOST ? 5 : 6);
 }
 
 template <bool REL, bool FIRST, bool PUSH, bool CORR = false, bool HOST = false>

@@ -24,6 +24,13 @@ FD_RTOL = 1e-5      # tangent / adjoint against central differences
 DOT_RTOL = 1e-9     # adjoint against tangent (same discrete derivative)
 
 
+def fd_rounding(objective, h):
+    """The central difference's own rounding: the two objectives carry a
+    few ulps of rounding each (the FP64 deposit's atomics sum in a varying
+    order), divided by 2h. It matters only where the derivative is tiny."""
+    return 8 * np.finfo(float).eps * abs(objective) / h
+
+
 def _problem(every=4):
     cfg = configs.laser64(n=(16, 8, 8), steps=24, ppc=2, wavelength=8.0, fwhm_steps=8)
     return Problem(cfg, nsteps=24, slab=(2, 8), checkpoint_every=every)
@@ -67,7 +74,7 @@ def test_tangent_matches_central_differences(with_theta):
     lp = P.objective(P.theta0 + h * dth, h * ddv)
     lm = P.objective(P.theta0 - h * dth, -h * ddv)
     fd = (lp - lm) / (2 * h)
-    assert abs(fd - t) <= FD_RTOL * abs(t), (fd, t)
+    assert abs(fd - t) <= FD_RTOL * abs(t) + fd_rounding(lp, h), (fd, t)
 
 
 def test_wave_gradient_matches_central_differences():

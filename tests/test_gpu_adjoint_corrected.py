@@ -30,6 +30,14 @@ pytestmark = pytest.mark.gpu
 FD_RTOL = 1e-5
 DOT_RTOL = 1e-9
 
+
+def fd_rounding(objective, h):
+    """The central difference's own rounding: the two objectives carry a
+    few ulps of rounding each (the FP64 deposit's atomics sum in a varying
+    order), divided by 2h. It matters only where the derivative is tiny."""
+    return 8 * np.finfo(float).eps * abs(objective) / h
+
+
 WALLS = {
     "reflecting": ("reflecting", "reflecting"),
     "absorbing": ("absorbing", "absorbing"),
@@ -73,7 +81,7 @@ def _fd(P, seed, with_theta=True):
     lp = P.objective(P.theta0 + h * dth, h * ddv)
     lm = P.objective(P.theta0 - h * dth, -h * ddv)
     fd = (lp - lm) / (2 * h)
-    assert abs(fd - t) <= FD_RTOL * abs(t), (fd, t)
+    assert abs(fd - t) <= FD_RTOL * abs(t) + fd_rounding(lp, h), (fd, t)
 
 
 @pytest.mark.parametrize("walls", sorted(WALLS))

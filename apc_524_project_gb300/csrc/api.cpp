@@ -386,10 +386,6 @@ void free_particles(emoo_handle *h) {
     h->pay = nullptr;
     if (h->pay4) cudaFree(h->pay4);
     h->pay4 = nullptr;
-    for (auto &q : h->pay4x) {
-        if (q) cudaFree(q);
-        q = nullptr;
-    }
 }
 
 // Particle storage for `cap` particles; existing content is preserved.
@@ -423,10 +419,6 @@ int reserve(emoo_handle *h, int64_t cap) {
     h->pay = nullptr;
     if (h->pay4) cudaFree(h->pay4);
     h->pay4 = nullptr;
-    for (auto &q : h->pay4x) {
-        if (q) cudaFree(q);
-        q = nullptr;
-    }
     // scratch of one array per element size: cap 8-byte elements (also the
     // staging area of the loaders, 7 doubles per particle in chunks) and cap
     // 4-byte elements; the sort swaps each array with the buffer of its size

@@ -156,7 +156,6 @@ struct emoo_handle {
     void *pay = nullptr;   // scratch of cap 8-byte elements (staging, and the sort's 8-byte payload swaps)
     size_t pay_bytes = 0;
     void *pay4 = nullptr;  // scratch of cap 4-byte elements (the sort's 4-byte payload swaps)
-    void *pay4x[3] = {nullptr, nullptr, nullptr};  // three more, for the mixed form's grouped payload gather
     int64_t *d_spec_count = nullptr;
 
     // reductions and counters

@@ -3,8 +3,8 @@
 // The key (species * ncell + cellID, < 2^32) is sorted by least-significant-
 // digit passes of a stable counting sort over digits of up to 9 bits (a
 // 26-bit key takes three passes instead of four 8-bit ones), carrying the
-// original particle index; the SoA payload is then gathered through the
-// resulting permutation, up to four 4-byte arrays per launch. Each pass: a per-tile digit histogram, an exclusive
+// original particle index; the SoA payload is then gathered once through the
+// resulting permutation. Each pass: a per-tile digit histogram, an exclusive
 // scan of the digit-major (digit, tile) table, and a scatter in which every
 // warp ranks its items in order with __match_any_sync, so equal keys keep
 // their input order (stability) and the permutation is deterministic.
@@ -267,65 +267,6 @@ int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
     return EMOO_OK;
 }
 
-// Up to four 4-byte arrays through one permutation read: dst[a][i] =
-// src[a][perm[i]] for a < K, four consecutive items per thread as k_gather.
-struct Gather4 {
-    const uint32_t *src[4];
-    uint32_t *dst[4];
-};
-
-template <int K>
-__global__ void k_gather_k(Gather4 g, const uint32_t *__restrict__ perm, int64_t n) {
-    const int64_t n4 = n >> 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n4; j += stride) {
-        const uint4 pp = __ldg(reinterpret_cast<const uint4 *>(perm) + j);
-        uint4 v[K];
-#pragma unroll
-        for (int a = 0; a < K; a++) {
-            const uint32_t *__restrict__ s = g.src[a];
-            v[a] = make_uint4(s[pp.x], s[pp.y], s[pp.z], s[pp.w]);
-        }
-#pragma unroll
-        for (int a = 0; a < K; a++) reinterpret_cast<uint4 *>(g.dst[a])[j] = v[a];
-    }
-    for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t q = perm[i];
-#pragma unroll
-        for (int a = 0; a < K; a++) g.dst[a][i] = g.src[a][q];
-    }
-}
-
-// Permutes k (<= 4) 4-byte SoA arrays with one launch, each into a scratch
-// buffer of cap 4-byte elements (h->pay4 and h->pay4x, allocated on first
-// use), then swaps every array with its buffer.
-int gather_group4(emoo_handle *h, void **arrs[], int k, const uint32_t *perm, int64_t n) {
-    if (k < 1 || k > 4 || n > h->cap) return EMOO_ERR_STATE;
-    void **scr[4] = {&h->pay4, &h->pay4x[0], &h->pay4x[1], &h->pay4x[2]};
-    for (int a = 0; a < k; a++)
-        if (!*scr[a]) EMOO_CUDA(cudaMalloc(scr[a], sizeof(uint32_t) * (size_t)h->cap));
-    Gather4 g{};
-    for (int a = 0; a < k; a++) {
-        g.src[a] = (const uint32_t *)*arrs[a];
-        g.dst[a] = (uint32_t *)*scr[a];
-    }
-    const int nb = std::max(1, (int)std::min<int64_t>((n / 4 + 255) / 256, 152 * 16));
-    h->launches++;
-    switch (k) {
-        case 1: k_gather_k<1><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
-        case 2: k_gather_k<2><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
-        case 3: k_gather_k<3><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
-        default: k_gather_k<4><<<nb, 256, 0, h->stream>>>(g, perm, n); break;
-    }
-    EMOO_CUDA(cudaGetLastError());
-    for (int a = 0; a < k; a++) {
-        void *t = *arrs[a];
-        *arrs[a] = *scr[a];
-        *scr[a] = t;
-    }
-    return EMOO_OK;
-}
-
 __global__ void k_species_bounds(const uint32_t *keys, int64_t n, int nspec, int64_t ncell, int64_t *bounds) {
     int s = threadIdx.x;
     if (s > nspec) return;
@@ -409,11 +350,14 @@ int gather_payload(emoo_handle *h, int64_t n) {
         EMOO_TRY(gather_one(h, h->vz, perm, n));
         EMOO_TRY(gather_one(h, h->gam, perm, n));
     } else {
-        // the seven (eight before the first push) 4-byte arrays in two launches
-        void **a1[4] = {(void **)&h->cell, (void **)&h->ox, (void **)&h->oy, (void **)&h->oz};
-        EMOO_TRY(gather_group4(h, a1, 4, perm, n));
-        void **a2[4] = {(void **)&h->ux, (void **)&h->uy, (void **)&h->uz, (void **)&h->g0};
-        EMOO_TRY(gather_group4(h, a2, (h->first_push && h->g0) ? 4 : 3, perm, n));
+        EMOO_TRY(gather_one(h, h->cell, perm, n));
+        EMOO_TRY(gather_one(h, h->ox, perm, n));
+        EMOO_TRY(gather_one(h, h->oy, perm, n));
+        EMOO_TRY(gather_one(h, h->oz, perm, n));
+        EMOO_TRY(gather_one(h, h->ux, perm, n));
+        EMOO_TRY(gather_one(h, h->uy, perm, n));
+        EMOO_TRY(gather_one(h, h->uz, perm, n));
+        if (h->first_push) EMOO_TRY(gather_one(h, h->g0, perm, n));
     }
     EMOO_TRY(gather_one(h, h->ids, perm, n));
     return EMOO_OK;

@@ -5,9 +5,9 @@ The corrected step's transposes: the charge-conserving current of each move
 (ad_math.cuh vb_eval / vb_rev) and its exit piece at absorbing walls, the
 whole-range periodic folds and ghost copies, the mirror fold at reflecting
 walls, and the plane sets between the Yee halves and after them. Cases: the
-small laser case of tests/test_gpu_adjoint.py with reflecting and with
-absorbing x walls, and a fully periodic thermal box differentiated with
-respect to the particle velocities.
+small laser case of tests/test_gpu_adjoint.py with reflecting, absorbing
+and mixed (reflecting left, absorbing right) x walls, and a fully periodic
+thermal box differentiated with respect to the particle velocities.
 
   * the adjoint gradient is the transpose of the tangent (dot-product test);
   * the tangent equals central finite differences of the primal objective;
@@ -41,6 +41,7 @@ def fd_rounding(objective, h):
 WALLS = {
     "reflecting": ("reflecting", "reflecting"),
     "absorbing": ("absorbing", "absorbing"),
+    "mixed": ("reflecting", "absorbing"),
 }
 
 

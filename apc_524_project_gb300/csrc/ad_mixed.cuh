@@ -71,14 +71,15 @@ AD_HD void gather_m_rev_offsets(const R pk[18], const R o[3], const R lf[6], R l
 // Field weights of the gather: E component i reads its 4 edge points
 // (F00, F10, F11, F01 over (t, r)) with (a_t a_r, b_t a_r, b_t b_r, a_t b_r),
 // B component i its 2 face points of B + B_tm1 with (a_i / 2, b_i / 2);
-// a = 2 - o, b = o - 1 (the ghost-offset vertex).
+// a = 2 - o, b = o - 1 (the ghost-offset vertex), or with corr (the corrected
+// policy's true vertex) a = 1 - o, b = o.
 template <class R>
-AD_HD void gather_m_weights(const R o[3], R we[12], R wb[6]) {
+AD_HD void gather_m_weights(const R o[3], R we[12], R wb[6], bool corr = false) {
     R a[3], b[3];
     AD_UNROLL
     for (int k = 0; k < 3; k++) {
-        a[k] = R(2) - o[k];
-        b[k] = o[k] - R(1);
+        a[k] = corr ? R(1) - o[k] : R(2) - o[k];
+        b[k] = corr ? o[k] : o[k] - R(1);
     }
     AD_UNROLL
     for (int i = 0; i < 3; i++) {
@@ -258,6 +259,69 @@ AD_HD void jterms_m_rev(R qd, const R o[3], const R v[3], const R l[12], R lo[3]
         lv[i] += qd * (l0 * aj * ak + l1 * bj * ak + l2 * bj * bk + l3 * aj * bk);
         lo[j] += J * (-l0 * ak + l1 * ak + l2 * bk - l3 * bk);
         lo[k] += J * (-l0 * aj - l1 * bj + l2 * bj + l3 * aj);
+    }
+}
+
+// ---- charge-conserving current, one straight piece (corrected policy) ------
+//
+// The twelve terms of a piece ua -> ub (old-cell units) lying in the cell
+// shifted by c (per axis -1, 0 or 1, decided from the mid-point and held), as
+// vb_piece in particles_mixed.cu: m = (ua + ub) / 2 - c, D = ub - ua, and for
+// axis a with transverse axes j, k:
+//   W[4a .. 4a+3] = qd D_a ddt_a ((1-m_j)(1-m_k) + cr, m_j (1-m_k) - cr,
+//                                 m_j m_k + cr, (1-m_j) m_k - cr),
+// cr = D_j D_k / 12.
+template <class T, class R>
+AD_HD void vb_piece_m_eval(const T ua[3], const T ub[3], R qd, const R ddt[3], const int c[3], T W[12]) {
+    T m[3], D[3];
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        m[a] = R(0.5) * (ua[a] + ub[a]) - R(c[a]);
+        D[a] = ub[a] - ua[a];
+    }
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+        const T wa = qd * D[a] * ddt[a];
+        const T cr = D[jb] * D[kb] * R(1.0 / 12.0);
+        W[4 * a + 0] = wa * ((R(1) - m[jb]) * (R(1) - m[kb]) + cr);
+        W[4 * a + 1] = wa * (m[jb] * (R(1) - m[kb]) - cr);
+        W[4 * a + 2] = wa * (m[jb] * m[kb] + cr);
+        W[4 * a + 3] = wa * ((R(1) - m[jb]) * m[kb] - cr);
+    }
+}
+
+// Adjoint of vb_piece_m_eval: l[12] the adjoints of the terms; adds the
+// derivatives with respect to the piece's ends to lua and lub.
+template <class R>
+AD_HD void vb_piece_m_rev(const R ua[3], const R ub[3], R qd, const R ddt[3], const int c[3], const R l[12],
+                          R lua[3], R lub[3]) {
+    R m[3], D[3], lD[3] = {R(0), R(0), R(0)}, lm[3] = {R(0), R(0), R(0)};
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        m[a] = R(0.5) * (ua[a] + ub[a]) - R(c[a]);
+        D[a] = ub[a] - ua[a];
+    }
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        const int jb = (a + 1) % 3, kb = (a + 2) % 3;
+        const R l0 = l[4 * a], l1 = l[4 * a + 1], l2 = l[4 * a + 2], l3 = l[4 * a + 3];
+        const R wa = qd * D[a] * ddt[a];
+        const R cr = D[jb] * D[kb] * R(1.0 / 12.0);
+        const R mj = m[jb], mk = m[kb];
+        const R lwa = l0 * ((R(1) - mj) * (R(1) - mk) + cr) + l1 * (mj * (R(1) - mk) - cr) + l2 * (mj * mk + cr) +
+                      l3 * ((R(1) - mj) * mk - cr);
+        const R lcr = wa * (l0 - l1 + l2 - l3);
+        lm[jb] += wa * (-l0 * (R(1) - mk) + l1 * (R(1) - mk) + l2 * mk - l3 * mk);
+        lm[kb] += wa * (-l0 * (R(1) - mj) - l1 * mj + l2 * mj + l3 * (R(1) - mj));
+        lD[a] += qd * ddt[a] * lwa;
+        lD[jb] += lcr * D[kb] * R(1.0 / 12.0);
+        lD[kb] += lcr * D[jb] * R(1.0 / 12.0);
+    }
+    AD_UNROLL
+    for (int a = 0; a < 3; a++) {
+        lua[a] += -lD[a] + R(0.5) * lm[a];
+        lub[a] += lD[a] + R(0.5) * lm[a];
     }
 }
 

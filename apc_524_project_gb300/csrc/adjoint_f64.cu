@@ -953,8 +953,6 @@ extern "C" int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, c
     if (!h || !spec || !out) return EMOO_ERR_ARG;
     if (h->host_mode) return EMOO_ERR_STATE;  // it steps the particle store
     if (h->info.electrostatic == 1) return EMOO_ERR_UNSUPPORTED;
-    // the mixed form's differentiated step is the reference policy's only
-    if (h->precision == EMOO_MIXED && h->policy != EMOO_POLICY_REFERENCE) return EMOO_ERR_UNSUPPORTED;
     if (mode < EMOO_AD_FORWARD || mode > EMOO_AD_ADJOINT) return EMOO_ERR_ARG;
     if (spec->nsteps < 0 || spec->slab_lo < 0 || spec->slab_hi > h->g.n[0] || spec->slab_lo >= spec->slab_hi)
         return EMOO_ERR_ARG;

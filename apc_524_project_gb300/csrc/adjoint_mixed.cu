@@ -3,7 +3,10 @@
 // respect to the wave parameters accumulated in FP64.
 //
 // The differentiated step is the mixed loop's step with J only (the push of
-// k_fused_m, the J fold, the FP32 Yee update, executeBC(-1) with LightBC).
+// k_fused_m, the J fold, the FP32 Yee update, executeBC(-1) with LightBC),
+// under either policy: the corrected one's reverse adds the adjoints of the
+// charge-conserving current (particles_mixed.cu), the whole-range folds and
+// copies, the mirror folds and the planes set between the Yee halves.
 // State is checkpointed every `checkpoint_every` steps as mixed snapshots
 // (28 bytes per particle, 36 bytes per grid point: a quarter of the FP64
 // form's, so sqrt(N) checkpointing of long horizons fits in HBM); each
@@ -264,6 +267,81 @@ struct LedgerM {
     size_t cap = 0;
 };
 
+// Adjoints of plane sets, last first, each recorded in the ledger.
+int planes_adj_m(emoo_handle *h, const std::vector<AdBcOp> &ops, float *const *lslot, LedgerM &pl) {
+    for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
+        const AdBcOp &op = *it;
+        if (op.kind != 1) continue;
+        if (pl.ops.size() >= pl.cap) return EMOO_ERR_STATE;
+        double *sums = pl.sums + 2 * adf::PLANE_BLOCKS * pl.ops.size();
+        pl.ops.push_back(op);
+        h->launches++;
+        adf::k_plane_adj<float><<<adf::PLANE_BLOCKS, 256, 0, h->stream>>>(h->g, lslot[op.slot], op.dim, op.idx, op.t1,
+                                                                          op.t2, sums);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// Adjoint of the corrected policy's whole-range periodic copies (fold = 0) or
+// folds (fold = 1) of the float adjoint slots `ids`, with the mirror folds of
+// J at reflecting walls (fold = 1): dimensions and sides reversed.
+int periodic_full_adj_m(emoo_handle *h, float *const *lslot, const int *ids, int nids, int fold) {
+    const Geom &g = h->g;
+    adf::Slots9T<float> fl{};
+    for (int k = 0; k < nids; k++) fl.p[k] = lslot[ids[k]];
+    dim3 blk(32, 8);
+    for (int d = 2; d >= 0; d--) {
+        const int o1 = (d == 0) ? 1 : 0, o2 = (d == 2) ? 1 : 2;
+        if (h->bc.fbc[2 * d] != FBC_PERIODIC) {
+            if (!fold) continue;
+            for (int r = 1; r >= 0; r--) {
+                if (h->bc.pbc[2 * d + r] != PBC_REFLECTING) continue;
+                dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, 3);
+                h->launches++;
+                adf::k_mirror_fold_adj<float><<<grd, blk, 0, h->stream>>>(g, fl, d, r);
+            }
+            continue;
+        }
+        dim3 grd((g.tot[o2] + 31) / 32, (g.tot[o1] + 7) / 8, nids);
+        h->launches++;
+        adf::k_periodic_full_adj<float><<<grd, blk, 0, h->stream>>>(g, fl, d, fold);
+    }
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
+// The field part of one corrected step in reverse (forward: J fold, E half,
+// E images, planes, B half, E/B/B_tm1 images, planes), the FP64 form's
+// sequence on the float adjoint slots; leaves the current adjoint in the J
+// slots for the particle kernel.
+int adj_fields_corrected_m(emoo_handle *h, const MSnap &S, const std::vector<AdBcOp> &ops, float *const *lslot,
+                           LedgerM &pl) {
+    static const int ids_e[3] = {EMOO_EX, EMOO_EY, EMOO_EZ};
+    static const int ids9[9] = {EMOO_EX, EMOO_EY, EMOO_EZ, EMOO_BX, EMOO_BY, EMOO_BZ,
+                                EMOO_BX_TM1, EMOO_BY_TM1, EMOO_BZ_TM1};
+    static const int ids_j[3] = {EMOO_JX, EMOO_JY, EMOO_JZ};
+    const Geom &g = h->g;
+    const FOutF A = field_out_f(lslot, S.bswap ^ 1);
+    JPtrsF LJ{{lslot[EMOO_JX], lslot[EMOO_JY], lslot[EMOO_JZ]}};
+    dim3 blk(32, 8);
+    const adf::YeeCoef<float> yc = adf::yee_coef<float>(g, h->dtp);
+    EMOO_TRY(planes_adj_m(h, ops, lslot, pl));
+    EMOO_TRY(periodic_full_adj_m(h, lslot, ids9, 9, 0));
+    h->launches += 2;
+    adf::k_yee_b_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, yc, A);
+    // the B half overwrote the B role's physical points
+    adf::Slots9T<float> lb{{A.B[0], A.B[1], A.B[2]}};
+    adf::k_clear_phys<float><<<dim3((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]), blk, 0, h->stream>>>(g, lb);
+    EMOO_TRY(planes_adj_m(h, ops, lslot, pl));
+    EMOO_TRY(periodic_full_adj_m(h, lslot, ids_e, 3, 0));
+    h->launches++;
+    adf::k_yee_e_adj<float><<<grid_all_m(g, blk), blk, 0, h->stream>>>(g, yc, A, LJ);
+    EMOO_TRY(periodic_full_adj_m(h, lslot, ids_j, 3, 1));
+    EMOO_CUDA(cudaGetLastError());
+    return EMOO_OK;
+}
+
 // adjoint of one step, given the state before it (S) and the cell array of
 // the state after it
 int adj_step_m(emoo_handle *h, AdRunM &R, const MSnap &S, const int32_t *cell_after, float *const lo[3],
@@ -280,6 +358,14 @@ int adj_step_m(emoo_handle *h, AdRunM &R, const MSnap &S, const int32_t *cell_af
         h->t = t_save;
         h->bswap = b_save;
         EMOO_TRY(rc);
+    }
+    if (h->policy == EMOO_POLICY_CORRECTED) {
+        EMOO_TRY(adj_fields_corrected_m(h, S, ops, lslot, pl));
+        const FOutF LF = field_out_f(lslot, S.bswap);
+        const float *lj[3] = {lslot[EMOO_JX], lslot[EMOO_JY], lslot[EMOO_JZ]};
+        float *lE[3] = {LF.E[0], LF.E[1], LF.E[2]}, *lB[3] = {LF.B[0], LF.B[1], LF.B[2]},
+              *lT[3] = {LF.T[0], LF.T[1], LF.T[2]};
+        return mixed_ad_particles(h, R.view(S), cell_after, lo, lu, lj, lE, lB, lT, mismatch);
     }
     for (auto it = ops.rbegin(); it != ops.rend(); ++it) {
         const AdBcOp &op = *it;
@@ -450,7 +536,7 @@ int ad_run_mixed(emoo_handle *h, const emoo_ad_spec *spec, int mode, emoo_ad_res
         EMOO_TRY(ad_bc_ops(h, ops));
         size_t per = 0;
         for (const AdBcOp &op : ops) per += op.kind == 1;
-        pl.cap = per * (size_t)N;
+        pl.cap = per * (size_t)N * (h->policy == EMOO_POLICY_CORRECTED ? 2 : 1);  // corrected: set twice a step
         if (pl.cap && !(pl.sums = (double *)R.alloc(sizeof(double) * 2 * adf::PLANE_BLOCKS * pl.cap)))
             return EMOO_ERR_OOM;
         pl.ops.reserve(pl.cap);

@@ -552,22 +552,35 @@ __device__ __forceinline__ void list_append(DepList &L, const MDeposit &D, int l
 // old cell's units (ix, iy, iz that cell): its cell's linear index (wrapped
 // into [1, n] along periodic axes; a ghost cell along walled ones) and its
 // twelve terms.
-__device__ __forceinline__ void vb_piece(const MGeom &g, const int io[3], const float ua[3], const float ub[3],
-                                         float qd, int &ct, float W[DEP_JSLOTS]) {
-    float m[3], Dd[3];
-    ct = 0;
+// The cell of the piece ua -> ub: its shift c (-1, 0, 1 per axis) from the
+// mid-point and its linear index, wrapped into [1, n] along periodic axes, the
+// ghost cell 0 or n + 1 along walled ones (mirrored back by the fold at a
+// reflecting wall). Shared by the loop and its adjoint, so both place a piece
+// alike.
+__device__ __forceinline__ int vb_piece_cell(const MGeom &g, const int io[3], const float ua[3], const float ub[3],
+                                             int c[3]) {
+    int ct = 0;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         const float mid = 0.5f * (ua[a] + ub[a]);
-        const bool below = mid < 0.0f, above = mid >= 1.0f;
-        const int c = below ? -1 : (above ? 1 : 0);
-        m[a] = mid - (below ? -1.0f : (above ? 1.0f : 0.0f));  // no int-to-float conversion (FP64 pipe)
-        Dd[a] = ub[a] - ua[a];
-        int ii = io[a] + c;
-        // periodic: wrapped into [1, n]; walled: the ghost cell 0 or n + 1
-        // (mirrored back by the fold at a reflecting wall)
+        c[a] = mid < 0.0f ? -1 : (mid >= 1.0f ? 1 : 0);
+        int ii = io[a] + c[a];
         if (g.wrap[a]) ii = ii < 1 ? ii + g.n[a] : (ii > g.n[a] ? ii - g.n[a] : ii);
         ct += ii * (a == 0 ? (int)g.sx : a == 1 ? (int)g.sy : 1);
+    }
+    return ct;
+}
+
+__device__ __forceinline__ void vb_piece(const MGeom &g, const int io[3], const float ua[3], const float ub[3],
+                                         float qd, int &ct, float W[DEP_JSLOTS]) {
+    float m[3], Dd[3];
+    int c[3];
+    ct = vb_piece_cell(g, io, ua, ub, c);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float mid = 0.5f * (ua[a] + ub[a]);
+        m[a] = mid - (c[a] < 0 ? -1.0f : (c[a] > 0 ? 1.0f : 0.0f));  // no int-to-float conversion (FP64 pipe)
+        Dd[a] = ub[a] - ua[a];
     }
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -1423,6 +1436,117 @@ struct MSnapC {
     const float *o[3], *u[3];
 };
 
+// Adjoint of vb_pieces_list's current for one particle (corrected policy):
+// the pieces are placed again with the loop's own operations (crossing
+// times by __fdividef, the three-element ordering, fminf, fmaf and
+// vb_piece_cell), so each piece lands in the primal's cell; the adjoint of a
+// piece's twelve terms is the current adjoint at its cell's points times q0
+// (the Jx index of the corrected policy: slot q = 3 at cell + 1); the chain
+// goes back through the piece ends and the crossing times to the move's
+// start s and end e (old-cell units), added to ls and le. The exit pieces at
+// absorbing walls likewise (their wall-plane coordinate is a constant).
+__device__ __forceinline__ int vb_point_m(const MGeom &g, int ct, int q) {
+    return ct + (q == 3 ? 1 : dep_offset(q, (int)g.sx, (int)g.sy));
+}
+
+__device__ void vb_adj_m(const MGeom &g, const BCTab &bc, const MAdjJ &LJ, float q0, const int io[3], const float s[3],
+                         const float e[3], float qd, float ls[3], float le[3]) {
+    float t[3];
+    int ax[3] = {0, 1, 2};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const bool lo = e[a] < 0.0f, hi = e[a] >= 1.0f;
+        t[a] = (lo || hi) ? __fdividef((hi ? 1.0f : 0.0f) - s[a], e[a] - s[a]) : 2.0f;
+    }
+    // the ordering network of vb_pieces_list, carrying each time's axis
+    auto cs = [&](int i, int j) {
+        if (t[j] < t[i]) {
+            const float tt = t[i];
+            t[i] = t[j];
+            t[j] = tt;
+            const int q = ax[i];
+            ax[i] = ax[j];
+            ax[j] = q;
+        }
+    };
+    cs(0, 1);
+    cs(1, 2);
+    cs(0, 1);
+    float de[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) de[a] = e[a] - s[a];
+    float lt[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float ta = k == 0 ? 0.0f : fminf(t[k - 1], 1.0f);
+        const float tb = k == 3 ? 1.0f : fminf(t[k], 1.0f);
+        if (!(tb > ta)) continue;
+        float ua[3], ub[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            ua[a] = fmaf(ta, de[a], s[a]);
+            ub[a] = fmaf(tb, de[a], s[a]);
+        }
+        int c[3];
+        const int ct = vb_piece_cell(g, io, ua, ub, c);
+        float l[12];
+#pragma unroll
+        for (int q = 0; q < 12; q++) l[q] = q0 * LJ.J[q >> 2][vb_point_m(g, ct, q)];
+        float lua[3] = {0.0f, 0.0f, 0.0f}, lub[3] = {0.0f, 0.0f, 0.0f};
+        ad::vb_piece_m_rev(ua, ub, qd, g.ddt, c, l, lua, lub);
+        float lta = 0.0f, ltb = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            ls[a] += lua[a] * (1.0f - ta) + lub[a] * (1.0f - tb);
+            le[a] += lua[a] * ta + lub[a] * tb;
+            lta += lua[a] * de[a];
+            ltb += lub[a] * de[a];
+        }
+        if (k > 0) lt[k - 1] += lta;
+        if (k < 3) lt[k] += ltb;
+    }
+    // a crossing time t = (b - s) / (e - s) of its axis (the others are
+    // constants clamped to 1)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (!(t[k] < 1.0f)) continue;
+        const int a = ax[k];
+        const float id = __fdividef(1.0f, de[a]);
+        ls[a] += lt[k] * (t[k] - 1.0f) * id;
+        le[a] += lt[k] * (-t[k] * id);
+    }
+    const bool absorbs = bc.pbc[0] == PBC_ABSORBING || bc.pbc[1] == PBC_ABSORBING || bc.pbc[2] == PBC_ABSORBING ||
+                         bc.pbc[3] == PBC_ABSORBING || bc.pbc[4] == PBC_ABSORBING || bc.pbc[5] == PBC_ABSORBING;
+    if (!absorbs) return;
+    // the exit pieces: forward to find them, then in reverse
+    float A[4][3];
+    int dk[3], K = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) A[0][a] = e[a];
+    for (int a = 0; a < 3; a++) {
+        const bool left = bc.pbc[2 * a] == PBC_ABSORBING && io[a] == 1 && A[K][a] < 0.0f;
+        const bool right = bc.pbc[2 * a + 1] == PBC_ABSORBING && io[a] == g.n[a] && A[K][a] >= 1.0f;
+        if (!(left || right)) continue;
+        for (int b = 0; b < 3; b++) A[K + 1][b] = A[K][b];
+        A[K + 1][a] = left ? -1.0f : 2.0f;
+        dk[K++] = a;
+    }
+    float lA[3] = {0.0f, 0.0f, 0.0f};
+    for (int k = K - 1; k >= 0; k--) {
+        int c[3];
+        const int ct = vb_piece_cell(g, io, A[k], A[k + 1], c);
+        float l[12];
+#pragma unroll
+        for (int q = 0; q < 12; q++) l[q] = q0 * LJ.J[q >> 2][vb_point_m(g, ct, q)];
+        float la[3] = {0.0f, 0.0f, 0.0f}, lb[3] = {lA[0], lA[1], lA[2]};
+        ad::vb_piece_m_rev(A[k], A[k + 1], qd, g.ddt, c, l, la, lb);
+        lb[dk[k]] = 0.0f;
+        for (int b = 0; b < 3; b++) lA[b] = la[b] + lb[b];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) le[a] += lA[a];
+}
+
 // Grid point, relative to the cell, of each of the 18 gather inputs in the
 // order of gather_m_weights: Ex F00 F10 F11 F01 over (y, z), Ey over (z, x),
 // Ez over (x, y), then the two faces of Bx, By, Bz; 3 bits each (x 4, y 2,
@@ -1443,8 +1567,11 @@ constexpr int ADJ_BLOCK = 256;
 constexpr int ADJ_WARPS = ADJ_BLOCK / 32;
 constexpr int GATHER_IN = 18;
 
-template <bool REL>
-__global__ void __launch_bounds__(ADJ_BLOCK, 4)
+// CORR: the corrected policy (true-vertex gather weights, the adjoint of the
+// charge-conserving current of the move, also for a particle an absorbing
+// wall removed).
+template <bool REL, bool CORR>
+__global__ void __launch_bounds__(ADJ_BLOCK, CORR ? 3 : 4)
     k_adj_particles_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MSnapC S,
                       const int32_t *cell_after, int64_t np, float q0, MAdjState L, MAdjJ LJ, MAdjFields LF,
                       unsigned long long *mismatch) {
@@ -1461,7 +1588,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
     float o_in[3] = {0.0f, 0.0f, 0.0f};
     if (p < np) c = S.cell[p];
     bool zero = false;
-    if (c >= 0 && cell_after) {
+    if (!CORR && c >= 0 && cell_after) {
         // every adjoint this particle's step reads is 0 (its offsets and
         // momenta after the step, the current adjoint where it deposited):
         // then so are all it writes, and the recorded cell after the step
@@ -1491,10 +1618,13 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
         gather_pack(pk, o_in[0], o_in[1], o_in[2], f);
         float u[3] = {u_in[0], u_in[1], u_in[2]}, v[3];
         push_m<REL, false>(f, st.qp[s], nullptr, p, u[0], u[1], u[2], v[0], v[1], v[2]);
-        float o[3];
+        float o[3], nn[3];
         int ii[3] = {ic[0], ic[1], ic[2]};
 #pragma unroll
-        for (int a = 0; a < 3; a++) cell_step(o_in[a] + v[a] * g.dtid[a], ii[a], o[a]);
+        for (int a = 0; a < 3; a++) {
+            nn[a] = o_in[a] + v[a] * g.dtid[a];  // the move's end in the old cell's units
+            cell_step(nn[a], ii[a], o[a]);
+        }
         // bit a: axis a reflected (u, v -> -u, -v); bit 3 + a: its offset mapped
         // to 1 - o (axis_bc keeps an offset of exactly 0)
         int mask = 0, flip = 0;
@@ -1511,17 +1641,18 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
             }
             mask |= m;
         }
-        float lo[3] = {0.0f, 0.0f, 0.0f}, lu[3] = {0.0f, 0.0f, 0.0f};
-        if (!(mask & 64)) {  // a particle removed in this step leaves nothing after it
+        float lo[3] = {0.0f, 0.0f, 0.0f}, lu[3] = {0.0f, 0.0f, 0.0f}, lv[3] = {0.0f, 0.0f, 0.0f};
+        float ls[3] = {0.0f, 0.0f, 0.0f};
+        const bool removed = (mask & 64) != 0;
+        if (!removed) {  // a particle removed in this step leaves nothing after it
             const int32_t onew = ii[0] * (int)g.sx + ii[1] * (int)g.sy + ii[2];
             if (cell_after && cell_after[p] != onew) atomicAdd(mismatch, 1ull);
-            float lv[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 lo[a] = L.o[a][p];
                 lu[a] = L.u[a][p];
             }
-            if (st.deposit[s]) {
+            if (!CORR && st.deposit[s]) {
                 float l12[12];
 #pragma unroll
                 for (int q = 0; q < 12; q++)
@@ -1536,6 +1667,15 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
                 lv[a] = -lv[a];
                 if (flip & (8 << a)) lo[a] = -lo[a];
             }
+        }
+        if (CORR && st.deposit[s]) {
+            // the current of the move (start o_in, end nn, before the boundaries)
+            float le[3] = {0.0f, 0.0f, 0.0f};
+            vb_adj_m(g, bc, LJ, q0, ic, o_in, nn, st.qdep[s], ls, le);
+#pragma unroll
+            for (int a = 0; a < 3; a++) lo[a] += le[a];
+        }
+        if (!removed || CORR) {
             // offset update o' = o + v dt / d (cell held)
 #pragma unroll
             for (int a = 0; a < 3; a++) lv[a] += lo[a] * g.dtid[a];
@@ -1547,6 +1687,8 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
 #pragma unroll
                 for (int a = 0; a < 3; a++) lu[a] = lvb[a];
             }
+#pragma unroll
+            for (int a = 0; a < 3; a++) lo[a] += ls[a];  // the move's start is the offset before the step
             // gather: the offsets through the pack polynomial
             float pkf[18];
             {
@@ -1568,7 +1710,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, 4)
     // the fields through the gather weights, summed over runs of equal cells
     {
         float we[12], wb[6];
-        ad::gather_m_weights(o_in, we, wb);
+        ad::gather_m_weights(o_in, we, wb, CORR);
         float *w = col + lane;
 #pragma unroll
         for (int k = 0; k < 12; k++) w[k * DEP_STRIDE] = we[k] * lf[k >> 2];
@@ -2551,7 +2693,8 @@ int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_a
         dim3 blk(32, 8);
         dim3 pg((g.n[2] + 31) / 32, (g.n[1] + 7) / 8, g.n[0]);
         h->launches++;
-        k_pack_m<false><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);  // the adjoint runs the reference policy
+        if (h->policy == EMOO_POLICY_CORRECTED) k_pack_m<true><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
+        else k_pack_m<false><<<pg, blk, 0, h->stream>>>(mg, P, h->mf->pack);
         EMOO_CUDA(cudaGetLastError());
     }
     MSnapC SC{S.cell, {S.o[0], S.o[1], S.o[2]}, {S.u[0], S.u[1], S.u[2]}};
@@ -2563,12 +2706,18 @@ int mixed_ad_particles(emoo_handle *h, const MSnapView &S, const int32_t *cell_a
     const float q0 = (float)h->mf->q0;
     const unsigned nb = (unsigned)((h->np + 255) / 256);
     h->launches++;
-    if (h->info.relativity)
-        k_adj_particles_m<true><<<nb, 256, 0, h->stream>>>(mg, dv, st, h->bc, h->mf->pack, SC, cell_after, h->np, q0, L,
-                                                           LJ, LF, mismatch);
-    else
-        k_adj_particles_m<false><<<nb, 256, 0, h->stream>>>(mg, dv, st, h->bc, h->mf->pack, SC, cell_after, h->np, q0,
-                                                            L, LJ, LF, mismatch);
+    const bool corr = h->policy == EMOO_POLICY_CORRECTED;
+#define EMOO_ADJ_M(R, C) \
+    k_adj_particles_m<R, C><<<nb, 256, 0, h->stream>>>(mg, dv, st, h->bc, h->mf->pack, SC, cell_after, h->np, q0, L, LJ, \
+                                                       LF, mismatch)
+    if (h->info.relativity) {
+        if (corr) EMOO_ADJ_M(true, true);
+        else EMOO_ADJ_M(true, false);
+    } else {
+        if (corr) EMOO_ADJ_M(false, true);
+        else EMOO_ADJ_M(false, false);
+    }
+#undef EMOO_ADJ_M
     EMOO_CUDA(cudaGetLastError());
     return EMOO_OK;
 }

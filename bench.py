@@ -553,13 +553,17 @@ def poisson_arm(device):
 def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
     """The laser-plasma workload at full size (512 x 128^2 cells, 117,440,512
     electrons, shaped pulse, absorbing x walls, sort every 20 steps): loop
-    throughput of the mixed and FP64 forms, and the mixed-precision adjoint
-    of the named objective (electron kinetic energy at x in [448, 512) after
-    512 steps) with respect to the 16 envelope coefficients, checkpoints
-    every 23 steps (sqrt(512); 47 mixed snapshots of 3.6 GB). Check: on the
-    workload scaled to 40 x 16^2 cells (30 steps, objective x in [8, 16)),
-    the mixed adjoint's derivative for envelope coefficient 1 against a
-    central difference of two FP64 primal runs."""
+    throughput of the mixed form (both policies) and the FP64 form, and the
+    mixed-precision adjoint with respect to the 16 envelope coefficients
+    after 512 steps, checkpoints every 23 steps (sqrt(512); 47 mixed snapshots
+    of 3.6 GB), under the corrected policy: the named objective (electron
+    kinetic energy at x in [448, 512)) and one the pulse reaches (x in
+    [64, 192)); the latter also under the reference policy, whose field
+    energy diverges on this workload (the final field energy of each run is
+    recorded). Check: on the workload scaled to 40 x 16^2 cells (30 steps,
+    objective x in [8, 16)), the mixed adjoint's derivative for envelope
+    coefficient 1 against a central difference of two FP64 primal runs, under
+    the corrected policy."""
     import torch
     from apc_524_project_gb300 import abi, configs
     from apc_524_project_gb300.differentiate import Problem
@@ -571,19 +575,22 @@ def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
                        "pulse with waist 30 and a 16-coefficient sine envelope, absorbing x, sort every 20"}
     cnt = (C.c_int64 * 6)()
     n = C.c_int64()
-    for prec, name, k in ((abi.MIXED, "mixed", steps), (abi.FP64, "fp64", fp64_steps)):
-        h = _make_handle(cfg, prec, N, device)
+    corr, ref = abi.POLICY_CORRECTED, abi.POLICY_REFERENCE
+    for prec, name, k, pol in ((abi.MIXED, "mixed", steps, ref), (abi.FP64, "fp64", fp64_steps, ref),
+                               (abi.MIXED, "mixed_corrected", steps, corr)):
+        h = _make_handle(cfg, prec, N, device, policy=pol)
         for _ in range(warmup if prec == abi.MIXED else 1):
             abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
         t = _timed_steps(h, k, lambda: None)
         abi.check(L.emoo_num_particles(h, -1, C.byref(n)), "emoo_num_particles")
         out[name] = {"value": n.value * k / t, "unit": UNIT, "steps": k, "ms_per_step": t / k * 1e3,
-                     "particles": n.value}
+                     "particles": n.value, "policy": "corrected" if pol == corr else "reference"}
         abi.check(L.emoo_destroy(h))
         torch.cuda.synchronize()
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
-    def adjoint(slab):
-        h = _make_handle(cfg, abi.MIXED, N, device)
+
+    def adjoint(slab, pol):
+        h = _make_handle(cfg, abi.MIXED, N, device, policy=pol)
         nth = L.emoo_ad_nparams(h)
         spec = abi.AdSpec(cfg.steps, ad_every, slab[0], slab[1], abi.AD_OBJ_KINETIC, 0)
         res = abi.AdResult()
@@ -591,19 +598,22 @@ def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
         abi.check(L.emoo_ad_run(h, C.byref(spec), abi.AD_ADJOINT, None, None, C.byref(res), g, None), "emoo_ad_run")
         st = abi.Stats()
         abi.check(L.emoo_get_stats(h, C.byref(st)), "emoo_get_stats")
+        row = (C.c_double * 8)()
+        abi.check(L.emoo_history(h, row), "emoo_history")
         abi.check(L.emoo_destroy(h))
         coef = list(g)[2:]
-        return {"form": "mixed", "steps": cfg.steps, "checkpoint_every": ad_every,
+        return {"form": "mixed", "policy": "corrected" if pol == corr else "reference", "steps": cfg.steps,
+                "checkpoint_every": ad_every,
                 "objective": f"electron kinetic energy, x in [{slab[0]}, {slab[1]})", "value": res.objective,
                 "forward_ms": res.forward_ms, "recompute_ms": res.recompute_ms, "reverse_ms": res.reverse_ms,
                 "adjoint_over_forward": (res.recompute_ms + res.reverse_ms) / res.forward_ms,
                 "max_abs_coef_gradient": max(abs(v) for v in coef), "coef_gradient_l2": math.sqrt(sum(v * v for v in coef)),
-                "cell_mismatch": st.ad_cell_mismatch}
+                "cell_mismatch": st.ad_cell_mismatch, "final_field_energy": row[5] + row[6]}
 
-    named = adjoint((448, 512))
+    named = adjoint((448, 512), corr)
     small = configs.laser512(n=(40, 16, 16), steps=30, ppc=2, wavelength=8.0, fwhm_steps=6, waist=5.0,
                              plasma_x0=8.0, vth=0.02, seed=11)
-    kw = dict(nsteps=30, slab=(8, 16), checkpoint_every=6, objective="kinetic", species=0)
+    kw = dict(nsteps=30, slab=(8, 16), checkpoint_every=6, objective="kinetic", species=0, policy=corr)
     gm = Problem(small, precision=abi.MIXED, **kw).gradient()["grad_theta"]
     P = Problem(small, **kw)
     k = 2  # envelope coefficient 1
@@ -622,10 +632,14 @@ def laser512_arm(device, steps=20, warmup=3, fp64_steps=3, ad_every=23):
                      "exactly 0 by causality")
     out["adjoint"] = named
     out["adjoint"]["fd_check"] = {"case": "laser-plasma 40x16x16, 2 ppc, 30 steps, kinetic energy x in [8, 16), "
-                                          "d objective / d envelope coefficient 1",
+                                          "d objective / d envelope coefficient 1, corrected policy",
                                   "mixed_adjoint": float(gm[k]), "fp64_central_difference": fd,
                                   "rel_err": abs(fd - gm[k]) / abs(fd)}
-    out["adjoint_reachable"] = adjoint((64, 192))
+    out["adjoint_reachable"] = adjoint((64, 192), corr)
+    out["adjoint_reachable_reference_policy"] = adjoint((64, 192), ref)
+    out["adjoint_reachable_reference_policy"]["note"] = (
+        "the reference scheme's field energy diverges on this workload (final_field_energy against the corrected "
+        "run's): its gradient is that of a diverging run")
     return out
 
 

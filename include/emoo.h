@@ -575,9 +575,9 @@ int emoo_restart_info(const char *path, emoo_restart_desc *out);
  * every particle, then vy, then vz, in storage order) give the tangent
  * direction (either may be NULL: zero); grad_theta (emoo_ad_nparams) and
  * grad_v (3 np, same layout) receive the adjoint gradient (either may be
- * NULL). FP64 handles differentiate either policy; mixed-precision handles
- * the reference policy only (EMOO_ERR_UNSUPPORTED under the corrected one).
- * Electrostatic runs are not differentiated (EMOO_ERR_UNSUPPORTED). */
+ * NULL). Both policies, both precisions (mixed-precision handles: objective
+ * and adjoint, no tangent). Electrostatic runs are not differentiated
+ * (EMOO_ERR_UNSUPPORTED). */
 int emoo_ad_run(emoo_handle *h, const emoo_ad_spec *spec, int mode, const double *dtheta, const double *dv,
                 emoo_ad_result *out, double *grad_theta, double *grad_v);
 

@@ -295,6 +295,28 @@ int main() {
             };
             check("vb current", 6, 48, x0, fd, fdual, frev, 1e-7);
         }
+        // ---- the mixed form's piece terms: inputs ua[3], ub[3] -> 12 terms
+        {
+            const double qd = U(-2, 2), ddt[3] = {U(0.5, 3), U(0.5, 3), U(0.5, 3)};
+            const int cs[3] = {-1, 0, 1};
+            double x0[6];
+            for (int a = 0; a < 3; a++) {
+                x0[a] = U(-0.9, 1.9);
+                x0[3 + a] = U(-0.9, 1.9);
+            }
+            auto fd = [&](const double *x, double *y) { vb_piece_m_eval(x, x + 3, qd, ddt, cs, y); };
+            auto fdual = [&](const double *x, const double *d, double *jd) {
+                Dual a[3], b[3], W[12];
+                for (int i = 0; i < 3; i++) { a[i] = mk(x[i], d[i]); b[i] = mk(x[3 + i], d[3 + i]); }
+                vb_piece_m_eval(a, b, qd, ddt, cs, W);
+                for (int i = 0; i < 12; i++) jd[i] = W[i].d;
+            };
+            auto frev = [&](const double *x, const double *l, double *jt) {
+                for (int i = 0; i < 6; i++) jt[i] = 0.0;
+                vb_piece_m_rev(x, x + 3, qd, ddt, cs, l, jt, jt + 3);
+            };
+            check("mixed vb piece", 6, 12, x0, fd, fdual, frev, 1e-7);
+        }
     }
     std::printf("%s (%d failures)\n", failures ? "FAILED" : "PASSED", failures);
     return failures ? 1 : 0;

@@ -13,7 +13,10 @@ thermal box differentiated with respect to the particle velocities.
   * the tangent equals central finite differences of the primal objective;
   * each wave parameter's adjoint derivative equals its central difference;
   * the checkpoint spacing does not change the gradient;
-  * the primal objective run equals the handle's own emoo_step loop.
+  * the primal objective run equals the handle's own emoo_step loop;
+  * the mixed form's adjoint (FP32) gives the FP64 form's gradients to FP32
+    accuracy, on the small laser case with each kind of wall and on the
+    scaled laser-plasma workload (absorbing walls, shaped pulse).
 As for the reference policy, cells and boundary events are held at the
 primal run's; the perturbations are small enough that none changes between
 the finite-difference evaluations at these sizes."""
@@ -170,8 +173,59 @@ def test_primal_run_is_the_time_loop():
     assert abs(0.5 * vol * e - obj) <= 1e-12 * obj
 
 
-def test_mixed_form_refuses_the_corrected_adjoint():
-    P = _laser()
-    P.precision = abi.MIXED
-    with pytest.raises(Exception):
-        P.gradient()
+# ---- the mixed-precision adjoint under the corrected policy -------------------
+
+MIXED_GRAD_RTOL = 2e-3  # mixed-form gradient against the FP64 form's (FP32 forward and adjoint)
+
+
+def _small_laser_plasma(steps=30):
+    """The laser-plasma workload scaled down (40 x 16^2 cells, absorbing x
+    walls, shaped pulse with a 16-coefficient envelope, plasma from x = 8)."""
+    return configs.laser512(n=(40, 16, 16), steps=steps, ppc=2, wavelength=8.0, fwhm_steps=6, waist=5.0,
+                            plasma_x0=8.0, vth=0.02, seed=11)
+
+
+@pytest.mark.parametrize("objective", ["kinetic", "field"])
+def test_mixed_adjoint_matches_fp64_gradient(objective):
+    """The mixed form's run (FP32 state, checkpoints and adjoint) under the
+    corrected policy gives the FP64 form's objective and gradients to FP32
+    accuracy on the small laser-plasma case, and recomputes every step's
+    cells exactly."""
+    cfg = _small_laser_plasma()
+    kw = dict(nsteps=30, slab=(8, 16), checkpoint_every=6, objective=objective, species=0,
+              policy=abi.POLICY_CORRECTED)
+    f = Problem(cfg, **kw).gradient()
+    m = Problem(cfg, precision=abi.MIXED, **kw).gradient()
+    assert m["cell_mismatch"] == 0
+    assert abs(m["objective"] - f["objective"]) <= 1e-4 * abs(f["objective"])
+    gf, gm = f["grad_theta"], m["grad_theta"]
+    err = np.linalg.norm(gm - gf) / np.linalg.norm(gf)
+    assert err <= MIXED_GRAD_RTOL, (err, gf[:6], gm[:6])
+    vf, vm = f["grad_v"], m["grad_v"]
+    assert np.linalg.norm(vm - vf) / np.linalg.norm(vf) <= 10 * MIXED_GRAD_RTOL
+
+
+@pytest.mark.parametrize("walls", sorted(WALLS))
+def test_mixed_adjoint_matches_fp64_on_the_laser_case(walls):
+    """The small laser case with each kind of wall: the mixed form's wave and
+    velocity gradients against the FP64 form's."""
+    P = _laser(walls)
+    f = P.gradient()
+    m = Problem(P.cfg, nsteps=24, slab=(2, 8), checkpoint_every=4, policy=abi.POLICY_CORRECTED,
+                precision=abi.MIXED, parts=P.parts).gradient()
+    assert m["cell_mismatch"] == 0
+    assert abs(m["objective"] - f["objective"]) <= 1e-4 * abs(f["objective"])
+    gf, gm = f["grad_theta"], m["grad_theta"]
+    assert np.linalg.norm(gm - gf) / np.linalg.norm(gf) <= MIXED_GRAD_RTOL, (gf, gm)
+    vf, vm = f["grad_v"], m["grad_v"]
+    assert np.linalg.norm(vm - vf) / np.linalg.norm(vf) <= 10 * MIXED_GRAD_RTOL
+
+
+def test_mixed_adjoint_checkpoint_spacing():
+    cfg = _small_laser_plasma()
+    kw = dict(nsteps=30, slab=(8, 16), objective="kinetic", species=0, policy=abi.POLICY_CORRECTED,
+              precision=abi.MIXED)
+    a = Problem(cfg, checkpoint_every=5, **kw).gradient()
+    b = Problem(cfg, checkpoint_every=30, **kw).gradient()
+    # same forward and reverse arithmetic; only the FP32 atomics' order differs
+    assert np.linalg.norm(a["grad_theta"] - b["grad_theta"]) <= 1e-4 * np.linalg.norm(b["grad_theta"])

@@ -167,14 +167,17 @@ typedef struct emoo_opts {
  * quirks (ghost-offset gather / deposit vertex, the Jx index of Grid::addJ,
  * src/grid/oGrid.cpp:101, ghost copies and folds over the physical
  * transverse range only, current from the velocity at the new position).
- * CORRECTED (no reference counterpart; both forms, periodic boundaries on
- * every side, EMOO_ERR_UNSUPPORTED otherwise): the cell's own lower corner
- * as vertex, the fixed Jx index, Villasenor and Buneman's charge-conserving
+ * CORRECTED (no reference counterpart; both forms; each dimension periodic,
+ * or walled with reflecting or absorbing particle sides and external field
+ * sides, EMOO_ERR_UNSUPPORTED otherwise): the cell's own lower corner as
+ * vertex, the fixed Jx index, Villasenor and Buneman's charge-conserving
  * current along each particle's path (so rho(t + dt) - rho(t) + dt div J = 0
- * and the Gauss-law residual stays at its initial value), periodic copies
- * and folds of every component over the whole range, and E's ghost planes
- * refreshed between the two halves of the Yee update (time-centred at the
- * periodic wrap). */
+ * and the Gauss-law residual stays at its initial value; the current beyond
+ * a reflecting wall folded back as its mirror image, a removed particle's
+ * path continued past an absorbing wall), periodic copies and folds of every
+ * component over the whole range, and E's boundary values (periodic images,
+ * LightBC planes) set between the two halves of the Yee update as well as
+ * after them (time-centred at the wrap and at the planes). */
 #define EMOO_POLICY_REFERENCE 0
 #define EMOO_POLICY_CORRECTED 1
 

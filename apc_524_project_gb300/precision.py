@@ -196,3 +196,35 @@ def measure(cfg, steps_at=(10, 50, 100), members=6, policy=1, device=0, rel=None
         f"fp64_from_{t1}": drift(ref, t1), f"mixed_from_{t1}": drift(mix, t1),
     }
     return out
+
+
+def drift_vs_debye(cfg, omegas=(0.5, 0.2, 0.1), steps=100, start=10, policy=1, device=0):
+    """Total-energy drift of cfg over steps start..steps in both forms at each
+    plasma frequency in `omegas` (the electron Debye length in cells is
+    v_th / omega_pe / dx). A drift that falls as lambda_D/dx grows, equally in
+    both forms, is the explicit scheme's grid heating, not the form's rounding."""
+    import dataclasses
+
+    L = abi.lib()
+    cnt = (C.c_int64 * 6)()
+    vth, dx = cfg.species[0].vth, min(cfg.dx)
+    rows = []
+    for w in omegas:
+        c = dataclasses.replace(cfg, omega_pe=w)
+        row = {"omega_pe": w, "lambda_D_over_dx": vth / w / dx}
+        for prec, name in ((abi.FP64, "fp64"), (abi.MIXED, "mixed")):
+            h = _handle(c, prec, policy, device)
+            tot = {}
+            for t in range(steps + 1):
+                if t in (0, start, steps):
+                    r = (C.c_double * 8)()
+                    abi.check(L.emoo_history(h, r), "emoo_history")
+                    tot[t] = float(r[7])
+                if t < steps:
+                    abi.check(L.emoo_step(h, 1, cnt), "emoo_step")
+            abi.check(L.emoo_check(h), "device error word")
+            abi.check(L.emoo_destroy(h))
+            row[f"{name}_from_{start}"] = abs(tot[steps] - tot[start]) / abs(tot[start])
+            row[f"{name}_from_0"] = abs(tot[steps] - tot[0]) / abs(tot[0])
+        rows.append(row)
+    return rows

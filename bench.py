@@ -59,7 +59,7 @@ def _args():
     ap.add_argument("--no-corrected", action="store_true")
     ap.add_argument("--no-mixed-error", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
-    ap.add_argument("--only", choices=["poisson", "twostream", "adjoint"], default=None,
+    ap.add_argument("--only", choices=["poisson", "twostream", "adjoint", "mixed_error"], default=None,
                     help="run one side measurement alone and print its JSON line")
     ap.add_argument("--ad-policy", choices=["reference", "corrected"], default="corrected",
                     help="--only adjoint: the policy differentiated")
@@ -318,6 +318,9 @@ def mixed_error_arm(device, n=64, members=6):
     r = precision.measure(cfg, steps_at=(10, 50, 100), members=members, policy=abi.POLICY_CORRECTED, device=device)
     r["workload"] = (f"thermal plasma {n}^3 cells, {cfg.total_particles():,} particles (2 species x 16 ppc), "
                      "v_th 0.1c, relativistic, dt 0.5, sort every 20, corrected policy, 100 steps")
+    # the drift at the workload's density (lambda_D = 0.2 dx) next to thinner plasmas
+    r["drift_vs_debye"] = precision.drift_vs_debye(cfg, omegas=(0.5, 0.2, 0.1), policy=abi.POLICY_CORRECTED,
+                                                   device=device)
     r["seconds"] = time.perf_counter() - t0
     worst = max(v["mixed"] for row in r["fields"].values() for v in row.values())
     worst_ratio = max(v["ratio"] or 0.0 for row in r["fields"].values() for v in row.values())
@@ -329,6 +332,7 @@ def mixed_error_arm(device, n=64, members=6):
         "target_rel_l2_1e-4_after_100_steps": worst <= 1e-4,
         "target_observables_1e-4": worst_obs <= 1e-4,
         "target_energy_drift_1e-3": r["energy_drift"]["mixed_from_10"] <= 1e-3,
+        "target_energy_drift_1e-3_at_lambda_D_dx": r["drift_vs_debye"][-1]["mixed_from_10"] <= 1e-3,
     }
     return r
 
@@ -898,6 +902,13 @@ def main():
                           "value": res["mixed"]["value"], "unit": UNIT, "higher_is_better": True,
                           "dtype": "f32 (mixed) / f64", "data": "synthetic", "config": {"workload": res["workload"]},
                           "twostream": res}), flush=True)
+        return
+    if args.only == "mixed_error":
+        res = mixed_error_arm(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"metric": "mixed form's error against FP64 after 100 steps (max rel L2 of E, B, J)",
+                          "value": res["summary"]["max_rel_l2_EBJ"], "unit": "rel L2", "higher_is_better": False,
+                          "dtype": "f32 (mixed) / f64", "data": "synthetic", "config": {"workload": res["workload"]},
+                          "mixed_error": res}), flush=True)
         return
     if args.only == "adjoint":
         # one gradient of the 64^3 laser workload (FP64), timed by emoo_ad_run's events

@@ -481,7 +481,7 @@ int do_sort(emoo_handle *h) {
     else EMOO_TRY(mixed_sort_keys(h));
     bool f64 = h->precision == EMOO_FP64;
     EMOO_TRY(radix_sort_perm(h, h->np, f64 ? key_bits(h) : mixed_key_bits(h)));
-    EMOO_TRY(gather_payload(h, h->np));
+    EMOO_TRY(gather_payload(h, h->np, !f64));
     int64_t cnt[EMOO_NSPEC];
     EMOO_TRY(count_species(h, h->np, f64 ? h->g.ncell : h->g.npts, cnt));
     int64_t off = 0;

@@ -277,7 +277,9 @@ int compact_keys_f64(emoo_handle *h);  // species index, nspec for removed parti
 
 // ---- sort (sort.cu) ----
 int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits);
-int gather_payload(emoo_handle *h, int64_t n);
+// Permutes the particle store through perm[0]; cells_from_keys (mixed form,
+// after mixed_sort_keys): the cells come from the sorted keys instead.
+int gather_payload(emoo_handle *h, int64_t n, bool cells_from_keys = false);
 int count_species(emoo_handle *h, int64_t n, int64_t stride, int64_t *counts_host);
 
 // ---- loader (loader.cu) ----

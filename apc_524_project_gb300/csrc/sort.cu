@@ -339,7 +339,19 @@ int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
     return EMOO_OK;
 }
 
-int gather_payload(emoo_handle *h, int64_t n) {
+// The mixed form's sorted cells straight from the sorted keys (species *
+// npts + cell; removed particles carry keys from live_end on): a streaming
+// pass in place of a gather through the permutation.
+__global__ void k_cells_from_keys(const uint32_t *__restrict__ key, int64_t n, uint32_t npts, uint32_t live_end,
+                                  int32_t *__restrict__ cell) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += stride) {
+        const uint32_t k = key[j];
+        cell[j] = k < live_end ? (int32_t)(k % npts) : -1;
+    }
+}
+
+int gather_payload(emoo_handle *h, int64_t n, bool cells_from_keys) {
     const uint32_t *perm = h->perm[0];
     if (h->precision == EMOO_FP64) {
         EMOO_TRY(gather_one(h, h->x, perm, n));
@@ -349,8 +361,17 @@ int gather_payload(emoo_handle *h, int64_t n) {
         EMOO_TRY(gather_one(h, h->vy, perm, n));
         EMOO_TRY(gather_one(h, h->vz, perm, n));
         EMOO_TRY(gather_one(h, h->gam, perm, n));
+    } else if (cells_from_keys) {
+        // the sort keys of mixed_sort_keys: the cell is the key modulo npts
+        int nb = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+        h->launches++;
+        k_cells_from_keys<<<std::max(nb, 1), 256, 0, h->stream>>>(
+            h->key[0], n, (uint32_t)h->g.npts, (uint32_t)((int64_t)h->nspec * h->g.npts), h->cell);
+        EMOO_CUDA(cudaGetLastError());
     } else {
         EMOO_TRY(gather_one(h, h->cell, perm, n));
+    }
+    if (h->precision != EMOO_FP64) {
         EMOO_TRY(gather_one(h, h->ox, perm, n));
         EMOO_TRY(gather_one(h, h->oy, perm, n));
         EMOO_TRY(gather_one(h, h->oz, perm, n));

@@ -424,7 +424,12 @@ __device__ __forceinline__ void push_m(const float f[6], const float qp, const f
 
 constexpr int FUSED_BLOCK = 256;
 constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
-constexpr int DEP_STRIDE = 33;  // column stride of the deposit transpose (odd: conflict-free both ways)
+constexpr int DEP_STRIDE = 33;  // column stride of the adjoint's transpose (odd: conflict-free both ways)
+// Column stride of the fused kernel's deposit transpose: rows start on
+// 16-byte boundaries, so a lane reads its 16 contributions of a row as four
+// 16-byte loads; the column writes (a warp's 32 lanes, one row) stay
+// conflict-free.
+constexpr int COL_STRIDE = 36;
 
 // One particle from FP64 position, velocity and gamma to the mixed state
 // (cell, in-cell offsets, u); false when the position is outside the box or
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
     k_fused_m(MGeom g, Div3 dv, MSpecies st, BCTab bc, const float4 *__restrict__ pack, MState S, int64_t np,
               MDeposit D, int with_rho, const float *g0, DevCounters *ctr, const MHost *__restrict__ Hp,
               int store_pre) {
-    __shared__ float s_w[FUSED_WARPS][20 * DEP_STRIDE];
+    __shared__ __align__(16) float s_w[FUSED_WARPS][20 * COL_STRIDE];
     __shared__ int s_key[FUSED_WARPS][32];
     constexpr bool VBL = CORR && PUSH;  // the corrected policy's pieces go through a list
     __shared__ float s_pl[VBL ? FUSED_WARPS : 1][DEP_JSLOTS][DEP_LIST + 1];
@@ -830,14 +835,14 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
                     if (with_rho) {  // rho at the new position, true-vertex weights
                         const float qd = st.qdep[s];
                         const float a[3] = {1.0f - ox, 1.0f - oy, 1.0f - oz}, b[3] = {ox, oy, oz};
-                        w[12 * DEP_STRIDE] = qd * a[0] * a[1] * a[2];
-                        w[13 * DEP_STRIDE] = qd * b[0] * a[1] * a[2];
-                        w[14 * DEP_STRIDE] = qd * b[0] * b[1] * a[2];
-                        w[15 * DEP_STRIDE] = qd * a[0] * b[1] * a[2];
-                        w[16 * DEP_STRIDE] = qd * a[0] * b[1] * b[2];
-                        w[17 * DEP_STRIDE] = qd * b[0] * b[1] * b[2];
-                        w[18 * DEP_STRIDE] = qd * b[0] * a[1] * b[2];
-                        w[19 * DEP_STRIDE] = qd * a[0] * a[1] * b[2];
+                        w[12 * COL_STRIDE] = qd * a[0] * a[1] * a[2];
+                        w[13 * COL_STRIDE] = qd * b[0] * a[1] * a[2];
+                        w[14 * COL_STRIDE] = qd * b[0] * b[1] * a[2];
+                        w[15 * COL_STRIDE] = qd * a[0] * b[1] * a[2];
+                        w[16 * COL_STRIDE] = qd * a[0] * b[1] * b[2];
+                        w[17 * COL_STRIDE] = qd * b[0] * b[1] * b[2];
+                        w[18 * COL_STRIDE] = qd * b[0] * a[1] * b[2];
+                        w[19 * COL_STRIDE] = qd * a[0] * a[1] * b[2];
                     }
                 } else if (st.deposit[s]) {
                     active = true;
@@ -853,27 +858,27 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
                     const float qd = st.qdep[s];
                     float jx = qd * vx, jy = qd * vy, jz = qd * vz;
                     float *w = col + lane;
-                    w[0 * DEP_STRIDE] = jx * a[1] * a[2];
-                    w[1 * DEP_STRIDE] = jx * b[1] * a[2];
-                    w[2 * DEP_STRIDE] = jx * b[1] * b[2];
-                    w[3 * DEP_STRIDE] = jx * a[1] * b[2];
-                    w[4 * DEP_STRIDE] = jy * a[2] * a[0];
-                    w[5 * DEP_STRIDE] = jy * b[2] * a[0];
-                    w[6 * DEP_STRIDE] = jy * b[2] * b[0];
-                    w[7 * DEP_STRIDE] = jy * a[2] * b[0];
-                    w[8 * DEP_STRIDE] = jz * a[0] * a[1];
-                    w[9 * DEP_STRIDE] = jz * b[0] * a[1];
-                    w[10 * DEP_STRIDE] = jz * b[0] * b[1];
-                    w[11 * DEP_STRIDE] = jz * a[0] * b[1];
+                    w[0 * COL_STRIDE] = jx * a[1] * a[2];
+                    w[1 * COL_STRIDE] = jx * b[1] * a[2];
+                    w[2 * COL_STRIDE] = jx * b[1] * b[2];
+                    w[3 * COL_STRIDE] = jx * a[1] * b[2];
+                    w[4 * COL_STRIDE] = jy * a[2] * a[0];
+                    w[5 * COL_STRIDE] = jy * b[2] * a[0];
+                    w[6 * COL_STRIDE] = jy * b[2] * b[0];
+                    w[7 * COL_STRIDE] = jy * a[2] * b[0];
+                    w[8 * COL_STRIDE] = jz * a[0] * a[1];
+                    w[9 * COL_STRIDE] = jz * b[0] * a[1];
+                    w[10 * COL_STRIDE] = jz * b[0] * b[1];
+                    w[11 * COL_STRIDE] = jz * a[0] * b[1];
                     if (with_rho) {
-                        w[12 * DEP_STRIDE] = qd * a[0] * a[1] * a[2];
-                        w[13 * DEP_STRIDE] = qd * b[0] * a[1] * a[2];
-                        w[14 * DEP_STRIDE] = qd * b[0] * b[1] * a[2];
-                        w[15 * DEP_STRIDE] = qd * a[0] * b[1] * a[2];
-                        w[16 * DEP_STRIDE] = qd * a[0] * b[1] * b[2];
-                        w[17 * DEP_STRIDE] = qd * b[0] * b[1] * b[2];
-                        w[18 * DEP_STRIDE] = qd * b[0] * a[1] * b[2];
-                        w[19 * DEP_STRIDE] = qd * a[0] * a[1] * b[2];
+                        w[12 * COL_STRIDE] = qd * a[0] * a[1] * a[2];
+                        w[13 * COL_STRIDE] = qd * b[0] * a[1] * a[2];
+                        w[14 * COL_STRIDE] = qd * b[0] * b[1] * a[2];
+                        w[15 * COL_STRIDE] = qd * a[0] * b[1] * a[2];
+                        w[16 * COL_STRIDE] = qd * a[0] * b[1] * b[2];
+                        w[17 * COL_STRIDE] = qd * b[0] * b[1] * b[2];
+                        w[18 * COL_STRIDE] = qd * b[0] * a[1] * b[2];
+                        w[19 * COL_STRIDE] = qd * a[0] * a[1] * b[2];
                     }
                 }
             }
@@ -892,7 +897,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
         if (PL.n) list_flush<true>(PL, D, lane);
         if (vb_dep && active) {
 #pragma unroll
-            for (int q = 0; q < DEP_JSLOTS; q++) col[q * DEP_STRIDE + lane] = wv[q];
+            for (int q = 0; q < DEP_JSLOTS; q++) col[q * COL_STRIDE + lane] = wv[q];
         }
     }
     if (__any_sync(0xffffffffu, mask & 63)) count_cross(ctr, mask & 63);
@@ -905,7 +910,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
     keys[lane] = active ? onew : -1;
     if (!active) {
 #pragma unroll
-        for (int q = 0; q < DEP_SLOTS; q++) col[q * DEP_STRIDE + lane] = 0.0f;
+        for (int q = 0; q < DEP_SLOTS; q++) col[q * COL_STRIDE + lane] = 0.0f;
     }
     __syncwarp();
     const int nq = with_rho ? DEP_SLOTS : 12;
@@ -916,7 +921,7 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
 #pragma unroll
             for (int q = 0; q < DEP_SLOTS; q++) {
                 if (q >= nq) break;
-                long long fx = f2ll_rn(col[q * DEP_STRIDE + lane]);
+                long long fx = f2ll_rn(col[q * COL_STRIDE + lane]);
                 if (fx != 0) atomicAdd((q < 12 ? dj : dr) + dep_pos(q), (unsigned long long)fx);
             }
         }
@@ -934,13 +939,16 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
         const int q = lane & 15, half = lane >> 4;
         if (q < DEP_JSLOTS) {
             unsigned long long *dst = D.wj + dep_pos(q);
-            const float *row = col + q * DEP_STRIDE + 16 * half;
+            const float4 *row = reinterpret_cast<const float4 *>(col + q * COL_STRIDE + 16 * half);
             const int *hkeys = keys + 16 * half;
             const unsigned hact = (act >> (16 * half)) & 0xffffu;
             const unsigned ends = (((ends32 >> (16 * half)) & 0xffffu) | 0x8000u) & hact;
             float r[16];
 #pragma unroll
-            for (int i = 0; i < 16; i++) r[i] = row[i];
+            for (int i = 0; i < 4; i++) {
+                const float4 v = row[i];
+                r[4 * i] = v.x, r[4 * i + 1] = v.y, r[4 * i + 2] = v.z, r[4 * i + 3] = v.w;
+            }
             float acc = 0.0f;
 #pragma unroll
             for (int i = 0; i < 16; i++) {
@@ -959,14 +967,17 @@ __global__ void __launch_bounds__(FUSED_BLOCK, fused_min_blocks<CORR, HOST>())
         const bool jrow = lane < 12;
         unsigned long long *dst = (jrow ? D.wj : D.wr) + dep_pos(lane);
         const int stride = jrow ? DEP_JSLOTS : DEP_RSLOTS;
-        const float *row = col + lane * DEP_STRIDE;
+        const float4 *row = reinterpret_cast<const float4 *>(col + lane * COL_STRIDE);
         const unsigned ends = ends32;
         float acc = 0.0f;
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             float r[16];
 #pragma unroll
-            for (int i = 0; i < 16; i++) r[i] = row[16 * h + i];
+            for (int i = 0; i < 4; i++) {
+                const float4 v = row[4 * h + i];
+                r[4 * i] = v.x, r[4 * i + 1] = v.y, r[4 * i + 2] = v.z, r[4 * i + 3] = v.w;
+            }
 #pragma unroll
             for (int i = 0; i < 16; i++) {
                 acc += r[i];

@@ -892,6 +892,12 @@ int emoo_create(const emoo_input_info *info, const emoo_opts *opts, emoo_handle 
             break;
         }
     h->nspec = info->nspecies;
+    // the sort keys (species * cells + cell, and the removed-particle key
+    // above them) are 32-bit words
+    if ((h->precision == EMOO_FP64 ? key_bits(h) : mixed_key_bits(h)) > 32) {
+        emoo_destroy(h);
+        return EMOO_ERR_UNSUPPORTED;
+    }
     double mindx = std::min(std::min(h->g.d[0], h->g.d[1]), h->g.d[2]);
     h->dt = o.dt > 0 ? o.dt : (mindx / 1) / 100.0;  // src/main.cpp:213-214
     h->t = info->t0;

@@ -285,6 +285,7 @@ __global__ void k_species_bounds(const uint32_t *keys, int64_t n, int nspec, int
 // Digit widths: ceil(key_bits / 9) passes of equal width (at most 9 bits);
 // a pass wider than 8 bits uses the 512-bin kernels.
 int radix_sort_perm(emoo_handle *h, int64_t n, int key_bits) {
+    if (key_bits > 32) return EMOO_ERR_UNSUPPORTED;  // keys are 32-bit words
     if (n <= 0) return EMOO_OK;
     const int kb = std::max(1, key_bits);
     const int passes = (kb + 8) / 9;

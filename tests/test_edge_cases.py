@@ -143,3 +143,25 @@ def test_ragged_species_host_resident_equals_round_trip():
     assert np.array_equal(A.get_field(abi.EX), B.get_field(abi.EX))
     A.close()
     B.close()
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.MIXED])
+def test_sort_keys_beyond_32_bits_are_refused(precision):
+    """Four species on a 1024^3 grid need sort keys (species * cells + cell)
+    of more than 32 bits: the handle is refused before its grid is allocated."""
+    L = abi.lib()
+
+    def create(nspec):
+        cfg = configs.tiny("wide", n=(1024, 1024, 1024))
+        cfg.species = (cfg.species * 2)[:nspec]
+        info = configs.input_info(cfg)
+        info.nspecies = nspec
+        o = abi.Opts()
+        L.emoo_default_opts(C.byref(o))
+        o.precision = precision
+        h = C.c_void_p()
+        rc = L.emoo_create(C.byref(info), C.byref(o), C.byref(h))
+        return rc, h
+
+    rc, h = create(4)
+    assert rc == abi.ERR_UNSUPPORTED and not h.value

@@ -1487,7 +1487,7 @@ int emoo_history(emoo_handle *h, double out8[8]) {
 }
 
 int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n) {
-    if (!h || !n) return EMOO_ERR_ARG;
+    if (!h || !n || (rows && cap < 0)) return EMOO_ERR_ARG;
     int have = (int)(h->hist_rows.size() / 8);
     *n = have;
     if (rows) {

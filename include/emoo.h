@@ -325,7 +325,8 @@ int emoo_step(emoo_handle *h, int nsteps, int64_t counts6[6]);
 int emoo_history(emoo_handle *h, double out8[8]);
 
 /* Rows recorded by emoo_step (every history_every steps, before the push,
- * like the reference). Copies up to cap rows of 8 doubles; *n = rows held. */
+ * like the reference). Copies up to cap rows of 8 doubles; *n = rows held.
+ * EMOO_ERR_ARG: n null, or rows given with a negative cap. */
 int emoo_history_rows(emoo_handle *h, int cap, double *rows, int *n);
 
 /* Gauss-law residual of the current state: max and L2 norm over physical

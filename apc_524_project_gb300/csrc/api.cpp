@@ -1282,13 +1282,14 @@ int emoo_set_waves(emoo_handle *h, int nwaves, const double *amp, const double *
     HANDLE_CHECK(h);
     if (nwaves != h->info.nwaves || nwaves < 0 || nwaves > EMOO_NWAVE || (nwaves && (!amp || !phase_deg)))
         return EMOO_ERR_ARG;
-    for (int w = 0; w < nwaves; w++) {
+    for (int w = 0; w < nwaves; w++)  // all checked before any is applied
         if (!std::isfinite(amp[w]) || !std::isfinite(phase_deg[w])) return EMOO_ERR_ARG;
+    LightState *L = light_of(h);
+    if (!L) return EMOO_ERR_STATE;
+    for (int w = 0; w < nwaves; w++) {
         h->info.peakamps[w] = amp[w];
         h->info.phases[w] = phase_deg[w];
     }
-    LightState *L = light_of(h);
-    if (!L) return EMOO_ERR_STATE;
     *L = build_light(h->info);
     return EMOO_OK;
 }

@@ -68,6 +68,11 @@ def test_refused_calls_leave_the_handle_usable(precision):
     assert L.emoo_set_field(h, abi.NFIELDS, _ptr(f)) == abi.ERR_ARG
     assert L.emoo_set_field(h, abi.EX, None) == abi.ERR_ARG
 
+    # waves (this case injects none)
+    w = np.ones(1)
+    assert L.emoo_set_waves(h, 1, _ptr(w), _ptr(w)) == abi.ERR_ARG
+    assert L.emoo_set_wave_shape(h, 0, None) == abi.ERR_ARG
+
     # loop and diagnostics
     assert L.emoo_step(h, -1, None) == abi.ERR_ARG
     assert L.emoo_history(h, None) == abi.ERR_ARG

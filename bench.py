@@ -256,11 +256,18 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
     res["mixed"] = {"t": t, "fused_ms": fused_ms, "launches": launches, "clocks": clocks}
 
     # ---- one stable sort of the drifted particle state (part of the loop
-    # every 20 steps; timed alone here to show its share). Reading rho first
-    # deposits the charge density the steps left pending, which emoo_sort
-    # would otherwise do before sorting (the loop's own sort does not).
+    # every nstep_sort steps; timed alone here to show its share): the steps
+    # up to the next sort first, so that the store has drifted as long as the
+    # loop's own sort sees it. Reading rho first deposits the charge density
+    # the steps left pending, which emoo_sort would otherwise do before
+    # sorting (the loop's own sort does not).
     import numpy as np
 
+    if cfg.nstep_sort > 0:
+        more = (-(args.warmup + args.steps)) % cfg.nstep_sort
+        if more:
+            abi.check(L.emoo_step(h, more, cnt), "emoo_step")
+        res["sort_drift_steps"] = cfg.nstep_sort
     rho = np.empty(tuple(v + 3 for v in cfg.n))
     abi.check(L.emoo_get_field(h, abi.RHO, rho.ctypes.data_as(C.POINTER(C.c_double))), "emoo_get_field")
     st = _stream_of(h)
@@ -970,6 +977,7 @@ def main():
         "gpu_launches": m["launches"],
         "clocks": m["clocks"],
         "sort_ms": res.get("sort_ms"),
+        "sort_drift_steps": res.get("sort_drift_steps"),
     }
     if "fp64" in res:
         f = res["fp64"]

@@ -17,6 +17,25 @@ __device__ __forceinline__ int64_t gidx(const Geom &g, int i, int j, int k) {
     return (int64_t)i * g.sx + (int64_t)j * g.sy + k;
 }
 
+// The 1-based indices (i, j, k) of physical point t (0 <= t < n0 n1 n2, k
+// fastest). 32-bit divisions where t fits (every grid these forms allocate):
+// a 64-bit divide is a long emulated sequence.
+__device__ __forceinline__ void phys_ijk(const int n[3], int64_t t, int &i, int &j, int &k) {
+    if (t < ((int64_t)1 << 32)) {
+        const uint32_t u = (uint32_t)t, n2 = (uint32_t)n[2], n1 = (uint32_t)n[1];
+        const uint32_t r = u / n2;
+        k = (int)(u - r * n2) + 1;
+        const uint32_t q = r / n1;
+        j = (int)(r - q * n1) + 1;
+        i = (int)q + 1;
+    } else {
+        const int64_t r = t / n[2];
+        k = (int)(t - r * n[2]) + 1;
+        j = (int)(r % n[1]) + 1;
+        i = (int)(r / n[1]) + 1;
+    }
+}
+
 // Grid::getCellID, src/grid/oGrid.cpp:208-227: C truncation plus the ghost
 // offset, per axis.
 __device__ __forceinline__ void cell_of(const Geom &g, double x, double y, double z, int &ix, int &iy, int &iz) {

@@ -199,10 +199,8 @@ __global__ void k_jacobi_check(Geom g, const double *u1, const double *u2, doubl
     double m = 0.0;
     int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
-        int k = (int)(t % g.n[2]) + 1;
-        int64_t r = t / g.n[2];
-        int j = (int)(r % g.n[1]) + 1;
-        int i = (int)(r / g.n[1]) + 1;
+        int i, j, k;
+        phys_ijk(g.n, t, i, j, k);
         int64_t o = gidx(g, i, j, k);
         double a = fabs(u2[o] - u1[o]);
         m = a > m ? a : m;
@@ -345,10 +343,8 @@ __global__ void k_field_energy(Geom g, CF3 E, CF3 B, double *part) {
     int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
     double hv = 0.5 * g.vol;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
-        int k = (int)(t % g.n[2]) + 1;
-        int64_t r = t / g.n[2];
-        int j = (int)(r % g.n[1]) + 1;
-        int i = (int)(r / g.n[1]) + 1;
+        int i, j, k;
+        phys_ijk(g.n, t, i, j, k);
         int64_t o = gidx(g, i, j, k);
         int64_t nb[3] = {o + g.sx, o + g.sy, o + 1};
         for (int q = 0; q < 3; q++) {
@@ -378,10 +374,8 @@ __global__ void k_gauss(Geom g, CF3 E, const double *rho, double *part) {
     double mx = 0.0, s2 = 0.0;
     int64_t nphys = (int64_t)g.n[0] * g.n[1] * g.n[2];
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
-        int k = (int)(t % g.n[2]) + 1;
-        int64_t r = t / g.n[2];
-        int j = (int)(r % g.n[1]) + 1;
-        int i = (int)(r / g.n[1]) + 1;
+        int i, j, k;
+        phys_ijk(g.n, t, i, j, k);
         int64_t o = gidx(g, i, j, k);
         double dv = ddiv(E.p[0][o] - E.p[0][o - g.sx], g.d[0], g.id[0], g.p2[0]) +
                     ddiv(E.p[1][o] - E.p[1][o - g.sy], g.d[1], g.id[1], g.p2[1]) +

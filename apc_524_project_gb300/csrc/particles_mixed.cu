@@ -1371,10 +1371,8 @@ __global__ void k_energy_m(MGeom g, MCF3 E, MCF3 B, double hv, double *part) {
     float f[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int cnt = 0;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nphys; t += (int64_t)gridDim.x * blockDim.x) {
-        int k = (int)(t % g.n[2]) + 1;
-        int64_t r = t / g.n[2];
-        int j = (int)(r % g.n[1]) + 1;
-        int i = (int)(r / g.n[1]) + 1;
+        int i, j, k;
+        phys_ijk(g.n, t, i, j, k);
         int64_t o = (int64_t)i * g.sx + (int64_t)j * g.sy + k;
         int64_t nb[3] = {o + g.sx, o + g.sy, o + 1};
         for (int q = 0; q < 3; q++) {

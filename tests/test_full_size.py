@@ -1,0 +1,93 @@
+"""The benchmark workload at its full size: the thermal plasma on 256^3 cells,
+2 species x 16 particles per cell = 536,870,912 particles, mixed form (the
+configuration the throughput is quoted on). The oracle does not reach this
+size, so these tests check properties that hold at any size:
+
+* two runs from the same seed over 22 steps (a sort at step 20 and three
+  history rows) are identical bit for bit: fields, current, history; no
+  particle is lost;
+* under the corrected policy the discrete continuity equation
+  rho(t + dt) - rho(t) + dt div J = 0 holds at every one of the 16.8 M
+  points, for the step that sorts the store after 19 steps of drift.
+
+The particles are generated on the device (emoo_load_generated), as the
+benchmark loads them; the field start is the multigrid solve."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from apc_524_project_gb300 import abi, configs
+
+pytestmark = pytest.mark.gpu
+
+N_CELLS = 256
+STEPS = 22  # past the sort at step 20
+
+
+def _handle(cfg, policy):
+    from backends import GpuBackend
+
+    g = GpuBackend(configs.input_info(cfg), cfg.dt, precision=abi.MIXED, capacity=cfg.total_particles(),
+                   track_ids=0, policy=policy, poisson_solver=abi.POISSON_MULTIGRID)
+    for si in range(len(cfg.species)):
+        gp = configs.gen_params(cfg, si)
+        abi.check(g.L.emoo_load_generated(g.h, C.byref(gp), cfg.count(cfg.species[si])), "emoo_load_generated")
+    it = (C.c_int * 4)()
+    rc = g.L.emoo_init_fields(g.h, it)
+    assert rc in (abi.OK, abi.ERR_NOT_CONVERGED)
+    return g
+
+
+def _run(cfg, policy):
+    g = _handle(cfg, policy)
+    assert g.num_particles() == cfg.total_particles()
+    crossings = np.array(g.step(STEPS))
+    out = {f: g.get_field(f) for f in (abi.EX, abi.EY, abi.BZ, abi.JX, abi.JZ)}
+    out["history"] = g.history_rows()
+    out["n"] = g.num_particles()
+    out["crossings"] = crossings
+    abi.check(g.L.emoo_check(g.h), "device error word")
+    g.close()
+    return out
+
+
+def test_full_size_run_is_reproducible_and_keeps_its_particles():
+    cfg = configs.thermal256(N_CELLS)
+    a = _run(cfg, abi.POLICY_REFERENCE)
+    b = _run(cfg, abi.POLICY_REFERENCE)
+    assert a["n"] == b["n"] == cfg.total_particles()
+    assert a["history"].shape[0] == 3 and np.isfinite(a["history"]).all()
+    assert np.array_equal(a["crossings"], b["crossings"]) and a["crossings"].sum() > 0
+    for key in ("history", abi.EX, abi.EY, abi.BZ, abi.JX, abi.JZ):
+        assert np.array_equal(a[key], b[key]), key
+    assert np.abs(a[abi.JX]).max() > 0
+
+
+def _div(f, dx, n):
+    """Backward-difference divergence at the physical points, periodic."""
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    out = np.zeros((n[0], n[1], n[2]))
+    for d, a in enumerate(f):
+        phys = a[P]
+        out += (phys - np.roll(phys, 1, axis=d)) / dx[d]
+    return out
+
+
+def test_full_size_corrected_policy_conserves_charge_through_a_sort():
+    cfg = configs.thermal256(N_CELLS)
+    n = cfg.n
+    g = _handle(cfg, abi.POLICY_CORRECTED)
+    P = (slice(1, n[0] + 1), slice(1, n[1] + 1), slice(1, n[2] + 1))
+    g.step(cfg.nstep_sort - 1)
+    rho0 = g.get_field(abi.RHO)[P].copy()
+    g.step(1)  # sorts the drifted store, then moves every particle
+    rho1 = g.get_field(abi.RHO)[P]
+    divj = _div([g.get_field(i) for i in (abi.JX, abi.JY, abi.JZ)], cfg.dx, n)
+    cont = (rho1 - rho0) + cfg.dt * divj
+    scale = np.abs(rho0).max()
+    assert scale > 0
+    assert np.abs(cont).max() <= 1e-5 * scale, (np.abs(cont).max(), scale)
+    assert g.num_particles() == cfg.total_particles()
+    abi.check(g.L.emoo_check(g.h), "device error word")
+    g.close()

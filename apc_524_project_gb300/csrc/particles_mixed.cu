@@ -422,7 +422,7 @@ __device__ __forceinline__ void push_m(const float f[6], const float qp, const f
     }
 }
 
-constexpr int FUSED_BLOCK = 256;
+constexpr int FUSED_BLOCK = 128;
 constexpr int FUSED_WARPS = FUSED_BLOCK / 32;
 constexpr int DEP_STRIDE = 33;  // column stride of the adjoint's transpose (odd: conflict-free both ways)
 // Column stride of the fused kernel's deposit transpose: rows start on
@@ -684,16 +684,18 @@ __device__ __forceinline__ void vb_pieces_list(const MGeom &g, const BCTab &bc, 
 // written back to the caller's FP64 arrays (Hp) instead of the device store,
 // converted as the loader and readback convert (f64_to_m, m_to_f64), so one
 // launch moves every particle over the host link in both directions at once.
-// Resident blocks per SM the register budget is cut for, measured over a
-// 20-step sort interval at 256^3: 6 (40 registers, no spills) for the
-// reference policy on the device store, where more warps hide the L2 latency
-// that grows as particles drift between sorts (12.59 against 13.06 ms a launch
-// at 5); 4 (64 registers, no spills) for the corrected policy's pieces (19.23
-// against 20.01 ms at 5 with 148 bytes of spills, 24.6 ms at 6); 5 (48
-// registers) for the host-resident conversions.
+// Resident blocks per SM the register budget is cut for, counted in blocks of
+// 256 threads and measured over a 20-step sort interval at 256^3: 6 (40
+// registers, no spills) for the reference policy on the device store, where
+// more warps hide the L2 latency that grows as particles drift between sorts
+// (12.59 against 13.06 ms a launch at 5); 4 (64 registers, no spills) for the
+// corrected policy's pieces (19.23 against 20.01 ms at 5 with 148 bytes of
+// spills, 24.6 ms at 6); 5 (48 registers) for the host-resident conversions.
+// The same warps in blocks of 128 threads, twice as many blocks, take 12.36
+// ms (blocks of 64: 12.60; of 96: 12.63; of 512: 12.92).
 template <bool CORR, bool HOST>
 constexpr int fused_min_blocks() {
-    return CORR ? 4 : (HOST ? 5 : 6);
+    return 256 / FUSED_BLOCK * (CORR ? 4 : (HOST ? 5 : 6));
 }
 
 template <bool REL, bool FIRST, bool PUSH, bool CORR = false, bool HOST = false>

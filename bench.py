@@ -59,6 +59,7 @@ def _args():
     ap.add_argument("--no-corrected", action="store_true")
     ap.add_argument("--no-mixed-error", action="store_true")
     ap.add_argument("--no-full-run", action="store_true")
+    ap.add_argument("--no-cadence", action="store_true")
     ap.add_argument("--only", choices=["poisson", "twostream", "adjoint", "mixed_error"], default=None,
                     help="run one side measurement alone and print its JSON line")
     ap.add_argument("--ad-policy", choices=["reference", "corrected"], default="corrected",
@@ -305,6 +306,8 @@ def run_gpu_arm(args, rank, world, dist_barrier, dist_max):
         res["laser512"] = laser512_arm(device)
     if not args.no_corrected:
         res["corrected"] = corrected_arm(cfg, args, device)
+    if not args.no_cadence:
+        res["sort_cadence"] = cadence_arm(cfg, device)
     if not args.no_poisson:
         res["poisson"] = poisson_arm(device)
     if not args.no_mixed_error:
@@ -365,6 +368,38 @@ def corrected_arm(cfg, args, device):
            "ms_per_step": t / args.steps * 1e3, "fused_kernel_ms": st.timed_ms / max(1, st.timed_launches)}
     if not args.no_full_run:
         out["full_run"] = full_run(cfg, device)
+    return out
+
+
+def cadence_arm(cfg, device, cadences=(10, 14, 20), steps=140):
+    """The benchmark's workload at other sort cadences (the input's nstep_sort;
+    the headline keeps the configured 20): loop throughput over `steps` steps,
+    a whole number of intervals at each cadence, under the corrected policy
+    (over this many steps the reference policy's field energy grows, and its
+    particles speed up with it). A sort costs a pass over the store; the fused
+    kernel slows between sorts as particles leave their sorted cells."""
+    import dataclasses
+
+    import torch
+    from apc_524_project_gb300 import abi
+
+    L = abi.lib()
+    N = cfg.total_particles()
+    cnt = (C.c_int64 * 6)()
+    out = {"workload": "the benchmark's workload, mixed form, corrected policy", "steps": steps}
+    for T in cadences:
+        h = _make_handle(dataclasses.replace(cfg, nstep_sort=T), abi.MIXED, N, device, policy=abi.POLICY_CORRECTED)
+        abi.check(L.emoo_step(h, 1, cnt), "emoo_step")  # the first push, after the load's sort
+        st = _stream_of(h)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        abi.check(L.emoo_step(h, steps, cnt), "emoo_step")
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        abi.check(L.emoo_destroy(h))
+        out[str(T)] = {"value": N * steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / steps}
     return out
 
 
@@ -1002,6 +1037,8 @@ def main():
         line["poisson"] = res["poisson"]
     if "corrected" in res:
         line["corrected"] = res["corrected"]
+    if "sort_cadence" in res:
+        line["sort_cadence"] = res["sort_cadence"]
     if "mixed_error" in res:
         line["mixed_error"] = res["mixed_error"]
     if "e2e" in res:

@@ -263,9 +263,9 @@ int gather_one(emoo_handle *h, T *&arr, const uint32_t *perm, int64_t n) {
     T *tmp = (T *)scratch;
     // Four blocks per SM: the outputs in flight then read their sources from a
     // window of cells that stays in L2, so a fetched sector serves the other
-    // elements in it. Sixteen per SM spread the window until sectors were
-    // fetched twice (sort of a 536,870,912-particle store drifted 20 steps:
-    // 26.9 ms at four blocks per SM, 32.9 ms at sixteen, 34.3 ms at one).
+    // elements in it. At sixteen per SM the window is wider and DRAM reads ran
+    // at 1.47 times the bytes used (sort of a 536,870,912-particle store drifted
+    // 20 steps: 26.9 ms at four blocks per SM, 32.9 ms at sixteen, 34.3 ms at one).
     int nb = (int)std::min<int64_t>((n / 4 + 255) / 256, 152 * 4);
     h->launches++;
     k_gather<T><<<std::max(nb, 1), 256, 0, h->stream>>>(arr, tmp, perm, n);  // base pointers are cudaMalloc'd
